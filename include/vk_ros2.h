@@ -1,0 +1,187 @@
+/*
+ * vk_ros2.h -- C ABI of the GB300-native VULCAN Ros2 kinetics-diffusion step.
+ *
+ * Plain C types only (ints, doubles, pointers and sizes); host arrays are
+ * caller-owned and copied in/out; device buffers are owned by the handle.
+ * No C++ exception crosses this boundary: every entry point returns a
+ * status code (VK_OK = 0) and vk_last_error() gives the message.
+ *
+ * Reference interfaces replaced (paths inside the VULCAN project):
+ *   vk_network_compile  make_chem_funs.py:17-430 (network -> chemdf/df tables)
+ *                       and make_chem_funs.py:653-717 (symbolic Jacobian)
+ *   vk_set_columns      store.py:21-180 data contract (var.y, var.k, atm.*)
+ *   vk_ros2_attempt     op.py:2860-3007   Ros2.solver (one Rosenbrock attempt)
+ *   vk_one_step         op.py:3091-3103   Ros2.one_step (+ clip/loss/step_ok/
+ *                       step_reject, op.py:2447-2534)
+ *   vk_run              op.py:808-936     Integration.__call__ (accept/reject,
+ *                       step_size op.py:3105-3125, update_mu_dz op.py:944-984,
+ *                       conv/stop op.py:1018-1085) for a batch of columns
+ *   vk_get_state        var.y / var.ymix / var.dt / para.delta read-back
+ */
+#ifndef VK_ROS2_H
+#define VK_ROS2_H
+
+#if defined(__GNUC__)
+#define VK_API __attribute__((visibility("default")))
+#else
+#define VK_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define VK_OK            0
+#define VK_EINVAL        1   /* bad argument / size beyond the handle's limits */
+#define VK_ECUDA         2   /* CUDA runtime error */
+#define VK_ESINGULAR     3   /* zero pivot in a diagonal block */
+#define VK_ENAN          4   /* non-finite value in the state */
+#define VK_EMAXATTEMPT   5   /* attempt cap reached without an accepted step */
+#define VK_ETIMEOUT      6   /* host watchdog gave up waiting */
+#define VK_ENOMEM        7   /* device allocation failed */
+
+/* ---- linear-solve precision ---- */
+#define VK_PREC_FP64     0   /* FP64 block LU (matches the reference step) */
+#define VK_PREC_MIXED    1   /* FP32 scaled block LU + FP64 iterative refinement */
+
+/* ---- per-layer atmosphere fields (vk_set_columns, atm[L][VK_ATM_NF]) ----
+ * Interface quantities of layer j describe interface j+1/2 and are unused on
+ * the top layer of a column. */
+#define VK_ATM_M      0   /* third-body density M = n_0 at set-up (cm^-3)     */
+#define VK_ATM_N0     1   /* total density n_0 (hydrostatic renormalisation)  */
+#define VK_ATM_TCO    2   /* temperature (K)                                  */
+#define VK_ATM_G      3   /* gravity g(z)                                     */
+#define VK_ATM_DZI    4   /* dzi, interface spacing                           */
+#define VK_ATM_KZZ    5   /* eddy diffusion at the interface                  */
+#define VK_ATM_VZ     6   /* vertical wind at the interface                   */
+#define VK_ATM_TI     7   /* interface temperature Ti                         */
+#define VK_ATM_HPI    8   /* interface scale height Hpi                       */
+#define VK_ATM_HP     9   /* layer scale height Hp (steady-state slope)       */
+#define VK_ATM_PICO  10   /* pressure at the lower interface of the layer     */
+#define VK_ATM_PICOU 11   /* pressure at the upper interface of the layer     */
+#define VK_ATM_DZ    12   /* layer thickness dz                               */
+#define VK_ATM_NF    13
+
+/* ---- per-column species fields (vk_set_columns, spf[col][VK_SP_NF][ni]) ---- */
+#define VK_SP_MS        0   /* molar mass                                     */
+#define VK_SP_ALPHA     1   /* thermal diffusion factor                       */
+#define VK_SP_TOPFLUX   2
+#define VK_SP_BOTFLUX   3
+#define VK_SP_BOTVDEP   4
+#define VK_SP_NF        5
+
+/* ---- flags ---- */
+#define VK_F_MOLDIFF    1   /* vulcan_cfg.use_moldiff: diffdf / lhs_jac_tot   */
+#define VK_F_TOPFLUX    2   /* vulcan_cfg.use_topflux                          */
+#define VK_F_BOTFLUX    4   /* vulcan_cfg.use_botflux                          */
+
+/* Network description, in the written order of the network file.  Reaction
+ * pair p has forward k index 2p+1 and reverse 2p+2 (rows 2p and 2p+1 of the
+ * rate array).  Each side lists its terms as written ("H + H + M" is three
+ * terms, "2*X" one term with coefficient 2); species index -1 denotes M. */
+typedef struct vk_network_desc {
+    int ni;                 /* number of species                              */
+    int npair;              /* number of forward/reverse reaction pairs       */
+    const int *reac_ptr;    /* [npair+1] CSR into reac_sp / reac_nu           */
+    const int *reac_sp;     /* species index, -1 = M                          */
+    const int *reac_nu;     /* stoichiometric coefficient                     */
+    const int *prod_ptr;    /* [npair+1] CSR into prod_sp / prod_nu           */
+    const int *prod_sp;
+    const int *prod_nu;
+    int natom;              /* elements tracked by the conservation check     */
+    const double *compo;    /* [ni * natom] element counts                    */
+} vk_network_desc;
+
+typedef struct vk_network vk_network;   /* compiled tables (host memory)     */
+typedef struct vk_handle vk_handle;     /* device state for a batch          */
+
+/* Solver controls (defaults = the reference's vulcan_cfg values). */
+typedef struct vk_ctrl {
+    double rtol, atol, mtol, mtol_conv, pos_cut, nega_cut, loss_eps;
+    double dt_min, dt_max, dt_var_min, dt_var_max;
+    double yconv_cri, slope_cri, yconv_min, st_factor, trun_min, runtime;
+    int conv_step, count_min, count_max, update_frq;
+    int max_attempts;       /* attempt cap per step (device guard)            */
+    int flags;              /* VK_F_* */
+    double gs, Rp;          /* gravity update (update_mu_dz)                  */
+} vk_ctrl;
+
+/* ---- network ---- */
+VK_API int  vk_network_compile(const vk_network_desc *desc, vk_network **out);
+/* sizes of the compiled tables: Jacobian non-zeros per diagonal block,
+ * derivative terms, production/loss terms */
+VK_API int  vk_network_info(const vk_network *net, int *nnz_jac, int *n_dterm, int *n_src);
+/* Jacobian sparsity: row and column of each stored entry (arrays of nnz_jac) */
+VK_API int  vk_network_jac_pattern(const vk_network *net, int *rows, int *cols);
+VK_API void vk_network_free(vk_network *net);
+
+/* ---- handle ---- */
+VK_API int  vk_create(const vk_network *net, int max_cols, int max_layers, int precision,
+               vk_handle **out);
+VK_API void vk_destroy(vk_handle *h);
+VK_API const char *vk_last_error(const vk_handle *h);   /* h may be NULL */
+VK_API int  vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol);
+
+/* Load a batch of columns.  L = sum(nz).  k is [L][2*npair] (layer-major,
+ * row l holds k[1..nr] of that layer), atm is [L][VK_ATM_NF], Dzz is [L][ni]
+ * (interface values, top layer unused), spf is [ncols][VK_SP_NF][ni],
+ * y and ymix are [L][ni].  Copies everything to the device. */
+VK_API int  vk_set_columns(vk_handle *h, int ncols, const int *nz, const double *k,
+                    const double *atm, const double *Dzz, const double *spf,
+                    const double *y, const double *ymix);
+/* Update only the fields that change during a run (y, ymix, atm, k). */
+VK_API int  vk_update_state(vk_handle *h, const double *y, const double *ymix);
+VK_API int  vk_update_atm(vk_handle *h, const double *atm);
+VK_API int  vk_update_k(vk_handle *h, const double *k);
+
+/* One Ros2 attempt for every column with its own dt[col] (op.py:2860-3007):
+ * outputs sol (written to the device y), ymix, delta[col]; k1/k2 optional
+ * (NULL to skip the copy-out).  flags = VK_F_*. */
+VK_API int  vk_ros2_attempt(vk_handle *h, const double *dt, int flags, double *sol,
+                     double *ymix, double *delta, double *k1, double *k2);
+
+/* Element totals at set-up (InitialAbun.ele_sum) used by the loss check. */
+VK_API int  vk_set_atom_ini(vk_handle *h, const double *atom_ini /*[ncols][natom]*/);
+
+/* Per-column index of the 1-bar reference interface (f_mu_dz pref_indx) and
+ * a per-species mask [ni] of species ignored by the steady-state test
+ * (vulcan_cfg.conver_ignore); either pointer may be NULL. */
+VK_API int  vk_set_column_info(vk_handle *h, const int *pref_indx, const int *conv_ignore);
+
+/* Integrate every column on the device until each one reaches steady state
+ * or a limit (count_max / runtime), or until max_steps accepted steps per
+ * column have been taken in this call (0 = no cap).  dt/t/count live on the
+ * device; the loop is captured once into a CUDA graph and replayed. */
+VK_API int  vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s);
+
+/* Per-column state read-back: y/ymix [L][ni]; the scalar arrays are [ncols]
+ * (NULL to skip).  end_case: 0 running, 1 converged, 2 runtime, 3 count_max,
+ * negative = error status. */
+VK_API int  vk_get_state(vk_handle *h, double *y, double *ymix, double *dt, double *t,
+                  int *count, int *end_case, double *delta);
+/* Initial dt / t / count per column before vk_run (dt = vulcan_cfg.dttry). */
+VK_API int  vk_set_clock(vk_handle *h, const double *dt, const double *t, const int *count);
+
+/* Cumulative counters per column: [ncols][4] = attempts, delta rejections,
+ * negativity rejections, loss rejections. */
+VK_API int  vk_get_counters(vk_handle *h, int *counters);
+
+/* Kernel timing of the last vk_run / vk_ros2_attempt (ms per kernel class). */
+VK_API int  vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double *ms_solve,
+                   double *ms_stage, int *launches);
+
+/* ---- diagnostics (used by the parity tests) ---- */
+/* Message of the last failed vk_network_compile on this thread. */
+VK_API const char *vk_network_last_error(void);
+/* Chemistry source term alone (the generated chemdf) of state y [L][ni]. */
+VK_API int  vk_chem_source(vk_handle *h, const double *y, double *dydt);
+/* LHS pieces of the last attempt: -J entries [L][nnz_jac] in the order of
+ * vk_network_jac_pattern, and the transport coefficients dA/dB/dC [L][ni]
+ * (dy_j/dt = dA y_j + dB y_{j+1} + dC y_{j-1}). */
+VK_API int  vk_get_lhs(vk_handle *h, double *jv, double *dA, double *dB, double *dC);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VK_ROS2_H */

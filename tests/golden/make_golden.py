@@ -1,0 +1,328 @@
+"""Generate golden fixtures by running the reference VULCAN itself.
+
+Test infrastructure only: run in a container that has the reference source
+(default ``/root/reference``); the GPU machine only reads the committed
+``tests/golden/*.npz``.
+
+For each workload it
+  1. copies the reference tree to a temporary directory (the reference's code
+     generator rewrites its network file in place, so it never runs on the
+     original), adds a matplotlib stub and appends overrides to vulcan_cfg.py;
+  2. runs the reference's own ``make_chem_funs.py`` (its numpy-2 crash in
+     check_conserv comes after chem_funs.py is complete and is tolerated);
+  3. runs the reference's set-up sequence (vulcan.py order) with the seeded
+     synthetic temperature / Kzz / mixing ratios / frozen J injected, then the
+     reference's own ``op.Integration`` loop with a recording ``op.Ros2``
+     subclass that captures every Ros2 attempt's inputs and outputs
+     (y, ymix, dt, k1, k2, sol, delta) plus the per-step trajectory;
+  4. stores the compiled network (our parser's tables) beside the reference's
+     own view of it (species order, nr) and the atmosphere arrays.
+
+Usage:  python tests/golden/make_golden.py [c0|c1|c2 ...] [--ref /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import textwrap
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from vulcan_gb300 import configs  # noqa: E402
+from vulcan_gb300.network import Network  # noqa: E402
+
+# Which attempts go into the committed fixture (all attempts are recorded).
+KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
+        'c1': (0, 1, 2, 10, 29),
+        'c2': (0, 1, 2, 10, 29),
+        'c2long': (400, 800, 1200, 1600, 1999)}
+NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000}
+
+DRIVER = r'''
+import os, sys, time, json
+import numpy as np
+sys.path.insert(0, os.getcwd())
+sys.path.insert(0, os.path.join(os.getcwd(), '_mplstub'))
+import scipy.linalg
+_orig = scipy.linalg.solve_banded
+SB = []
+def _sb(*a, **kw):
+    x = _orig(*a, **kw)
+    SB.append(np.array(x, copy=True))
+    return x
+scipy.linalg.solve_banded = _sb
+import vulcan_cfg
+import store, build_atm, op, chem_funs
+from phy_const import kb
+inp = np.load('golden_inputs.npz', allow_pickle=True)
+meta = json.load(open('golden_meta.json'))
+
+var = store.Variables(); atm = store.AtmData(); para = store.Parameters()
+para.start_time = time.time()
+make_atm = build_atm.Atm()
+output = op.Output()
+atm = make_atm.f_pico(atm)
+atm = make_atm.load_TPK(atm)
+atm.Tco = inp['Tco'].copy()
+atm.M = atm.pco / (kb * atm.Tco)
+atm.n_0 = atm.M.copy()
+atm.Kzz = inp['Kzz'].copy()
+rate = op.ReadRate()
+var = rate.read_rate(var, atm)
+var = rate.rev_rate(var, atm)
+var = rate.remove_rate(var)
+ini = build_atm.InitialAbun()
+var = ini.ini_y(var, atm)
+var = ini.ele_sum(var)
+atm = make_atm.f_mu_dz(var, atm, output)
+make_atm.mol_diff(atm)
+make_atm.BC_flux(atm)
+for key, J in zip(meta['photo_keys'], inp['photo_J']):
+    var.k[var.pho_rate_index[(key[0], int(key[1]))]] = J.copy()
+nr = chem_funs.nr
+K = np.array([var.k[i] for i in range(1, nr + 1)])
+setup = dict(pico=atm.pico, M=atm.M, n_0=atm.n_0, mu=atm.mu, g=atm.g.copy(),
+             Hp=atm.Hp.copy(), dz=atm.dz.copy(), zco=atm.zco.copy(), dzi=atm.dzi,
+             Ti=atm.Ti, Hpi=atm.Hpi, Dzz=atm.Dzz, ms=atm.ms, alpha=atm.alpha,
+             Kzz=atm.Kzz, vz=atm.vz, Tco=atm.Tco, pco=atm.pco, k=K,
+             y_ini=var.y.copy(), ymix_ini=var.ymix.copy(),
+             atom_ini=np.array([var.atom_ini[a] for a in vulcan_cfg.atom_list]),
+             pref_indx=atm.pref_indx)
+# chemistry pins at the initial state
+setup['chemdf0'] = chem_funs.chemdf(var.y, atm.M, var.k)
+ATT, STEPS = [], []
+
+class RecRos2(op.Ros2):
+    def solver(self, v, a, p):
+        snap = dict(y=v.y.copy(), ymix=v.ymix.copy(), dt=float(v.dt),
+                    dzi=a.dzi.copy(), Hpi=a.Hpi.copy(), g=a.g.copy(), Hp=a.Hp.copy(),
+                    count=int(p.count), t=float(v.t))
+        del SB[:]
+        v, p = op.Ros2.solver(self, v, a, p)
+        snap.update(k1=SB[0], k2=SB[1], sol=v.y.copy(), delta=float(p.delta))
+        ATT.append(snap)
+        return v, p
+    def clip(self, v, p, a, **kw):
+        v, p = op.Ros2.clip(self, v, p, a, **kw)
+        ATT[-1]['y_clip'] = v.y.copy()
+        ATT[-1]['atom_loss'] = np.array([v.atom_loss[x] for x in vulcan_cfg.atom_list])
+        ATT[-1]['ok'] = bool(self.step_ok(v, p))
+        return v, p
+    def step_size(self, v, p, **kw):
+        STEPS.append(dict(count=int(p.count), t=float(v.t), dt_used=float(v.dt),
+                          delta=float(p.delta), y=v.y.copy(), natt=len(ATT)))
+        v = op.Ros2.step_size(self, v, p, **kw)
+        STEPS[-1]['dt_next'] = float(v.dt)
+        return v
+
+solver = RecRos2()
+integ = op.Integration(solver, output)
+solver.naming_solver(para)
+# chemistry Jacobian pins (a few diagonal blocks of neg_symjac at the start)
+ni = chem_funs.ni
+J0 = chem_funs.neg_symjac(var.y, atm.M, var.k)
+lays = [0, 1, len(atm.pco) // 2, len(atm.pco) - 1]
+setup['negjac_layers'] = np.array(lays)
+setup['negjac_blocks'] = np.array([J0[l*ni:(l+1)*ni, l*ni:(l+1)*ni] for l in lays])
+del J0
+t0 = time.time()
+integ(var, atm, para, make_atm)
+wall = time.time() - t0
+keep = meta['keep']
+att_keys = ['y', 'ymix', 'dt', 'dzi', 'Hpi', 'g', 'Hp', 'count', 't', 'k1', 'k2',
+            'sol', 'delta', 'y_clip', 'atom_loss', 'ok']
+out = dict(setup)
+sel = [i for i in keep if i < len(ATT)]
+out['att_index'] = np.array(sel)
+for key in att_keys:
+    out['att_' + key] = np.array([ATT[i][key] for i in sel])
+out['traj_count'] = np.array([s['count'] for s in STEPS])
+out['traj_t'] = np.array([s['t'] for s in STEPS])
+out['traj_dt_used'] = np.array([s['dt_used'] for s in STEPS])
+out['traj_dt_next'] = np.array([s['dt_next'] for s in STEPS])
+out['traj_delta'] = np.array([s['delta'] for s in STEPS])
+out['traj_natt'] = np.array([s['natt'] for s in STEPS])
+out['att_all_delta'] = np.array([a['delta'] for a in ATT])
+out['att_all_ok'] = np.array([a['ok'] for a in ATT])
+out['att_all_dt'] = np.array([a['dt'] for a in ATT])
+ysteps = [s for s in (0, 1, 99, 100, 101, 199, 299, 399, 499) if s < len(STEPS)]
+out['ystep_index'] = np.array(ysteps)
+out['ystep_y'] = np.array([STEPS[s]['y'] for s in ysteps])
+out['spec_list'] = np.array(chem_funs.spec_list)
+out['nr'] = nr
+out['end_case'] = para.end_case
+out['wall_s'] = wall
+out['n_attempts'] = len(ATT)
+np.savez_compressed('golden_out.npz', **out)
+# full record for local deep checks (not committed)
+np.savez_compressed('golden_full.npz',
+    **{('a%d_' % i) + k: np.asarray(ATT[i][k]) for i in range(len(ATT)) for k in att_keys})
+print('attempts', len(ATT), 'steps', len(STEPS), 'wall', wall)
+'''
+
+MPL_STUB = {
+    '__init__.py': 'use = lambda *a, **k: None\n',
+    'pyplot.py': textwrap.dedent('''
+        def __getattr__(name):
+            def _f(*a, **k):
+                return None
+            return _f
+        '''),
+    'legend.py': textwrap.dedent('''
+        def __getattr__(name):
+            def _f(*a, **k):
+                return None
+            return _f
+        '''),
+}
+
+
+def cfg_overrides(spec, nz, count_max, use_photo):
+    mix = {k: float(v) for k, v in spec.const_mix.items()}
+    return textwrap.dedent(f'''
+        # ---- overrides appended by the golden-fixture generator ----
+        network = 'thermo/{spec.network}'
+        use_photo = {use_photo}
+        atom_list = {spec.atom_list!r}
+        nz = {nz}
+        P_b = {configs.P_B!r}
+        P_t = {configs.P_T!r}
+        atm_type = 'isothermal'
+        Tiso = 1500.
+        Kzz_prof = 'const'
+        const_Kzz = 1e9
+        use_Kzz = True
+        use_moldiff = True
+        use_vz = False
+        use_vm_mol = False
+        atm_base = 'H2'
+        rocky = False
+        gs = {configs.GS!r}
+        Rp = {configs.RP!r}
+        ini_mix = 'const_mix'
+        const_mix = {mix!r}
+        diff_esc = []
+        use_topflux = False
+        use_botflux = False
+        use_fix_sp_bot = {{}}
+        use_condense = False
+        use_settling = False
+        use_ion = False
+        remove_list = []
+        use_lowT_limit_rates = False
+        use_live_plot = False
+        use_live_flux = False
+        use_plot_end = False
+        use_plot_evo = False
+        use_save_movie = False
+        plot_TP = False
+        use_print_prog = False
+        use_print_delta = False
+        use_adapt_rtol = False
+        conver_ignore = {spec.conver_ignore!r}
+        count_max = {count_max}
+        out_name = 'golden.vul'
+        ''')
+
+
+def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
+    nz = spec.pco.size
+    dst = os.path.join(workdir, 'vref_' + tag)
+    shutil.copytree(ref_root, dst, ignore=shutil.ignore_patterns('output', 'plot', '.DS_Store'))
+    os.chmod(dst, 0o755)
+    for root, dirs, files in os.walk(dst):
+        for d in dirs:
+            os.chmod(os.path.join(root, d), 0o755)
+        for f in files:
+            os.chmod(os.path.join(root, f), 0o644)
+    stub = os.path.join(dst, '_mplstub', 'matplotlib')
+    os.makedirs(stub)
+    for name, src in MPL_STUB.items():
+        with open(os.path.join(stub, name), 'w') as f:
+            f.write(src)
+    with open(os.path.join(ref_root, 'vulcan_cfg.py')) as f:
+        base_cfg = f.read()
+    env = dict(os.environ, PYTHONPATH=os.path.join(dst, '_mplstub'), OMP_NUM_THREADS='1')
+    # code generation (photo reactions included when the workload has J rates)
+    with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
+        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, spec.use_photo))
+    subprocess.run([sys.executable, 'make_chem_funs.py'], cwd=dst, env=env,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    with open(os.path.join(dst, 'chem_funs.py')) as f:
+        if 'def neg_symjac' not in f.read():
+            raise RuntimeError('reference code generation failed for ' + tag)
+    # run time: photochemistry (radiative transfer) off, J frozen in k
+    with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
+        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, False))
+    keys = sorted(spec.photo_J) if spec.photo_J else []
+    np.savez(os.path.join(dst, 'golden_inputs.npz'), Tco=spec.Tco, Kzz=spec.Kzz,
+             photo_J=np.array([spec.photo_J[k] for k in keys]) if keys else np.zeros((0, nz)))
+    with open(os.path.join(dst, 'golden_meta.json'), 'w') as f:
+        json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep)}, f)
+    with open(os.path.join(dst, 'golden_driver.py'), 'w') as f:
+        f.write(DRIVER)
+    r = subprocess.run([sys.executable, 'golden_driver.py'], cwd=dst, env=env,
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('reference run failed:\n' + r.stdout[-3000:] + r.stderr[-3000:])
+    print(r.stdout.strip().splitlines()[-1])
+    return dst
+
+
+def make(tag, ref_root, workdir, full_dir=None):
+    if tag == 'c0':
+        spec = configs.config0()
+    elif tag in ('c2', 'c2long'):
+        spec = configs.config2_columns(ncols=1, seed=2)[0]
+    elif tag == 'c1':
+        net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
+                                use_photo=True)
+        spec = configs.config1(sorted(net.photo_index()))
+    else:
+        raise ValueError(tag)
+    net = Network.from_file(os.path.join(ref_root, 'thermo', spec.network),
+                            use_photo=spec.use_photo)
+    dst = run_reference(ref_root, tag, spec, NSTEPS[tag], KEEP[tag], workdir)
+    d = dict(np.load(os.path.join(dst, 'golden_out.npz'), allow_pickle=False))
+    d['atom_list'] = np.array(spec.atom_list)
+    d['conver_ignore'] = np.array(spec.conver_ignore, dtype='U16')
+    d['const_mix_sp'] = np.array(list(spec.const_mix))
+    d['const_mix_x'] = np.array(list(spec.const_mix.values()))
+    if spec.photo_J:
+        keys = sorted(spec.photo_J)
+        d['photo_sp'] = np.array([k[0] for k in keys])
+        d['photo_br'] = np.array([k[1] for k in keys])
+    out = os.path.join(HERE, 'golden_%s.npz' % tag)
+    np.savez_compressed(out, **d)
+    net.to_npz(os.path.join(HERE, 'net_%s.npz' % spec.network.replace('_network.txt', '')
+                            + ('_photo' if spec.use_photo and 'photo' not in spec.network else '')))
+    if full_dir:
+        os.makedirs(full_dir, exist_ok=True)
+        shutil.copy(os.path.join(dst, 'golden_full.npz'),
+                    os.path.join(full_dir, 'golden_full_%s.npz' % tag))
+    print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('tags', nargs='*', default=['c0', 'c1', 'c2'])
+    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--full-dir', default=None,
+                    help='also keep every recorded attempt here (not committed)')
+    a = ap.parse_args()
+    with tempfile.TemporaryDirectory() as w:
+        for t in a.tags:
+            make(t, a.ref, w, a.full_dir)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,60 @@
+"""Shared helpers: golden fixtures -> oracle inputs and GPU column batches."""
+import os
+
+import numpy as np
+
+from conftest import GOLDEN
+from oracle import ros2 as O
+from vulcan_gb300 import column as C
+from vulcan_gb300 import configs
+from vulcan_gb300.network import Network
+
+NETS = {'c0': 'net_CHO_thermo.npz', 'c1': 'net_NCHO_photo.npz', 'c2': 'net_NCHO_thermo.npz',
+        'c2long': 'net_NCHO_thermo.npz'}
+
+
+def golden(tag):
+    return dict(np.load(os.path.join(GOLDEN, 'golden_%s.npz' % tag), allow_pickle=False))
+
+
+def network(tag):
+    return Network.from_npz(os.path.join(GOLDEN, NETS[tag]))
+
+
+def oracle_net(tag, g):
+    return O.OracleNet.from_npz(os.path.join(GOLDEN, NETS[tag]), [str(a) for a in g['atom_list']])
+
+
+def base_atm(g):
+    return dict(M=g['M'], n_0=g['n_0'], Tco=g['Tco'], Kzz=g['Kzz'], vz=g['vz'], Dzz=g['Dzz'],
+                Ti=g['Ti'], ms=g['ms'], alpha=g['alpha'], pico=g['pico'], dzi=g['dzi'],
+                Hpi=g['Hpi'], g=g['g'], Hp=g['Hp'], dz=g['dz'], zco=g['zco'])
+
+
+def attempt_atm(g, n):
+    return dict(base_atm(g), dzi=g['att_dzi'][n], Hpi=g['att_Hpi'][n], g=g['att_g'][n],
+                Hp=g['att_Hp'][n])
+
+
+def column_from_golden(g, n=None):
+    """column.Column with the reference's set-up arrays (attempt n's dynamic ones)."""
+    net_ymix = g['ymix_ini']
+    col = C.Column(pco=g['pco'], Tco=g['Tco'], Kzz=g['Kzz'], vz=g['vz'], gs=configs.GS,
+                   Rp=configs.RP, rocky=False, use_moldiff=True)
+    col.pico, col.M, col.n_0 = g['pico'], g['M'], g['n_0']
+    col.g, col.Hp, col.dz, col.zco = g['g'].copy(), g['Hp'].copy(), g['dz'].copy(), g['zco'].copy()
+    col.dzi, col.Ti, col.Hpi = g['dzi'].copy(), g['Ti'], g['Hpi'].copy()
+    col.Dzz, col.ms, col.alpha = g['Dzz'], g['ms'], g['alpha']
+    col.pref_indx = int(g['pref_indx'])
+    ni = g['ms'].size
+    col.top_flux, col.bot_flux, col.bot_vdep = np.zeros(ni), np.zeros(ni), np.zeros(ni)
+    if n is not None:
+        col.dzi, col.Hpi = g['att_dzi'][n].copy(), g['att_Hpi'][n].copy()
+        col.g, col.Hp = g['att_g'][n].copy(), g['att_Hp'][n].copy()
+    del net_ymix
+    return col
+
+
+def floor_err(a, b, n0, floor=1e-10):
+    """max |a-b| / (|b| + floor * n_0): relative error with a mixing-ratio floor."""
+    return float(np.max(np.abs(a - b) / (np.abs(b) + floor * n0[:, None])))

@@ -1,0 +1,188 @@
+"""GPU Ros2 step vs the reference's recorded attempts and vs the CPU oracle.
+
+Tolerances (see tests/test_oracle.py for the reasoning):
+  per attempt  |sol_gpu - sol_ref| <= 1e-10 (|sol_ref| + 1e-10 n_0)  for dt < 1e-2 s,
+               1e-9 for the late ill-conditioned steps; delta to 1e-6 relative.
+  chemistry    bit-identical to the reference's generated chemdf.
+"""
+import types
+
+import numpy as np
+import pytest
+
+from helpers import (attempt_atm, column_from_golden, floor_err, golden, network,
+                     oracle_net)
+from oracle import ros2 as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from vulcan_gb300 import _build
+    _build.build()
+
+
+def make_handle(tag, ncols=1, ns=None, precision=0):
+    from vulcan_gb300.solver import ColumnBatch, GPUNetwork, Ros2Handle
+    g = golden(tag)
+    net = network(tag)
+    gn = GPUNetwork(net, [str(a) for a in g['atom_list']])
+    ns = ns if ns is not None else [None] * ncols
+    items = []
+    for n in ns:
+        col = column_from_golden(g, n)
+        y = g['y_ini'] if n is None else g['att_y'][n]
+        ym = g['ymix_ini'] if n is None else g['att_ymix'][n]
+        items.append(dict(col=col, k=g['k'], y=y, ymix=ym))
+    b = ColumnBatch(items, net.ni)
+    h = Ros2Handle(gn, len(items), b.L, precision)
+    h.set_columns(b)
+    return g, net, gn, h, b
+
+
+@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'])
+def test_chem_source_bit_exact(tag):
+    g, net, gn, h, b = make_handle(tag)
+    np.testing.assert_array_equal(h.chem_source(g['y_ini']), g['chemdf0'])
+
+
+@pytest.mark.parametrize('tag', ['c0', 'c2'])
+def test_lhs_matches_oracle(tag):
+    g, net, gn, h, b = make_handle(tag, ns=[0])
+    h.attempt(g['att_dt'][0])
+    jv, dA, dB, dC = h.lhs()
+    on = oracle_net(tag, g)
+    y = g['att_y'][0]
+    J = O.neg_jac_blocks(on, y, g['M'], g['k'])
+    rows, cols = gn.jac_pattern()
+    for l in (0, 1, y.shape[0] // 2, y.shape[0] - 1):
+        ref = J[l][rows, cols]
+        scale = np.abs(J[l]).max()
+        assert np.max(np.abs(jv[l] - ref)) <= 1e-14 * scale
+    A, B, C, Ai, Bi, Ci = O.diff_coeffs(y, attempt_atm(g, 0), O.Flags())
+    np.testing.assert_allclose(dA, A[:, None] + Ai, rtol=1e-13, atol=0)
+    np.testing.assert_allclose(dB[:-1], (B[:, None] + Bi)[:-1], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(dC[1:], (C[:, None] + Ci)[1:], rtol=1e-13, atol=0)
+
+
+def _cases():
+    out = []
+    for tag in ('c0', 'c1', 'c2', 'c2long'):
+        try:
+            g = golden(tag)
+        except FileNotFoundError:
+            continue
+        out += [(tag, n) for n in range(len(g['att_index']))]
+    return out
+
+
+@pytest.mark.parametrize('tag,n', _cases())
+def test_attempt_matches_reference(tag, n):
+    g, net, gn, h, b = make_handle(tag, ns=[n])
+    out = h.attempt(g['att_dt'][n], want_k=True)
+    tol = 1e-10 if g['att_dt'][n] < 1e-2 else 1e-9
+    n0 = g['n_0']
+    assert floor_err(out['sol'], g['att_sol'][n], n0) <= tol
+    yk2_ref = g['att_y'][n] + g['att_k1'][n].reshape(out['k1'].shape) / O.R_ROS
+    yk2 = g['att_y'][n] + out['k1'] / O.R_ROS
+    assert floor_err(yk2, yk2_ref, n0) <= 10 * tol
+    assert abs(out['delta'][0] / g['att_delta'][n] - 1) <= 1e-6
+    ym = out['sol'] / out['sol'].sum(axis=1, keepdims=True)
+    np.testing.assert_allclose(out['ymix'], ym, rtol=1e-14, atol=0)
+
+
+def test_batch_invariance_and_determinism():
+    """Columns in one batch give bit-identical results to single-column runs,
+    and repeated runs are bit-identical (no atomics on the FP64 path)."""
+    g = golden('c0')
+    ns = [0, 5, 13, 99]
+    _, _, _, hb, bb = make_handle('c0', ns=ns)
+    dts = np.array([g['att_dt'][n] for n in ns])
+    ob = hb.attempt(dts)
+    ob2 = hb.attempt(dts)
+    np.testing.assert_array_equal(ob['sol'], ob2['sol'])
+    sols = bb.split(ob['sol'])
+    for c, n in enumerate(ns):
+        _, _, _, h1, _ = make_handle('c0', ns=[n])
+        o1 = h1.attempt(g['att_dt'][n])
+        np.testing.assert_array_equal(sols[c], o1['sol'])
+        assert ob['delta'][c] == o1['delta'][0]
+
+
+def test_singular_block_reports_status():
+    """A zero diagonal block is reported as VK_ESINGULAR (host-visible status)."""
+    from vulcan_gb300 import capi
+    g, net, gn, h, b = make_handle('c0', ns=[0])
+    b.k[:] = 0.0
+    b.atm[:, capi.ATM_KZZ] = 0.0
+    b.Dzz[:] = 0.0
+    b.atm[:, capi.ATM_VZ] = 0.0
+    h.set_columns(b)
+    with pytest.raises(capi.VkError) as e:
+        h.attempt(1e300, flags=0)
+    assert e.value.code == capi.VK_ESINGULAR
+
+
+def test_dropin_solver_contract():
+    """Ros2GPU.solver reads var/atm like op.Ros2.solver and writes var.y,
+    var.ymix and para.delta (a stand-in op module; the reference itself is
+    not needed on the GPU machine)."""
+    from vulcan_gb300.solver import make_ros2gpu
+    g = golden('c0')
+    net = network('c0')
+    n = 3
+
+    class FakeRos2:
+        pass
+
+    op = types.SimpleNamespace(Ros2=FakeRos2)
+    cfg = types.SimpleNamespace(network=None, use_photo=False, atom_list=list(g['atom_list']),
+                                use_moldiff=True, use_topflux=False, use_botflux=False)
+    cls = make_ros2gpu(op, cfg, net.species)
+    cls._vk_net_cls = types.SimpleNamespace(from_file=lambda path, use_photo: net)
+    s = cls()
+    var = types.SimpleNamespace(y=g['att_y'][n].copy(), ymix=g['att_ymix'][n].copy(),
+                                dt=float(g['att_dt'][n]),
+                                k={i: g['k'][i - 1] for i in range(1, net.nr + 1)})
+    col = column_from_golden(g, n)
+    atm = types.SimpleNamespace(**{k: getattr(col, k) for k in (
+        'M', 'n_0', 'Tco', 'g', 'dzi', 'Kzz', 'vz', 'Ti', 'Hpi', 'Hp', 'pico', 'dz', 'Dzz',
+        'ms', 'alpha', 'top_flux', 'bot_flux', 'bot_vdep', 'pref_indx')})
+    para = types.SimpleNamespace(delta=0.0)
+    var, para = s.solver(var, atm, para)
+    assert floor_err(var.y, g['att_sol'][n], g['n_0']) <= 1e-10
+    assert abs(para.delta / g['att_delta'][n] - 1) <= 1e-6
+
+
+def test_device_run_tracks_reference_trajectory():
+    """vk_run (device accept/reject, step size, update_mu_dz, renormalisation)
+    from the reference's initial state reproduces its first 100 steps."""
+    from vulcan_gb300 import configs
+    from vulcan_gb300.solver import ctrl_from
+    g, net, gn, h, b = make_handle('c0')
+    h.set_atom_ini(g['atom_ini'][None, :])
+    h.set_clock(dt=1e-10, t=0.0, count=0)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    h.run(ctrl, max_steps=100, timeout_s=600)
+    st = h.state()
+    cnt = h.counters()
+    assert st['count'][0] == 100
+    assert cnt[0, 0] == g['traj_natt'][99]
+    np.testing.assert_allclose(st['t'][0], g['traj_t'][99], rtol=1e-9)
+    np.testing.assert_allclose(st['dt'][0], g['traj_dt_next'][99], rtol=1e-8)
+    y100 = g['ystep_y'][list(g['ystep_index']).index(99)]
+    assert floor_err(st['y'], y100, g['n_0']) <= 1e-8
+
+
+def test_run_watchdog_returns_timeout():
+    from vulcan_gb300 import capi, configs
+    from vulcan_gb300.solver import ctrl_from
+    g, net, gn, h, b = make_handle('c0')
+    h.set_atom_ini(g['atom_ini'][None, :])
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    with pytest.raises(capi.VkError) as e:
+        h.run(ctrl, max_steps=1000, timeout_s=1e-9)
+    assert e.value.code == capi.VK_ETIMEOUT
+    st = h.state()                    # the handle stays usable
+    assert np.isfinite(st['y']).all()

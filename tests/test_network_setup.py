@@ -1,0 +1,88 @@
+"""Network compiler, rate constants and column set-up vs the reference's own values."""
+import numpy as np
+import pytest
+
+from helpers import column_from_golden, golden, network
+from vulcan_gb300 import column as C
+from vulcan_gb300 import configs
+
+
+@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'])
+def test_species_order_and_nr(tag):
+    g = golden(tag)
+    net = network(tag)
+    assert net.species == [str(s) for s in g['spec_list']]
+    assert net.nr == int(g['nr'])
+
+
+@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'])
+def test_rate_constants_bit_exact(tag):
+    """k (forward Arrhenius / fall-off / special, reverse via NASA-9 Gibbs)."""
+    g = golden(tag)
+    net = network(tag)
+    k = net.rate_constants(g['Tco'], g['M'])
+    if 'photo_sp' in g:
+        pidx = net.photo_index()
+        for sp, br in zip(g['photo_sp'], g['photo_br']):
+            i = pidx[(str(sp), int(br))]
+            assert np.all(k[i - 1] == 0)           # placeholder before J is injected
+            k[i - 1] = g['k'][i - 1]
+    np.testing.assert_array_equal(k, g['k'])
+
+
+@pytest.mark.parametrize('tag', ['c0', 'c2'])
+def test_column_setup_bit_exact(tag):
+    g = golden(tag)
+    net = network(tag)
+    col = C.build_column(net, g['pco'], g['Tco'], g['Kzz'], gs=configs.GS, Rp=configs.RP,
+                         ymix0=g['ymix_ini'])
+    assert col.pref_indx == int(g['pref_indx'])
+    for key in ('pico', 'M', 'n_0', 'mu', 'g', 'Hp', 'dz', 'dzi', 'Ti', 'Hpi', 'Dzz', 'ms', 'alpha'):
+        np.testing.assert_array_equal(getattr(col, key), g[key], err_msg=key)
+
+
+def test_initial_state_and_atoms():
+    g = golden('c0')
+    net = network('c0')
+    mix = dict(zip([str(s) for s in g['const_mix_sp']], g['const_mix_x']))
+    y, ymix = C.const_mix_state(net, g['n_0'], mix)
+    np.testing.assert_array_equal(y, g['y_ini'])
+    np.testing.assert_allclose(ymix, g['ymix_ini'], rtol=1e-15, atol=0)
+    at = C.atom_totals(net, y, [str(a) for a in g['atom_list']])
+    np.testing.assert_allclose(at, g['atom_ini'], rtol=1e-14)
+
+
+def test_config_generators_match_fixture_inputs():
+    g = golden('c0')
+    spec = configs.config0()
+    np.testing.assert_array_equal(spec.Tco, g['Tco'])
+    np.testing.assert_array_equal(spec.Kzz, g['Kzz'])
+
+
+def test_pair_tables():
+    net = network('c0')
+    t = net.pair_tables()
+    assert t['fwd_ptr'].size == net.npair + 1
+    # 'H + H + M -> H2 + M' merges to H^2 with one M on each side
+    p = [r.text for r in net.reactions].index('H + H + M -> H2 + M')
+    h = net.species.index('H')
+    f0, f1 = t['fwd_ptr'][p], t['fwd_ptr'][p + 1]
+    assert list(t['fwd_sp'][f0:f1]) == [h] and list(t['fwd_nu'][f0:f1]) == [2]
+    assert t['fwd_m'][p] == 1 and t['rev_m'][p] == 1
+
+
+def test_network_roundtrip(tmp_path):
+    net = network('c1')
+    path = tmp_path / 'n.npz'
+    net.to_npz(path)
+    n2 = type(net).from_npz(path)
+    assert n2.species == net.species
+    assert [r.text for r in n2.reactions] == [r.text for r in net.reactions]
+    T = np.linspace(500, 3000, 7)
+    np.testing.assert_array_equal(n2.rate_constants(T, T * 1e15), net.rate_constants(T, T * 1e15))
+
+
+def test_column_helper_consistent():
+    g = golden('c0')
+    col = column_from_golden(g)
+    assert col.nz == g['pco'].size

@@ -1,0 +1,123 @@
+"""ctypes binding of libvk_gb300.so (declared in include/vk_ros2.h).
+
+The library is built in-tree by ``vulcan_gb300._build.build()``.  Loading
+fails loudly when it is missing: there is no CPU fallback for the step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._build import LIB
+
+VK_OK, VK_EINVAL, VK_ECUDA, VK_ESINGULAR, VK_ENAN, VK_EMAXATTEMPT, VK_ETIMEOUT, VK_ENOMEM = range(8)
+VK_PREC_FP64, VK_PREC_MIXED = 0, 1
+VK_F_MOLDIFF, VK_F_TOPFLUX, VK_F_BOTFLUX = 1, 2, 4
+(ATM_M, ATM_N0, ATM_TCO, ATM_G, ATM_DZI, ATM_KZZ, ATM_VZ, ATM_TI, ATM_HPI, ATM_HP,
+ ATM_PICO, ATM_PICOU, ATM_DZ) = range(13)
+ATM_NF = 13
+SP_MS, SP_ALPHA, SP_TOPFLUX, SP_BOTFLUX, SP_BOTVDEP = range(5)
+SP_NF = 5
+MAX_NATOM = 16
+
+_ERRNAMES = {1: 'VK_EINVAL', 2: 'VK_ECUDA', 3: 'VK_ESINGULAR', 4: 'VK_ENAN',
+             5: 'VK_EMAXATTEMPT', 6: 'VK_ETIMEOUT', 7: 'VK_ENOMEM'}
+
+# Every entry point include/vk_ros2.h declares.
+EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
+           'vk_network_free', 'vk_create', 'vk_destroy', 'vk_last_error',
+           'vk_set_precision', 'vk_set_columns', 'vk_update_state', 'vk_update_atm',
+           'vk_update_k', 'vk_ros2_attempt', 'vk_set_atom_ini', 'vk_set_column_info',
+           'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
+           'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs')
+
+
+class VkNetworkDesc(C.Structure):
+    _fields_ = [('ni', C.c_int), ('npair', C.c_int),
+                ('reac_ptr', C.POINTER(C.c_int)), ('reac_sp', C.POINTER(C.c_int)),
+                ('reac_nu', C.POINTER(C.c_int)),
+                ('prod_ptr', C.POINTER(C.c_int)), ('prod_sp', C.POINTER(C.c_int)),
+                ('prod_nu', C.POINTER(C.c_int)),
+                ('natom', C.c_int), ('compo', C.POINTER(C.c_double))]
+
+
+class VkCtrl(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        'rtol', 'atol', 'mtol', 'mtol_conv', 'pos_cut', 'nega_cut', 'loss_eps',
+        'dt_min', 'dt_max', 'dt_var_min', 'dt_var_max',
+        'yconv_cri', 'slope_cri', 'yconv_min', 'st_factor', 'trun_min', 'runtime')] + \
+        [(n, C.c_int) for n in ('conv_step', 'count_min', 'count_max', 'update_frq',
+                                'max_attempts', 'flags')] + \
+        [('gs', C.c_double), ('Rp', C.c_double)]
+
+
+class VkError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__('%s: %s' % (_ERRNAMES.get(code, str(code)), msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib(path=None):
+    """Load libvk_gb300.so once (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or os.environ.get('VK_GB300_LIB', LIB)
+    if not os.path.exists(path):
+        raise RuntimeError('libvk_gb300.so not found at %s: build it with '
+                           'vulcan_gb300._build.build() (there is no CPU fallback)' % path)
+    L = C.CDLL(path)
+    P = C.POINTER
+    d, i, vp = C.c_double, C.c_int, C.c_void_p
+    pd, pi = P(d), P(i)
+    sig = {
+        'vk_network_compile': (i, [P(VkNetworkDesc), P(vp)]),
+        'vk_network_info': (i, [vp, pi, pi, pi]),
+        'vk_network_jac_pattern': (i, [vp, pi, pi]),
+        'vk_network_free': (None, [vp]),
+        'vk_network_last_error': (C.c_char_p, []),
+        'vk_create': (i, [vp, i, i, i, P(vp)]),
+        'vk_destroy': (None, [vp]),
+        'vk_last_error': (C.c_char_p, [vp]),
+        'vk_set_precision': (i, [vp, i, i, d]),
+        'vk_set_columns': (i, [vp, i, pi, pd, pd, pd, pd, pd, pd]),
+        'vk_update_state': (i, [vp, pd, pd]),
+        'vk_update_atm': (i, [vp, pd]),
+        'vk_update_k': (i, [vp, pd]),
+        'vk_ros2_attempt': (i, [vp, pd, i, pd, pd, pd, pd, pd]),
+        'vk_set_atom_ini': (i, [vp, pd]),
+        'vk_set_column_info': (i, [vp, pi, pi]),
+        'vk_run': (i, [vp, P(VkCtrl), i, d]),
+        'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
+        'vk_set_clock': (i, [vp, pd, pd, pi]),
+        'vk_get_counters': (i, [vp, pi]),
+        'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
+        'vk_chem_source': (i, [vp, pd, pd]),
+        'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def ptr(a, ctype=C.c_double):
+    """Pointer to a C-contiguous numpy array (or NULL for None)."""
+    if a is None:
+        return None
+    assert a.flags['C_CONTIGUOUS'], 'array must be C-contiguous'
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def check(rc, handle=None):
+    if rc != VK_OK:
+        L = lib()
+        msg = L.vk_last_error(handle)
+        raise VkError(rc, msg.decode() if msg else '')

@@ -1,0 +1,558 @@
+// C ABI: handle life cycle, uploads and the Ros2 attempt pipeline.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <chrono>
+#include <climits>
+
+#include "vk_control.cuh"
+#include "vk_internal.cuh"
+
+namespace vk {
+void launch_chem_only(const DevNet &net, const DevBatch &b, const double *y, double *f,
+                      cudaStream_t s);
+cudaError_t init_kernels(const DevNet &net);
+}
+
+struct vk_handle {
+    std::string err;
+    int ni = 0, npair = 0, nr = 0, nnz = 0, nw = 0, natom = 0;
+    int max_cols = 0, max_layers = 0, precision = VK_PREC_FP64;
+    int max_refine = 3;
+    double refine_tol = 1e-13;
+    int ncols = 0, L = 0;
+    std::vector<int> col_off;
+    // network tables
+    PairDesc *d_pairs = nullptr;
+    int *d_src_ptr = nullptr;
+    int2 *d_src = nullptr;
+    WDesc *d_w = nullptr;
+    int *d_jptr = nullptr;
+    int2 *d_jterm = nullptr;
+    int *d_jpos = nullptr;
+    double *d_compo = nullptr;
+    // batch
+    int *d_col_off = nullptr, *d_lay_col = nullptr;
+    double *d_k = nullptr, *d_atm = nullptr, *d_Dzz = nullptr, *d_spf = nullptr;
+    vk::Work w{};
+    // batched-run state
+    vk::RunState rs{};
+    int rs_ready = 0;           // run-state buffers allocated
+    int hist_R = 0;             // ring length the history was sized for
+    int *d_nactive = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned char gkey[sizeof(vk::RunCtrl) + 2 * sizeof(int)] = {};
+    std::vector<void *> allocs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    float ms[4] = {0, 0, 0, 0};
+    int launches = 0;
+
+    DevNet net() const {
+        DevNet n;
+        n.ni = ni; n.npair = npair; n.nr = nr; n.nw = nw; n.nnz = nnz; n.natom = natom;
+        n.pairs = d_pairs; n.src_ptr = d_src_ptr; n.src = d_src; n.w = d_w;
+        n.jptr = d_jptr; n.jterm = d_jterm; n.jpos = d_jpos; n.compo = d_compo;
+        return n;
+    }
+    DevBatch batch() const {
+        DevBatch b;
+        b.ncols = ncols; b.L = L; b.col_off = d_col_off; b.lay_col = d_lay_col;
+        b.k = d_k; b.atm = d_atm; b.Dzz = d_Dzz; b.spf = d_spf;
+        b.active = nullptr;
+        return b;
+    }
+};
+
+static thread_local std::string g_err;
+
+static int fail(vk_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg; else g_err = msg;
+    return code;
+}
+
+#define VK_CUDA(h, call)                                                              \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail((h), VK_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+static int dalloc(vk_handle *h, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, VK_ENOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
+                                      " bytes: " + cudaGetErrorString(e));
+    }
+    h->allocs.push_back((void *)*p);
+    return VK_OK;
+}
+
+template <typename T>
+static int upload(vk_handle *h, T **p, const std::vector<T> &v) {
+    int rc = dalloc(h, p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) VK_CUDA(h, cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" const char *vk_last_error(const vk_handle *h) {
+    return h ? h->err.c_str() : g_err.c_str();
+}
+
+extern "C" void vk_destroy(vk_handle *h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->rs.hist_y) cudaFree(h->rs.hist_y);
+    if (h->rs.hist_t) cudaFree(h->rs.hist_t);
+    for (void *p : h->allocs) cudaFree(p);
+    for (auto &e : h->ev) if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, int precision,
+                         vk_handle **out) {
+    if (!out) return fail(nullptr, VK_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (!net) return fail(nullptr, VK_EINVAL, "network is NULL");
+    if (max_cols <= 0 || max_layers < 2 * max_cols)
+        return fail(nullptr, VK_EINVAL, "need max_cols > 0 and max_layers >= 2*max_cols");
+    if (precision != VK_PREC_FP64 && precision != VK_PREC_MIXED)
+        return fail(nullptr, VK_EINVAL, "unknown precision mode");
+    vk_handle *h = new (std::nothrow) vk_handle();
+    if (!h) return fail(nullptr, VK_ENOMEM, "host allocation failed");
+    h->ni = net->ni; h->npair = net->npair; h->nr = 2 * net->npair;
+    h->nnz = (int)net->jpos.size(); h->nw = (int)net->w.size(); h->natom = net->natom;
+    h->max_cols = max_cols; h->max_layers = max_layers; h->precision = precision;
+    int rc = VK_OK;
+#define TRY(x) do { rc = (x); if (rc) { g_err = h->err; vk_destroy(h); return rc; } } while (0)
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            g_err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+            delete h;
+            return VK_ECUDA;
+        }
+    }
+    for (auto &e : h->ev) TRY(cudaEventCreate(&e) == cudaSuccess ? VK_OK : fail(h, VK_ECUDA, "cudaEventCreate"));
+    TRY(upload(h, &h->d_pairs, net->pairs));
+    TRY(upload(h, &h->d_src_ptr, net->src_ptr));
+    TRY(upload(h, &h->d_src, net->src));
+    TRY(upload(h, &h->d_w, net->w));
+    TRY(upload(h, &h->d_jptr, net->jptr));
+    TRY(upload(h, &h->d_jterm, net->jterm));
+    TRY(upload(h, &h->d_jpos, net->jpos));
+    TRY(upload(h, &h->d_compo, net->compo));
+    const size_t L = (size_t)max_layers, ni = (size_t)h->ni;
+    TRY(dalloc(h, &h->d_col_off, max_cols + 1));
+    TRY(dalloc(h, &h->d_lay_col, L));
+    TRY(dalloc(h, &h->d_k, L * h->nr));
+    TRY(dalloc(h, &h->d_atm, L * VK_ATM_NF));
+    TRY(dalloc(h, &h->d_Dzz, L * ni));
+    TRY(dalloc(h, &h->d_spf, (size_t)max_cols * VK_SP_NF * ni));
+    vk::Work &w = h->w;
+    double **vecs[] = {&w.y, &w.ymix, &w.yk2, &w.f, &w.k1, &w.k2, &w.z, &w.sol, &w.ymix_out,
+                       &w.dA, &w.dB, &w.dC, &w.r, &w.dx, &w.rs, &w.cs};
+    for (double **p : vecs) TRY(dalloc(h, p, L * ni));
+    TRY(dalloc(h, &w.jv, L * (size_t)std::max(h->nnz, 1)));
+    if (precision == VK_PREC_FP64) TRY(dalloc(h, &w.G, L * ni * ni));
+    else TRY(dalloc(h, &w.G32, L * ni * ni));
+    TRY(dalloc(h, &w.dt, max_cols));
+    TRY(dalloc(h, &w.delta, max_cols));
+    TRY(dalloc(h, &w.status, max_cols));
+    TRY(vk::init_kernels(h->net()) == cudaSuccess ? VK_OK
+                                                  : fail(h, VK_ECUDA, "cudaFuncSetAttribute failed"));
+    // per-column run state (small); the history ring is sized at the first vk_run
+    vk::RunState &r = h->rs;
+    r.y = w.y; r.ymix = w.ymix; r.dt = w.dt; r.delta = w.delta; r.atm = h->d_atm;
+    TRY(dalloc(h, &r.y_prev, L * ni));
+    double **cd[] = {&r.t, &r.longdy, &r.longdydt};
+    for (double **p : cd) TRY(dalloc(h, p, max_cols));
+    int **ci[] = {&r.count, &r.end_case, &r.active, &r.natt, &r.steps_call, &r.pref};
+    for (int **p : ci) TRY(dalloc(h, p, max_cols));
+    TRY(dalloc(h, &r.counters, (size_t)max_cols * 4));
+    TRY(dalloc(h, &r.atom_ini, (size_t)max_cols * VK_MAX_NATOM));
+    TRY(dalloc(h, &r.loss, (size_t)max_cols * VK_MAX_NATOM));
+    TRY(dalloc(h, &r.loss_prev, (size_t)max_cols * VK_MAX_NATOM));
+    TRY(dalloc(h, &r.ignore, ni));
+    TRY(dalloc(h, &h->d_nactive, 1));
+    TRY(cudaMemset(r.ignore, 0, ni * sizeof(int)) == cudaSuccess ? VK_OK : fail(h, VK_ECUDA, "memset"));
+#undef TRY
+    *out = h;
+    return VK_OK;
+}
+
+extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol) {
+    if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
+    if (precision == VK_PREC_FP64 && !h->w.G) {
+        int rc = dalloc(h, &h->w.G, (size_t)h->max_layers * h->ni * h->ni);
+        if (rc) return rc;
+    }
+    if (precision == VK_PREC_MIXED && !h->w.G32) {
+        int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * h->ni * h->ni);
+        if (rc) return rc;
+    }
+    if (precision != VK_PREC_FP64 && precision != VK_PREC_MIXED)
+        return fail(h, VK_EINVAL, "unknown precision mode");
+    if (max_refine < 0 || max_refine > 20) return fail(h, VK_EINVAL, "max_refine out of range");
+    h->precision = precision;
+    h->max_refine = max_refine;
+    h->refine_tol = refine_tol;
+    return VK_OK;
+}
+
+extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const double *k,
+                              const double *atm, const double *Dzz, const double *spf,
+                              const double *y, const double *ymix) {
+    if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
+    if (ncols <= 0 || ncols > h->max_cols)
+        return fail(h, VK_EINVAL, "ncols must be in 1.." + std::to_string(h->max_cols));
+    if (!nz || !k || !atm || !Dzz || !spf || !y || !ymix)
+        return fail(h, VK_EINVAL, "NULL input array");
+    std::vector<int> off(ncols + 1, 0);
+    for (int c = 0; c < ncols; ++c) {
+        if (nz[c] < 2 || nz[c] > 1024) return fail(h, VK_EINVAL, "every column needs 2 <= nz <= 1024");
+        off[c + 1] = off[c] + nz[c];
+        if (off[c + 1] > h->max_layers)
+            return fail(h, VK_EINVAL, "total layers exceed max_layers=" + std::to_string(h->max_layers));
+    }
+    const int L = off[ncols];
+    std::vector<int> lay_col(L);
+    for (int c = 0; c < ncols; ++c)
+        for (int l = off[c]; l < off[c + 1]; ++l) lay_col[l] = c;
+    const size_t ni = h->ni;
+    cudaStream_t s = h->stream;
+    VK_CUDA(h, cudaMemcpyAsync(h->d_col_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->d_lay_col, lay_col.data(), L * sizeof(int), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->d_k, k, (size_t)L * h->nr * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->d_atm, atm, (size_t)L * VK_ATM_NF * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->d_Dzz, Dzz, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->d_spf, spf, (size_t)ncols * VK_SP_NF * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->w.y, y, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemcpyAsync(h->w.ymix, ymix, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, ncols * sizeof(int), s));
+    {
+        vk::RunState &r = h->rs;
+        VK_CUDA(h, cudaMemsetAsync(r.t, 0, ncols * sizeof(double), s));
+        VK_CUDA(h, cudaMemsetAsync(r.count, 0, ncols * sizeof(int), s));
+        VK_CUDA(h, cudaMemsetAsync(r.end_case, 0, ncols * sizeof(int), s));
+        VK_CUDA(h, cudaMemsetAsync(r.counters, 0, ncols * 4 * sizeof(int), s));
+        VK_CUDA(h, cudaMemsetAsync(r.pref, 0, ncols * sizeof(int), s));
+        VK_CUDA(h, cudaMemsetAsync(r.loss, 0, ncols * VK_MAX_NATOM * sizeof(double), s));
+        std::vector<double> dt0(ncols, 1e-10);
+        VK_CUDA(h, cudaMemcpyAsync(h->w.dt, dt0.data(), ncols * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    VK_CUDA(h, cudaStreamSynchronize(s));
+    if (h->gexec && (h->ncols != ncols || h->L != off[ncols])) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    h->ncols = ncols;
+    h->L = L;
+    h->col_off = off;
+    return VK_OK;
+}
+
+static int need_batch(vk_handle *h) {
+    if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
+    if (h->ncols == 0) return fail(h, VK_EINVAL, "no columns loaded (call vk_set_columns)");
+    return VK_OK;
+}
+
+extern "C" int vk_update_state(vk_handle *h, const double *y, const double *ymix) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    size_t bytes = (size_t)h->L * h->ni * sizeof(double);
+    if (y) VK_CUDA(h, cudaMemcpyAsync(h->w.y, y, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (ymix) VK_CUDA(h, cudaMemcpyAsync(h->w.ymix, ymix, bytes, cudaMemcpyHostToDevice, h->stream));
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
+extern "C" int vk_update_atm(vk_handle *h, const double *atm) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!atm) return fail(h, VK_EINVAL, "atm is NULL");
+    VK_CUDA(h, cudaMemcpyAsync(h->d_atm, atm, (size_t)h->L * VK_ATM_NF * sizeof(double),
+                               cudaMemcpyHostToDevice, h->stream));
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
+extern "C" int vk_update_k(vk_handle *h, const double *k) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!k) return fail(h, VK_EINVAL, "k is NULL");
+    VK_CUDA(h, cudaMemcpyAsync(h->d_k, k, (size_t)h->L * h->nr * sizeof(double),
+                               cudaMemcpyHostToDevice, h->stream));
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
+// Enqueue one Ros2 attempt for every loaded column (device state in, w.sol /
+// w.ymix_out / w.delta out).
+static int enqueue_attempt(vk_handle *h, int flags, bool timed) {
+    const DevNet net = h->net();
+    const DevBatch b = h->batch();
+    vk::Work &w = h->w;
+    cudaStream_t s = h->stream;
+    if (h->precision != VK_PREC_FP64 || !w.G)
+        return fail(h, VK_EINVAL, "mixed-precision attempt not available on this handle");
+    if (timed) cudaEventRecord(h->ev[0], s);
+    vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, flags, true, s);
+    if (timed) cudaEventRecord(h->ev[1], s);
+    vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, flags, s);
+    if (timed) cudaEventRecord(h->ev[2], s);
+    vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
+    vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, flags, false, s);
+    vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+    if (timed) cudaEventRecord(h->ev[3], s);
+    vk::launch_stage(net, b, w, flags, 1.E-22, 1.E-1, s);
+    if (timed) cudaEventRecord(h->ev[4], s);
+    h->launches += 6;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(h, VK_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return VK_OK;
+}
+
+extern "C" int vk_ros2_attempt(vk_handle *h, const double *dt, int flags, double *sol,
+                               double *ymix, double *delta, double *k1, double *k2) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!dt) return fail(h, VK_EINVAL, "dt is NULL");
+    for (int c = 0; c < h->ncols; ++c)
+        if (!(dt[c] > 0.0)) return fail(h, VK_EINVAL, "dt must be positive");
+    cudaStream_t s = h->stream;
+    VK_CUDA(h, cudaMemcpyAsync(h->w.dt, dt, h->ncols * sizeof(double), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, h->ncols * sizeof(int), s));
+    h->launches = 0;
+    rc = enqueue_attempt(h, flags, true);
+    if (rc) return rc;
+    size_t bytes = (size_t)h->L * h->ni * sizeof(double);
+    if (sol) VK_CUDA(h, cudaMemcpyAsync(sol, h->w.sol, bytes, cudaMemcpyDeviceToHost, s));
+    if (ymix) VK_CUDA(h, cudaMemcpyAsync(ymix, h->w.ymix_out, bytes, cudaMemcpyDeviceToHost, s));
+    if (k1) VK_CUDA(h, cudaMemcpyAsync(k1, h->w.k1, bytes, cudaMemcpyDeviceToHost, s));
+    if (k2) VK_CUDA(h, cudaMemcpyAsync(k2, h->w.k2, bytes, cudaMemcpyDeviceToHost, s));
+    if (delta) VK_CUDA(h, cudaMemcpyAsync(delta, h->w.delta, h->ncols * sizeof(double), cudaMemcpyDeviceToHost, s));
+    std::vector<int> st(h->ncols);
+    VK_CUDA(h, cudaMemcpyAsync(st.data(), h->w.status, h->ncols * sizeof(int), cudaMemcpyDeviceToHost, s));
+    VK_CUDA(h, cudaStreamSynchronize(s));
+    cudaEventElapsedTime(&h->ms[0], h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&h->ms[1], h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&h->ms[2], h->ev[2], h->ev[3]);
+    cudaEventElapsedTime(&h->ms[3], h->ev[3], h->ev[4]);
+    for (int c = 0; c < h->ncols; ++c)
+        if (st[c] == VK_ESINGULAR)
+            return fail(h, VK_ESINGULAR, "singular diagonal block in column " + std::to_string(c));
+    return VK_OK;
+}
+
+// Test hook: chemistry source term only (the generated chemdf) of the state y.
+extern "C" int vk_chem_source(vk_handle *h, const double *y, double *dydt) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    size_t bytes = (size_t)h->L * h->ni * sizeof(double);
+    if (y) VK_CUDA(h, cudaMemcpyAsync(h->w.y, y, bytes, cudaMemcpyHostToDevice, h->stream));
+    vk::launch_chem_only(h->net(), h->batch(), h->w.y, h->w.f, h->stream);
+    VK_CUDA(h, cudaGetLastError());
+    VK_CUDA(h, cudaMemcpyAsync(dydt, h->w.f, bytes, cudaMemcpyDeviceToHost, h->stream));
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
+// Test hook: the LHS pieces of the last attempt (-J entries, diffusion coefficients).
+extern "C" int vk_get_lhs(vk_handle *h, double *jv, double *dA, double *dB, double *dC) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    size_t nb = (size_t)h->L * h->ni * sizeof(double);
+    if (jv) VK_CUDA(h, cudaMemcpy(jv, h->w.jv, (size_t)h->L * h->nnz * sizeof(double), cudaMemcpyDeviceToHost));
+    if (dA) VK_CUDA(h, cudaMemcpy(dA, h->w.dA, nb, cudaMemcpyDeviceToHost));
+    if (dB) VK_CUDA(h, cudaMemcpy(dB, h->w.dB, nb, cudaMemcpyDeviceToHost));
+    if (dC) VK_CUDA(h, cudaMemcpy(dC, h->w.dC, nb, cudaMemcpyDeviceToHost));
+    return VK_OK;
+}
+
+extern "C" int vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double *ms_solve,
+                             double *ms_stage, int *launches) {
+    if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
+    if (ms_rates) *ms_rates = h->ms[0];
+    if (ms_lu) *ms_lu = h->ms[1];
+    if (ms_solve) *ms_solve = h->ms[2];
+    if (ms_stage) *ms_stage = h->ms[3];
+    if (launches) *launches = h->launches;
+    return VK_OK;
+}
+
+extern "C" int vk_set_atom_ini(vk_handle *h, const double *atom_ini) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!atom_ini) return fail(h, VK_EINVAL, "atom_ini is NULL");
+    std::vector<double> buf((size_t)h->ncols * VK_MAX_NATOM, 0.0);
+    for (int c = 0; c < h->ncols; ++c)
+        for (int a = 0; a < h->natom; ++a) buf[(size_t)c * VK_MAX_NATOM + a] = atom_ini[(size_t)c * h->natom + a];
+    VK_CUDA(h, cudaMemcpy(h->rs.atom_ini, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" int vk_set_column_info(vk_handle *h, const int *pref_indx, const int *conv_ignore) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (pref_indx) {
+        for (int c = 0; c < h->ncols; ++c)
+            if (pref_indx[c] < 0 || pref_indx[c] >= h->col_off[c + 1] - h->col_off[c])
+                return fail(h, VK_EINVAL, "pref_indx outside the column");
+        VK_CUDA(h, cudaMemcpy(h->rs.pref, pref_indx, h->ncols * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    if (conv_ignore)
+        VK_CUDA(h, cudaMemcpy(h->rs.ignore, conv_ignore, h->ni * sizeof(int), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" int vk_set_clock(vk_handle *h, const double *dt, const double *t, const int *count) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (dt) VK_CUDA(h, cudaMemcpy(h->w.dt, dt, h->ncols * sizeof(double), cudaMemcpyHostToDevice));
+    if (t) VK_CUDA(h, cudaMemcpy(h->rs.t, t, h->ncols * sizeof(double), cudaMemcpyHostToDevice));
+    if (count) VK_CUDA(h, cudaMemcpy(h->rs.count, count, h->ncols * sizeof(int), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" int vk_get_state(vk_handle *h, double *y, double *ymix, double *dt, double *t,
+                            int *count, int *end_case, double *delta) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    size_t nb = (size_t)h->L * h->ni * sizeof(double);
+    cudaStream_t s = h->stream;
+    if (y) VK_CUDA(h, cudaMemcpyAsync(y, h->w.y, nb, cudaMemcpyDeviceToHost, s));
+    if (ymix) VK_CUDA(h, cudaMemcpyAsync(ymix, h->w.ymix, nb, cudaMemcpyDeviceToHost, s));
+    if (dt) VK_CUDA(h, cudaMemcpyAsync(dt, h->w.dt, h->ncols * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (t) VK_CUDA(h, cudaMemcpyAsync(t, h->rs.t, h->ncols * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (count) VK_CUDA(h, cudaMemcpyAsync(count, h->rs.count, h->ncols * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (end_case) VK_CUDA(h, cudaMemcpyAsync(end_case, h->rs.end_case, h->ncols * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (delta) VK_CUDA(h, cudaMemcpyAsync(delta, h->w.delta, h->ncols * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VK_CUDA(h, cudaStreamSynchronize(s));
+    return VK_OK;
+}
+
+extern "C" int vk_get_counters(vk_handle *h, int *counters) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!counters) return fail(h, VK_EINVAL, "counters is NULL");
+    VK_CUDA(h, cudaMemcpy(counters, h->rs.counters, (size_t)h->ncols * 4 * sizeof(int), cudaMemcpyDeviceToHost));
+    return VK_OK;
+}
+
+static vk::RunCtrl to_run_ctrl(const vk_ctrl *c, int max_steps) {
+    vk::RunCtrl r;
+    std::memset(&r, 0, sizeof(r));
+    r.rtol = c->rtol; r.atol = c->atol; r.mtol = c->mtol; r.mtol_conv = c->mtol_conv;
+    r.pos_cut = c->pos_cut; r.nega_cut = c->nega_cut; r.loss_eps = c->loss_eps;
+    r.dt_min = c->dt_min; r.dt_max = c->dt_max; r.dt_var_min = c->dt_var_min; r.dt_var_max = c->dt_var_max;
+    r.yconv_cri = c->yconv_cri; r.slope_cri = c->slope_cri; r.yconv_min = c->yconv_min;
+    r.st_factor = c->st_factor; r.trun_min = c->trun_min; r.runtime = c->runtime;
+    r.gs = c->gs; r.Rp = c->Rp;
+    r.conv_step = c->conv_step; r.count_min = c->count_min; r.count_max = c->count_max;
+    r.update_frq = c->update_frq; r.max_attempts = c->max_attempts; r.flags = c->flags;
+    r.max_steps = max_steps > 0 ? max_steps : INT_MAX;
+    return r;
+}
+
+static const int kGraphAttempts = 8;
+
+extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!ctrl) return fail(h, VK_EINVAL, "ctrl is NULL");
+    if (ctrl->conv_step < 2 || ctrl->update_frq < 1 || ctrl->max_attempts < 1 || ctrl->rtol <= 0)
+        return fail(h, VK_EINVAL, "bad control values");
+    vk::RunCtrl cc = to_run_ctrl(ctrl, max_steps);
+    cudaStream_t s = h->stream;
+    // history ring: conv_step accepted states of the whole batch
+    if (h->hist_R != cc.conv_step || !h->rs.hist_y) {
+        if (h->rs.hist_y) { cudaFree(h->rs.hist_y); cudaFree(h->rs.hist_t); }
+        h->rs.hist_y = nullptr; h->rs.hist_t = nullptr;
+        cudaError_t e1 = cudaMalloc(&h->rs.hist_y, (size_t)cc.conv_step * h->max_layers * h->ni * sizeof(double));
+        cudaError_t e2 = cudaMalloc(&h->rs.hist_t, (size_t)cc.conv_step * h->max_cols * sizeof(double));
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            if (h->rs.hist_y) cudaFree(h->rs.hist_y);
+            if (h->rs.hist_t) cudaFree(h->rs.hist_t);
+            h->rs.hist_y = nullptr; h->rs.hist_t = nullptr; h->hist_R = 0;
+            return fail(h, VK_ENOMEM, "history ring allocation failed");
+        }
+        h->hist_R = cc.conv_step;
+        if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+    }
+    if (h->precision != VK_PREC_FP64 || !h->w.G)
+        return fail(h, VK_EINVAL, "vk_run needs the FP64 solver on this handle");
+    DevNet net = h->net();
+    DevBatch b = h->batch();
+    b.active = h->rs.active;
+    VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, h->ncols * sizeof(int), s));
+    vk::launch_start(net, b, h->rs, cc, s);
+    VK_CUDA(h, cudaGetLastError());
+    // (re)capture the attempt + control sequence when the configuration changed
+    unsigned char key[sizeof(h->gkey)];
+    std::memcpy(key, &cc, sizeof(cc));
+    std::memcpy(key + sizeof(cc), &h->ncols, sizeof(int));
+    std::memcpy(key + sizeof(cc) + sizeof(int), &h->L, sizeof(int));
+    if (!h->gexec || std::memcmp(key, h->gkey, sizeof(key)) != 0) {
+        if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+        cudaGraph_t g;
+        VK_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        vk::Work &w = h->w;
+        for (int it = 0; it < kGraphAttempts; ++it) {
+            vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, cc.flags, true, s);
+            vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, cc.flags, s);
+            vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
+            vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, cc.flags, false, s);
+            vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+            vk::launch_stage(net, b, w, cc.flags, cc.mtol, cc.atol, s);
+            vk::launch_control(net, b, h->rs, cc, w.sol, w.ymix_out, w.delta, w.status, s);
+        }
+        vk::launch_count_active(h->rs.active, h->ncols, h->d_nactive, s);
+        cudaError_t ec = cudaStreamEndCapture(s, &g);
+        if (ec != cudaSuccess) return fail(h, VK_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+        ec = cudaGraphInstantiate(&h->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ec != cudaSuccess) { h->gexec = nullptr; return fail(h, VK_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ec)); }
+        std::memcpy(h->gkey, key, sizeof(key));
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    cudaEventRecord(h->ev[0], s);
+    int launches = 0;
+    for (;;) {
+        VK_CUDA(h, cudaGraphLaunch(h->gexec, s));
+        launches += kGraphAttempts * 7 + 1;
+        int nact = 0;
+        VK_CUDA(h, cudaMemcpyAsync(&nact, h->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+        VK_CUDA(h, cudaStreamSynchronize(s));
+        if (nact == 0) break;
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_s > 0 && el > timeout_s) {
+            h->launches = launches;
+            return fail(h, VK_ETIMEOUT, "vk_run watchdog: columns still active after " + std::to_string(el) + " s");
+        }
+    }
+    cudaEventRecord(h->ev[1], s);
+    cudaEventSynchronize(h->ev[1]);
+    cudaEventElapsedTime(&h->ms[0], h->ev[0], h->ev[1]);
+    h->ms[1] = h->ms[2] = h->ms[3] = 0.f;
+    h->launches = launches;
+    std::vector<int> ec(h->ncols);
+    VK_CUDA(h, cudaMemcpy(ec.data(), h->rs.end_case, h->ncols * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < h->ncols; ++c)
+        if (ec[c] < 0) return fail(h, -ec[c], "column " + std::to_string(c) + " stopped with error " + std::to_string(-ec[c]));
+    return VK_OK;
+}

@@ -1,0 +1,113 @@
+// Internal declarations shared by the vk_* translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/vk_ros2.h"
+
+#define VK_MAXF 4              // distinct species on one side of a reaction
+#define VK_MAX_NI 160          // largest species count a diagonal block may have
+#define VK_MAX_NATOM 16
+
+#define VK_MAXT 5              // written terms on one side (incl. M)
+
+// One forward/reverse reaction pair (64 bytes).  The written-order terms
+// reproduce the reference's generated rate lambdas k*t1*t2*... exactly; the
+// merged factors (species with summed exponents, M separate) feed the
+// Jacobian.
+struct PairDesc {
+    int16_t tsp[2][VK_MAXT];   // written terms per side, -1 = M, side 0 = reactants
+    uint8_t tnu[2][VK_MAXT];   // coefficients of the written terms
+    uint8_t nt[2];             // written-term counts
+    int16_t fsp[VK_MAXF];      // merged reactant species, -1 unused
+    int16_t rsp[VK_MAXF];      // merged product species
+    uint8_t fnu[VK_MAXF];      // merged exponents
+    uint8_t rnu[VK_MAXF];
+    uint8_t nf, nr, fm, rm;    // merged counts, powers of M
+    uint8_t pad[4];
+};
+static_assert(sizeof(PairDesc) == 64, "PairDesc layout");
+
+// Derivative term: d v_p / d y_q (q may sit on either side).
+struct WDesc {
+    int pair;
+    int q;
+    int fpos;                  // index of q in the forward factor list or -1
+    int rpos;                  // index of q in the reverse factor list or -1
+};
+
+// Host-side compiled network (what vk_network_compile builds).
+struct vk_network {
+    int ni = 0, npair = 0, natom = 0;
+    std::vector<PairDesc> pairs;
+    std::vector<int> src_ptr;          // [ni+1]
+    std::vector<int2> src;             // {pair, net stoichiometry}
+    std::vector<WDesc> w;              // derivative terms
+    std::vector<int> jptr;             // [nnz+1]
+    std::vector<int2> jterm;           // {w index, net stoichiometry}
+    std::vector<int> jrow, jcol, jpos; // entry -> (s, q), s*ni+q
+    std::vector<double> compo;         // [ni*natom]
+};
+
+// Device view of the network tables (passed by value to kernels).
+struct DevNet {
+    int ni, npair, nr, nw, nnz, natom;
+    const PairDesc *pairs;
+    const int *src_ptr;
+    const int2 *src;
+    const WDesc *w;
+    const int *jptr;
+    const int2 *jterm;
+    const int *jpos;
+    const double *compo;
+};
+
+// Device view of a loaded batch of columns.
+struct DevBatch {
+    int ncols;
+    int L;                     // total layers
+    const int *col_off;        // [ncols+1] first layer of each column
+    const int *lay_col;        // [L] column of each layer
+    const double *k;           // [L][nr]
+    const double *atm;         // [L][VK_ATM_NF]
+    const double *Dzz;         // [L][ni]
+    const double *spf;         // [ncols][VK_SP_NF][ni]
+    const int *active;         // [ncols] non-zero = column takes part (NULL = all)
+};
+
+// Launch helpers implemented in vk_kernels.cu (all asynchronous on stream).
+namespace vk {
+
+constexpr double R_ROS = 1.0 + 0.70710678118654752440;   // 1 + 1/sqrt(2)
+
+struct Work {                  // per-handle device work buffers
+    double *y, *ymix, *yk2, *f, *k1, *k2, *z, *sol, *ymix_out;
+    double *jv;                // [L][nnz]  -J_chem entries
+    double *dA, *dB, *dC;      // [L][ni]   diffusion coefficients (A+Ai, B+Bi, C+Ci)
+    double *G;                 // [L][ni*ni] FP64 block inverses
+    float *G32;                // [L][ni*ni] FP32 block inverses (mixed mode)
+    double *rs, *cs;           // [L][ni] row / column scales (mixed mode)
+    double *r, *dx;            // refinement residual / correction
+    double *dt;                // [ncols]
+    double *delta;             // [ncols]
+    int *status;               // [ncols]  VK_* per column (singular pivot ...)
+};
+
+void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
+                  double *jv, double *dA, double *dB, double *dC, const double *k1,
+                  const double *dt, int flags, bool with_jac, cudaStream_t s);
+void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
+                       const double *rhs, double *z, int flags, cudaStream_t s);
+void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G,
+                     const double *dB, const double *z, double *x,
+                     const double *y, double *yk2, cudaStream_t s);
+void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G,
+                      const double *dB, const double *dC, const double *rhs,
+                      double *zbuf, double *x, cudaStream_t s);
+void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags,
+                  double mtol, double atol, cudaStream_t s);
+
+}  // namespace vk

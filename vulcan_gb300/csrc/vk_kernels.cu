@@ -1,0 +1,572 @@
+// Device kernels of the Ros2 kinetics-diffusion step (FP64 path).
+//
+//   k_rates      (a) rate/source: net rate of every reaction pair of one layer
+//                    and the production/loss gather dy/dt, plus the transport
+//                    operator; with JAC also (b): the sparse per-layer
+//                    chemistry Jacobian and the diffusion coefficients that form
+//                    the block-tridiagonal LHS.
+//   k_lu_fwd_f64 (c) block-Thomas factorisation of c0 I - J along a column with
+//                    in-place Gauss-Jordan inversion (partial pivoting) of each
+//                    Schur-complemented diagonal block, fused with the forward
+//                    sweep of the first right-hand side.
+//   k_back_f64       back substitution -> k1, fused yk2 = y + k1/r.
+//   k_solve_f64      forward + back sweeps for the second right-hand side.
+//   k_stage      (d) sol, truncation error delta (masked, column max), ymix.
+//
+// Reference semantics: chem_funs.chemdf / neg_symjac (generated by
+// make_chem_funs.py:113-430, 686-717), op.ODESolver.diffdf / diffdf_no_mol
+// (op.py:1438-1597), lhs_jac_tot / lhs_jac_no_mol (op.py:1973-2042,
+// 2122-2166), Ros2.solver (op.py:2860-3007).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "vk_internal.cuh"
+
+namespace vk {
+
+constexpr double KB = 1.38064852E-16;
+constexpr double NAVO = 6.02214086E+23;
+
+__device__ __forceinline__ double ipow(double x, int e) {
+    double r = x;
+    for (int i = 1; i < e; ++i) r = __dmul_rn(r, x);
+    return r;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Column geometry accessors --------------------------------------------------
+struct Col {
+    const double *atm;   // layer-major, VK_ATM_NF per layer
+    const double *Dzz;   // [layer][ni]
+    const double *ms;    // [ni]
+    const double *alpha;
+    int l0, nz, ni;
+    __device__ double a(int j, int f) const { return atm[(size_t)(l0 + j) * VK_ATM_NF + f]; }
+    __device__ double dzz(int j, int i) const { return Dzz[(size_t)(l0 + j) * ni + i]; }
+    // -1/Hpi + ms g/(Navo kb Ti) + alpha/Ti (T_{j+1}-T_j)/dzi at interface j+1/2
+    __device__ double phi(int j, int i, double g) const {
+        double Ti = a(j, VK_ATM_TI);
+        return -1. / a(j, VK_ATM_HPI) + ms[i] * g / (NAVO * KB * Ti)
+               + alpha[i] / Ti * (a(j + 1, VK_ATM_TCO) - a(j, VK_ATM_TCO)) / a(j, VK_ATM_DZI);
+    }
+};
+
+__device__ __forceinline__ Col make_col(const DevBatch &b, int c, int ni) {
+    Col cv;
+    cv.atm = b.atm;
+    cv.Dzz = b.Dzz;
+    cv.ms = b.spf + (size_t)c * VK_SP_NF * ni + VK_SP_MS * ni;
+    cv.alpha = b.spf + (size_t)c * VK_SP_NF * ni + VK_SP_ALPHA * ni;
+    cv.l0 = b.col_off[c];
+    cv.nz = b.col_off[c + 1] - cv.l0;
+    cv.ni = ni;
+    return cv;
+}
+
+// Transport coefficients of species i in layer j: dy_j/dt|_diff =
+// cA y_j + cB y_{j+1} + cC y_{j-1} (eddy A,B,C plus molecular Ai,Bi,Ci).
+__device__ void diff_coef(const Col &cv, int j, int i, double ysm, double ys0, double ysp,
+                          int flags, double &cA, double &cB, double &cC) {
+    const int nz = cv.nz;
+    double A = 0, B = 0, C = 0, Ai = 0, Bi = 0, Ci = 0;
+    const bool mol = flags & VK_F_MOLDIFF;
+    if (j == 0) {
+        double dzi = cv.a(0, VK_ATM_DZI), K = cv.a(0, VK_ATM_KZZ), vz = cv.a(0, VK_ATM_VZ);
+        A = -1. / dzi * (K / dzi) * (ysp + ys0) / 2. / ys0;
+        B = 1. / dzi * (K / dzi) * (ysp + ys0) / 2. / ysp;
+        A += -((vz > 0) * vz) / dzi;
+        B += -((vz < 0) * vz) / dzi;
+        if (mol) {
+            double D = cv.dzz(0, i), ph = cv.phi(0, i, cv.a(0, VK_ATM_G));
+            Ai = -1. / dzi * (D / dzi) * (ysp + ys0) / 2. / ys0 + 1. / dzi * D / 2. * ph;
+            Bi = 1. / dzi * (D / dzi) * (ysp + ys0) / 2. / ysp + 1. / dzi * D / 2. * ph;
+        }
+    } else if (j == nz - 1) {
+        int t = nz - 2;
+        double dzi = cv.a(t, VK_ATM_DZI), K = cv.a(t, VK_ATM_KZZ), vz = cv.a(t, VK_ATM_VZ);
+        A = -1. / dzi * (K / dzi) * (ys0 + ysm) / 2. / ys0;
+        C = 1. / dzi * (K / dzi) * (ys0 + ysm) / 2. / ysm;
+        A += ((vz < 0) * vz) / dzi;
+        C += ((vz > 0) * vz) / dzi;
+        if (mol) {
+            double D = cv.dzz(t, i), ph = cv.phi(t, i, cv.a(nz - 1, VK_ATM_G));
+            Ai = -1. / dzi * (D / dzi) * (ys0 + ysm) / 2. / ys0 - 1. / dzi * D / 2. * ph;
+            Ci = 1. / dzi * (D / dzi) * (ys0 + ysm) / 2. / ysm - 1. / dzi * D / 2. * ph;
+        }
+    } else {
+        double dm = cv.a(j - 1, VK_ATM_DZI), dp = cv.a(j, VK_ATM_DZI);
+        double Km = cv.a(j - 1, VK_ATM_KZZ), Kp = cv.a(j, VK_ATM_KZZ);
+        double vm = cv.a(j - 1, VK_ATM_VZ), vp = cv.a(j, VK_ATM_VZ);
+        double da = 0.5 * (dm + dp);
+        if (mol) {
+            A = -1. / da * (Kp / dp * (ysp + ys0) / 2. + Km / dm * (ys0 + ysm) / 2.) / ys0;
+            B = 1. / da * Kp / dp * (ysp + ys0) / 2. / ysp;
+            C = 1. / da * Km / dm * (ys0 + ysm) / 2. / ysm;
+        } else {
+            A = -2. / (dm + dp) * (Kp / dp * (ysp + ys0) / 2. + Km / dm * (ys0 + ysm) / 2.) / ys0;
+            B = 2. / (dm + dp) * Kp / dp * (ysp + ys0) / 2. / ysp;
+            C = 2. / (dm + dp) * Km / dm * (ys0 + ysm) / 2. / ysm;
+        }
+        A += -((vp > 0) * vp - (vm < 0) * vm) / da;
+        B += -((vp < 0) * vp) / da;
+        C += ((vm > 0) * vm) / da;
+        if (mol) {
+            double Dm = cv.dzz(j - 1, i), Dp = cv.dzz(j, i);
+            double gm = cv.a(j - 1, VK_ATM_G), g0 = cv.a(j, VK_ATM_G), gp = cv.a(j + 1, VK_ATM_G);
+            Ai = -1. / da * (Dp / dp * (ysp + ys0) / 2. + Dm / dm * (ys0 + ysm) / 2.) / ys0;
+            Bi = 1. / da * Dp / dp * (ysp + ys0) / 2. / ysp;
+            Ci = 1. / da * Dm / dm * (ys0 + ysm) / 2. / ysm;
+            Ai += 1. / (2. * da) * (Dp * cv.phi(j, i, g0) - Dm * cv.phi(j - 1, i, g0));
+            Bi += 1. / (2. * da) * Dp * cv.phi(j, i, gp);
+            Ci += -1. / (2. * da) * Dm * cv.phi(j - 1, i, gm);
+        }
+    }
+    cA = A + Ai;
+    cB = B + Bi;
+    cC = C + Ci;
+}
+
+// Value of one side of pair p in the generated lambda order k*t1*t2*...
+__device__ __forceinline__ double side_rate(double kk, const PairDesc &pd, int side,
+                                            const double *yl, double M) {
+    double v = kk;
+    for (int t = 0; t < pd.nt[side]; ++t) {
+        int s = pd.tsp[side][t];
+        double f = s < 0 ? M : yl[s];
+        v = __dmul_rn(v, ipow(f, pd.tnu[side][t]));
+    }
+    return v;
+}
+
+// d/dy_q of kk * M^m * prod y_s^e over merged factors; pos = index of q.
+__device__ __forceinline__ double side_deriv(double kk, const int16_t *sp, const uint8_t *nu,
+                                             int n, int m, int pos, const double *yl, double M) {
+    double v = kk;
+    for (int t = 0; t < m; ++t) v *= M;
+    for (int t = 0; t < n; ++t) {
+        double yv = yl[sp[t]];
+        int e = nu[t];
+        if (t == pos) {
+            if (e > 1) v *= (double)e * ipow(yv, e - 1);
+        } else {
+            v *= ipow(yv, e);
+        }
+    }
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// (a)+(b) rate / source / Jacobian kernel: one CTA per layer.
+template <bool JAC>
+__global__ void __launch_bounds__(128)
+k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict__ f,
+        double *__restrict__ jv, double *__restrict__ dA, double *__restrict__ dB,
+        double *__restrict__ dC, const double *__restrict__ k1, const double *__restrict__ dt,
+        int flags, int chem_only) {
+    extern __shared__ double sm[];
+    const int ni = net.ni;
+    const int l = blockIdx.x;
+    const int c = b.lay_col[l];
+    if (b.active && !b.active[c]) return;
+    const Col cv = make_col(b, c, ni);
+    const int j = l - cv.l0;
+    double *ys = sm;                       // [3][ni] layers j-1, j, j+1
+    double *sums = ys + 3 * ni;            // [4]
+    double *v = sums + 4;                  // [max(npair, nw)]
+    const int tid = threadIdx.x, nth = blockDim.x;
+    for (int t = tid; t < 3 * ni; t += nth) {
+        int jj = j - 1 + t / ni;
+        ys[t] = (jj >= 0 && jj < cv.nz) ? y[(size_t)(cv.l0 + jj) * ni + (t % ni)] : 0.0;
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < 3) {
+        double s = 0;
+        for (int i = lane; i < ni; i += 32) s += ys[warp * ni + i];
+        s = warp_sum(s);
+        if (lane == 0) sums[warp] = s;
+    }
+    const double *yl = ys + ni;
+    const double M = cv.a(j, VK_ATM_M);
+    const double *kl = b.k + (size_t)l * net.nr;
+    // net rate of each pair
+    for (int p = tid; p < net.npair; p += nth) {
+        const PairDesc pd = net.pairs[p];
+        const double2 kk = reinterpret_cast<const double2 *>(kl)[p];
+        v[p] = side_rate(kk.x, pd, 0, yl, M) - side_rate(kk.y, pd, 1, yl, M);
+    }
+    __syncthreads();
+    // production - loss gather (generated chemdf order) + transport
+    const double ysm = sums[0], ys0 = sums[1], ysp = sums[2];
+    const double hinv = k1 ? 2. / (R_ROS * dt[c]) : 0.0;
+    for (int s = tid; s < ni; s += nth) {
+        double acc = 0.0;
+        for (int e = net.src_ptr[s]; e < net.src_ptr[s + 1]; ++e) {
+            const int2 t = net.src[e];
+            acc = __dadd_rn(acc, __dmul_rn((double)t.y, v[t.x]));
+        }
+        double cA, cB, cC;
+        diff_coef(cv, j, s, ysm, ys0, ysp, flags, cA, cB, cC);
+        double out = acc;
+        if (!chem_only) {
+            double dif = cA * yl[s];
+            if (j + 1 < cv.nz) dif += cB * ys[2 * ni + s];
+            if (j > 0) dif += cC * ys[s];
+            if ((flags & VK_F_TOPFLUX) && j == cv.nz - 1)
+                dif += b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_TOPFLUX * ni + s] / cv.a(cv.nz - 2, VK_ATM_DZI);
+            if ((flags & VK_F_BOTFLUX) && j == 0)
+                dif += (b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_BOTFLUX * ni + s]
+                        - yl[s] * b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_BOTVDEP * ni + s])
+                       / cv.a(0, VK_ATM_DZI);
+            out = acc + dif;
+            if (k1) out = out - hinv * k1[(size_t)l * ni + s];
+        }
+        f[(size_t)l * ni + s] = out;
+        if (JAC) {
+            if ((flags & VK_F_BOTFLUX) && j == 0)
+                cA -= b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_BOTVDEP * ni + s] / cv.a(0, VK_ATM_DZI);
+            dA[(size_t)l * ni + s] = cA;
+            dB[(size_t)l * ni + s] = cB;
+            dC[(size_t)l * ni + s] = cC;
+        }
+    }
+    if (!JAC) return;
+    __syncthreads();
+    // derivative terms d v_p / d y_q
+    for (int t = tid; t < net.nw; t += nth) {
+        const WDesc wd = net.w[t];
+        const PairDesc pd = net.pairs[wd.pair];
+        const double2 kk = reinterpret_cast<const double2 *>(kl)[wd.pair];
+        double d = 0.0;
+        if (wd.fpos >= 0) d += side_deriv(kk.x, pd.fsp, pd.fnu, pd.nf, pd.fm, wd.fpos, yl, M);
+        if (wd.rpos >= 0) d -= side_deriv(kk.y, pd.rsp, pd.rnu, pd.nr, pd.rm, wd.rpos, yl, M);
+        v[t] = d;
+    }
+    __syncthreads();
+    double *jl = jv + (size_t)l * net.nnz;
+    for (int e = tid; e < net.nnz; e += nth) {
+        double acc = 0.0;
+        for (int t = net.jptr[e]; t < net.jptr[e + 1]; ++t) {
+            const int2 jt = net.jterm[t];
+            acc += (double)jt.y * v[jt.x];
+        }
+        jl[e] = -acc;                      // entries of -J (neg_symjac)
+    }
+}
+
+// ---------------------------------------------------------------------------
+// (c) block-Thomas factorisation + forward sweep, FP64.  One CTA per column.
+// The diagonal block D'_j = c0 I - J_j - diag(dA_j) - diag(dC_j) G_{j-1} diag(dB_{j-1})
+// is inverted in place in shared memory by Gauss-Jordan elimination with
+// partial pivoting (largest |a|, lowest row on ties).
+__device__ void gj_invert_f64(double *A, int n, double *colk, double *rowk, int *perm,
+                              int *s_piv, double *s_pval, int *s_sing) {
+    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nn = n * n;
+    for (int k = 0; k < n; ++k) {
+        if (warp == 0) {
+            double best = -1.0;
+            int bi = n;
+            for (int i = k + lane; i < n; i += 32) {
+                double a = fabs(A[i * n + k]);
+                if (a > best) { best = a; bi = i; }
+            }
+            for (int o = 16; o; o >>= 1) {
+                double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) {
+                if (!(best > 0.0) || bi >= n) { *s_sing = 1; bi = k; }
+                *s_piv = bi;
+                *s_pval = A[bi * n + k];
+                perm[k] = bi;
+            }
+        }
+        __syncthreads();
+        const int p = *s_piv;
+        const double pval = *s_pval;
+        const double pinv = 1.0 / pval;
+        for (int t = tid; t < n; t += nth) {
+            double ak = A[k * n + t], ap = A[p * n + t];
+            rowk[t] = (t == k) ? pinv : ap * pinv;
+            if (p != k) A[p * n + t] = ak;
+            colk[t] = (t == k) ? pval : ((t == p) ? A[k * n + k] : A[t * n + k]);
+        }
+        __syncthreads();
+        for (int e = tid; e < nn; e += nth) {
+            int i = e / n, jj = e - i * n;
+            if (i == k) A[e] = rowk[jj];
+            else A[e] = (jj == k ? 0.0 : A[e]) - colk[i] * rowk[jj];
+        }
+        __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        int p = perm[k];
+        if (p != k) {
+            for (int t = tid; t < n; t += nth) {
+                double a = A[t * n + k];
+                A[t * n + k] = A[t * n + p];
+                A[t * n + p] = a;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
+             const double *__restrict__ dB, const double *__restrict__ dC,
+             const double *__restrict__ dt, const double *__restrict__ rhs,
+             double *__restrict__ G, double *__restrict__ z, int *__restrict__ status) {
+    extern __shared__ double sm[];
+    const int n = net.ni, nn = n * n;
+    const int c = blockIdx.x;
+    if (b.active && !b.active[c]) return;
+    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    double *A = sm;
+    double *colk = A + nn;
+    double *rowk = colk + n;
+    double *zp = rowk + n;
+    double *bb = zp + n;
+    int *perm = reinterpret_cast<int *>(bb + n);
+    __shared__ int s_piv, s_sing;
+    __shared__ double s_pval;
+    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarp = nth >> 5;
+    if (tid == 0) s_sing = 0;
+    const double c0 = 1.0 / (R_ROS * dt[c]);
+    for (int j = 0; j < nz; ++j) {
+        const size_t l = (size_t)l0 + j;
+        const double *cj = dC + l * n;
+        const double *bm = dB + (l - 1) * n;   // valid for j > 0
+        const double *aj = dA + l * n;
+        for (int e = tid; e < nn; e += nth) {
+            int r = e / n, q = e - r * n;
+            double v = j > 0 ? -cj[r] * A[e] * bm[q] : 0.0;
+            if (r == q) v += c0 - aj[r];
+            A[e] = v;
+        }
+        for (int t = tid; t < n; t += nth)
+            bb[t] = rhs[l * n + t] + (j > 0 ? cj[t] * zp[t] : 0.0);
+        __syncthreads();
+        const double *jl = jv + l * net.nnz;
+        for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
+        __syncthreads();
+        gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
+        double *Gl = G + l * nn;
+        for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
+        for (int r = warp; r < n; r += nwarp) {
+            double s = 0.0;
+            for (int q = lane; q < n; q += 32) s += A[r * n + q] * bb[q];
+            s = warp_sum(s);
+            if (lane == 0) rowk[r] = s;
+        }
+        __syncthreads();
+        for (int t = tid; t < n; t += nth) {
+            zp[t] = rowk[t];
+            z[l * n + t] = rowk[t];
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && s_sing) status[c] = VK_ESINGULAR;
+}
+
+// x_j = z_j + G_j (dB_j o x_{j+1}); optional yk2 = y + x / r.
+__global__ void __launch_bounds__(256)
+k_back_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *__restrict__ dB,
+           const double *__restrict__ z, double *__restrict__ x, const double *__restrict__ y,
+           double *__restrict__ yk2) {
+    extern __shared__ double sm[];
+    const int n = net.ni, nn = n * n;
+    const int c = blockIdx.x;
+    if (b.active && !b.active[c]) return;
+    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    double *xs = sm;          // x_{j+1} * dB_j
+    double *xn = sm + n;
+    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarp = nth >> 5;
+    for (int j = nz - 1; j >= 0; --j) {
+        const size_t l = (size_t)l0 + j;
+        if (j == nz - 1) {
+            for (int t = tid; t < n; t += nth) xn[t] = z[l * n + t];
+        } else {
+            const double *Gl = G + l * nn;
+            for (int r = warp; r < n; r += nwarp) {
+                double s = 0.0;
+                for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * xs[q];
+                s = warp_sum(s);
+                if (lane == 0) xn[r] = z[l * n + r] + s;
+            }
+        }
+        __syncthreads();
+        for (int t = tid; t < n; t += nth) {
+            double xv = xn[t];
+            x[l * n + t] = xv;
+            if (yk2) yk2[l * n + t] = y[l * n + t] + xv / R_ROS;
+            if (j > 0) xs[t] = dB[(l - 1) * n + t] * xv;
+        }
+        __syncthreads();
+    }
+}
+
+// Forward + back sweep with stored inverses for a new right-hand side.
+__global__ void __launch_bounds__(256)
+k_solve_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *__restrict__ dB,
+            const double *__restrict__ dC, const double *__restrict__ rhs,
+            double *__restrict__ zbuf, double *__restrict__ x) {
+    extern __shared__ double sm[];
+    const int n = net.ni, nn = n * n;
+    const int c = blockIdx.x;
+    if (b.active && !b.active[c]) return;
+    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    double *vin = sm;
+    double *vout = sm + n;
+    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
+    const int nwarp = nth >> 5;
+    for (int j = 0; j < nz; ++j) {
+        const size_t l = (size_t)l0 + j;
+        for (int t = tid; t < n; t += nth)
+            vin[t] = rhs[l * n + t] + (j > 0 ? dC[l * n + t] * vout[t] : 0.0);
+        __syncthreads();
+        const double *Gl = G + l * nn;
+        for (int r = warp; r < n; r += nwarp) {
+            double s = 0.0;
+            for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
+            s = warp_sum(s);
+            if (lane == 0) { vout[r] = s; zbuf[l * n + r] = s; }
+        }
+        __syncthreads();
+    }
+    for (int j = nz - 1; j >= 0; --j) {
+        const size_t l = (size_t)l0 + j;
+        if (j < nz - 1) {
+            const double *Gl = G + l * nn;
+            for (int r = warp; r < n; r += nwarp) {
+                double s = 0.0;
+                for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
+                s = warp_sum(s);
+                if (lane == 0) vout[r] = zbuf[l * n + r] + s;
+            }
+        } else {
+            for (int t = tid; t < n; t += nth) vout[t] = zbuf[l * n + t];
+        }
+        __syncthreads();
+        for (int t = tid; t < n; t += nth) {
+            x[l * n + t] = vout[t];
+            if (j > 0) vin[t] = dB[(l - 1) * n + t] * vout[t];
+        }
+        __syncthreads();
+    }
+}
+
+// (d) stage: sol, masked relative truncation error (column max), ymix.
+__global__ void __launch_bounds__(256)
+k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__restrict__ ymix,
+        const double *__restrict__ k1, const double *__restrict__ k2,
+        const double *__restrict__ yk2, double *__restrict__ sol, double *__restrict__ ymix_out,
+        double *__restrict__ delta, int flags, double mtol, double atol) {
+    __shared__ double wmax[8];
+    const int n = net.ni;
+    const int c = blockIdx.x;
+    if (b.active && !b.active[c]) return;
+    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;
+    const double c1 = 3. / (2. * R_ROS), c2 = 1 / (2. * R_ROS);
+    double dmax = 0.0;
+    for (int j = warp; j < nz; j += nwarp) {
+        const size_t l = (size_t)l0 + j;
+        double s = 0.0;
+        for (int i = lane; i < n; i += 32) {
+            const size_t e = l * n + i;
+            double sv = __dadd_rn(__dadd_rn(y[e], __dmul_rn(c1, k1[e])), __dmul_rn(c2, k2[e]));
+            sol[e] = sv;
+            s += sv;
+            double d = fabs(sv - yk2[e]);
+            if (ymix[e] < mtol) d = 0.0;
+            if (sv < atol) d = 0.0;
+            if ((flags & VK_F_BOTFLUX) && j == 0) d = 0.0;
+            if (sv > 0.0) dmax = fmax(dmax, d / sv);
+        }
+        s = warp_sum(s);
+        for (int i = lane; i < n; i += 32) ymix_out[l * n + i] = sol[l * n + i] / s;
+    }
+    for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    if (lane == 0) wmax[warp] = dmax;
+    __syncthreads();
+    if (tid == 0) {
+        double m = 0.0;
+        for (int w = 0; w < nwarp; ++w) m = fmax(m, wmax[w]);
+        delta[c] = m;
+    }
+}
+
+// ---------------------------------------------------------------------------
+static size_t rates_smem(const DevNet &net);
+
+// Opt the kernels into the dynamic shared memory this network needs; called
+// once per handle, outside any stream capture.
+cudaError_t init_kernels(const DevNet &net) {
+    size_t sr = rates_smem(net);
+    const int n = net.ni;
+    size_t sl = (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_rates<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
+    if ((e = cudaFuncSetAttribute(k_rates<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
+    if ((e = cudaFuncSetAttribute(k_lu_fwd_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
+    return cudaSuccess;
+}
+
+static size_t rates_smem(const DevNet &net) {
+    int m = net.npair > net.nw ? net.npair : net.nw;
+    return (size_t)(3 * net.ni + 4 + m) * sizeof(double);
+}
+
+void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
+                  double *jv, double *dA, double *dB, double *dC, const double *k1,
+                  const double *dt, int flags, bool with_jac, cudaStream_t s) {
+    size_t sm = rates_smem(net);
+    if (with_jac)
+        k_rates<true><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, flags, 0);
+    else
+        k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, flags, 0);
+}
+
+void launch_chem_only(const DevNet &net, const DevBatch &b, const double *y, double *f,
+                      cudaStream_t s) {
+    size_t sm = rates_smem(net);
+    k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, nullptr, nullptr, nullptr, nullptr,
+                                        nullptr, nullptr, 0, 1);
+}
+
+void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
+                       const double *rhs, double *z, int flags, cudaStream_t s) {
+    (void)flags;
+    const int n = net.ni;
+    size_t sm = (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int);
+    k_lu_fwd_f64<<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
+                                          w.status);
+}
+
+void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
+                     const double *z, double *x, const double *y, double *yk2, cudaStream_t s) {
+    k_back_f64<<<b.ncols, 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, z, x, y, yk2);
+}
+
+void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
+                      const double *dC, const double *rhs, double *zbuf, double *x,
+                      cudaStream_t s) {
+    k_solve_f64<<<b.ncols, 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, dC, rhs, zbuf, x);
+}
+
+void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags, double mtol,
+                  double atol, cudaStream_t s) {
+    k_stage<<<b.ncols, 256, 0, s>>>(net, b, w.y, w.ymix, w.k1, w.k2, w.yk2, w.sol, w.ymix_out,
+                                    w.delta, flags, mtol, atol);
+}
+
+}  // namespace vk

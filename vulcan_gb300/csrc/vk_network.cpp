@@ -1,0 +1,146 @@
+// Network compiler: reaction-pair factor lists -> the gather tables the
+// rate/source and Jacobian kernels read.
+//
+// Replaces the code generation of the reference (make_chem_funs.py:113-430,
+// which writes chemdf/df as Python source, and :653-717, which differentiates
+// df symbolically with sympy).  Instead of generated code we build, once per
+// network:
+//   * src   : for every species s the list of (pair p, +-coefficient), one
+//             entry per written term, in the order the generated chemdf sums
+//             them (reaction order; reactants before products, :288-305);
+//   * w     : one derivative term d v_p / d y_q per (pair, distinct species);
+//   * J     : for every structurally non-zero entry (s, q) of the per-layer
+//             chemistry Jacobian the list of (w, stoichiometry) to gather.
+// All tables are gathers, so the device kernels are deterministic (no atomics).
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "vk_internal.cuh"
+
+static thread_local std::string g_net_err;
+
+extern "C" const char *vk_network_last_error(void) { return g_net_err.c_str(); }
+
+extern "C" int vk_network_compile(const vk_network_desc *d, vk_network **out) {
+    if (!d || !out) { g_net_err = "null argument"; return VK_EINVAL; }
+    *out = nullptr;
+    if (d->ni <= 0 || d->ni > VK_MAX_NI) {
+        g_net_err = "ni must be in 1.." + std::to_string(VK_MAX_NI);
+        return VK_EINVAL;
+    }
+    if (d->npair <= 0) { g_net_err = "npair must be positive"; return VK_EINVAL; }
+    if (d->natom < 0 || d->natom > VK_MAX_NATOM) {
+        g_net_err = "natom out of range"; return VK_EINVAL;
+    }
+    vk_network *n = new (std::nothrow) vk_network();
+    if (!n) { g_net_err = "host allocation failed"; return VK_ENOMEM; }
+    const int ni = d->ni, np = d->npair;
+    n->ni = ni; n->npair = np; n->natom = d->natom;
+    n->pairs.resize(np);
+    std::vector<std::vector<std::pair<int, int>>> nu(np);   // merged net stoichiometry
+    std::vector<std::vector<int2>> per_sp(ni);              // written-order source terms
+    for (int p = 0; p < np; ++p) {
+        PairDesc &pd = n->pairs[p];
+        std::memset(&pd, 0, sizeof(pd));
+        for (int i = 0; i < VK_MAXF; ++i) { pd.fsp[i] = -1; pd.rsp[i] = -1; }
+        for (int side = 0; side < 2; ++side) {
+            const int *ptr = side ? d->prod_ptr : d->reac_ptr;
+            const int *sp = side ? d->prod_sp : d->reac_sp;
+            const int *cf = side ? d->prod_nu : d->reac_nu;
+            int t0 = ptr[p], t1 = ptr[p + 1];
+            if (t1 < t0 || t1 - t0 > VK_MAXT) {
+                g_net_err = "pair " + std::to_string(p) + ": more than 5 terms on one side";
+                delete n; return VK_EINVAL;
+            }
+            pd.nt[side] = (uint8_t)(t1 - t0);
+            std::vector<std::pair<int, int>> merged;   // (species, exponent) first-seen order
+            int mpow = 0;
+            for (int t = t0; t < t1; ++t) {
+                int s = sp[t], e = cf[t];
+                if (s < -1 || s >= ni || e < 1 || e > 15) {
+                    g_net_err = "pair " + std::to_string(p) + ": bad term";
+                    delete n; return VK_EINVAL;
+                }
+                pd.tsp[side][t - t0] = (int16_t)s;
+                pd.tnu[side][t - t0] = (uint8_t)e;
+                if (s < 0) { mpow += e; continue; }
+                // generated chemdf: reactant terms subtract, product terms add
+                per_sp[s].push_back(make_int2(p, side ? e : -e));
+                bool found = false;
+                for (auto &m : merged) if (m.first == s) { m.second += e; found = true; }
+                if (!found) merged.push_back({s, e});
+            }
+            if ((int)merged.size() > VK_MAXF || mpow > 3) {
+                g_net_err = "pair " + std::to_string(p) + ": too many distinct species or M";
+                delete n; return VK_EINVAL;
+            }
+            for (size_t i = 0; i < merged.size(); ++i) {
+                if (side) { pd.rsp[i] = (int16_t)merged[i].first; pd.rnu[i] = (uint8_t)merged[i].second; }
+                else      { pd.fsp[i] = (int16_t)merged[i].first; pd.fnu[i] = (uint8_t)merged[i].second; }
+            }
+            if (side) { pd.nr = (uint8_t)merged.size(); pd.rm = (uint8_t)mpow; }
+            else      { pd.nf = (uint8_t)merged.size(); pd.fm = (uint8_t)mpow; }
+        }
+        std::map<int, int> net;
+        for (int i = 0; i < pd.nf; ++i) net[pd.fsp[i]] -= pd.fnu[i];
+        for (int i = 0; i < pd.nr; ++i) net[pd.rsp[i]] += pd.rnu[i];
+        for (auto &kv : net)
+            if (kv.second != 0) nu[p].push_back(kv);
+    }
+    n->src_ptr.assign(ni + 1, 0);
+    for (int s = 0; s < ni; ++s) {
+        n->src_ptr[s + 1] = n->src_ptr[s] + (int)per_sp[s].size();
+        n->src.insert(n->src.end(), per_sp[s].begin(), per_sp[s].end());
+    }
+    // derivative terms and Jacobian entries
+    std::map<std::pair<int, int>, std::vector<int2>> jac;   // (s,q) -> terms
+    for (int p = 0; p < np; ++p) {
+        if (nu[p].empty()) continue;           // e.g. He -> He: no contribution
+        const PairDesc &pd = n->pairs[p];
+        std::vector<int> qs;
+        for (int i = 0; i < pd.nf; ++i) qs.push_back(pd.fsp[i]);
+        for (int i = 0; i < pd.nr; ++i)
+            if (std::find(qs.begin(), qs.end(), pd.rsp[i]) == qs.end()) qs.push_back(pd.rsp[i]);
+        for (int q : qs) {
+            WDesc wd;
+            wd.pair = p; wd.q = q; wd.fpos = -1; wd.rpos = -1;
+            for (int i = 0; i < pd.nf; ++i) if (pd.fsp[i] == q) wd.fpos = i;
+            for (int i = 0; i < pd.nr; ++i) if (pd.rsp[i] == q) wd.rpos = i;
+            int wi = (int)n->w.size();
+            n->w.push_back(wd);
+            for (auto &kv : nu[p]) jac[{kv.first, q}].push_back(make_int2(wi, kv.second));
+        }
+    }
+    n->jptr.push_back(0);
+    for (auto &e : jac) {
+        n->jrow.push_back(e.first.first);
+        n->jcol.push_back(e.first.second);
+        n->jpos.push_back(e.first.first * ni + e.first.second);
+        n->jterm.insert(n->jterm.end(), e.second.begin(), e.second.end());
+        n->jptr.push_back((int)n->jterm.size());
+    }
+    n->compo.assign(d->compo, d->compo + (size_t)ni * d->natom);
+    *out = n;
+    return VK_OK;
+}
+
+extern "C" int vk_network_info(const vk_network *n, int *nnz, int *nw, int *nsrc) {
+    if (!n) return VK_EINVAL;
+    if (nnz) *nnz = (int)n->jpos.size();
+    if (nw) *nw = (int)n->w.size();
+    if (nsrc) *nsrc = (int)n->src.size();
+    return VK_OK;
+}
+
+extern "C" int vk_network_jac_pattern(const vk_network *n, int *rows, int *cols) {
+    if (!n || !rows || !cols) return VK_EINVAL;
+    std::copy(n->jrow.begin(), n->jrow.end(), rows);
+    std::copy(n->jcol.begin(), n->jcol.end(), cols);
+    return VK_OK;
+}
+
+extern "C" void vk_network_free(vk_network *n) { delete n; }

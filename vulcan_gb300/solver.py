@@ -1,0 +1,366 @@
+"""Host side of the GPU Ros2 step: network upload, column batches, handles.
+
+* ``GPUNetwork``    compiles a ``network.Network`` into the device tables
+                    (C-ABI ``vk_network_compile``).
+* ``ColumnBatch``   packs columns (state, rate constants, atmosphere) into the
+                    flat layer-major arrays of ``vk_set_columns``.
+* ``Ros2Handle``    owns a ``vk_handle``: one attempt for every column
+                    (``attempt``, = op.Ros2.solver) or a device-side run to
+                    steady state (``run``, = op.Integration for every column).
+* ``make_ros2gpu``  builds the drop-in solver class for the reference's
+                    ``op`` module (see ``Ros2GPU`` below).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import check, lib, ptr
+from .configs import SOLVER_DEFAULTS
+
+
+class GPUNetwork:
+    """Device tables of one network (species order = ``net.species``)."""
+
+    def __init__(self, net, atom_list):
+        self.net = net
+        self.atom_list = list(atom_list)
+        sidx = {s: i for i, s in enumerate(net.species)}
+        rp, rs, rn, pp, ps, pn = [0], [], [], [0], [], []
+        for r in net.reactions:
+            for nu, name in r.reac:
+                rs.append(-1 if name == 'M' else sidx[name])
+                rn.append(nu)
+            for nu, name in r.prod:
+                ps.append(-1 if name == 'M' else sidx[name])
+                pn.append(nu)
+            rp.append(len(rs))
+            pp.append(len(ps))
+        a = lambda v: np.ascontiguousarray(v, dtype=np.int32)
+        self._keep = [a(rp), a(rs), a(rn), a(pp), a(ps), a(pn),
+                      net.compo_for(self.atom_list)]
+        k = self._keep
+        desc = capi.VkNetworkDesc(
+            net.ni, net.npair, ptr(k[0], C.c_int), ptr(k[1], C.c_int), ptr(k[2], C.c_int),
+            ptr(k[3], C.c_int), ptr(k[4], C.c_int), ptr(k[5], C.c_int),
+            len(self.atom_list), ptr(k[6]))
+        L = lib()
+        h = C.c_void_p()
+        rc = L.vk_network_compile(C.byref(desc), C.byref(h))
+        if rc != capi.VK_OK:
+            raise capi.VkError(rc, L.vk_network_last_error().decode())
+        self.handle = h
+        nnz, nw, nsrc = C.c_int(), C.c_int(), C.c_int()
+        check(L.vk_network_info(h, C.byref(nnz), C.byref(nw), C.byref(nsrc)))
+        self.nnz, self.nw, self.nsrc = nnz.value, nw.value, nsrc.value
+
+    def jac_pattern(self):
+        rows = np.zeros(self.nnz, dtype=np.int32)
+        cols = np.zeros(self.nnz, dtype=np.int32)
+        check(lib().vk_network_jac_pattern(self.handle, ptr(rows, C.c_int), ptr(cols, C.c_int)))
+        return rows, cols
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h:
+            lib().vk_network_free(h)
+            self.handle = None
+
+
+def pack_atm(col, M=None, n_0=None, Tco=None):
+    """Layer-major [nz][ATM_NF] atmosphere array of one Column."""
+    nz = col.nz
+    a = np.zeros((nz, capi.ATM_NF))
+    a[:, capi.ATM_M] = col.M if M is None else M
+    a[:, capi.ATM_N0] = col.n_0 if n_0 is None else n_0
+    a[:, capi.ATM_TCO] = col.Tco if Tco is None else Tco
+    a[:, capi.ATM_G] = col.g
+    a[:-1, capi.ATM_DZI] = col.dzi
+    a[:-1, capi.ATM_KZZ] = col.Kzz
+    a[:-1, capi.ATM_VZ] = col.vz
+    if col.Ti is not None:
+        a[:-1, capi.ATM_TI] = col.Ti
+    if col.Hpi is not None:
+        a[:-1, capi.ATM_HPI] = col.Hpi
+    a[:, capi.ATM_HP] = col.Hp
+    a[:, capi.ATM_PICO] = col.pico[:-1]
+    a[:, capi.ATM_PICOU] = col.pico[1:]
+    if col.dz is not None:
+        a[:, capi.ATM_DZ] = col.dz
+    return a
+
+
+def pack_spf(col, ni):
+    s = np.zeros((capi.SP_NF, ni))
+    s[capi.SP_MS] = col.ms
+    s[capi.SP_ALPHA] = col.alpha
+    s[capi.SP_TOPFLUX] = col.top_flux
+    s[capi.SP_BOTFLUX] = col.bot_flux
+    s[capi.SP_BOTVDEP] = col.bot_vdep
+    return s
+
+
+class ColumnBatch:
+    """Flat arrays for vk_set_columns built from a list of column inputs.
+
+    Each item is a dict with ``col`` (column.Column), ``k`` ([nr, nz] rate
+    constants, row i-1 = k[i]), ``y`` and ``ymix`` ([nz, ni])."""
+
+    def __init__(self, items, ni):
+        self.nz = np.array([it['col'].nz for it in items], dtype=np.int32)
+        self.off = np.concatenate([[0], np.cumsum(self.nz)]).astype(np.int64)
+        self.ncols = len(items)
+        self.L = int(self.off[-1])
+        self.ni = ni
+        self.k = np.ascontiguousarray(np.concatenate([it['k'].T for it in items]))
+        self.atm = np.ascontiguousarray(np.concatenate([pack_atm(it['col']) for it in items]))
+        Dz = []
+        for it in items:
+            d = np.zeros((it['col'].nz, ni))
+            d[:-1] = it['col'].Dzz
+            Dz.append(d)
+        self.Dzz = np.ascontiguousarray(np.concatenate(Dz))
+        self.spf = np.ascontiguousarray(np.stack([pack_spf(it['col'], ni) for it in items]))
+        self.y = np.ascontiguousarray(np.concatenate([it['y'] for it in items]))
+        self.ymix = np.ascontiguousarray(np.concatenate([it['ymix'] for it in items]))
+        self.pref = np.array([it['col'].pref_indx for it in items], dtype=np.int32)
+
+    def split(self, arr):
+        return [arr[self.off[c]:self.off[c + 1]] for c in range(self.ncols)]
+
+
+def ctrl_from(cfg=None, flags=capi.VK_F_MOLDIFF, gs=2140., Rp=1.138 * 7.1492E9,
+              max_attempts=400):
+    """vk_ctrl from a dict / module of vulcan_cfg-style knobs (defaults = reference)."""
+    v = dict(SOLVER_DEFAULTS)
+    if cfg is not None:
+        for k in v:
+            if isinstance(cfg, dict):
+                if k in cfg:
+                    v[k] = cfg[k]
+            elif hasattr(cfg, k):
+                v[k] = getattr(cfg, k)
+    c = capi.VkCtrl()
+    for k in ('rtol', 'atol', 'mtol', 'mtol_conv', 'pos_cut', 'nega_cut', 'loss_eps',
+              'dt_min', 'dt_max', 'dt_var_min', 'dt_var_max', 'yconv_cri', 'slope_cri',
+              'yconv_min', 'st_factor', 'trun_min', 'runtime'):
+        setattr(c, k, float(v[k]))
+    for k in ('conv_step', 'count_min', 'count_max', 'update_frq'):
+        setattr(c, k, int(v[k]))
+    c.max_attempts = int(max_attempts)
+    c.flags = int(flags)
+    c.gs, c.Rp = float(gs), float(Rp)
+    return c
+
+
+class Ros2Handle:
+    """A device batch of columns on one network."""
+
+    def __init__(self, gnet: GPUNetwork, max_cols, max_layers, precision=capi.VK_PREC_FP64):
+        self.gnet = gnet
+        self.ni = gnet.net.ni
+        L = lib()
+        h = C.c_void_p()
+        rc = L.vk_create(gnet.handle, int(max_cols), int(max_layers), int(precision), C.byref(h))
+        if rc != capi.VK_OK:
+            raise capi.VkError(rc, L.vk_last_error(None).decode())
+        self.h = h
+        self.batch = None
+
+    def close(self):
+        if getattr(self, 'h', None):
+            lib().vk_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_columns(self, batch: ColumnBatch):
+        self.batch = batch
+        L = lib()
+        check(L.vk_set_columns(self.h, batch.ncols, ptr(batch.nz, C.c_int), ptr(batch.k),
+                               ptr(batch.atm), ptr(batch.Dzz), ptr(batch.spf), ptr(batch.y),
+                               ptr(batch.ymix)), self.h)
+        check(L.vk_set_column_info(self.h, ptr(batch.pref, C.c_int), None), self.h)
+
+    def set_state(self, y, ymix):
+        check(lib().vk_update_state(self.h, ptr(np.ascontiguousarray(y)),
+                                    ptr(np.ascontiguousarray(ymix))), self.h)
+
+    def set_atm(self, atm):
+        check(lib().vk_update_atm(self.h, ptr(np.ascontiguousarray(atm))), self.h)
+
+    def set_k(self, k):
+        check(lib().vk_update_k(self.h, ptr(np.ascontiguousarray(k))), self.h)
+
+    def attempt(self, dt, flags=capi.VK_F_MOLDIFF, want_k=False):
+        """One Ros2 attempt per column: returns dict(sol, ymix, delta[, k1, k2])."""
+        b = self.batch
+        dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, float), (b.ncols,)))
+        sol = np.empty((b.L, self.ni))
+        ymix = np.empty((b.L, self.ni))
+        delta = np.empty(b.ncols)
+        k1 = np.empty((b.L, self.ni)) if want_k else None
+        k2 = np.empty((b.L, self.ni)) if want_k else None
+        check(lib().vk_ros2_attempt(self.h, ptr(dt), int(flags), ptr(sol), ptr(ymix),
+                                    ptr(delta), ptr(k1), ptr(k2)), self.h)
+        out = dict(sol=sol, ymix=ymix, delta=delta)
+        if want_k:
+            out.update(k1=k1, k2=k2)
+        return out
+
+    def chem_source(self, y):
+        out = np.empty((self.batch.L, self.ni))
+        check(lib().vk_chem_source(self.h, ptr(np.ascontiguousarray(y)), ptr(out)), self.h)
+        return out
+
+    def lhs(self):
+        b = self.batch
+        jv = np.empty((b.L, self.gnet.nnz))
+        dA, dB, dC = (np.empty((b.L, self.ni)) for _ in range(3))
+        check(lib().vk_get_lhs(self.h, ptr(jv), ptr(dA), ptr(dB), ptr(dC)), self.h)
+        return jv, dA, dB, dC
+
+    def timing(self):
+        v = [C.c_double() for _ in range(4)]
+        n = C.c_int()
+        check(lib().vk_get_timing(self.h, *[C.byref(x) for x in v], C.byref(n)), self.h)
+        return dict(rates=v[0].value, lu=v[1].value, solve=v[2].value, stage=v[3].value,
+                    launches=n.value)
+
+    # ------------------------------------------------------------- run mode
+    def set_atom_ini(self, atom_ini):
+        check(lib().vk_set_atom_ini(self.h, ptr(np.ascontiguousarray(atom_ini, dtype=float))), self.h)
+
+    def set_conv_ignore(self, mask):
+        check(lib().vk_set_column_info(self.h, None, ptr(np.ascontiguousarray(mask, dtype=np.int32), C.c_int)), self.h)
+
+    def set_clock(self, dt=None, t=None, count=None):
+        b = self.batch
+        f = lambda a, dt_: None if a is None else np.ascontiguousarray(np.broadcast_to(np.asarray(a, dt_), (b.ncols,)))
+        dt, t, count = f(dt, float), f(t, float), f(count, np.int32)
+        check(lib().vk_set_clock(self.h, ptr(dt), ptr(t), ptr(count, C.c_int)), self.h)
+
+    def run(self, ctrl, max_steps=0, timeout_s=0.0):
+        check(lib().vk_run(self.h, C.byref(ctrl), int(max_steps), float(timeout_s)), self.h)
+
+    def state(self):
+        b = self.batch
+        y = np.empty((b.L, self.ni))
+        ymix = np.empty((b.L, self.ni))
+        dt, t, delta = np.empty(b.ncols), np.empty(b.ncols), np.empty(b.ncols)
+        count = np.empty(b.ncols, dtype=np.int32)
+        end = np.empty(b.ncols, dtype=np.int32)
+        check(lib().vk_get_state(self.h, ptr(y), ptr(ymix), ptr(dt), ptr(t), ptr(count, C.c_int),
+                                 ptr(end, C.c_int), ptr(delta)), self.h)
+        return dict(y=y, ymix=ymix, dt=dt, t=t, count=count, end_case=end, delta=delta)
+
+    def counters(self):
+        c = np.empty((self.batch.ncols, 4), dtype=np.int32)
+        check(lib().vk_get_counters(self.h, ptr(c, C.c_int)), self.h)
+        return c
+
+
+# --------------------------------------------------------------------------
+# Drop-in solver for the reference: op.Ros2 with the step on the GPU.
+
+def _flags_from_cfg(cfg):
+    f = 0
+    if getattr(cfg, 'use_moldiff', True):
+        f |= capi.VK_F_MOLDIFF
+    if getattr(cfg, 'use_topflux', False):
+        f |= capi.VK_F_TOPFLUX
+    if getattr(cfg, 'use_botflux', False):
+        f |= capi.VK_F_BOTFLUX
+    return f
+
+
+def _unsupported(cfg):
+    """Reference options this GPU step does not implement (raise, never fall back)."""
+    bad = []
+    for key in ('use_vm_mol', 'use_settling', 'use_condense', 'use_ion'):
+        if getattr(cfg, key, False):
+            bad.append(key)
+    if getattr(cfg, 'use_fix_sp_bot', {}):
+        bad.append('use_fix_sp_bot')
+    if getattr(cfg, 'non_gas_sp', []):
+        bad.append('non_gas_sp')
+    return bad
+
+
+class Ros2GPUMixin:
+    """Overrides ``solver`` of the reference's ``op.Ros2`` (op.py:2860-3007).
+
+    Same contract as the reference: reads var.y, var.ymix, var.dt, var.k and
+    the atmosphere arrays, writes var.y = sol, var.ymix and para.delta, and
+    returns (var, para).  clip / step_ok / step_reject / step_size stay the
+    reference's own (inherited), so a run through ``op.Integration`` takes the
+    same accept/reject decisions."""
+
+    _vk_net_cls = None      # network.Network, set by make_ros2gpu
+    _vk_cfg = None
+
+    def _vk_setup(self, var, atm):
+        cfg = self._vk_cfg
+        bad = _unsupported(cfg)
+        if bad:
+            raise NotImplementedError('Ros2GPU does not implement: ' + ', '.join(bad))
+        net = self._vk_net_cls.from_file(cfg.network, use_photo=cfg.use_photo)
+        species = self._vk_species
+        if list(net.species) != list(species):
+            raise RuntimeError('species order of %s differs from chem_funs.spec_list' % cfg.network)
+        self._vk_gnet = GPUNetwork(net, [a for a in cfg.atom_list])
+        nz = var.y.shape[0]
+        self._vk_h = Ros2Handle(self._vk_gnet, 1, nz)
+        self._vk_nz = nz
+
+    def _vk_pack(self, var, atm):
+        nz, ni = var.y.shape
+        k = np.array([var.k[i] for i in range(1, 2 * len(self._vk_gnet.net.reactions) + 1)])
+        col = _AtmView(atm, ni)
+        from .solver import ColumnBatch
+        b = ColumnBatch([dict(col=col, k=k, y=var.y, ymix=var.ymix)], ni)
+        return b
+
+    def solver(self, var, atm, para):
+        if getattr(self, '_vk_h', None) is None:
+            self._vk_setup(var, atm)
+        b = self._vk_pack(var, atm)
+        self._vk_h.set_columns(b)
+        out = self._vk_h.attempt(var.dt, _flags_from_cfg(self._vk_cfg))
+        var.y = out['sol']
+        var.ymix = out['ymix']
+        para.delta = float(out['delta'][0])
+        return var, para
+
+
+class _AtmView:
+    """Adapter: a reference AtmData object seen as a column.Column."""
+
+    def __init__(self, atm, ni):
+        self.nz = atm.Tco.size
+        self.M, self.n_0, self.Tco = atm.M, atm.n_0, atm.Tco
+        self.g, self.dzi, self.Kzz, self.vz = atm.g, atm.dzi, atm.Kzz, atm.vz
+        self.Ti = getattr(atm, 'Ti', None)
+        self.Hpi = getattr(atm, 'Hpi', None)
+        self.Hp, self.pico = atm.Hp, atm.pico
+        self.dz = getattr(atm, 'dz', None)
+        self.Dzz, self.ms, self.alpha = atm.Dzz, atm.ms, atm.alpha
+        self.top_flux, self.bot_flux, self.bot_vdep = atm.top_flux, atm.bot_flux, atm.bot_vdep
+        self.pref_indx = int(getattr(atm, 'pref_indx', 0))
+
+
+def make_ros2gpu(op_module, cfg_module, species):
+    """Return ``Ros2GPU``: a subclass of the reference's ``op.Ros2`` whose
+    ``solver`` runs on the GPU.  Register it as ``op.Ros2GPU`` and set
+    ``vulcan_cfg.ode_solver = 'Ros2GPU'`` (vulcan.py:161-163 resolves the
+    solver with getattr(op, vulcan_cfg.ode_solver))."""
+    from .network import Network
+
+    class Ros2GPU(Ros2GPUMixin, op_module.Ros2):
+        _vk_net_cls = Network
+        _vk_cfg = cfg_module
+        _vk_species = list(species)
+
+    return Ros2GPU
