@@ -61,9 +61,12 @@ def test_lhs_matches_oracle(tag):
         scale = np.abs(J[l]).max()
         assert np.max(np.abs(jv[l] - ref)) <= 1e-14 * scale
     A, B, C, Ai, Bi, Ci = O.diff_coeffs(y, attempt_atm(g, 0), O.Flags())
-    np.testing.assert_allclose(dA, A[:, None] + Ai, rtol=1e-13, atol=0)
-    np.testing.assert_allclose(dB[:-1], (B[:, None] + Bi)[:-1], rtol=1e-13, atol=0)
-    np.testing.assert_allclose(dC[1:], (C[:, None] + Ci)[1:], rtol=1e-13, atol=0)
+    # eddy + molecular parts can nearly cancel: compare against their magnitudes
+    for got, e, m, sl in ((dA, A, Ai, slice(None)), (dB, B, Bi, slice(0, -1)),
+                          (dC, C, Ci, slice(1, None))):
+        ref = e[:, None] + m
+        mag = np.abs(e[:, None]) + np.abs(m)
+        assert np.all(np.abs(got[sl] - ref[sl]) <= 1e-13 * mag[sl])
 
 
 def _cases():
@@ -96,7 +99,7 @@ def test_batch_invariance_and_determinism():
     """Columns in one batch give bit-identical results to single-column runs,
     and repeated runs are bit-identical (no atomics on the FP64 path)."""
     g = golden('c0')
-    ns = [0, 5, 13, 99]
+    ns = [0, 5, 9, 13]
     _, _, _, hb, bb = make_handle('c0', ns=ns)
     dts = np.array([g['att_dt'][n] for n in ns])
     ob = hb.attempt(dts)
@@ -110,18 +113,29 @@ def test_batch_invariance_and_determinism():
         assert ob['delta'][c] == o1['delta'][0]
 
 
-def test_singular_block_reports_status():
-    """A zero diagonal block is reported as VK_ESINGULAR (host-visible status)."""
+def test_nan_state_reports_status():
+    """A NaN injected into the state is reported as VK_ENAN (host-visible
+    status, the context stays usable)."""
     from vulcan_gb300 import capi
     g, net, gn, h, b = make_handle('c0', ns=[0])
-    b.k[:] = 0.0
-    b.atm[:, capi.ATM_KZZ] = 0.0
-    b.Dzz[:] = 0.0
-    b.atm[:, capi.ATM_VZ] = 0.0
-    h.set_columns(b)
+    y = g['att_y'][0].copy()
+    y[7, 3] = np.nan
+    h.set_state(y, g['att_ymix'][0])
     with pytest.raises(capi.VkError) as e:
-        h.attempt(1e300, flags=0)
-    assert e.value.code == capi.VK_ESINGULAR
+        h.attempt(g['att_dt'][0])
+    assert e.value.code == capi.VK_ENAN
+    h.set_state(g['att_y'][0], g['att_ymix'][0])
+    out = h.attempt(g['att_dt'][0])
+    assert floor_err(out['sol'], g['att_sol'][0], g['n_0']) <= 1e-10
+
+
+def test_bad_dt_rejected():
+    from vulcan_gb300 import capi
+    g, net, gn, h, b = make_handle('c0', ns=[0])
+    for dt in (0.0, -1.0, np.inf, np.nan):
+        with pytest.raises(capi.VkError) as e:
+            h.attempt(dt)
+        assert e.value.code == capi.VK_EINVAL
 
 
 def test_dropin_solver_contract():

@@ -10,6 +10,7 @@
 
 #include <chrono>
 #include <climits>
+#include <cmath>
 
 #include "vk_control.cuh"
 #include "vk_internal.cuh"
@@ -333,7 +334,8 @@ extern "C" int vk_ros2_attempt(vk_handle *h, const double *dt, int flags, double
     if (rc) return rc;
     if (!dt) return fail(h, VK_EINVAL, "dt is NULL");
     for (int c = 0; c < h->ncols; ++c)
-        if (!(dt[c] > 0.0)) return fail(h, VK_EINVAL, "dt must be positive");
+        if (!(dt[c] > 0.0) || !std::isfinite(dt[c]))
+            return fail(h, VK_EINVAL, "dt must be positive and finite");
     cudaStream_t s = h->stream;
     VK_CUDA(h, cudaMemcpyAsync(h->w.dt, dt, h->ncols * sizeof(double), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, h->ncols * sizeof(int), s));
@@ -353,9 +355,12 @@ extern "C" int vk_ros2_attempt(vk_handle *h, const double *dt, int flags, double
     cudaEventElapsedTime(&h->ms[1], h->ev[1], h->ev[2]);
     cudaEventElapsedTime(&h->ms[2], h->ev[2], h->ev[3]);
     cudaEventElapsedTime(&h->ms[3], h->ev[3], h->ev[4]);
-    for (int c = 0; c < h->ncols; ++c)
+    for (int c = 0; c < h->ncols; ++c) {
         if (st[c] == VK_ESINGULAR)
             return fail(h, VK_ESINGULAR, "singular diagonal block in column " + std::to_string(c));
+        if (st[c] == VK_ENAN)
+            return fail(h, VK_ENAN, "non-finite pivot (NaN state) in column " + std::to_string(c));
+    }
     return VK_OK;
 }
 

@@ -281,7 +281,9 @@ __device__ void gj_invert_f64(double *A, int n, double *colk, double *rowk, int 
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
             if (lane == 0) {
-                if (!(best > 0.0) || bi >= n) { *s_sing = 1; bi = k; }
+                // no finite candidate -> NaN state (2); all zero -> singular (1)
+                if (best < 0.0 || bi >= n) { *s_sing = 2; bi = k; }
+                else if (!(best > 0.0)) { if (*s_sing == 0) *s_sing = 1; bi = k; }
                 *s_piv = bi;
                 *s_pval = A[bi * n + k];
                 perm[k] = bi;
@@ -343,7 +345,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
     for (int j = 0; j < nz; ++j) {
         const size_t l = (size_t)l0 + j;
         const double *cj = dC + l * n;
-        const double *bm = dB + (l - 1) * n;   // valid for j > 0
+        const double *bm = j > 0 ? dB + (l - 1) * n : dB;
         const double *aj = dA + l * n;
         for (int e = tid; e < nn; e += nth) {
             int r = e / n, q = e - r * n;
@@ -373,7 +375,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
         }
         __syncthreads();
     }
-    if (tid == 0 && s_sing) status[c] = VK_ESINGULAR;
+    if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
 }
 
 // x_j = z_j + G_j (dB_j o x_{j+1}); optional yk2 = y + x / r.
