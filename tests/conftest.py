@@ -1,6 +1,12 @@
 import os
 import sys
 
+# Single-threaded BLAS for the CPU oracle, as the reference runs
+# (vulcan.py:52 sets OMP_NUM_THREADS=1); threaded OpenBLAS is ~25x slower on
+# the banded solves.  Must be set before numpy is imported.
+for _v in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+    os.environ.setdefault(_v, '1')
+
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

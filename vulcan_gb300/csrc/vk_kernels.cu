@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(256)
 k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__restrict__ ymix,
         const double *__restrict__ k1, const double *__restrict__ k2,
         const double *__restrict__ yk2, double *__restrict__ sol, double *__restrict__ ymix_out,
-        double *__restrict__ delta, int flags, double mtol, double atol) {
+        double *__restrict__ delta, int *__restrict__ status, int flags, double mtol, double atol) {
     __shared__ double wmax[8];
     const int n = net.ni;
     const int c = blockIdx.x;
@@ -480,6 +480,7 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;
     const double c1 = 3. / (2. * R_ROS), c2 = 1 / (2. * R_ROS);
     double dmax = 0.0;
+    int bad = 0;
     for (int j = warp; j < nz; j += nwarp) {
         const size_t l = (size_t)l0 + j;
         double s = 0.0;
@@ -487,6 +488,7 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
             const size_t e = l * n + i;
             double sv = __dadd_rn(__dadd_rn(y[e], __dmul_rn(c1, k1[e])), __dmul_rn(c2, k2[e]));
             sol[e] = sv;
+            bad |= !isfinite(sv);
             s += sv;
             double d = fabs(sv - yk2[e]);
             if (ymix[e] < mtol) d = 0.0;
@@ -499,8 +501,9 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
     }
     for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     if (lane == 0) wmax[warp] = dmax;
-    __syncthreads();
+    bad = __syncthreads_or(bad);
     if (tid == 0) {
+        if (bad && status[c] == 0) status[c] = VK_ENAN;
         double m = 0.0;
         for (int w = 0; w < nwarp; ++w) m = fmax(m, wmax[w]);
         delta[c] = m;
@@ -568,7 +571,7 @@ void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G, con
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags, double mtol,
                   double atol, cudaStream_t s) {
     k_stage<<<b.ncols, 256, 0, s>>>(net, b, w.y, w.ymix, w.k1, w.k2, w.yk2, w.sol, w.ymix_out,
-                                    w.delta, flags, mtol, atol);
+                                    w.delta, w.status, flags, mtol, atol);
 }
 
 }  // namespace vk
