@@ -226,12 +226,19 @@ def diffdf(y, atm, flags: Flags, coeffs=None):
     return diff
 
 
-def lhs_blocks(net, y, M, k, dt, atm, flags: Flags, negjac=None):
+def lhs_blocks(net, y, M, k, dt, atm, flags: Flags, negjac=None, perturb=None):
     """Block-tridiagonal c0 I - J: diagonal blocks D [nz,ni,ni] and the
-    diagonal vectors of the off-diagonal blocks U (j,j+1) and L (j,j-1)."""
+    diagonal vectors of the off-diagonal blocks U (j,j+1) and L (j,j-1).
+
+    ``perturb=(eps, seed)`` multiplies every chemistry Jacobian entry by
+    (1 + eps u), u ~ U(-1, 1): used to measure how far rounding-level changes
+    of the matrix move the step (its conditioning floor)."""
     nz, ni = y.shape
     c0 = 1. / (R_ROS * dt)
     D = neg_jac_blocks(net, y, M, k) if negjac is None else negjac.copy()
+    if perturb is not None:
+        rng = np.random.default_rng(perturb[1])
+        D = D * (1.0 + perturb[0] * rng.uniform(-1.0, 1.0, D.shape))
     idx = np.arange(ni)
     A, B, C, Ai, Bi, Ci = diff_coeffs(y, atm, flags)
     D[:, idx, idx] = c0 + D[:, idx, idx]
@@ -318,13 +325,14 @@ class Tol:
     update_frq: int = 100
 
 
-def ros2_attempt(net, y, ymix, dt, k, atm, flags: Flags, tol: Tol, solve='banded'):
+def ros2_attempt(net, y, ymix, dt, k, atm, flags: Flags, tol: Tol, solve='banded',
+                 perturb=None):
     """One Rosenbrock-2 attempt from state (y, ymix) with step dt."""
     nz, ni = y.shape
     M = atm['M']
     r = R_ROS
     df = chemdf(net, y, M, k).flatten() + diffdf(y, atm, flags).flatten()
-    D, U, L = lhs_blocks(net, y, M, k, dt, atm, flags)
+    D, U, L = lhs_blocks(net, y, M, k, dt, atm, flags, perturb=perturb)
     if solve == 'banded':
         ab, bw = band_from_blocks(D, U, L)
         k1_flat = scipy.linalg.solve_banded((bw, bw), ab, df)

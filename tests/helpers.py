@@ -58,3 +58,27 @@ def column_from_golden(g, n=None):
 def floor_err(a, b, n0, floor=1e-10):
     """max |a-b| / (|b| + floor * n_0): relative error with a mixing-ratio floor."""
     return float(np.max(np.abs(a - b) / (np.abs(b) + floor * n0[:, None])))
+
+
+def reference_floor(tag, g, n, samples=3, eps=4e-16):
+    """Conditioning floor of one recorded attempt: how far the reference's own
+    algorithm (LAPACK banded solve) moves when its Jacobian changes at the
+    rounding level -- the analytic Jacobian, and that Jacobian with every
+    entry scaled by (1 + eps u), u ~ U(-1,1), for a few seeds.  Returns the
+    largest (floor-metric error of sol, relative error of delta) vs the
+    recorded reference attempt."""
+    on = oracle_net(tag, g)
+    args = (on, g['att_y'][n], g['att_ymix'][n], float(g['att_dt'][n]), g['k'],
+            attempt_atm(g, n), O.Flags(), O.Tol(), 'banded')
+    e = d = 0.0
+    for s in [None] + [(eps, seed) for seed in range(samples)]:
+        r = O.ros2_attempt(*args, perturb=s)
+        e = max(e, floor_err(r.sol, g['att_sol'][n], g['n_0']))
+        d = max(d, abs(r.delta / g['att_delta'][n] - 1))
+    return e, d
+
+
+def step_tolerance(e_floor, d_floor):
+    """Per-attempt tolerances: 1e-10 (floor metric) and 1e-6 (delta) where the
+    step is well conditioned, else 10x the reference's own conditioning floor."""
+    return max(1e-10, 10 * e_floor), max(1e-6, 10 * d_floor)
