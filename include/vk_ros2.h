@@ -171,6 +171,26 @@ VK_API int  vk_get_counters(vk_handle *h, int *counters);
 VK_API int  vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double *ms_solve,
                    double *ms_stage, int *launches);
 
+/* ---- block-tridiagonal solve without allocation ----
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a framework that owns all device memory through its own pool, a plugin
+ * that is handed its buffers, code about to be captured into a stream): the
+ * solver's scratch (block inverses and sweep vector) is a fixed 16 MiB
+ * __device__ array inside this library, held by every GPU that loads it until
+ * the process exits.  Solves lower[j] o x[j-1] + D[j] x[j] + upper[j] o x[j+1]
+ * = b[j] for one column; D is [nz][ni][ni], lower/upper/b/x are [nz][ni], all
+ * device pointers supplied by the caller; lower[0] and upper[nz-1] are not
+ * read.  Requires nz*ni*ni + nz*ni + 1 <= 2^21 (e.g. nz = 200 at ni = 100);
+ * larger sizes return VK_EINVAL.  Runs on `stream` (a cudaStream_t, NULL for
+ * the default stream) and synchronizes it to return VK_ESINGULAR / VK_ENAN.
+ * The first call on a device resolves the array's address on that device, so
+ * make it before any stream capture.  All calls share the one array: calls
+ * that overlap on the GPU (other threads or streams) race; serialize them.
+ * Errors: vk_last_error(NULL). */
+VK_API int  vk_block_solve_noalloc(int nz, int ni, const double *D, const double *lower,
+                                   const double *upper, const double *b, double *x,
+                                   void *stream);
+
 /* ---- diagnostics (used by the parity tests) ---- */
 /* Message of the last failed vk_network_compile on this thread. */
 VK_API const char *vk_network_last_error(void);

@@ -31,7 +31,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_set_precision', 'vk_set_columns', 'vk_update_state', 'vk_update_atm',
            'vk_update_k', 'vk_ros2_attempt', 'vk_set_atom_ini', 'vk_set_column_info',
            'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
-           'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs')
+           'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
+           'vk_block_solve_noalloc')
 
 
 class VkNetworkDesc(C.Structure):
@@ -99,6 +100,7 @@ def lib(path=None):
         'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
         'vk_chem_source': (i, [vp, pd, pd]),
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),
+        'vk_block_solve_noalloc': (i, [i, i, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

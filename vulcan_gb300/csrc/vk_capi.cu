@@ -73,6 +73,8 @@ struct vk_handle {
 
 static thread_local std::string g_err;
 
+void vk::set_global_error(const std::string &msg) { g_err = msg; }
+
 static int fail(vk_handle *h, int code, const std::string &msg) {
     if (h) h->err = msg; else g_err = msg;
     return code;

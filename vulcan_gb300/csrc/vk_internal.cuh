@@ -83,6 +83,9 @@ namespace vk {
 
 constexpr double R_ROS = 1.0 + 0.70710678118654752440;   // 1 + 1/sqrt(2)
 
+// Message returned by vk_last_error(NULL) on this thread (not exported).
+void set_global_error(const std::string &msg);
+
 struct Work {                  // per-handle device work buffers
     double *y, *ymix, *yk2, *f, *k1, *k2, *z, *sol, *ymix_out;
     double *jv;                // [L][nnz]  -J_chem entries
