@@ -255,12 +255,13 @@ def run_profile(args):
     net = Network.from_npz(NET)
     specs = configs.config2_columns(ncols=NCOLS, seed=SEED)[:args.ncols]
     items = batch.build_items(specs, net)
-    h, b = batch.make_batch_handle(net, items, ATOMS)
+    prec = 1 if args.precision == 'mixed' else 0
+    h, b = batch.make_batch_handle(net, items, ATOMS, precision=prec)
     dt = np.full(b.ncols, 1e-10)
     for _ in range(args.attempts):
         h.attempt(dt)
-    print(json.dumps({'profile': True, 'ncols': b.ncols, 'layers': int(b.L), 'attempts': args.attempts,
-                      'attempt_ms': h.timing()}))
+    print(json.dumps({'profile': True, 'precision': args.precision, 'ncols': b.ncols,
+                      'layers': int(b.L), 'attempts': args.attempts, 'attempt_ms': h.timing()}))
     h.close()
 
 
@@ -291,6 +292,7 @@ def main():
     ap.add_argument('--profile', action='store_true',
                     help='only run --attempts instrumented attempts (for ncu captures)')
     ap.add_argument('--attempts', type=int, default=2)
+    ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
     ap.add_argument('--cpu-workers', type=int, default=min(16, os.cpu_count() or 1))
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', '0'))

@@ -163,11 +163,17 @@ VK_API int  vk_get_state(vk_handle *h, double *y, double *ymix, double *dt, doub
 /* Initial dt / t / count per column before vk_run (dt = vulcan_cfg.dttry). */
 VK_API int  vk_set_clock(vk_handle *h, const double *dt, const double *t, const int *count);
 
-/* Cumulative counters per column: [ncols][4] = attempts, delta rejections,
- * negativity rejections, loss rejections. */
+/* Cumulative counters per column: [ncols][VK_NCOUNTERS] = attempts, delta
+ * rejections, negativity rejections, loss rejections, attempts redone in FP64
+ * because mixed-precision refinement did not converge, accepted steps. */
+#define VK_NCOUNTERS 6
 VK_API int  vk_get_counters(vk_handle *h, int *counters);
 
-/* Kernel timing of the last vk_run / vk_ros2_attempt (ms per kernel class). */
+/* Device time of the last call in ms: after vk_ros2_attempt the rate +
+ * Jacobian kernel, the block factorisation, the solves (including the second
+ * right-hand side and any FP64 fallback) and the stage kernel; after vk_run
+ * ms_rates holds the whole run and the others are 0.  launches = kernels
+ * launched by the call. */
 VK_API int  vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double *ms_solve,
                    double *ms_stage, int *launches);
 

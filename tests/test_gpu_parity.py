@@ -99,6 +99,39 @@ def test_attempt_matches_reference(tag, n):
     np.testing.assert_allclose(out['ymix'], ym, rtol=1e-14, atol=0)
 
 
+@pytest.mark.parametrize('tag,n', _cases())
+def test_mixed_attempt_matches_reference(tag, n):
+    """FP32 scaled block LU + FP64 refinement: same per-attempt tolerances as
+    the FP64 path (refinement runs to 1e-13 of |x| + |y|, or the column is
+    redone in FP64)."""
+    g, net, gn, h, b = make_handle(tag, ns=[n], precision=1)
+    out = h.attempt(g['att_dt'][n], want_k=True)
+    n0 = g['n_0']
+    if g['att_dt'][n] < 1e-2:
+        tol, dtol = 1e-10, 1e-6
+    else:
+        tol, dtol = step_tolerance(*reference_floor(tag, g, n))
+    assert floor_err(out['sol'], g['att_sol'][n], n0) <= tol
+    assert abs(out['delta'][0] / g['att_delta'][n] - 1) <= dtol
+
+
+def test_mixed_matches_fp64_path_batch():
+    """Mixed and FP64 solves of the same batch of attempts agree to the
+    refinement tolerance (well-conditioned early steps)."""
+    g = golden('c0')
+    ns = [0, 3, 5, 9]
+    dts = np.array([g['att_dt'][n] for n in ns])
+    _, _, _, h64, b = make_handle('c0', ns=ns)
+    _, _, _, h32, _ = make_handle('c0', ns=ns, precision=1)
+    o64 = h64.attempt(dts)
+    o32 = h32.attempt(dts)
+    for c, n in enumerate(ns):
+        n0 = g['n_0']
+        sl = slice(b.off[c], b.off[c + 1])
+        assert floor_err(o32['sol'][sl], o64['sol'][sl], n0) <= 1e-11
+    np.testing.assert_allclose(o32['delta'], o64['delta'], rtol=1e-8)
+
+
 def test_batch_invariance_and_determinism():
     """Columns in one batch give bit-identical results to single-column runs,
     and repeated runs are bit-identical (no atomics on the FP64 path)."""

@@ -21,6 +21,7 @@ ATM_NF = 13
 SP_MS, SP_ALPHA, SP_TOPFLUX, SP_BOTFLUX, SP_BOTVDEP = range(5)
 SP_NF = 5
 MAX_NATOM = 16
+NCOUNTERS = 6   # attempts, delta/negative/loss rejections, FP64 redo, accepted steps
 
 _ERRNAMES = {1: 'VK_EINVAL', 2: 'VK_ECUDA', 3: 'VK_ESINGULAR', 4: 'VK_ENAN',
              5: 'VK_EMAXATTEMPT', 6: 'VK_ETIMEOUT', 7: 'VK_ENOMEM'}

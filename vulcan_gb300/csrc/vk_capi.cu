@@ -17,7 +17,7 @@
 
 namespace vk {
 void launch_chem_only(const DevNet &net, const DevBatch &b, const double *y, double *f,
-                      cudaStream_t s);
+                      const double *geo, cudaStream_t s);
 cudaError_t init_kernels(const DevNet &net);
 }
 
@@ -25,8 +25,9 @@ struct vk_handle {
     std::string err;
     int ni = 0, npair = 0, nr = 0, nnz = 0, nw = 0, natom = 0;
     int max_cols = 0, max_layers = 0, precision = VK_PREC_FP64;
-    int max_refine = 3;
+    int max_refine = 6;
     double refine_tol = 1e-13;
+    int geo_flags = -1;         // flags the transport geometry was built for (-1: stale)
     int ncols = 0, L = 0;
     std::vector<int> col_off;
     // network tables
@@ -37,6 +38,7 @@ struct vk_handle {
     int *d_jptr = nullptr;
     int2 *d_jterm = nullptr;
     int *d_jpos = nullptr;
+    int *d_jrow = nullptr, *d_jcol = nullptr, *d_jrowptr = nullptr;
     double *d_compo = nullptr;
     // batch
     int *d_col_off = nullptr, *d_lay_col = nullptr;
@@ -60,6 +62,7 @@ struct vk_handle {
         n.ni = ni; n.npair = npair; n.nr = nr; n.nw = nw; n.nnz = nnz; n.natom = natom;
         n.pairs = d_pairs; n.src_ptr = d_src_ptr; n.src = d_src; n.w = d_w;
         n.jptr = d_jptr; n.jterm = d_jterm; n.jpos = d_jpos; n.compo = d_compo;
+        n.jrow = d_jrow; n.jcol = d_jcol; n.jrowptr = d_jrowptr;
         return n;
     }
     DevBatch batch() const {
@@ -158,6 +161,9 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_jterm, net->jterm));
     TRY(upload(h, &h->d_jpos, net->jpos));
     TRY(upload(h, &h->d_compo, net->compo));
+    TRY(upload(h, &h->d_jrow, net->jrow));
+    TRY(upload(h, &h->d_jcol, net->jcol));
+    TRY(upload(h, &h->d_jrowptr, net->jrowptr));
     const size_t L = (size_t)max_layers, ni = (size_t)h->ni;
     TRY(dalloc(h, &h->d_col_off, max_cols + 1));
     TRY(dalloc(h, &h->d_lay_col, L));
@@ -170,13 +176,20 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
                        &w.dA, &w.dB, &w.dC, &w.r, &w.dx, &w.rs, &w.cs};
     for (double **p : vecs) TRY(dalloc(h, p, L * ni));
     TRY(dalloc(h, &w.jv, L * (size_t)std::max(h->nnz, 1)));
-    if (precision == VK_PREC_FP64) TRY(dalloc(h, &w.G, L * ni * ni));
-    else TRY(dalloc(h, &w.G32, L * ni * ni));
+    TRY(dalloc(h, &w.geo, L * 5 * ni));
+    // FP64 inverses always (the mixed path falls back to them per column)
+    TRY(dalloc(h, &w.G, L * ni * ni));
+    if (precision == VK_PREC_MIXED) TRY(dalloc(h, &w.G32, L * ni * ni));
+    TRY(dalloc(h, &w.zf, L * ni));
+    TRY(dalloc(h, &w.fallback, max_cols));
+    TRY(dalloc(h, &w.sweeps, 1));
     TRY(dalloc(h, &w.dt, max_cols));
     TRY(dalloc(h, &w.delta, max_cols));
     TRY(dalloc(h, &w.status, max_cols));
     TRY(vk::init_kernels(h->net()) == cudaSuccess ? VK_OK
                                                   : fail(h, VK_ECUDA, "cudaFuncSetAttribute failed"));
+    TRY(vk::init_mixed_kernels(h->ni) == cudaSuccess ? VK_OK
+                                                     : fail(h, VK_ECUDA, "cudaFuncSetAttribute (mixed) failed"));
     // per-column run state (small); the history ring is sized at the first vk_run
     vk::RunState &r = h->rs;
     r.y = w.y; r.ymix = w.ymix; r.dt = w.dt; r.delta = w.delta; r.atm = h->d_atm;
@@ -185,7 +198,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     for (double **p : cd) TRY(dalloc(h, p, max_cols));
     int **ci[] = {&r.count, &r.end_case, &r.active, &r.natt, &r.steps_call, &r.pref};
     for (int **p : ci) TRY(dalloc(h, p, max_cols));
-    TRY(dalloc(h, &r.counters, (size_t)max_cols * 4));
+    TRY(dalloc(h, &r.counters, (size_t)max_cols * VK_NCOUNTERS));
     TRY(dalloc(h, &r.atom_ini, (size_t)max_cols * VK_MAX_NATOM));
     TRY(dalloc(h, &r.loss, (size_t)max_cols * VK_MAX_NATOM));
     TRY(dalloc(h, &r.loss_prev, (size_t)max_cols * VK_MAX_NATOM));
@@ -199,10 +212,6 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
 
 extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol) {
     if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
-    if (precision == VK_PREC_FP64 && !h->w.G) {
-        int rc = dalloc(h, &h->w.G, (size_t)h->max_layers * h->ni * h->ni);
-        if (rc) return rc;
-    }
     if (precision == VK_PREC_MIXED && !h->w.G32) {
         int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * h->ni * h->ni);
         if (rc) return rc;
@@ -213,6 +222,7 @@ extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, dou
     h->precision = precision;
     h->max_refine = max_refine;
     h->refine_tol = refine_tol;
+    if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
     return VK_OK;
 }
 
@@ -251,7 +261,7 @@ extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const doub
         VK_CUDA(h, cudaMemsetAsync(r.t, 0, ncols * sizeof(double), s));
         VK_CUDA(h, cudaMemsetAsync(r.count, 0, ncols * sizeof(int), s));
         VK_CUDA(h, cudaMemsetAsync(r.end_case, 0, ncols * sizeof(int), s));
-        VK_CUDA(h, cudaMemsetAsync(r.counters, 0, ncols * 4 * sizeof(int), s));
+        VK_CUDA(h, cudaMemsetAsync(r.counters, 0, ncols * VK_NCOUNTERS * sizeof(int), s));
         VK_CUDA(h, cudaMemsetAsync(r.pref, 0, ncols * sizeof(int), s));
         VK_CUDA(h, cudaMemsetAsync(r.loss, 0, ncols * VK_MAX_NATOM * sizeof(double), s));
         std::vector<double> dt0(ncols, 1e-10);
@@ -265,6 +275,7 @@ extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const doub
     h->ncols = ncols;
     h->L = L;
     h->col_off = off;
+    h->geo_flags = -1;
     return VK_OK;
 }
 
@@ -291,6 +302,7 @@ extern "C" int vk_update_atm(vk_handle *h, const double *atm) {
     VK_CUDA(h, cudaMemcpyAsync(h->d_atm, atm, (size_t)h->L * VK_ATM_NF * sizeof(double),
                                cudaMemcpyHostToDevice, h->stream));
     VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->geo_flags = -1;
     return VK_OK;
 }
 
@@ -304,27 +316,57 @@ extern "C" int vk_update_k(vk_handle *h, const double *k) {
     return VK_OK;
 }
 
-// Enqueue one Ros2 attempt for every loaded column (device state in, w.sol /
-// w.ymix_out / w.delta out).
-static int enqueue_attempt(vk_handle *h, int flags, bool timed) {
-    const DevNet net = h->net();
-    const DevBatch b = h->batch();
+// Transport geometry for the current atmosphere (recomputed only when the
+// atmosphere or the transport flags changed).
+static void ensure_geometry(vk_handle *h, int flags) {
+    if (h->geo_flags == flags) return;
+    vk::launch_geometry(h->net(), h->batch(), h->w.geo, flags, h->stream);
+    h->geo_flags = flags;
+}
+
+// Enqueue the kernels of one Ros2 attempt for the columns b.active selects
+// (all when NULL): device state in, w.sol / w.ymix_out / w.delta out.
+static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBatch &b, int flags,
+                                    double mtol, double atol, bool timed) {
     vk::Work &w = h->w;
     cudaStream_t s = h->stream;
-    if (h->precision != VK_PREC_FP64 || !w.G)
-        return fail(h, VK_EINVAL, "mixed-precision attempt not available on this handle");
     if (timed) cudaEventRecord(h->ev[0], s);
-    vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, flags, true, s);
+    vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
     if (timed) cudaEventRecord(h->ev[1], s);
-    vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, flags, s);
-    if (timed) cudaEventRecord(h->ev[2], s);
-    vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
-    vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, flags, false, s);
-    vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+    if (h->precision == VK_PREC_FP64) {
+        vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, flags, s);
+        if (timed) cudaEventRecord(h->ev[2], s);
+        vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
+        vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
+        vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+        h->launches += 6;
+    } else {
+        cudaMemsetAsync(w.fallback, 0, b.ncols * sizeof(int), s);
+        vk::launch_lu_f32(net, b, w, s);
+        if (timed) cudaEventRecord(h->ev[2], s);
+        vk::launch_refine(net, b, w, w.f, w.k1, w.y, w.yk2, h->max_refine, h->refine_tol, s);
+        vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
+        vk::launch_refine(net, b, w, w.f, w.k2, w.y, nullptr, h->max_refine, h->refine_tol, s);
+        // columns whose refinement did not converge redo the attempt in FP64
+        DevBatch bf = b;
+        bf.active = w.fallback;
+        vk::launch_rates(net, bf, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
+        vk::launch_lu_fwd_f64(net, bf, w, w.f, w.z, flags, s);
+        vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
+        vk::launch_rates(net, bf, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
+        vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+        h->launches += 11;
+    }
     if (timed) cudaEventRecord(h->ev[3], s);
-    vk::launch_stage(net, b, w, flags, 1.E-22, 1.E-1, s);
+    vk::launch_stage(net, b, w, flags, mtol, atol, s);
     if (timed) cudaEventRecord(h->ev[4], s);
-    h->launches += 6;
+}
+
+static int enqueue_attempt(vk_handle *h, int flags, bool timed) {
+    if (h->precision == VK_PREC_MIXED && !h->w.G32)
+        return fail(h, VK_EINVAL, "mixed precision not allocated on this handle");
+    ensure_geometry(h, flags);
+    enqueue_attempt_kernels(h, h->net(), h->batch(), flags, 1.E-22, 1.E-1, timed);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(h, VK_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     return VK_OK;
@@ -372,7 +414,8 @@ extern "C" int vk_chem_source(vk_handle *h, const double *y, double *dydt) {
     if (rc) return rc;
     size_t bytes = (size_t)h->L * h->ni * sizeof(double);
     if (y) VK_CUDA(h, cudaMemcpyAsync(h->w.y, y, bytes, cudaMemcpyHostToDevice, h->stream));
-    vk::launch_chem_only(h->net(), h->batch(), h->w.y, h->w.f, h->stream);
+    ensure_geometry(h, 0);
+    vk::launch_chem_only(h->net(), h->batch(), h->w.y, h->w.f, h->w.geo, h->stream);
     VK_CUDA(h, cudaGetLastError());
     VK_CUDA(h, cudaMemcpyAsync(dydt, h->w.f, bytes, cudaMemcpyDeviceToHost, h->stream));
     VK_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -457,7 +500,7 @@ extern "C" int vk_get_counters(vk_handle *h, int *counters) {
     int rc = need_batch(h);
     if (rc) return rc;
     if (!counters) return fail(h, VK_EINVAL, "counters is NULL");
-    VK_CUDA(h, cudaMemcpy(counters, h->rs.counters, (size_t)h->ncols * 4 * sizeof(int), cudaMemcpyDeviceToHost));
+    VK_CUDA(h, cudaMemcpy(counters, h->rs.counters, (size_t)h->ncols * VK_NCOUNTERS * sizeof(int), cudaMemcpyDeviceToHost));
     return VK_OK;
 }
 
@@ -501,8 +544,9 @@ extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double t
         h->hist_R = cc.conv_step;
         if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
     }
-    if (h->precision != VK_PREC_FP64 || !h->w.G)
-        return fail(h, VK_EINVAL, "vk_run needs the FP64 solver on this handle");
+    if (h->precision == VK_PREC_MIXED && !h->w.G32)
+        return fail(h, VK_EINVAL, "mixed precision not allocated on this handle");
+    ensure_geometry(h, cc.flags);
     DevNet net = h->net();
     DevBatch b = h->batch();
     b.active = h->rs.active;
@@ -520,13 +564,9 @@ extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double t
         VK_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         vk::Work &w = h->w;
         for (int it = 0; it < kGraphAttempts; ++it) {
-            vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, cc.flags, true, s);
-            vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, cc.flags, s);
-            vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
-            vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, cc.flags, false, s);
-            vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
-            vk::launch_stage(net, b, w, cc.flags, cc.mtol, cc.atol, s);
-            vk::launch_control(net, b, h->rs, cc, w.sol, w.ymix_out, w.delta, w.status, s);
+            enqueue_attempt_kernels(h, net, b, cc.flags, cc.mtol, cc.atol, false);
+            vk::launch_control(net, b, h->rs, cc, w.sol, w.ymix_out, w.delta, w.status,
+                               h->precision == VK_PREC_MIXED ? w.fallback : nullptr, w.geo, s);
         }
         vk::launch_count_active(h->rs.active, h->ncols, h->d_nactive, s);
         cudaError_t ec = cudaStreamEndCapture(s, &g);
@@ -541,7 +581,7 @@ extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double t
     int launches = 0;
     for (;;) {
         VK_CUDA(h, cudaGraphLaunch(h->gexec, s));
-        launches += kGraphAttempts * 7 + 1;
+        launches += kGraphAttempts * (h->precision == VK_PREC_MIXED ? 13 : 7) + 1;
         int nact = 0;
         VK_CUDA(h, cudaMemcpyAsync(&nact, h->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
         VK_CUDA(h, cudaStreamSynchronize(s));

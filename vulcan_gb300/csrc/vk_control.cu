@@ -17,6 +17,7 @@
 
 #include "vk_internal.cuh"
 #include "vk_control.cuh"
+#include "vk_geo.cuh"
 
 namespace vk {
 
@@ -193,8 +194,6 @@ __device__ void update_mu_dz(const DevNet &net, const DevBatch &b, const RunStat
         const int pref = rs.pref[c];
         double zco = 0.0;          // zco[pref] = 0 (reference level)
         // upward from the reference level
-        double zlo = 0.0;
-        double dz_prev = 0.0;
         for (int i = pref; i < nz; ++i) {
             double g = (i == pref) ? cc.gs : cc.gs * (cc.Rp / (cc.Rp + zco)) * (cc.Rp / (cc.Rp + zco));
             double Hp = KB_ * A(i, VK_ATM_TCO) / (mu[i] / NAVO_ * g);
@@ -204,7 +203,6 @@ __device__ void update_mu_dz(const DevNet &net, const DevBatch &b, const RunStat
             A(i, VK_ATM_DZ) = dz;
             zco += dz;
         }
-        (void)zlo; (void)dz_prev;
         // downward below the reference level
         double zup = 0.0;
         for (int i = pref - 1; i >= 0; --i) {
@@ -228,7 +226,9 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
                                                  const double *__restrict__ sol,
                                                  const double *__restrict__ ymix_sol,
                                                  const double *__restrict__ delta,
-                                                 const int *__restrict__ status) {
+                                                 const int *__restrict__ status,
+                                                 const int *__restrict__ fallback,
+                                                 double *__restrict__ geo) {
     __shared__ double red[8];
     __shared__ int redi[8];
     __shared__ double loss[VK_MAX_NATOM];
@@ -274,7 +274,8 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
         const double d = delta[c];
         rs.delta[c] = d;
         rs.natt[c] += 1;
-        rs.counters[c * 4 + 0] += 1;
+        rs.counters[c * VK_NCOUNTERS + 0] += 1;
+        if (fallback && fallback[c]) rs.counters[c * VK_NCOUNTERS + 4] += 1;
         int ok = (!neg) && (dl < cc.loss_eps) && (d <= cc.rtol);
         int giveup = 0;
         if (bad || status[c] != 0) {
@@ -282,9 +283,9 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
             rs.active[c] = 0;
             ok = 0;
         } else if (!ok) {
-            if (d > cc.rtol) rs.counters[c * 4 + 1] += 1;
-            else if (neg) rs.counters[c * 4 + 2] += 1;
-            else rs.counters[c * 4 + 3] += 1;
+            if (d > cc.rtol) rs.counters[c * VK_NCOUNTERS + 1] += 1;
+            else if (neg) rs.counters[c * VK_NCOUNTERS + 2] += 1;
+            else rs.counters[c * VK_NCOUNTERS + 3] += 1;
             double dt = rs.dt[c] * cc.dt_var_min;
             if (dt < cc.dt_min) { dt = cc.dt_min; giveup = 1; }
             rs.dt[c] = dt;
@@ -311,7 +312,19 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
     }
     // ---- accepted step: finalise (Integration loop body after one_step)
     const int count = rs.count[c];
-    if (count % cc.update_frq == 0) update_mu_dz(net, b, rs, cc, c, l0, nz, mu);
+    if (count % cc.update_frq == 0) {
+        update_mu_dz(net, b, rs, cc, c, l0, nz, mu);
+        // the transport geometry depends on g, dzi, Hpi: rebuild this column's
+        const GeoCol gc = make_geocol(rs.atm, b.Dzz, b.spf, b.col_off, c, n);
+        for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+            const int j = e / n, i = e - j * n;
+            double out[GEO_NF];
+            geo_coef(gc, j, i, cc.flags, out);
+            double *gl = geo + (size_t)(l0 + j) * GEO_NF * n;
+            for (int k = 0; k < GEO_NF; ++k) gl[k * n + i] = out[k];
+        }
+        __syncthreads();
+    }
     const double dtv = rs.dt[c];
     const double tn = rs.t[c] + dtv;
     const int R = cc.conv_step;
@@ -328,6 +341,7 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
         rs.t[c] = tn;
         rs.count[c] = count + 1;
         rs.steps_call[c] += 1;
+        rs.counters[c * VK_NCOUNTERS + 5] += 1;
         double d = rs.delta[c];
         if (d == 0) d = 0.01 * cc.rtol;
         double hf = 0.9 * sqrt(cc.rtol / d);
@@ -358,8 +372,8 @@ void launch_start(const DevNet &net, const DevBatch &b, const RunState &rs, cons
 
 void launch_control(const DevNet &net, const DevBatch &b, const RunState &rs, const RunCtrl &cc,
                     const double *sol, const double *ymix_sol, const double *delta,
-                    const int *status, cudaStream_t s) {
-    k_control<<<b.ncols, 256, 0, s>>>(net, b, rs, cc, sol, ymix_sol, delta, status);
+                    const int *status, const int *fallback, double *geo, cudaStream_t s) {
+    k_control<<<b.ncols, 256, 0, s>>>(net, b, rs, cc, sol, ymix_sol, delta, status, fallback, geo);
 }
 
 void launch_count_active(const int *active, int ncols, int *nactive, cudaStream_t s) {

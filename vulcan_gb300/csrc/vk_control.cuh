@@ -9,7 +9,7 @@ struct RunState {
     double *atm;                        // [L][VK_ATM_NF], same storage as DevBatch::atm
     double *dt, *t, *delta, *longdy, *longdydt;   // [ncols]
     int *count, *end_case, *active, *natt, *steps_call, *pref;  // [ncols]
-    int *counters;                      // [ncols][4]
+    int *counters;                      // [ncols][VK_NCOUNTERS]
     double *atom_ini, *loss, *loss_prev;  // [ncols][VK_MAX_NATOM]
     double *hist_y;                     // [conv_step][L][ni] ring of accepted states
     double *hist_t;                     // [ncols][conv_step]
@@ -28,7 +28,7 @@ void launch_start(const DevNet &net, const DevBatch &b, const RunState &rs, cons
                   cudaStream_t s);
 void launch_control(const DevNet &net, const DevBatch &b, const RunState &rs, const RunCtrl &cc,
                     const double *sol, const double *ymix_sol, const double *delta,
-                    const int *status, cudaStream_t s);
+                    const int *status, const int *fallback, double *geo, cudaStream_t s);
 void launch_count_active(const int *active, int ncols, int *nactive, cudaStream_t s);
 
 }  // namespace vk

@@ -49,6 +49,7 @@ struct vk_network {
     std::vector<int> jptr;             // [nnz+1]
     std::vector<int2> jterm;           // {w index, net stoichiometry}
     std::vector<int> jrow, jcol, jpos; // entry -> (s, q), s*ni+q
+    std::vector<int> jrowptr;          // [ni+1] entries are sorted by row
     std::vector<double> compo;         // [ni*natom]
 };
 
@@ -62,6 +63,7 @@ struct DevNet {
     const int *jptr;
     const int2 *jterm;
     const int *jpos;
+    const int *jrow, *jcol, *jrowptr;
     const double *compo;
 };
 
@@ -90,10 +92,14 @@ struct Work {                  // per-handle device work buffers
     double *y, *ymix, *yk2, *f, *k1, *k2, *z, *sol, *ymix_out;
     double *jv;                // [L][nnz]  -J_chem entries
     double *dA, *dB, *dC;      // [L][ni]   diffusion coefficients (A+Ai, B+Bi, C+Ci)
+    double *geo;               // [L][5][ni] state-free transport geometry (vk_geo.cuh)
     double *G;                 // [L][ni*ni] FP64 block inverses
-    float *G32;                // [L][ni*ni] FP32 block inverses (mixed mode)
-    double *rs, *cs;           // [L][ni] row / column scales (mixed mode)
+    float *G32;                // [L][ni*ni] FP32 inverses of the scaled blocks (mixed mode)
+    double *rs, *cs;           // [L][ni] power-of-two row / column scales (mixed mode)
     double *r, *dx;            // refinement residual / correction
+    float *zf;                 // [L][ni] FP32 forward-sweep vector (mixed mode)
+    int *fallback;             // [ncols] refinement did not converge -> FP64 path
+    int *sweeps;               // [1] most refinement sweeps any column needed
     double *dt;                // [ncols]
     double *delta;             // [ncols]
     int *status;               // [ncols]  VK_* per column (singular pivot ...)
@@ -101,7 +107,8 @@ struct Work {                  // per-handle device work buffers
 
 void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
                   double *jv, double *dA, double *dB, double *dC, const double *k1,
-                  const double *dt, int flags, bool with_jac, cudaStream_t s);
+                  const double *dt, const double *geo, int flags, bool with_jac, cudaStream_t s);
+void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flags, cudaStream_t s);
 void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
                        const double *rhs, double *z, int flags, cudaStream_t s);
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G,
@@ -112,5 +119,10 @@ void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G,
                       double *zbuf, double *x, cudaStream_t s);
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags,
                   double mtol, double atol, cudaStream_t s);
+void launch_lu_f32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
+void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
+                   double *x, const double *yscale, double *yk2, int max_sweeps, double tol,
+                   cudaStream_t s);
+cudaError_t init_mixed_kernels(int n);
 
 }  // namespace vk

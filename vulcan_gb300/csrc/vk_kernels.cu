@@ -21,12 +21,10 @@
 #include <math.h>
 
 #include "vk_internal.cuh"
+#include "vk_geo.cuh"
 #include "vk_gj.cuh"
 
 namespace vk {
-
-constexpr double KB = 1.38064852E-16;
-constexpr double NAVO = 6.02214086E+23;
 
 __device__ __forceinline__ double ipow(double x, int e) {
     double r = x;
@@ -37,98 +35,6 @@ __device__ __forceinline__ double ipow(double x, int e) {
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// Column geometry accessors --------------------------------------------------
-struct Col {
-    const double *atm;   // layer-major, VK_ATM_NF per layer
-    const double *Dzz;   // [layer][ni]
-    const double *ms;    // [ni]
-    const double *alpha;
-    int l0, nz, ni;
-    __device__ double a(int j, int f) const { return atm[(size_t)(l0 + j) * VK_ATM_NF + f]; }
-    __device__ double dzz(int j, int i) const { return Dzz[(size_t)(l0 + j) * ni + i]; }
-    // -1/Hpi + ms g/(Navo kb Ti) + alpha/Ti (T_{j+1}-T_j)/dzi at interface j+1/2
-    __device__ double phi(int j, int i, double g) const {
-        double Ti = a(j, VK_ATM_TI);
-        return -1. / a(j, VK_ATM_HPI) + ms[i] * g / (NAVO * KB * Ti)
-               + alpha[i] / Ti * (a(j + 1, VK_ATM_TCO) - a(j, VK_ATM_TCO)) / a(j, VK_ATM_DZI);
-    }
-};
-
-__device__ __forceinline__ Col make_col(const DevBatch &b, int c, int ni) {
-    Col cv;
-    cv.atm = b.atm;
-    cv.Dzz = b.Dzz;
-    cv.ms = b.spf + (size_t)c * VK_SP_NF * ni + VK_SP_MS * ni;
-    cv.alpha = b.spf + (size_t)c * VK_SP_NF * ni + VK_SP_ALPHA * ni;
-    cv.l0 = b.col_off[c];
-    cv.nz = b.col_off[c + 1] - cv.l0;
-    cv.ni = ni;
-    return cv;
-}
-
-// Transport coefficients of species i in layer j: dy_j/dt|_diff =
-// cA y_j + cB y_{j+1} + cC y_{j-1} (eddy A,B,C plus molecular Ai,Bi,Ci).
-__device__ void diff_coef(const Col &cv, int j, int i, double ysm, double ys0, double ysp,
-                          int flags, double &cA, double &cB, double &cC) {
-    const int nz = cv.nz;
-    double A = 0, B = 0, C = 0, Ai = 0, Bi = 0, Ci = 0;
-    const bool mol = flags & VK_F_MOLDIFF;
-    if (j == 0) {
-        double dzi = cv.a(0, VK_ATM_DZI), K = cv.a(0, VK_ATM_KZZ), vz = cv.a(0, VK_ATM_VZ);
-        A = -1. / dzi * (K / dzi) * (ysp + ys0) / 2. / ys0;
-        B = 1. / dzi * (K / dzi) * (ysp + ys0) / 2. / ysp;
-        A += -((vz > 0) * vz) / dzi;
-        B += -((vz < 0) * vz) / dzi;
-        if (mol) {
-            double D = cv.dzz(0, i), ph = cv.phi(0, i, cv.a(0, VK_ATM_G));
-            Ai = -1. / dzi * (D / dzi) * (ysp + ys0) / 2. / ys0 + 1. / dzi * D / 2. * ph;
-            Bi = 1. / dzi * (D / dzi) * (ysp + ys0) / 2. / ysp + 1. / dzi * D / 2. * ph;
-        }
-    } else if (j == nz - 1) {
-        int t = nz - 2;
-        double dzi = cv.a(t, VK_ATM_DZI), K = cv.a(t, VK_ATM_KZZ), vz = cv.a(t, VK_ATM_VZ);
-        A = -1. / dzi * (K / dzi) * (ys0 + ysm) / 2. / ys0;
-        C = 1. / dzi * (K / dzi) * (ys0 + ysm) / 2. / ysm;
-        A += ((vz < 0) * vz) / dzi;
-        C += ((vz > 0) * vz) / dzi;
-        if (mol) {
-            double D = cv.dzz(t, i), ph = cv.phi(t, i, cv.a(nz - 1, VK_ATM_G));
-            Ai = -1. / dzi * (D / dzi) * (ys0 + ysm) / 2. / ys0 - 1. / dzi * D / 2. * ph;
-            Ci = 1. / dzi * (D / dzi) * (ys0 + ysm) / 2. / ysm - 1. / dzi * D / 2. * ph;
-        }
-    } else {
-        double dm = cv.a(j - 1, VK_ATM_DZI), dp = cv.a(j, VK_ATM_DZI);
-        double Km = cv.a(j - 1, VK_ATM_KZZ), Kp = cv.a(j, VK_ATM_KZZ);
-        double vm = cv.a(j - 1, VK_ATM_VZ), vp = cv.a(j, VK_ATM_VZ);
-        double da = 0.5 * (dm + dp);
-        if (mol) {
-            A = -1. / da * (Kp / dp * (ysp + ys0) / 2. + Km / dm * (ys0 + ysm) / 2.) / ys0;
-            B = 1. / da * Kp / dp * (ysp + ys0) / 2. / ysp;
-            C = 1. / da * Km / dm * (ys0 + ysm) / 2. / ysm;
-        } else {
-            A = -2. / (dm + dp) * (Kp / dp * (ysp + ys0) / 2. + Km / dm * (ys0 + ysm) / 2.) / ys0;
-            B = 2. / (dm + dp) * Kp / dp * (ysp + ys0) / 2. / ysp;
-            C = 2. / (dm + dp) * Km / dm * (ys0 + ysm) / 2. / ysm;
-        }
-        A += -((vp > 0) * vp - (vm < 0) * vm) / da;
-        B += -((vp < 0) * vp) / da;
-        C += ((vm > 0) * vm) / da;
-        if (mol) {
-            double Dm = cv.dzz(j - 1, i), Dp = cv.dzz(j, i);
-            double gm = cv.a(j - 1, VK_ATM_G), g0 = cv.a(j, VK_ATM_G), gp = cv.a(j + 1, VK_ATM_G);
-            Ai = -1. / da * (Dp / dp * (ysp + ys0) / 2. + Dm / dm * (ys0 + ysm) / 2.) / ys0;
-            Bi = 1. / da * Dp / dp * (ysp + ys0) / 2. / ysp;
-            Ci = 1. / da * Dm / dm * (ys0 + ysm) / 2. / ysm;
-            Ai += 1. / (2. * da) * (Dp * cv.phi(j, i, g0) - Dm * cv.phi(j - 1, i, g0));
-            Bi += 1. / (2. * da) * Dp * cv.phi(j, i, gp);
-            Ci += -1. / (2. * da) * Dm * cv.phi(j - 1, i, gm);
-        }
-    }
-    cA = A + Ai;
-    cB = B + Bi;
-    cC = C + Ci;
 }
 
 // Value of one side of pair p in the generated lambda order k*t1*t2*...
@@ -167,21 +73,21 @@ __global__ void __launch_bounds__(128)
 k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict__ f,
         double *__restrict__ jv, double *__restrict__ dA, double *__restrict__ dB,
         double *__restrict__ dC, const double *__restrict__ k1, const double *__restrict__ dt,
-        int flags, int chem_only) {
+        const double *__restrict__ geo, int flags, int chem_only) {
     extern __shared__ double sm[];
     const int ni = net.ni;
     const int l = blockIdx.x;
     const int c = b.lay_col[l];
     if (b.active && !b.active[c]) return;
-    const Col cv = make_col(b, c, ni);
-    const int j = l - cv.l0;
+    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    const int j = l - l0;
     double *ys = sm;                       // [3][ni] layers j-1, j, j+1
     double *sums = ys + 3 * ni;            // [4]
     double *v = sums + 4;                  // [max(npair, nw)]
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int t = tid; t < 3 * ni; t += nth) {
         int jj = j - 1 + t / ni;
-        ys[t] = (jj >= 0 && jj < cv.nz) ? y[(size_t)(cv.l0 + jj) * ni + (t % ni)] : 0.0;
+        ys[t] = (jj >= 0 && jj < nz) ? y[(size_t)(l0 + jj) * ni + (t % ni)] : 0.0;
     }
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
@@ -192,7 +98,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
         if (lane == 0) sums[warp] = s;
     }
     const double *yl = ys + ni;
-    const double M = cv.a(j, VK_ATM_M);
+    const double *al = b.atm + (size_t)l * VK_ATM_NF;
+    const double M = al[VK_ATM_M];
     const double *kl = b.k + (size_t)l * net.nr;
     // net rate of each pair
     for (int p = tid; p < net.npair; p += nth) {
@@ -201,35 +108,42 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
         v[p] = side_rate(kk.x, pd, 0, yl, M) - side_rate(kk.y, pd, 1, yl, M);
     }
     __syncthreads();
-    // production - loss gather (generated chemdf order) + transport
+    // ysum ratios of the transport operator (state dependent part)
     const double ysm = sums[0], ys0 = sums[1], ysp = sums[2];
+    const bool has_up = j + 1 < nz, has_dn = j > 0;
+    const double qU0 = has_up ? (ysp + ys0) / (2. * ys0) : 0.0;
+    const double qD0 = has_dn ? (ys0 + ysm) / (2. * ys0) : 0.0;
+    const double qUp = has_up ? (ysp + ys0) / (2. * ysp) : 0.0;
+    const double qDm = has_dn ? (ys0 + ysm) / (2. * ysm) : 0.0;
     const double hinv = k1 ? 2. / (R_ROS * dt[c]) : 0.0;
+    const double *gl = geo + (size_t)l * GEO_NF * ni;
+    const double *spf = b.spf + (size_t)c * VK_SP_NF * ni;
+    // production - loss gather (generated chemdf order) + transport
     for (int s = tid; s < ni; s += nth) {
         double acc = 0.0;
         for (int e = net.src_ptr[s]; e < net.src_ptr[s + 1]; ++e) {
             const int2 t = net.src[e];
             acc = __dadd_rn(acc, __dmul_rn((double)t.y, v[t.x]));
         }
-        double cA, cB, cC;
-        diff_coef(cv, j, s, ysm, ys0, ysp, flags, cA, cB, cC);
+        const double gU = gl[s], gD = gl[ni + s];
+        double cA = -gU * qU0 - gD * qD0 + gl[2 * ni + s];
+        double cB = has_up ? gU * qUp + gl[3 * ni + s] : 0.0;
+        double cC = has_dn ? gD * qDm + gl[4 * ni + s] : 0.0;
         double out = acc;
         if (!chem_only) {
             double dif = cA * yl[s];
-            if (j + 1 < cv.nz) dif += cB * ys[2 * ni + s];
-            if (j > 0) dif += cC * ys[s];
-            if ((flags & VK_F_TOPFLUX) && j == cv.nz - 1)
-                dif += b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_TOPFLUX * ni + s] / cv.a(cv.nz - 2, VK_ATM_DZI);
+            if (has_up) dif += cB * ys[2 * ni + s];
+            if (has_dn) dif += cC * ys[s];
+            if ((flags & VK_F_TOPFLUX) && j == nz - 1)
+                dif += spf[VK_SP_TOPFLUX * ni + s] / b.atm[(size_t)(l - 1) * VK_ATM_NF + VK_ATM_DZI];
             if ((flags & VK_F_BOTFLUX) && j == 0)
-                dif += (b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_BOTFLUX * ni + s]
-                        - yl[s] * b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_BOTVDEP * ni + s])
-                       / cv.a(0, VK_ATM_DZI);
+                dif += (spf[VK_SP_BOTFLUX * ni + s] - yl[s] * spf[VK_SP_BOTVDEP * ni + s]) / al[VK_ATM_DZI];
             out = acc + dif;
             if (k1) out = out - hinv * k1[(size_t)l * ni + s];
         }
         f[(size_t)l * ni + s] = out;
         if (JAC) {
-            if ((flags & VK_F_BOTFLUX) && j == 0)
-                cA -= b.spf[(size_t)c * VK_SP_NF * ni + VK_SP_BOTVDEP * ni + s] / cv.a(0, VK_ATM_DZI);
+            if ((flags & VK_F_BOTFLUX) && j == 0) cA -= spf[VK_SP_BOTVDEP * ni + s] / al[VK_ATM_DZI];
             dA[(size_t)l * ni + s] = cA;
             dB[(size_t)l * ni + s] = cB;
             dC[(size_t)l * ni + s] = cC;
@@ -454,6 +368,27 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
     }
 }
 
+// Transport geometry of every (layer, species) of the active columns.
+__global__ void __launch_bounds__(256)
+k_geometry(DevNet net, DevBatch b, double *__restrict__ geo, int flags) {
+    const int ni = net.ni;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)b.L * ni) return;
+    const int l = (int)(e / ni), i = (int)(e - (long long)l * ni);
+    const int c = b.lay_col[l];
+    if (b.active && !b.active[c]) return;
+    const GeoCol cv = make_geocol(b.atm, b.Dzz, b.spf, b.col_off, c, ni);
+    double out[GEO_NF];
+    geo_coef(cv, l - cv.l0, i, flags, out);
+    double *gl = geo + (size_t)l * GEO_NF * ni;
+    for (int k = 0; k < GEO_NF; ++k) gl[k * ni + i] = out[k];
+}
+
+void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flags, cudaStream_t s) {
+    long long n = (long long)b.L * net.ni;
+    k_geometry<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(net, b, geo, flags);
+}
+
 // ---------------------------------------------------------------------------
 static size_t rates_smem(const DevNet &net);
 
@@ -477,19 +412,19 @@ static size_t rates_smem(const DevNet &net) {
 
 void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
                   double *jv, double *dA, double *dB, double *dC, const double *k1,
-                  const double *dt, int flags, bool with_jac, cudaStream_t s) {
+                  const double *dt, const double *geo, int flags, bool with_jac, cudaStream_t s) {
     size_t sm = rates_smem(net);
     if (with_jac)
-        k_rates<true><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, flags, 0);
+        k_rates<true><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, geo, flags, 0);
     else
-        k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, flags, 0);
+        k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, geo, flags, 0);
 }
 
 void launch_chem_only(const DevNet &net, const DevBatch &b, const double *y, double *f,
-                      cudaStream_t s) {
+                      const double *geo, cudaStream_t s) {
     size_t sm = rates_smem(net);
     k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, nullptr, nullptr, nullptr, nullptr,
-                                        nullptr, nullptr, 0, 1);
+                                        nullptr, nullptr, geo, 0, 1);
 }
 
 void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,

@@ -123,6 +123,9 @@ extern "C" int vk_network_compile(const vk_network_desc *d, vk_network **out) {
         n->jterm.insert(n->jterm.end(), e.second.begin(), e.second.end());
         n->jptr.push_back((int)n->jterm.size());
     }
+    n->jrowptr.assign(ni + 1, 0);
+    for (int r : n->jrow) n->jrowptr[r + 1]++;
+    for (int r = 0; r < ni; ++r) n->jrowptr[r + 1] += n->jrowptr[r];
     n->compo.assign(d->compo, d->compo + (size_t)ni * d->natom);
     *out = n;
     return VK_OK;

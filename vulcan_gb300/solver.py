@@ -256,8 +256,13 @@ class Ros2Handle:
                                  ptr(end, C.c_int), ptr(delta)), self.h)
         return dict(y=y, ymix=ymix, dt=dt, t=t, count=count, end_case=end, delta=delta)
 
+    def set_precision(self, precision, max_refine=6, refine_tol=1e-13):
+        check(lib().vk_set_precision(self.h, int(precision), int(max_refine), float(refine_tol)), self.h)
+
     def counters(self):
-        c = np.empty((self.batch.ncols, 4), dtype=np.int32)
+        """[ncols][6]: attempts, delta / negativity / loss rejections, attempts
+        redone in FP64 (mixed mode), accepted steps."""
+        c = np.empty((self.batch.ncols, capi.NCOUNTERS), dtype=np.int32)
         check(lib().vk_get_counters(self.h, ptr(c, C.c_int)), self.h)
         return c
 
