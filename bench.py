@@ -261,7 +261,8 @@ def run_profile(args):
     for _ in range(args.attempts):
         h.attempt(dt)
     print(json.dumps({'profile': True, 'precision': args.precision, 'ncols': b.ncols,
-                      'layers': int(b.L), 'attempts': args.attempts, 'attempt_ms': h.timing()}))
+                      'layers': int(b.L), 'attempts': args.attempts, 'attempt_ms': h.timing(),
+                      'refine_sweeps_fallbacks': h.refine_stats()}))
     h.close()
 
 

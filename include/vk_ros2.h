@@ -121,6 +121,9 @@ VK_API int  vk_create(const vk_network *net, int max_cols, int max_layers, int p
                vk_handle **out);
 VK_API void vk_destroy(vk_handle *h);
 VK_API const char *vk_last_error(const vk_handle *h);   /* h may be NULL */
+/* Switch the linear-solve precision; max_refine caps the refinement sweeps
+ * (default 6) and refine_tol is the convergence test on the correction
+ * relative to |x| + |y| + 1e-10 n_0 (default 1e-10). */
 VK_API int  vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol);
 
 /* Load a batch of columns.  L = sum(nz).  k is [L][2*npair] (layer-major,
@@ -198,6 +201,9 @@ VK_API int  vk_block_solve_noalloc(int nz, int ni, const double *D, const double
                                    void *stream);
 
 /* ---- diagnostics (used by the parity tests) ---- */
+/* Mixed precision, last attempt: the most refinement sweeps any column
+ * needed, and how many columns were redone in FP64 (0/0 in FP64 mode). */
+VK_API int  vk_get_refine_stats(vk_handle *h, int *max_sweeps, int *n_fallback);
 /* Message of the last failed vk_network_compile on this thread. */
 VK_API const char *vk_network_last_error(void);
 /* Chemistry source term alone (the generated chemdf) of state y [L][ni]. */

@@ -33,7 +33,7 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_update_k', 'vk_ros2_attempt', 'vk_set_atom_ini', 'vk_set_column_info',
            'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
-           'vk_block_solve_noalloc')
+           'vk_block_solve_noalloc', 'vk_get_refine_stats')
 
 
 class VkNetworkDesc(C.Structure):
@@ -102,6 +102,7 @@ def lib(path=None):
         'vk_chem_source': (i, [vp, pd, pd]),
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),
         'vk_block_solve_noalloc': (i, [i, i, vp, vp, vp, vp, vp, vp]),
+        'vk_get_refine_stats': (i, [vp, pi, pi]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

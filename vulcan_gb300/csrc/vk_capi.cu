@@ -26,7 +26,7 @@ struct vk_handle {
     int ni = 0, npair = 0, nr = 0, nnz = 0, nw = 0, natom = 0;
     int max_cols = 0, max_layers = 0, precision = VK_PREC_FP64;
     int max_refine = 6;
-    double refine_tol = 1e-13;
+    double refine_tol = 1e-10;
     int geo_flags = -1;         // flags the transport geometry was built for (-1: stale)
     int ncols = 0, L = 0;
     std::vector<int> col_off;
@@ -34,11 +34,12 @@ struct vk_handle {
     PairDesc *d_pairs = nullptr;
     int *d_src_ptr = nullptr;
     int2 *d_src = nullptr;
+    double *d_src_nu = nullptr, *d_jterm_nu = nullptr;
     WDesc *d_w = nullptr;
     int *d_jptr = nullptr;
     int2 *d_jterm = nullptr;
     int *d_jpos = nullptr;
-    int *d_jrow = nullptr, *d_jcol = nullptr, *d_jrowptr = nullptr;
+    int *d_jrow = nullptr, *d_jcol = nullptr, *d_jrowptr = nullptr, *d_jmap = nullptr;
     double *d_compo = nullptr;
     // batch
     int *d_col_off = nullptr, *d_lay_col = nullptr;
@@ -61,8 +62,9 @@ struct vk_handle {
         DevNet n;
         n.ni = ni; n.npair = npair; n.nr = nr; n.nw = nw; n.nnz = nnz; n.natom = natom;
         n.pairs = d_pairs; n.src_ptr = d_src_ptr; n.src = d_src; n.w = d_w;
+        n.src_nu = d_src_nu; n.jterm_nu = d_jterm_nu;
         n.jptr = d_jptr; n.jterm = d_jterm; n.jpos = d_jpos; n.compo = d_compo;
-        n.jrow = d_jrow; n.jcol = d_jcol; n.jrowptr = d_jrowptr;
+        n.jrow = d_jrow; n.jcol = d_jcol; n.jrowptr = d_jrowptr; n.jmap = d_jmap;
         return n;
     }
     DevBatch batch() const {
@@ -156,6 +158,8 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_pairs, net->pairs));
     TRY(upload(h, &h->d_src_ptr, net->src_ptr));
     TRY(upload(h, &h->d_src, net->src));
+    TRY(upload(h, &h->d_src_nu, net->src_nu));
+    TRY(upload(h, &h->d_jterm_nu, net->jterm_nu));
     TRY(upload(h, &h->d_w, net->w));
     TRY(upload(h, &h->d_jptr, net->jptr));
     TRY(upload(h, &h->d_jterm, net->jterm));
@@ -164,6 +168,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_jrow, net->jrow));
     TRY(upload(h, &h->d_jcol, net->jcol));
     TRY(upload(h, &h->d_jrowptr, net->jrowptr));
+    TRY(upload(h, &h->d_jmap, net->jmap));
     const size_t L = (size_t)max_layers, ni = (size_t)h->ni;
     TRY(dalloc(h, &h->d_col_off, max_cols + 1));
     TRY(dalloc(h, &h->d_lay_col, L));
@@ -190,6 +195,8 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
                                                   : fail(h, VK_ECUDA, "cudaFuncSetAttribute failed"));
     TRY(vk::init_mixed_kernels(h->ni) == cudaSuccess ? VK_OK
                                                      : fail(h, VK_ECUDA, "cudaFuncSetAttribute (mixed) failed"));
+    TRY(vk::init_lureg_kernels(h->ni) == cudaSuccess ? VK_OK
+                                                     : fail(h, VK_ECUDA, "cudaFuncSetAttribute (LU) failed"));
     // per-column run state (small); the history ring is sized at the first vk_run
     vk::RunState &r = h->rs;
     r.y = w.y; r.ymix = w.ymix; r.dt = w.dt; r.delta = w.delta; r.atm = h->d_atm;
@@ -334,7 +341,7 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
     vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
     if (timed) cudaEventRecord(h->ev[1], s);
     if (h->precision == VK_PREC_FP64) {
-        vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, flags, s);
+        vk::launch_lu_reg64(net, b, w, w.f, w.z, s);
         if (timed) cudaEventRecord(h->ev[2], s);
         vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
         vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
@@ -342,7 +349,8 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         h->launches += 6;
     } else {
         cudaMemsetAsync(w.fallback, 0, b.ncols * sizeof(int), s);
-        vk::launch_lu_f32(net, b, w, s);
+        cudaMemsetAsync(w.sweeps, 0, sizeof(int), s);
+        vk::launch_lu_reg32(net, b, w, s);
         if (timed) cudaEventRecord(h->ev[2], s);
         vk::launch_refine(net, b, w, w.f, w.k1, w.y, w.yk2, h->max_refine, h->refine_tol, s);
         vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
@@ -351,7 +359,7 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         DevBatch bf = b;
         bf.active = w.fallback;
         vk::launch_rates(net, bf, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
-        vk::launch_lu_fwd_f64(net, bf, w, w.f, w.z, flags, s);
+        vk::launch_lu_reg64(net, bf, w, w.f, w.z, s);
         vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
         vk::launch_rates(net, bf, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
         vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
@@ -601,5 +609,26 @@ extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double t
     VK_CUDA(h, cudaMemcpy(ec.data(), h->rs.end_case, h->ncols * sizeof(int), cudaMemcpyDeviceToHost));
     for (int c = 0; c < h->ncols; ++c)
         if (ec[c] < 0) return fail(h, -ec[c], "column " + std::to_string(c) + " stopped with error " + std::to_string(-ec[c]));
+    return VK_OK;
+}
+
+extern "C" int vk_get_refine_stats(vk_handle *h, int *max_sweeps, int *n_fallback) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (h->precision != VK_PREC_MIXED) {
+        if (max_sweeps) *max_sweeps = 0;
+        if (n_fallback) *n_fallback = 0;
+        return VK_OK;
+    }
+    int sw = 0;
+    std::vector<int> fb(h->ncols);
+    VK_CUDA(h, cudaMemcpy(&sw, h->w.sweeps, sizeof(int), cudaMemcpyDeviceToHost));
+    VK_CUDA(h, cudaMemcpy(fb.data(), h->w.fallback, h->ncols * sizeof(int), cudaMemcpyDeviceToHost));
+    if (max_sweeps) *max_sweeps = sw;
+    if (n_fallback) {
+        int nf = 0;
+        for (int v : fb) nf += v != 0;
+        *n_fallback = nf;
+    }
     return VK_OK;
 }

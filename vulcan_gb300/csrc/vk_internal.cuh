@@ -44,12 +44,15 @@ struct vk_network {
     int ni = 0, npair = 0, natom = 0;
     std::vector<PairDesc> pairs;
     std::vector<int> src_ptr;          // [ni+1]
-    std::vector<int2> src;             // {pair, net stoichiometry}
+    std::vector<int2> src;             // {pair, coefficient code}  (code: +1, -1, 0 = see src_nu)
+    std::vector<double> src_nu;        // coefficient of each src term
     std::vector<WDesc> w;              // derivative terms
     std::vector<int> jptr;             // [nnz+1]
-    std::vector<int2> jterm;           // {w index, net stoichiometry}
+    std::vector<int2> jterm;           // {w index, coefficient code}
+    std::vector<double> jterm_nu;
     std::vector<int> jrow, jcol, jpos; // entry -> (s, q), s*ni+q
     std::vector<int> jrowptr;          // [ni+1] entries are sorted by row
+    std::vector<int> jmap;             // [ni*ni] entry at (s, q) or -1
     std::vector<double> compo;         // [ni*natom]
 };
 
@@ -59,11 +62,13 @@ struct DevNet {
     const PairDesc *pairs;
     const int *src_ptr;
     const int2 *src;
+    const double *src_nu;
     const WDesc *w;
     const int *jptr;
     const int2 *jterm;
+    const double *jterm_nu;
     const int *jpos;
-    const int *jrow, *jcol, *jrowptr;
+    const int *jrow, *jcol, *jrowptr, *jmap;
     const double *compo;
 };
 
@@ -124,5 +129,9 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
                    double *x, const double *yscale, double *yk2, int max_sweeps, double tol,
                    cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
+cudaError_t init_lureg_kernels(int n);
+void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
+                     double *z, cudaStream_t s);
+void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
 
 }  // namespace vk

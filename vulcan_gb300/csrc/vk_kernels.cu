@@ -37,33 +37,48 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// acc + c*v for a coefficient code (+1, -1: signed add without a multiply;
+// 0: multiply by the tabulated coefficient).  Bit-identical to the
+// reference's "acc -1*v" / "acc +2*v" terms.
+__device__ __forceinline__ double add_coef(double acc, int code, double nu, double v) {
+    if (code == 1) return __dadd_rn(acc, v);
+    if (code == -1) return __dadd_rn(acc, __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull));
+    return __dadd_rn(acc, __dmul_rn(nu, v));
+}
+
 // Value of one side of pair p in the generated lambda order k*t1*t2*...
-__device__ __forceinline__ double side_rate(double kk, const PairDesc &pd, int side,
+__device__ __forceinline__ double side_rate(double kk, const PairDesc *pd, int side,
                                             const double *yl, double M) {
     double v = kk;
-    for (int t = 0; t < pd.nt[side]; ++t) {
-        int s = pd.tsp[side][t];
-        double f = s < 0 ? M : yl[s];
-        v = __dmul_rn(v, ipow(f, pd.tnu[side][t]));
+    const int nt = __ldg(&pd->nt[side]);
+    for (int t = 0; t < nt; ++t) {
+        const int s = __ldg(&pd->tsp[side][t]);
+        const double f = s < 0 ? M : yl[s];
+        const int e = __ldg(&pd->tnu[side][t]);
+        v = __dmul_rn(v, e == 1 ? f : ipow(f, e));
     }
     return v;
 }
 
-// d/dy_q of kk * M^m * prod y_s^e over merged factors; pos = index of q.
-__device__ __forceinline__ double side_deriv(double kk, const int16_t *sp, const uint8_t *nu,
-                                             int n, int m, int pos, const double *yl, double M) {
-    double v = kk;
-    for (int t = 0; t < m; ++t) v *= M;
+// d/dy_q of kM * prod y_s^e over merged factors (kM = k M^m); pos = index of q.
+__device__ __forceinline__ double side_deriv(double kM, const int16_t *sp, const uint8_t *nu,
+                                             int n, int pos, const double *yl) {
+    double v = kM;
     for (int t = 0; t < n; ++t) {
-        double yv = yl[sp[t]];
-        int e = nu[t];
+        const double yv = yl[__ldg(sp + t)];
+        const int e = __ldg(nu + t);
         if (t == pos) {
-            if (e > 1) v *= (double)e * ipow(yv, e - 1);
+            if (e == 2) v *= yv + yv;
+            else if (e > 2) v *= (double)e * ipow(yv, e - 1);
         } else {
             v *= ipow(yv, e);
         }
     }
     return v;
+}
+
+__device__ __forceinline__ double mpow(double M, int m) {
+    return m == 0 ? 1.0 : (m == 1 ? M : (m == 2 ? M * M : M * M * M));
 }
 
 // ---------------------------------------------------------------------------
@@ -84,6 +99,7 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     double *ys = sm;                       // [3][ni] layers j-1, j, j+1
     double *sums = ys + 3 * ni;            // [4]
     double *v = sums + 4;                  // [max(npair, nw)]
+    double *kM = v + (net.npair > net.nw ? net.npair : net.nw);   // [2*npair] (JAC only)
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int t = tid; t < 3 * ni; t += nth) {
         int jj = j - 1 + t / ni;
@@ -103,9 +119,13 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     const double *kl = b.k + (size_t)l * net.nr;
     // net rate of each pair
     for (int p = tid; p < net.npair; p += nth) {
-        const PairDesc pd = net.pairs[p];
+        const PairDesc *pd = net.pairs + p;
         const double2 kk = reinterpret_cast<const double2 *>(kl)[p];
         v[p] = side_rate(kk.x, pd, 0, yl, M) - side_rate(kk.y, pd, 1, yl, M);
+        if (JAC) {
+            kM[2 * p] = kk.x * mpow(M, __ldg(&pd->fm));
+            kM[2 * p + 1] = kk.y * mpow(M, __ldg(&pd->rm));
+        }
     }
     __syncthreads();
     // ysum ratios of the transport operator (state dependent part)
@@ -123,7 +143,7 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
         double acc = 0.0;
         for (int e = net.src_ptr[s]; e < net.src_ptr[s + 1]; ++e) {
             const int2 t = net.src[e];
-            acc = __dadd_rn(acc, __dmul_rn((double)t.y, v[t.x]));
+            acc = add_coef(acc, t.y, t.y ? 0.0 : net.src_nu[e], v[t.x]);
         }
         const double gU = gl[s], gD = gl[ni + s];
         double cA = -gU * qU0 - gD * qD0 + gl[2 * ni + s];
@@ -154,11 +174,10 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     // derivative terms d v_p / d y_q
     for (int t = tid; t < net.nw; t += nth) {
         const WDesc wd = net.w[t];
-        const PairDesc pd = net.pairs[wd.pair];
-        const double2 kk = reinterpret_cast<const double2 *>(kl)[wd.pair];
+        const PairDesc *pd = net.pairs + wd.pair;
         double d = 0.0;
-        if (wd.fpos >= 0) d += side_deriv(kk.x, pd.fsp, pd.fnu, pd.nf, pd.fm, wd.fpos, yl, M);
-        if (wd.rpos >= 0) d -= side_deriv(kk.y, pd.rsp, pd.rnu, pd.nr, pd.rm, wd.rpos, yl, M);
+        if (wd.fpos >= 0) d = side_deriv(kM[2 * wd.pair], pd->fsp, pd->fnu, __ldg(&pd->nf), wd.fpos, yl);
+        if (wd.rpos >= 0) d -= side_deriv(kM[2 * wd.pair + 1], pd->rsp, pd->rnu, __ldg(&pd->nr), wd.rpos, yl);
         v[t] = d;
     }
     __syncthreads();
@@ -167,7 +186,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
         double acc = 0.0;
         for (int t = net.jptr[e]; t < net.jptr[e + 1]; ++t) {
             const int2 jt = net.jterm[t];
-            acc += (double)jt.y * v[jt.x];
+            acc = jt.y == 1 ? acc + v[jt.x]
+                : (jt.y == -1 ? acc - v[jt.x] : fma(net.jterm_nu[t], v[jt.x], acc));
         }
         jl[e] = -acc;                      // entries of -J (neg_symjac)
     }
@@ -407,7 +427,7 @@ cudaError_t init_kernels(const DevNet &net) {
 
 static size_t rates_smem(const DevNet &net) {
     int m = net.npair > net.nw ? net.npair : net.nw;
-    return (size_t)(3 * net.ni + 4 + m) * sizeof(double);
+    return (size_t)(3 * net.ni + 4 + m + 2 * net.npair) * sizeof(double);
 }
 
 void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,

@@ -234,10 +234,8 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 float s = 0.0f;
                 for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
                 for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) zf[l * n + r] = s;
+                if (lane == 0) { zf[l * n + r] = s; vout[r] = s; }
             }
-            __syncthreads();
-            for (int t = tid; t < n; t += nth) vout[t] = zf[l * n + t];
             __syncthreads();
         }
         // back: x~_j = z~_j + G~_j (R_j dB_j S_{j+1} x~_{j+1}); x += S_j x~_j

@@ -126,6 +126,18 @@ extern "C" int vk_network_compile(const vk_network_desc *d, vk_network **out) {
     n->jrowptr.assign(ni + 1, 0);
     for (int r : n->jrow) n->jrowptr[r + 1]++;
     for (int r = 0; r < ni; ++r) n->jrowptr[r + 1] += n->jrowptr[r];
+    n->jmap.assign((size_t)ni * ni, -1);
+    for (size_t e = 0; e < n->jpos.size(); ++e) n->jmap[n->jpos[e]] = (int)e;
+    // coefficient codes: +1 / -1 are applied as a signed add (exact, no
+    // multiply); other coefficients multiply from the double table
+    for (auto &t : n->src) {
+        n->src_nu.push_back((double)t.y);
+        t.y = (t.y == 1 || t.y == -1) ? t.y : 0;
+    }
+    for (auto &t : n->jterm) {
+        n->jterm_nu.push_back((double)t.y);
+        t.y = (t.y == 1 || t.y == -1) ? t.y : 0;
+    }
     n->compo.assign(d->compo, d->compo + (size_t)ni * d->natom);
     *out = n;
     return VK_OK;

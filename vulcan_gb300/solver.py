@@ -256,7 +256,13 @@ class Ros2Handle:
                                  ptr(end, C.c_int), ptr(delta)), self.h)
         return dict(y=y, ymix=ymix, dt=dt, t=t, count=count, end_case=end, delta=delta)
 
-    def set_precision(self, precision, max_refine=6, refine_tol=1e-13):
+    def refine_stats(self):
+        """(most sweeps any column needed, columns redone in FP64) of the last attempt."""
+        a, b = C.c_int(), C.c_int()
+        check(lib().vk_get_refine_stats(self.h, C.byref(a), C.byref(b)), self.h)
+        return a.value, b.value
+
+    def set_precision(self, precision, max_refine=6, refine_tol=1e-10):
         check(lib().vk_set_precision(self.h, int(precision), int(max_refine), float(refine_tol)), self.h)
 
     def counters(self):
