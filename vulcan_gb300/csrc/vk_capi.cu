@@ -184,7 +184,10 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &w.geo, L * 5 * ni));
     // FP64 inverses always (the mixed path falls back to them per column)
     TRY(dalloc(h, &w.G, L * ni * ni));
-    if (precision == VK_PREC_MIXED) TRY(dalloc(h, &w.G32, L * ni * ni));
+    if (precision == VK_PREC_MIXED) {
+        TRY(dalloc(h, &w.G32, L * (size_t)((ni * ni + 3) & ~3)));
+        TRY(dalloc(h, &w.D32, L * (size_t)((ni * ni + 3) & ~3)));
+    }
     TRY(dalloc(h, &w.zf, L * ni));
     TRY(dalloc(h, &w.fallback, max_cols));
     TRY(dalloc(h, &w.sweeps, 1));
@@ -195,7 +198,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
                                                   : fail(h, VK_ECUDA, "cudaFuncSetAttribute failed"));
     TRY(vk::init_mixed_kernels(h->ni) == cudaSuccess ? VK_OK
                                                      : fail(h, VK_ECUDA, "cudaFuncSetAttribute (mixed) failed"));
-    TRY(vk::init_lureg_kernels(h->ni) == cudaSuccess ? VK_OK
+    TRY(vk::init_lureg_kernels(h->net()) == cudaSuccess ? VK_OK
                                                      : fail(h, VK_ECUDA, "cudaFuncSetAttribute (LU) failed"));
     // per-column run state (small); the history ring is sized at the first vk_run
     vk::RunState &r = h->rs;
@@ -220,7 +223,9 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
 extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol) {
     if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
     if (precision == VK_PREC_MIXED && !h->w.G32) {
-        int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * h->ni * h->ni);
+        const size_t st = (size_t)((h->ni * h->ni + 3) & ~3);
+        int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * st);
+        if (!rc) rc = dalloc(h, &h->w.D32, (size_t)h->max_layers * st);
         if (rc) return rc;
     }
     if (precision != VK_PREC_FP64 && precision != VK_PREC_MIXED)
@@ -341,7 +346,7 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
     vk::launch_rates(net, b, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
     if (timed) cudaEventRecord(h->ev[1], s);
     if (h->precision == VK_PREC_FP64) {
-        vk::launch_lu_reg64(net, b, w, w.f, w.z, s);
+        vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, flags, s);
         if (timed) cudaEventRecord(h->ev[2], s);
         vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
         vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
@@ -359,7 +364,7 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         DevBatch bf = b;
         bf.active = w.fallback;
         vk::launch_rates(net, bf, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
-        vk::launch_lu_reg64(net, bf, w, w.f, w.z, s);
+        vk::launch_lu_fwd_f64(net, bf, w, w.f, w.z, flags, s);
         vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
         vk::launch_rates(net, bf, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
         vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);

@@ -103,6 +103,7 @@ struct Work {                  // per-handle device work buffers
     double *rs, *cs;           // [L][ni] power-of-two row / column scales (mixed mode)
     double *r, *dx;            // refinement residual / correction
     float *zf;                 // [L][ni] FP32 forward-sweep vector (mixed mode)
+    float *D32;                // [L][stride] dense scaled FP32 blocks (mixed mode)
     int *fallback;             // [ncols] refinement did not converge -> FP64 path
     int *sweeps;               // [1] most refinement sweeps any column needed
     double *dt;                // [ncols]
@@ -124,12 +125,11 @@ void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G,
                       double *zbuf, double *x, cudaStream_t s);
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags,
                   double mtol, double atol, cudaStream_t s);
-void launch_lu_f32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
 void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
                    double *x, const double *yscale, double *yk2, int max_sweeps, double tol,
                    cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
-cudaError_t init_lureg_kernels(int n);
+cudaError_t init_lureg_kernels(const DevNet &net);
 void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
                      double *z, cudaStream_t s);
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);

@@ -12,6 +12,7 @@
 
 #include "vk_gjreg.cuh"
 #include "vk_internal.cuh"
+#include "vk_tma.cuh"
 
 namespace vk {
 
@@ -109,22 +110,96 @@ k_lu_reg64(DevNet net, DevBatch b, const double *__restrict__ jv, const double *
     if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
 }
 
+// Per-layer preparation for the FP32 factorisation (fully parallel over
+// layers): power-of-two row scales (row maxima of D_j) and column scales
+// (column maxima of R_j D_j) in FP64, and the dense scaled block R_j D_j S_j
+// rounded once to FP32, written with a 16-byte-aligned stride for TMA.
+__global__ void __launch_bounds__(256)
+k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
+         const double *__restrict__ dt, float *__restrict__ D32, double *__restrict__ rsc,
+         double *__restrict__ csc) {
+    extern __shared__ double sp[];
+    const int n = net.ni, nn = n * n, nnz = net.nnz;
+    const int l = blockIdx.x;
+    const int c = b.lay_col[l];
+    if (b.active && !b.active[c]) return;
+    double *jls = sp;                       // [nnz]
+    double *rs = jls + nnz;                 // [n]
+    double *cs = rs + n;                    // [n]
+    double *dg = cs + n;                    // [n] c0 - dA
+    float *dense = reinterpret_cast<float *>(dg + n);   // [nn]
+    int *cexp = reinterpret_cast<int *>(dense + nn);    // [n]
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const double c0 = 1.0 / (R_ROS * dt[c]);
+    const double *jl = jv + (size_t)l * nnz;
+    for (int e = tid; e < nnz; e += nth) jls[e] = jl[e];
+    for (int e = tid; e < nn; e += nth) dense[e] = 0.0f;
+    for (int t = tid; t < n; t += nth) {
+        dg[t] = c0 - dA[(size_t)l * n + t];
+        cexp[t] = -100000;
+    }
+    __syncthreads();
+    for (int r = tid; r < n; r += nth) {
+        double m = fabs(dg[r]);
+        for (int e = net.jrowptr[r]; e < net.jrowptr[r + 1]; ++e) {
+            double v = jls[e] + (net.jcol[e] == r ? dg[r] : 0.0);
+            m = fmax(m, fabs(v));
+        }
+        rs[r] = pow2_scale_r(m);
+    }
+    __syncthreads();
+    for (int e = tid; e < nnz + n; e += nth) {
+        int r, q;
+        double v;
+        if (e < nnz) {
+            r = net.jrow[e]; q = net.jcol[e];
+            v = jls[e] + (r == q ? dg[r] : 0.0);
+        } else {
+            r = q = e - nnz;
+            v = dg[r];
+        }
+        v = fabs(v * rs[r]);
+        if (v > 0.0 && isfinite(v)) {
+            int ex;
+            frexp(v, &ex);
+            atomicMax(&cexp[q], ex);
+        }
+    }
+    __syncthreads();
+    for (int t = tid; t < n; t += nth) cs[t] = cexp[t] > -100000 ? ldexp(1.0, -cexp[t]) : 1.0;
+    __syncthreads();
+    for (int e = tid; e < nnz; e += nth) {
+        const int r = net.jrow[e], q = net.jcol[e];
+        const double v = jls[e] + (r == q ? dg[r] : 0.0);
+        dense[r * n + q] = (float)(rs[r] * v * cs[q]);
+    }
+    for (int r = tid; r < n; r += nth)
+        if (net.jmap[r * n + r] < 0) dense[r * n + r] = (float)(rs[r] * dg[r] * cs[r]);
+    __syncthreads();
+    float *Dl = D32 + (size_t)l * block_stride32(n);
+    for (int e = tid; e < nn; e += nth) Dl[e] = dense[e];
+    for (int t = tid; t < n; t += nth) {
+        rsc[(size_t)l * n + t] = rs[t];
+        csc[(size_t)l * n + t] = cs[t];
+    }
+}
+
+// FP32 block-Thomas factorisation of the scaled system, one CTA per column.
+// The dense scaled block of layer j+1 streams into shared memory by TMA while
+// layer j is inverted (register-resident Gauss-Jordan).
 template <int TY, int RA, int RB>
-__global__ void __launch_bounds__(16 * TY, TY == 16 ? 3 : 1)
-k_lu_reg32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
-           const double *__restrict__ dB, const double *__restrict__ dC,
-           const double *__restrict__ dt, float *__restrict__ G32, double *__restrict__ rsc,
-           double *__restrict__ csc, int *__restrict__ status) {
-    extern __shared__ double smd[];
-    const int n = net.ni, nn = n * n;
+__global__ void __launch_bounds__(16 * TY, TY == 16 && RA <= 5 ? 2 : 1)
+k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__restrict__ dB,
+       const double *__restrict__ dC, const double *__restrict__ rsc,
+       const double *__restrict__ csc, float *__restrict__ G32, int *__restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smb[];
+    const int n = net.ni, nn = n * n, NNP = block_stride32(n);
     const int c = blockIdx.x;
     if (b.active && !b.active[c]) return;
     const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
-    double *rs = smd;
-    double *cs = rs + n;
-    double *rs_prev = cs + n;
-    double *cs_prev = rs_prev + n;
-    float *Gs = reinterpret_cast<float *>(cs_prev + n);     // [n*n]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smb);             // [2]
+    float *Dbuf = reinterpret_cast<float *>(smb + 16);             // [2][NNP]
+    float *Gs = Dbuf + 2 * NNP;                                    // [nn]
     float *rowv = Gs + nn;
     float *colv = rowv + n;
     float *alpha = colv + n;
@@ -132,60 +207,48 @@ k_lu_reg32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *
     int *perm = reinterpret_cast<int *>(beta + n);
     int *kinv = perm + n;
     int *used = kinv + n;
-    int *cexp = used + n;
-    __shared__ int s_piv, s_sing;
+    __shared__ int s_piv, s_sing, s_to;
     __shared__ float s_pval;
     GJShared<float> sh{rowv, colv, perm, kinv, used, &s_piv, &s_pval, &s_sing};
     int ty, tx;
     tile_coords<TY>(ty, tx);
-    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const int nwarp = nth >> 5;
-    if (tid == 0) s_sing = 0;
-    const double c0 = 1.0 / (R_ROS * dt[c]);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const uint32_t bytes = (uint32_t)NNP * sizeof(float);
+    if (tid == 0) {
+        s_sing = 0;
+        s_to = 0;
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) tma_load_1d(Dbuf, D32 + (size_t)l0 * NNP, bytes, &bar[0]);
+    // per-thread copies of this layer's scales (threads t < n own species t)
+    double rs_cur = 0, cs_cur = 0, dB_cur = 0;
+    if (tid < n) {
+        rs_cur = rsc[(size_t)l0 * n + tid];
+        cs_cur = csc[(size_t)l0 * n + tid];
+        dB_cur = dB[(size_t)l0 * n + tid];
+    }
     for (int j = 0; j < nz; ++j) {
         const size_t l = (size_t)l0 + j;
-        const double *jl = jv + l * net.nnz;
-        const double *aj = dA + l * n;
-        // row scales: row maxima of the FP64 diagonal block D_j
-        for (int r = warp; r < n; r += nwarp) {
-            double m = 0.0;
-            for (int e = net.jrowptr[r] + lane; e < net.jrowptr[r + 1]; e += 32) {
-                double v = jl[e];
-                if (net.jcol[e] == r) v += c0 - aj[r];
-                m = fmax(m, fabs(v));
-            }
-            for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-            if (lane == 0) rs[r] = pow2_scale_r(fmax(m, fabs(c0 - aj[r])));
+        const int buf = j & 1;
+        // prefetch the scales of the next layer into registers
+        double rs_nx = 0, cs_nx = 0, dC_nx = 0, dB_nx = 0;
+        if (tid < n && j + 1 < nz) {
+            rs_nx = rsc[(l + 1) * n + tid];
+            cs_nx = csc[(l + 1) * n + tid];
+            dC_nx = dC[(l + 1) * n + tid];
+            dB_nx = dB[(l + 1) * n + tid];
         }
-        for (int t = tid; t < n; t += nth) { cexp[t] = -100000; used[t] = 0; }
-        __syncthreads();
-        // column scales: column maxima of R_j D_j (exponents)
-        for (int e = tid; e < net.nnz + n; e += nth) {
-            int r, q;
-            double v;
-            if (e < net.nnz) {
-                r = net.jrow[e]; q = net.jcol[e];
-                v = jl[e] + (r == q ? c0 - aj[r] : 0.0);
-            } else {
-                r = q = e - net.nnz;
-                v = c0 - aj[r];
-            }
-            v = fabs(v * rs[r]);
-            if (v > 0.0 && isfinite(v)) {
-                int ex;
-                frexp(v, &ex);
-                atomicMax(&cexp[q], ex);
-            }
+        const bool ok = mbar_wait(&bar[buf], (j >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) status[c] = VK_ETIMEOUT;
+            return;                          // no other copy was issued after this one
         }
-        __syncthreads();
-        for (int t = tid; t < n; t += nth) {
-            cs[t] = cexp[t] > -100000 ? ldexp(1.0, -cexp[t]) : 1.0;
-            if (j > 0) {
-                alpha[t] = (float)(rs[t] * dC[l * n + t] * cs_prev[t]);
-                beta[t] = (float)(rs_prev[t] * dB[(l - 1) * n + t] * cs[t]);
-            }
-        }
-        __syncthreads();
+        if (tid == 0 && j + 1 < nz)
+            tma_load_1d(Dbuf + (buf ^ 1) * NNP, D32 + (l + 1) * NNP, bytes, &bar[buf ^ 1]);
+        const float *Dj = Dbuf + buf * NNP;
         float M[RA][RB];
 #pragma unroll
         for (int a = 0; a < RA; ++a) {
@@ -195,25 +258,24 @@ k_lu_reg32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *
                 const int cc = tx + 16 * q;
                 float v = 0.0f;
                 if (r < n && cc < n) {
-                    if (j > 0) v = -alpha[r] * Gs[r * n + cc] * beta[cc];
-                    double d = (r == cc) ? c0 - aj[r] : 0.0;
-                    const int e = net.jmap[r * n + cc];
-                    if (e >= 0) d += jl[e];
-                    if (d != 0.0) v += (float)(rs[r] * d * cs[cc]);
+                    v = Dj[r * n + cc];
+                    if (j > 0) v -= alpha[r] * Gs[r * n + cc] * beta[cc];
                 }
                 M[a][q] = v;
             }
         }
+        for (int t = tid; t < n; t += nth) used[t] = 0;
         __syncthreads();
         gj_invert_reg<float, TY, RA, RB>(M, n, ty, tx, sh);
         gj_store_natural<float, TY, RA, RB>(M, n, ty, tx, sh, Gs);
-        float *Gl = G32 + l * nn;
+        float *Gl = G32 + l * NNP;
         for (int e = tid; e < nn; e += nth) Gl[e] = Gs[e];
-        for (int t = tid; t < n; t += nth) {
-            rsc[l * n + t] = rs[t];
-            csc[l * n + t] = cs[t];
-            rs_prev[t] = rs[t];
-            cs_prev[t] = cs[t];
+        if (tid < n && j + 1 < nz) {
+            alpha[tid] = (float)(rs_nx * dC_nx * cs_cur);
+            beta[tid] = (float)(rs_cur * dB_cur * cs_nx);
+            rs_cur = rs_nx;
+            cs_cur = cs_nx;
+            dB_cur = dB_nx;
         }
         __syncthreads();
     }
@@ -223,7 +285,12 @@ k_lu_reg32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *
 // ---------------------------------------------------------------------------
 static size_t smem64(int n) { return (size_t)(n * n + 5 * n) * sizeof(double) + 3 * n * sizeof(int) + 16; }
 static size_t smem32(int n) {
-    return (size_t)4 * n * sizeof(double) + (size_t)(n * n + 4 * n) * sizeof(float) + 4 * n * sizeof(int) + 16;
+    return 16 + (size_t)2 * block_stride32(n) * sizeof(float) + (size_t)(n * n + 4 * n) * sizeof(float)
+           + 3 * n * sizeof(int) + 16;
+}
+static size_t smem_prep(const DevNet &net) {
+    const int n = net.ni;
+    return (size_t)(net.nnz + 3 * n) * sizeof(double) + (size_t)n * n * sizeof(float) + n * sizeof(int) + 16;
 }
 
 #define VK_LU_TILINGS(X) X(16, 3, 3) X(16, 5, 5) X(16, 7, 7) X(32, 5, 10)
@@ -235,13 +302,15 @@ static int tiling_of(int n) {
     return 3;
 }
 
-cudaError_t init_lureg_kernels(int n) {
-    cudaError_t e = cudaSuccess;
+cudaError_t init_lureg_kernels(const DevNet &net) {
+    const int n = net.ni;
+    cudaError_t e = cudaFuncSetAttribute(k_prep32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_prep(net));
     size_t s64 = smem64(n), s32 = smem32(n);
 #define SETATTR(TY, RA, RB)                                                                      \
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu_reg64<TY, RA, RB>,                       \
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s64); \
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu_reg32<TY, RA, RB>,                       \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu32<TY, RA, RB>,                           \
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s32);
     VK_LU_TILINGS(SETATTR)
 #undef SETATTR
@@ -262,12 +331,13 @@ void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const 
 
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s) {
     const int n = net.ni;
+    k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs);
     size_t sm = smem32(n);
     switch (tiling_of(n)) {
-    case 0: k_lu_reg32<16, 3, 3><<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, w.G32, w.rs, w.cs, w.status); break;
-    case 1: k_lu_reg32<16, 5, 5><<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, w.G32, w.rs, w.cs, w.status); break;
-    case 2: k_lu_reg32<16, 7, 7><<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, w.G32, w.rs, w.cs, w.status); break;
-    default: k_lu_reg32<32, 5, 10><<<b.ncols, 512, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, w.G32, w.rs, w.cs, w.status); break;
+    case 0: k_lu32<16, 3, 3><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
+    case 1: k_lu32<16, 5, 5><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
+    case 2: k_lu32<16, 7, 7><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
+    default: k_lu32<32, 5, 10><<<b.ncols, 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
     }
 }
 
