@@ -155,95 +155,177 @@ def fp64_peak_tflops():
 
 
 # ------------------------------------------------------------ GPU arm
-def run_gpu(args):
-    from vulcan_gb300 import _build, batch, capi, configs
+def _setup(args, precision, ncols=None):
+    from vulcan_gb300 import _build, batch, configs
     from vulcan_gb300.network import Network
     from vulcan_gb300.solver import ctrl_from
     _build.build()
     net = Network.from_npz(NET)
-    specs = configs.config2_columns(ncols=NCOLS, seed=SEED)[:args.ncols]
+    specs = configs.config2_columns(ncols=NCOLS, seed=SEED)[:ncols or args.ncols]
     items = batch.build_items(specs, net)
-    h, b = batch.make_batch_handle(net, items, ATOMS)
-    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
-    # warm-up steps (also advances the columns past the very first steps)
+    h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
+    return net, items, h, b, ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+
+
+def _measure(args, precision, clocks=None):
+    """Warm-up, then args.steps timed steps of every column (state resident)."""
+    net, items, h, b, ctrl = _setup(args, precision)
     h.run(ctrl, max_steps=args.warmup, timeout_s=1800)
-    st0 = h.state()
-    c0 = h.counters()
-    clocks = Clocks(os.path.join(REPO, 'gpurun_out', 'bench_clocks.csv')
-                    if os.path.isdir(os.path.join(REPO, 'gpurun_out')) else '/tmp/bench_clocks.csv')
-    with clocks:
+    st0, c0 = h.state(), h.counters()
+    if clocks is not None:
+        clocks.__enter__()
         time.sleep(0.3)
-        t0 = time.perf_counter()
+    try:
         h.run(ctrl, max_steps=args.steps, timeout_s=3600)
-        wall = time.perf_counter() - t0
+    finally:
+        if clocks is not None:
+            clocks.__exit__()
     tm = h.timing()
-    st1 = h.state()
-    c1 = h.counters()
+    st1, c1 = h.state(), h.counters()
     steps = int((st1['count'] - st0['count']).sum())
     attempts = int((c1[:, 0] - c0[:, 0]).sum())
-    ms_dev = tm['rates']                 # device time of the whole run (CUDA events)
-    value = steps / (ms_dev * 1e-3)
-    # per-kernel attempt timing (for the roofline): one instrumented attempt
-    dt = st1['dt'].copy()
-    h2, _ = batch.make_batch_handle(net, items, ATOMS)
-    h2.set_state(st1['y'], st1['ymix'])
+    ms_dev = tm['rates']                  # device time of the whole run (CUDA events)
+    out = dict(value=steps / (ms_dev * 1e-3), ms=ms_dev, steps=steps, attempts=attempts,
+               launches=tm['launches'], fallbacks=int((c1[:, 4] - c0[:, 4]).sum()))
+    # per-kernel device times of one attempt from the current state
+    h.set_state(st1['y'], st1['ymix'])
     for _ in range(2):
-        h2.attempt(dt)
-    kt = h2.timing()
-    h2.close()
+        h.attempt(st1['dt'])
+    out['attempt_ms'] = {k: round(v, 3) for k, v in h.timing().items() if k != 'launches'}
     # e2e: host state in, one step, host state out -- through the public API
     y_host = np.ascontiguousarray(st1['y'])
     ym_host = np.ascontiguousarray(st1['ymix'])
-    e2e_steps = max(2, min(args.steps, 5))
-    t0 = time.perf_counter()
-    n_e2e = 0
-    for _ in range(e2e_steps):
+    h.set_clock(dt=st1['dt'], t=st1['t'], count=st1['count'])
+    n_e2e, t0 = 0, time.perf_counter()
+    for _ in range(max(2, min(args.steps, 5))):
         c_before = h.state()['count']
         h.set_state(y_host, ym_host)
         h.run(ctrl, max_steps=1, timeout_s=600)
         s = h.state()
         y_host, ym_host = s['y'], s['ymix']
         n_e2e += int((s['count'] - c_before).sum())
-    e2e_wall = time.perf_counter() - t0
-    bytes_state = b.L * net.ni * 8
-    # roofline of the dominant kernel (block LU, FP64): algorithmic flops
-    nz = b.nz.astype(np.float64)
-    ni = net.ni
-    lu_flops = float(np.sum(nz) * 2.0 * ni ** 3)      # in-place Gauss-Jordan: n^3 FMA per layer
-    peak64 = fp64_peak_tflops()
-    lu_tflops = lu_flops / (kt['lu'] * 1e-3) / 1e12
+    out['e2e'] = n_e2e / (time.perf_counter() - t0)
+    out['bytes_state'] = b.L * net.ni * 8
+    out['layers'] = int(b.L)
+    out['ni'] = net.ni
+    h.close()
+    return out
+
+
+def run_gpu(args):
     hbm, hbm_kind = peaks()
-    rate_bytes = float(b.L * (2 * net.npair * 8 + 3 * ni * 8))   # k + y (3 layers) per layer, 2 evals
+    clocks = Clocks(os.path.join(REPO, 'gpurun_out', 'bench_clocks.csv')
+                    if os.path.isdir(os.path.join(REPO, 'gpurun_out')) else '/tmp/bench_clocks.csv')
+    mixed = _measure(args, 1, clocks)
+    plain = _measure(args, 0)
+    ni, L = mixed['ni'], mixed['layers']
+    # roofline of the dominant kernel of the headline path
+    am = mixed['attempt_ms']
+    dom = max(('lu', 'solve', 'rates'), key=lambda k: am[k])
+    stride = (ni * ni + 3) // 4 * 4
+    if dom == 'lu':
+        fl = float(L) * ni ** 3 * 2.0          # FP32 Gauss-Jordan: ni^3 FMA per layer
+        peak = fp32_peak_tflops()
+        roof = {'bound': 'fp32', 'kernel': 'k_lu32 (+k_prep32)', 'achieved': fl / (am['lu'] * 1e-3) / 1e12,
+                'peak': peak, 'unit': 'TFLOP/s', 'peak_source': 'measured cuBLAS SGEMM 8192^3 (no TF32) in this run'}
+    else:
+        # refinement + second RHS: every sweep streams the FP32 inverses twice
+        by = float(L) * stride * 4 * 2 * 2 * 3
+        roof = {'bound': 'hbm', 'kernel': 'k_refine', 'achieved': by / (am['solve'] * 1e-3) / 1e9,
+                'peak': hbm, 'unit': 'GB/s', 'peak_source': hbm_kind}
+    roof['frac'] = roof['achieved'] / roof['peak']
+    roof['traffic'] = None
+    for k in ('achieved', 'peak', 'frac'):
+        roof[k] = round(roof[k], 4)
+    peak64 = fp64_peak_tflops()
+    lu64 = float(L) * ni ** 3 * 2.0 / (plain['attempt_ms']['lu'] * 1e-3) / 1e12
+    rate_bytes = float(L) * (782 * 8 + 3 * ni * 8 + 4 * ni * 8)
     out = {
-        'metric': METRIC, 'value': round(value, 2), 'unit': UNIT, 'n_gpus': 1,
+        'metric': METRIC, 'value': round(mixed['value'], 2), 'unit': UNIT, 'n_gpus': 1,
         'steps': args.steps, 'warmup': args.warmup,
-        'ms_per_step': round(ms_dev / max(args.steps, 1), 3),
-        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'ms_per_step': round(mixed['ms'] / max(args.steps, 1), 3),
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
         'data': 'synthetic (seeded columns; no dataset)',
-        'config': {'workload': 'batched Ros2, 512 uneven NCHO-thermo columns (ni=69, nz 60-200, '
-                               'sum nz=%d), plain FP64 block LU' % b.L,
-                   'ncols': NCOLS, 'layers': int(b.L), 'network': 'NCHO_thermo (69 species, 391 pairs)',
-                   'precision': 'fp64', 'l2': 'inputs larger than L2 (state+inverses %.1f GB)'
-                   % ((b.L * ni * ni * 8 + bytes_state * 6) / 1e9)},
-        'e2e': {'value': round(n_e2e / e2e_wall, 2), 'unit': UNIT,
-                'h2d_bytes_per_step': 2 * bytes_state, 'd2h_bytes_per_step': 2 * bytes_state},
-        'gpu_launches': int(tm['launches']),
-        'attempts_per_step': round(attempts / max(steps, 1), 3),
-        'roofline': {'bound': 'fp64', 'kernel': 'k_lu_fwd_f64',
-                     'achieved': round(lu_tflops, 4), 'peak': round(peak64, 4),
-                     'unit': 'TFLOP/s', 'frac': round(lu_tflops / peak64, 4),
-                     'peak_source': 'measured cuBLAS DGEMM 8192^3 in this run',
-                     'traffic': None},
-        'rates_kernel': {'bound': 'hbm', 'achieved': round(rate_bytes / (kt['rates'] * 1e-3) / 1e9, 1),
+        'config': {'workload': 'batched Ros2 steps, %d uneven NCHO-thermo columns (ni=69, nz 60-200, '
+                               'sum nz=%d); FP32 scaled block LU + FP64 refinement' % (args.ncols, L),
+                   'ncols': args.ncols, 'layers': L, 'network': 'NCHO_thermo (69 species, 391 pairs)',
+                   'precision': 'mixed (FP64 rates/residual/error control, FP32 LU)',
+                   'l2': 'inputs larger than L2 (state, k, Jacobian, inverses > 3 GB)'},
+        'e2e': {'value': round(mixed['e2e'], 2), 'unit': UNIT,
+                'h2d_bytes_per_step': 2 * mixed['bytes_state'], 'd2h_bytes_per_step': 2 * mixed['bytes_state']},
+        'gpu_launches': int(mixed['launches']),
+        'attempts_per_step': round(mixed['attempts'] / max(mixed['steps'], 1), 3),
+        'fp64_fallback_attempts': mixed['fallbacks'],
+        'roofline': roof,
+        'attempt_ms': mixed['attempt_ms'],
+        'plain_fp64': {'value': round(plain['value'], 2), 'unit': UNIT, 'e2e': round(plain['e2e'], 2),
+                       'attempt_ms': plain['attempt_ms'],
+                       'lu_roofline': {'bound': 'fp64', 'achieved': round(lu64, 4), 'peak': round(peak64, 4),
+                                       'unit': 'TFLOP/s', 'frac': round(lu64 / peak64, 4),
+                                       'peak_source': 'measured cuBLAS DGEMM 8192^3 in this run'}},
+        'mixed_over_plain': round(mixed['value'] / plain['value'], 3),
+        'rates_kernel': {'bound': 'hbm', 'achieved': round(rate_bytes / (am['rates'] * 1e-3) / 1e9, 1),
                          'peak': hbm, 'unit': 'GB/s', 'peak_source': hbm_kind,
-                         'frac': round(rate_bytes / (kt['rates'] * 1e-3) / 1e9 / hbm, 4)},
-        'attempt_ms': {k: round(v, 3) for k, v in kt.items() if k != 'launches'},
+                         'frac': round(rate_bytes / (am['rates'] * 1e-3) / 1e9 / hbm, 4)},
     }
     out['clocks'] = clocks.summary()
     if not args.no_cpu:
         out['cpu_baseline'] = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
     print(json.dumps(out))
-    h.close()
+
+
+def fp32_peak_tflops():
+    """cuBLAS SGEMM throughput with TF32 off (the measured FP32 denominator)."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float32, device='cuda')
+    b = torch.randn(n, n, dtype=torch.float32, device='cuda')
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def run_converge(args):
+    """Every column to steady state on both paths; steps, time, agreement."""
+    res = {}
+    finals = {}
+    for name, prec in (('mixed', 1), ('plain_fp64', 0)):
+        net, items, h, b, ctrl = _setup(args, prec)
+        t0 = time.perf_counter()
+        h.run(ctrl, max_steps=0, timeout_s=args.converge_timeout)
+        wall = time.perf_counter() - t0
+        st, cnt = h.state(), h.counters()
+        conv = st['end_case'] == 1
+        res[name] = {'wall_s': round(wall, 2), 'device_s': round(h.timing()['rates'] * 1e-3, 2),
+                     'converged': int(conv.sum()), 'ncols': b.ncols,
+                     'steps_mean': float(st['count'].mean()), 'steps_max': int(st['count'].max()),
+                     'attempts': int(cnt[:, 0].sum()), 'fp64_fallbacks': int(cnt[:, 4].sum()),
+                     'columns_per_hour': round(conv.sum() / wall * 3600, 1),
+                     'column_steps_per_s': round(float(st['count'].sum()) / wall, 1),
+                     'end_cases': {str(k): int(v) for k, v in zip(*np.unique(st['end_case'], return_counts=True))}}
+        finals[name] = (st['ymix'], st['end_case'])
+        h.close()
+    ym, yp = finals['mixed'][0], finals['plain_fp64'][0]
+    mask = yp > 1e-20
+    both = (finals['mixed'][1] == 1) & (finals['plain_fp64'][1] == 1)
+    rel = np.abs(ym - yp) / np.where(mask, yp, 1.0)
+    res['mixed_vs_fp64_max_rel_ymix_gt_1e-20'] = float(rel[mask].max()) if mask.any() else None
+    res['metric'] = METRIC
+    res['workload'] = '%d uneven NCHO-thermo columns to steady state (reference conv criterion)' % args.ncols
+    res['speedup_columns_per_hour'] = round(res['mixed']['columns_per_hour'] /
+                                            max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
+    print(json.dumps(res))
 
 
 def run_profile(args):
@@ -294,6 +376,9 @@ def main():
                     help='only run --attempts instrumented attempts (for ncu captures)')
     ap.add_argument('--attempts', type=int, default=2)
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
+    ap.add_argument('--converge', action='store_true',
+                    help='run --ncols columns to steady state on both paths')
+    ap.add_argument('--converge-timeout', type=float, default=1800.0)
     ap.add_argument('--cpu-workers', type=int, default=min(16, os.cpu_count() or 1))
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', '0'))
@@ -303,6 +388,9 @@ def main():
         return
     if args.profile:
         run_profile(args)
+        return
+    if args.converge:
+        run_converge(args)
         return
     run_gpu(args)
 

@@ -44,8 +44,9 @@ from vulcan_gb300.network import Network  # noqa: E402
 KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c1': (0, 1, 2, 10, 29),
         'c2': (0, 1, 2, 10, 29),
-        'c2long': (400, 800, 1200, 1600, 1999)}
-NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000}
+        'c2long': (400, 800, 1200, 1600, 1999),
+        'c2conv': (0,)}
+NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000}
 
 DRIVER = r'''
 import os, sys, time, json
@@ -157,6 +158,10 @@ out['att_all_dt'] = np.array([a['dt'] for a in ATT])
 ysteps = [s for s in (0, 1, 99, 100, 101, 199, 299, 399, 499) if s < len(STEPS)]
 out['ystep_index'] = np.array(ysteps)
 out['ystep_y'] = np.array([STEPS[s]['y'] for s in ysteps])
+out['final_y'] = STEPS[-1]['y']
+out['final_ymix'] = var.ymix.copy()
+out['final_t'] = STEPS[-1]['t']
+out['final_count'] = STEPS[-1]['count']
 out['spec_list'] = np.array(chem_funs.spec_list)
 out['nr'] = nr
 out['end_case'] = para.end_case
@@ -281,7 +286,7 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
 def make(tag, ref_root, workdir, full_dir=None):
     if tag == 'c0':
         spec = configs.config0()
-    elif tag in ('c2', 'c2long'):
+    elif tag in ('c2', 'c2long', 'c2conv'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]
     elif tag == 'c1':
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
@@ -305,7 +310,7 @@ def make(tag, ref_root, workdir, full_dir=None):
     np.savez_compressed(out, **d)
     net.to_npz(os.path.join(HERE, 'net_%s.npz' % spec.network.replace('_network.txt', '')
                             + ('_photo' if spec.use_photo and 'photo' not in spec.network else '')))
-    if full_dir:
+    if full_dir and tag != 'c2conv':
         os.makedirs(full_dir, exist_ok=True)
         shutil.copy(os.path.join(dst, 'golden_full.npz'),
                     os.path.join(full_dir, 'golden_full_%s.npz' % tag))
