@@ -297,32 +297,60 @@ def fp32_peak_tflops():
 
 
 def run_converge(args):
-    """Every column to steady state on both paths; steps, time, agreement."""
+    """Every column to steady state on both paths, in chunks of steps: steps to
+    converge, columns per hour, agreement of the final states."""
+    from vulcan_gb300 import capi
     res = {}
     finals = {}
     for name, prec in (('mixed', 1), ('plain_fp64', 0)):
         net, items, h, b, ctrl = _setup(args, prec)
+        ctrl.count_max = args.count_max
+        curve = []
         t0 = time.perf_counter()
-        h.run(ctrl, max_steps=0, timeout_s=args.converge_timeout)
-        wall = time.perf_counter() - t0
-        st, cnt = h.state(), h.counters()
+        dev_s = 0.0
+        while True:
+            try:
+                h.run(ctrl, max_steps=args.chunk, timeout_s=args.converge_timeout)
+            except capi.VkError as e:
+                if e.code != capi.VK_ETIMEOUT:
+                    raise
+            dev_s += h.timing()['rates'] * 1e-3
+            st = h.state()
+            wall = time.perf_counter() - t0
+            curve.append((round(wall, 1), int(st['count'].max()), int((st['end_case'] == 1).sum()),
+                          int((st['end_case'] != 0).sum())))
+            if (st['end_case'] != 0).all() or wall > args.converge_timeout:
+                break
+        cnt = h.counters()
         conv = st['end_case'] == 1
-        res[name] = {'wall_s': round(wall, 2), 'device_s': round(h.timing()['rates'] * 1e-3, 2),
+        res[name] = {'wall_s': round(wall, 2), 'device_s': round(dev_s, 2),
                      'converged': int(conv.sum()), 'ncols': b.ncols,
-                     'steps_mean': float(st['count'].mean()), 'steps_max': int(st['count'].max()),
+                     'steps_to_converge_mean': float(st['count'][conv].mean()) if conv.any() else None,
+                     'steps_to_converge_median': float(np.median(st['count'][conv])) if conv.any() else None,
+                     'steps_max': int(st['count'].max()),
                      'attempts': int(cnt[:, 0].sum()), 'fp64_fallbacks': int(cnt[:, 4].sum()),
                      'columns_per_hour': round(conv.sum() / wall * 3600, 1),
                      'column_steps_per_s': round(float(st['count'].sum()) / wall, 1),
-                     'end_cases': {str(k): int(v) for k, v in zip(*np.unique(st['end_case'], return_counts=True))}}
-        finals[name] = (st['ymix'], st['end_case'])
+                     'end_cases': {str(k): int(v) for k, v in zip(*np.unique(st['end_case'], return_counts=True))},
+                     'curve_wall_maxcount_converged_done': curve}
+        finals[name] = (st['ymix'], st['end_case'], st['count'])
         h.close()
     ym, yp = finals['mixed'][0], finals['plain_fp64'][0]
-    mask = yp > 1e-20
     both = (finals['mixed'][1] == 1) & (finals['plain_fp64'][1] == 1)
-    rel = np.abs(ym - yp) / np.where(mask, yp, 1.0)
-    res['mixed_vs_fp64_max_rel_ymix_gt_1e-20'] = float(rel[mask].max()) if mask.any() else None
+    bsz = [it.pco.size for it in __import__('vulcan_gb300.configs', fromlist=['x']).config2_columns(
+        ncols=NCOLS, seed=SEED)[:args.ncols]]
+    off = np.concatenate([[0], np.cumsum(bsz)])
+    errs = []
+    for c in np.nonzero(both)[0]:
+        a, r = ym[off[c]:off[c + 1]], yp[off[c]:off[c + 1]]
+        m = r > 1e-20
+        errs.append(float(np.max(np.abs(a[m] - r[m]) / r[m])))
+    res['both_converged'] = int(both.sum())
+    res['mixed_vs_fp64_ymix_rel_gt_1e-20'] = {'max': max(errs) if errs else None,
+                                              'median': float(np.median(errs)) if errs else None}
     res['metric'] = METRIC
-    res['workload'] = '%d uneven NCHO-thermo columns to steady state (reference conv criterion)' % args.ncols
+    res['workload'] = ('%d uneven NCHO-thermo columns to steady state (reference conv criterion, '
+                       'count_max %d)' % (args.ncols, args.count_max))
     res['speedup_columns_per_hour'] = round(res['mixed']['columns_per_hour'] /
                                             max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
     print(json.dumps(res))
@@ -379,6 +407,8 @@ def main():
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
+    ap.add_argument('--count-max', type=int, default=30000)
+    ap.add_argument('--chunk', type=int, default=500)
     ap.add_argument('--cpu-workers', type=int, default=min(16, os.cpu_count() or 1))
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', '0'))
