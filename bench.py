@@ -302,7 +302,10 @@ def run_converge(args):
     from vulcan_gb300 import capi
     res = {}
     finals = {}
-    for name, prec in (('mixed', 1), ('plain_fp64', 0)):
+    paths = (('mixed', 1), ('plain_fp64', 0))
+    if args.precision_only:
+        paths = tuple(p for p in paths if p[0] == args.precision_only)
+    for name, prec in paths:
         net, items, h, b, ctrl = _setup(args, prec)
         ctrl.count_max = args.count_max
         curve = []
@@ -335,6 +338,10 @@ def run_converge(args):
                      'curve_wall_maxcount_converged_done': curve}
         finals[name] = (st['ymix'], st['end_case'], st['count'])
         h.close()
+    if len(finals) < 2:
+        res['metric'] = METRIC
+        print(json.dumps(res))
+        return
     ym, yp = finals['mixed'][0], finals['plain_fp64'][0]
     both = (finals['mixed'][1] == 1) & (finals['plain_fp64'][1] == 1)
     bsz = [it.pco.size for it in __import__('vulcan_gb300.configs', fromlist=['x']).config2_columns(
@@ -409,6 +416,7 @@ def main():
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
     ap.add_argument('--count-max', type=int, default=30000)
     ap.add_argument('--chunk', type=int, default=500)
+    ap.add_argument('--precision-only', default=None, choices=['mixed', 'plain_fp64'])
     ap.add_argument('--cpu-workers', type=int, default=min(16, os.cpu_count() or 1))
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', '0'))

@@ -191,6 +191,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &w.zf, L * ni));
     TRY(dalloc(h, &w.fallback, max_cols));
     TRY(dalloc(h, &w.sweeps, 1));
+    TRY(dalloc(h, &w.refine_err, max_cols));
     TRY(dalloc(h, &w.dt, max_cols));
     TRY(dalloc(h, &w.delta, max_cols));
     TRY(dalloc(h, &w.status, max_cols));
@@ -355,6 +356,7 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
     } else {
         cudaMemsetAsync(w.fallback, 0, b.ncols * sizeof(int), s);
         cudaMemsetAsync(w.sweeps, 0, sizeof(int), s);
+        cudaMemsetAsync(w.refine_err, 0, b.ncols * sizeof(double), s);
         vk::launch_lu_reg32(net, b, w, s);
         if (timed) cudaEventRecord(h->ev[2], s);
         vk::launch_refine(net, b, w, w.f, w.k1, w.y, w.yk2, h->max_refine, h->refine_tol, s);

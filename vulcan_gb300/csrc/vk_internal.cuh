@@ -106,6 +106,7 @@ struct Work {                  // per-handle device work buffers
     float *D32;                // [L][stride] dense scaled FP32 blocks (mixed mode)
     int *fallback;             // [ncols] refinement did not converge -> FP64 path
     int *sweeps;               // [1] most refinement sweeps any column needed
+    double *refine_err;        // [ncols] last accepted correction size of the attempt
     double *dt;                // [ncols]
     double *delta;             // [ncols]
     int *status;               // [ncols]  VK_* per column (singular pivot ...)

@@ -38,7 +38,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
          const double *__restrict__ rhs, double *__restrict__ x, double *__restrict__ res,
          float *__restrict__ zf, const double *__restrict__ yscale, double *__restrict__ yk2,
          const double *__restrict__ y, int max_sweeps, double tol, int *__restrict__ fallback,
-         int *__restrict__ sweeps_out, int *__restrict__ status) {
+         int *__restrict__ sweeps_out, int *__restrict__ status, double *__restrict__ err_out) {
     extern __shared__ __align__(16) unsigned char smr[];
     const int n = net.ni, NNP = block_stride32(n);
     const int c = blockIdx.x;
@@ -75,6 +75,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
     __syncthreads();
     if (tid == 0) issue(0);
     int sweep = 0, converged = 0, timed_out = 0;
+    double m_prev = INFINITY;
     for (; sweep < max_sweeps && !converged && !timed_out; ++sweep) {
         double dmax = 0.0;
         for (int v = 0; v < per_sweep; ++v) {
@@ -151,7 +152,11 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
         double m = red[0];
         for (int w = 1; w < nwarp; ++w) m = fmax(m, red[w]);
         __syncthreads();
-        converged = (m <= tol);
+        // converged; or stagnating at the FP64 residual's noise floor (the
+        // correction stopped shrinking while already below 1e-6 of |x|+|y|)
+        converged = (m <= tol) || (sweep >= 1 && m > 0.25 * m_prev && m <= 1e-6);
+        if (!(m <= m_prev) && sweep >= 2) break;        // diverging: leave to the FP64 path
+        m_prev = m;
         if (converged) break;
         // residual r = b - A x  (FP64, matrix-free; every (layer, species) at once)
         for (int q = tid; q < nz * n; q += nth) {
@@ -178,6 +183,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
         else {
             if (!converged) fallback[c] = 1;
             if (sweeps_out) atomicMax(sweeps_out, sweep + (converged ? 1 : 0));
+            if (err_out) err_out[c] = fmax(err_out[c], m_prev);
         }
     }
     __syncthreads();
@@ -198,7 +204,7 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
     size_t sm = 16 + (size_t)2 * block_stride32(n) * sizeof(float) + 2 * n * sizeof(float);
     k_refine<<<b.ncols, 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
                                       rhs, x, w.r, w.zf, yscale, yk2, w.y, max_sweeps, tol,
-                                      w.fallback, w.sweeps, w.status);
+                                      w.fallback, w.sweeps, w.status, w.refine_err);
 }
 
 }  // namespace vk
