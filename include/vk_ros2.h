@@ -180,6 +180,23 @@ VK_API int  vk_get_counters(vk_handle *h, int *counters);
 VK_API int  vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double *ms_solve,
                    double *ms_stage, int *launches);
 
+/* ---- learned warm start: BF16 MLP kernels ----
+ * No counterpart in the reference (its initial state comes from ini_mix,
+ * build_atm.py:141-279).  Device pointers owned by the caller; BF16 weights
+ * and activations, FP32 accumulation, FP32 biases/gradients/optimiser state.
+ * X [B][K] bf16, W [K][N] bf16 (row-major), Z [B][N] f32, H [B][N] bf16. */
+/* Z = X W + bias; H = silu(Z) (silu_act = 1) or Z.  Z or H may be NULL. */
+VK_API int  vk_mlp_forward(int B, int K, int N, const void *X, const void *W, const float *bias,
+                           float *Z, void *H, int silu_act, void *stream);
+/* dZ = dH o silu'(Z) into dZ_scratch [B][N] bf16; dW = X^T dZ [K][N];
+ * db = column sums of dZ [N]; dX = dZ W^T [B][K] (each output may be NULL). */
+VK_API int  vk_mlp_backward(int B, int K, int N, const void *X, const void *W, const float *Z,
+                            const float *dH, int silu_act, void *dZ_scratch, float *dW,
+                            float *db, float *dX, void *stream);
+/* One Adam step on n parameters (w FP32 master, optional BF16 copy). */
+VK_API int  vk_mlp_adam(long long n, float *w, void *w_bf16, const float *g, float *m, float *v,
+                        float lr, float beta1, float beta2, float eps, int step, void *stream);
+
 /* ---- block-tridiagonal solve without allocation ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a framework that owns all device memory through its own pool, a plugin

@@ -237,3 +237,36 @@ def test_run_watchdog_returns_timeout():
     assert e.value.code == capi.VK_ETIMEOUT
     st = h.state()                    # the handle stays usable
     assert np.isfinite(st['y']).all()
+
+
+@pytest.mark.parametrize('precision', [0, 1])
+def test_device_run_reaches_reference_steady_state(precision):
+    """vk_run from the reference's initial state to its convergence criterion
+    (op.py conv / stop) lands on the reference's steady state.
+
+    Trajectories part at the late stiff steps' conditioning floor, so the
+    comparison is between converged states: the reference stops once the
+    relative change over its window is below yconv_cri (1 %), which bounds how
+    far either run can sit from the true steady state."""
+    from vulcan_gb300 import configs
+    from vulcan_gb300.solver import ctrl_from
+    g, net, gn, h, b = make_handle('c2conv', precision=precision)
+    h.set_atom_ini(g['atom_ini'][None, :])
+    mask = np.zeros(net.ni, dtype=np.int32)
+    for sp in g['conver_ignore']:
+        if str(sp) in net.species:
+            mask[net.species.index(str(sp))] = 1
+    h.set_conv_ignore(mask)
+    h.set_clock(dt=1e-10, t=0.0, count=0)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    h.run(ctrl, max_steps=20000, timeout_s=900)
+    st = h.state()
+    assert st['end_case'][0] == 1                      # converged, like the reference
+    assert 0.5 * g['final_count'] <= st['count'][0] <= 2.0 * g['final_count']
+    ref = g['final_ymix']
+    sel = ref > 1e-20
+    rel = np.abs(st['ymix'][sel] - ref[sel]) / ref[sel]
+    print('steady state: count %d (ref %d), rel median %.3g p99 %.3g max %.3g'
+          % (st['count'][0], g['final_count'], np.median(rel), np.percentile(rel, 99), rel.max()))
+    assert np.median(rel) <= 1e-3
+    assert np.percentile(rel, 99) <= 5e-2

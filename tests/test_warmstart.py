@@ -1,0 +1,111 @@
+"""Learned warm start: MLP kernels vs a CPU restatement, element projection."""
+import numpy as np
+import pytest
+
+from helpers import network
+from vulcan_gb300 import configs
+from vulcan_gb300.warmstart import column_features, project_elements
+
+
+def bf16(a):
+    """Round-to-nearest-even to bfloat16, returned as float32."""
+    a = np.asarray(a, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def silu(z):
+    return z / (1.0 + np.exp(-z))
+
+
+def dsilu(z):
+    s = 1.0 / (1.0 + np.exp(-z))
+    return s * (1.0 + z * (1.0 - s))
+
+
+def test_project_elements_matches_composition():
+    net = network('c2')
+    spec = configs.config2_columns(ncols=1, seed=5)[0]
+    comp = net.compo.astype(float)
+    rng = np.random.default_rng(0)
+    x = 10.0 ** rng.uniform(-20, 0, size=(7, net.ni))
+    x0 = np.zeros(net.ni)
+    for sp, v in spec.const_mix.items():
+        x0[net.species.index(sp)] = v
+    x0 /= x0.sum()
+    target = x0 @ comp
+    xp = project_elements(x, comp, target, iters=2000, tol=1e-12)
+    np.testing.assert_allclose(xp.sum(axis=1), 1.0, rtol=1e-12)
+    act = target > 0
+    np.testing.assert_allclose((xp @ comp)[:, act], np.broadcast_to(target[act], (7, act.sum())), rtol=1e-8)
+
+
+def test_column_features_shape():
+    net = network('c2')
+    spec = configs.config2_columns(ncols=1, seed=2)[0]
+    f = column_features(spec, net)
+    assert f.shape == (spec.pco.size, 3 + 4 + 16)
+    assert np.isfinite(f).all()
+
+
+@pytest.mark.gpu
+def test_mlp_kernels_match_cpu_restatement():
+    torch = pytest.importorskip('torch')
+    from vulcan_gb300 import _build
+    from vulcan_gb300.warmstart import MLP
+    _build.build()
+    rng = np.random.default_rng(1)
+    d_in, d_out, B = 23, 69, 200
+    m = MLP(d_in, d_out, width=96, depth=2, seed=3)
+    for l in range(len(m.b)):
+        m.b[l] = torch.tensor(rng.normal(0, 0.1, m.b[l].shape[0]), dtype=torch.float32, device='cuda')
+    X = bf16(rng.normal(size=(B, d_in)))
+    Xt = torch.tensor(X, device='cuda').to(torch.bfloat16)
+    Zs, Hs = m.forward(Xt)
+    W = [bf16(w.cpu().numpy()).astype(np.float64) for w in m.W]
+    bs = [b.cpu().numpy().astype(np.float64) for b in m.b]
+    # CPU restatement with the kernels' rounding points (bf16 activations)
+    h = X.astype(np.float64)
+    Hc, Zc = [h], []
+    for l in range(len(W)):
+        z = h @ W[l] + bs[l]
+        Zc.append(z)
+        if l < len(W) - 1:
+            h = bf16(silu(z)).astype(np.float64)
+            Hc.append(h)
+    out = Zs[-1].cpu().numpy()
+    assert np.max(np.abs(out - Zc[-1])) <= 1e-4 * np.abs(Zc[-1]).max() + 1e-5
+    G = rng.normal(size=out.shape).astype(np.float32)
+    dW, db = m.backward(Zs, Hs, torch.tensor(G, device='cuda'))
+    dH = G.astype(np.float64)
+    for l in range(len(W) - 1, -1, -1):
+        z = Zs[l].cpu().numpy().astype(np.float64)
+        dz = dH * dsilu(z) if l < len(W) - 1 else dH
+        dz = bf16(dz).astype(np.float64)
+        ref_dW = Hc[l].T @ dz
+        ref_db = dz.sum(axis=0)
+        gw, gb = dW[l].cpu().numpy(), db[l].cpu().numpy()
+        assert np.linalg.norm(gw - ref_dW) <= 1e-4 * np.linalg.norm(ref_dW)
+        assert np.linalg.norm(gb - ref_db) <= 1e-4 * np.linalg.norm(ref_db) + 1e-6
+        dH = dz @ W[l].T
+    # Adam step against the textbook update
+    w0 = m.W[0].cpu().numpy().copy()
+    g0 = dW[0].cpu().numpy()
+    m.adam(dW, db, lr=1e-2)
+    ref = w0 - 1e-2 * ((0.1 * g0) / 0.1) / (np.sqrt((0.001 * g0 * g0) / 0.001) + 1e-8)
+    np.testing.assert_allclose(m.W[0].cpu().numpy(), ref, rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.gpu
+def test_mlp_training_reduces_loss():
+    pytest.importorskip('torch')
+    from vulcan_gb300 import _build
+    from vulcan_gb300.warmstart import MLP
+    _build.build()
+    rng = np.random.default_rng(2)
+    X = rng.normal(size=(8192, 23))
+    Y = np.tanh(X @ rng.normal(size=(23, 69)) * 0.3)
+    m = MLP(23, 69, width=128, depth=2, seed=0)
+    hist = m.fit(X, Y, epochs=8, batch=1024, lr=3e-3)
+    assert hist[-1] < 0.2 * hist[0]

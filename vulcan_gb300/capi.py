@@ -33,7 +33,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_update_k', 'vk_ros2_attempt', 'vk_set_atom_ini', 'vk_set_column_info',
            'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
-           'vk_block_solve_noalloc', 'vk_get_refine_stats')
+           'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
+           'vk_mlp_backward', 'vk_mlp_adam')
 
 
 class VkNetworkDesc(C.Structure):
@@ -103,6 +104,11 @@ def lib(path=None):
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),
         'vk_block_solve_noalloc': (i, [i, i, vp, vp, vp, vp, vp, vp]),
         'vk_get_refine_stats': (i, [vp, pi, pi]),
+        'vk_mlp_forward': (i, [i, i, i, vp, vp, P(C.c_float), P(C.c_float), vp, i, vp]),
+        'vk_mlp_backward': (i, [i, i, i, vp, vp, P(C.c_float), P(C.c_float), i, vp,
+                                P(C.c_float), P(C.c_float), P(C.c_float), vp]),
+        'vk_mlp_adam': (i, [C.c_longlong, P(C.c_float), vp, P(C.c_float), P(C.c_float),
+                            P(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float, i, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
