@@ -155,7 +155,9 @@ def fp64_peak_tflops():
 
 
 # ------------------------------------------------------------ GPU arm
-def _setup(args, precision, ncols=None):
+def _setup(args, precision, ncols=None, warm_model=None):
+    """Handle over the workload's columns; with warm_model, the columns whose
+    learned proposal beats const_mix start from it (returns the mask too)."""
     from vulcan_gb300 import _build, batch, configs
     from vulcan_gb300.network import Network
     from vulcan_gb300.solver import ctrl_from
@@ -163,8 +165,15 @@ def _setup(args, precision, ncols=None):
     net = Network.from_npz(NET)
     specs = configs.config2_columns(ncols=NCOLS, seed=SEED)[:ncols or args.ncols]
     items = batch.build_items(specs, net)
+    used = None
+    if warm_model is not None:
+        from vulcan_gb300 import warmstart
+        items, used = warmstart.warm_items(warm_model, specs, net, items, ATOMS, precision)
     h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
-    return net, items, h, b, ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    if warm_model is not None:
+        return net, items, h, b, ctrl, used
+    return net, items, h, b, ctrl
 
 
 def _measure(args, precision, clocks=None):
@@ -302,14 +311,28 @@ def run_converge(args):
     from vulcan_gb300 import capi
     res = {}
     finals = {}
-    paths = (('mixed', 1), ('plain_fp64', 0))
+    paths = [('learned_mixed', 1), ('mixed', 1), ('plain_fp64', 0)]
+    model = None
+    if os.path.exists(args.weights):
+        from vulcan_gb300 import warmstart
+        model = warmstart.MLP.load(args.weights)
+    else:
+        paths = paths[1:]
+        res['learned_mixed'] = {'skipped': 'no warm-start weights at %s' % args.weights}
     if args.precision_only:
-        paths = tuple(p for p in paths if p[0] == args.precision_only)
+        paths = [p for p in paths if p[0] == args.precision_only]
     for name, prec in paths:
-        net, items, h, b, ctrl = _setup(args, prec)
+        t0 = time.perf_counter()
+        if name == 'learned_mixed':
+            net, items, h, b, ctrl, used = _setup(args, prec, warm_model=model)
+            res_extra = {'warm_started': int(used.sum()),
+                         'proposal_s': round(time.perf_counter() - t0, 2)}
+        else:
+            net, items, h, b, ctrl = _setup(args, prec)
+            res_extra = {}
+            t0 = time.perf_counter()
         ctrl.count_max = args.count_max
         curve = []
-        t0 = time.perf_counter()
         dev_s = 0.0
         while True:
             try:
@@ -335,31 +358,36 @@ def run_converge(args):
                      'columns_per_hour': round(conv.sum() / wall * 3600, 1),
                      'column_steps_per_s': round(float(st['count'].sum()) / wall, 1),
                      'end_cases': {str(k): int(v) for k, v in zip(*np.unique(st['end_case'], return_counts=True))},
-                     'curve_wall_maxcount_converged_done': curve}
+                     'curve_wall_maxcount_converged_done': curve, **res_extra}
         finals[name] = (st['ymix'], st['end_case'], st['count'])
         h.close()
-    if len(finals) < 2:
-        res['metric'] = METRIC
-        print(json.dumps(res))
-        return
-    ym, yp = finals['mixed'][0], finals['plain_fp64'][0]
-    both = (finals['mixed'][1] == 1) & (finals['plain_fp64'][1] == 1)
-    bsz = [it.pco.size for it in __import__('vulcan_gb300.configs', fromlist=['x']).config2_columns(
-        ncols=NCOLS, seed=SEED)[:args.ncols]]
-    off = np.concatenate([[0], np.cumsum(bsz)])
-    errs = []
-    for c in np.nonzero(both)[0]:
-        a, r = ym[off[c]:off[c + 1]], yp[off[c]:off[c + 1]]
-        m = r > 1e-20
-        errs.append(float(np.max(np.abs(a[m] - r[m]) / r[m])))
-    res['both_converged'] = int(both.sum())
-    res['mixed_vs_fp64_ymix_rel_gt_1e-20'] = {'max': max(errs) if errs else None,
-                                              'median': float(np.median(errs)) if errs else None}
     res['metric'] = METRIC
     res['workload'] = ('%d uneven NCHO-thermo columns to steady state (reference conv criterion, '
                        'count_max %d)' % (args.ncols, args.count_max))
-    res['speedup_columns_per_hour'] = round(res['mixed']['columns_per_hour'] /
-                                            max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
+    if 'plain_fp64' in finals:
+        bsz = [it.pco.size for it in __import__('vulcan_gb300.configs', fromlist=['x']).config2_columns(
+            ncols=NCOLS, seed=SEED)[:args.ncols]]
+        off = np.concatenate([[0], np.cumsum(bsz)])
+        yp, ep = finals['plain_fp64'][0], finals['plain_fp64'][1]
+        for name in finals:
+            if name == 'plain_fp64':
+                continue
+            ym, em = finals[name][0], finals[name][1]
+            both = (em == 1) & (ep == 1)
+            errs, meds = [], []
+            for c in np.nonzero(both)[0]:
+                a, r = ym[off[c]:off[c + 1]], yp[off[c]:off[c + 1]]
+                m = r > 1e-20
+                rel = np.abs(a[m] - r[m]) / r[m]
+                errs.append(float(rel.max()))
+                meds.append(float(np.median(rel)))
+            res[name]['both_converged_with_fp64'] = int(both.sum())
+            res[name]['vs_fp64_ymix_rel_gt_1e-20'] = {
+                'max_over_columns_of_max': max(errs) if errs else None,
+                'median_over_columns_of_max': float(np.median(errs)) if errs else None,
+                'median_over_columns_of_median': float(np.median(meds)) if meds else None}
+            res[name]['speedup_columns_per_hour_vs_fp64'] = round(
+                res[name]['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
     print(json.dumps(res))
 
 
@@ -416,7 +444,11 @@ def main():
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
     ap.add_argument('--count-max', type=int, default=30000)
     ap.add_argument('--chunk', type=int, default=500)
-    ap.add_argument('--precision-only', default=None, choices=['mixed', 'plain_fp64'])
+    ap.add_argument('--precision-only', default=None,
+                    choices=['learned_mixed', 'mixed', 'plain_fp64'])
+    ap.add_argument('--weights', default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                                                      'vulcan_gb300', 'warmstart_weights.npz'),
+                    help='learned warm-start weights (converge mode)')
     ap.add_argument('--cpu-workers', type=int, default=min(16, os.cpu_count() or 1))
     args = ap.parse_args()
     rank = int(os.environ.get('RANK', '0'))

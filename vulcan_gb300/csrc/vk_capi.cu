@@ -178,7 +178,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &h->d_spf, (size_t)max_cols * VK_SP_NF * ni));
     vk::Work &w = h->w;
     double **vecs[] = {&w.y, &w.ymix, &w.yk2, &w.f, &w.k1, &w.k2, &w.z, &w.sol, &w.ymix_out,
-                       &w.dA, &w.dB, &w.dC, &w.r, &w.dx, &w.rs, &w.cs};
+                       &w.dA, &w.dB, &w.dC, &w.r, &w.f2, &w.rs, &w.cs};
     for (double **p : vecs) TRY(dalloc(h, p, L * ni));
     TRY(dalloc(h, &w.jv, L * (size_t)std::max(h->nnz, 1)));
     TRY(dalloc(h, &w.geo, L * 5 * ni));
@@ -190,6 +190,8 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     }
     TRY(dalloc(h, &w.zf, L * ni));
     TRY(dalloc(h, &w.fallback, max_cols));
+    TRY(dalloc(h, &w.act32, max_cols));
+    TRY(dalloc(h, &w.thr64, max_cols));
     TRY(dalloc(h, &w.sweeps, 1));
     TRY(dalloc(h, &w.refine_err, max_cols));
     TRY(dalloc(h, &w.dt, max_cols));
@@ -269,6 +271,7 @@ extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const doub
     VK_CUDA(h, cudaMemcpyAsync(h->w.y, y, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaMemcpyAsync(h->w.ymix, ymix, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, ncols * sizeof(int), s));
+    vk::launch_reset_route(h->w, ncols, s);          // every column starts on the mixed path
     {
         vk::RunState &r = h->rs;
         VK_CUDA(h, cudaMemsetAsync(r.t, 0, ncols * sizeof(double), s));
@@ -354,23 +357,25 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
         h->launches += 6;
     } else {
-        cudaMemsetAsync(w.fallback, 0, b.ncols * sizeof(int), s);
+        // route: fallback[c] = column goes to FP64 this attempt, act32[c] = mixed
         cudaMemsetAsync(w.sweeps, 0, sizeof(int), s);
         cudaMemsetAsync(w.refine_err, 0, b.ncols * sizeof(double), s);
-        vk::launch_lu_reg32(net, b, w, s);
+        vk::launch_route(b, w, s);
+        DevBatch b32 = b;
+        b32.active = w.act32;
+        vk::launch_lu_reg32(net, b32, w, s);
         if (timed) cudaEventRecord(h->ev[2], s);
-        vk::launch_refine(net, b, w, w.f, w.k1, w.y, w.yk2, h->max_refine, h->refine_tol, s);
-        vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
-        vk::launch_refine(net, b, w, w.f, w.k2, w.y, nullptr, h->max_refine, h->refine_tol, s);
-        // columns whose refinement did not converge redo the attempt in FP64
+        vk::launch_refine(net, b32, w, w.f, w.k1, w.y, w.yk2, h->max_refine, h->refine_tol, s);
+        vk::launch_rates(net, b32, w.yk2, w.f2, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
+        vk::launch_refine(net, b32, w, w.f2, w.k2, w.y, nullptr, h->max_refine, h->refine_tol, s);
+        // FP64 columns: f(y) and the LHS of the first launch are still in place
         DevBatch bf = b;
         bf.active = w.fallback;
-        vk::launch_rates(net, bf, w.y, w.f, w.jv, w.dA, w.dB, w.dC, nullptr, w.dt, w.geo, flags, true, s);
         vk::launch_lu_fwd_f64(net, bf, w, w.f, w.z, flags, s);
         vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
         vk::launch_rates(net, bf, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
         vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
-        h->launches += 11;
+        h->launches += 12;
     }
     if (timed) cudaEventRecord(h->ev[3], s);
     vk::launch_stage(net, b, w, flags, mtol, atol, s);

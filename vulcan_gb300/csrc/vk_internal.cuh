@@ -101,10 +101,14 @@ struct Work {                  // per-handle device work buffers
     double *G;                 // [L][ni*ni] FP64 block inverses
     float *G32;                // [L][ni*ni] FP32 inverses of the scaled blocks (mixed mode)
     double *rs, *cs;           // [L][ni] power-of-two row / column scales (mixed mode)
-    double *r, *dx;            // refinement residual / correction
+    double *r;                 // refinement residual
+    double *f2;                // [L][ni] second-stage right-hand side (mixed mode)
     float *zf;                 // [L][ni] FP32 forward-sweep vector (mixed mode)
     float *D32;                // [L][stride] dense scaled FP32 blocks (mixed mode)
-    int *fallback;             // [ncols] refinement did not converge -> FP64 path
+    int *fallback;             // [ncols] attempt solved in FP64 (routed or refinement failed)
+    int *act32;                // [ncols] attempt solved by the FP32 factors + refinement
+    double *thr64;             // [ncols] step size at which refinement last failed: an
+                               //         attempt with dt >= thr64 goes straight to FP64
     int *sweeps;               // [1] most refinement sweeps any column needed
     double *refine_err;        // [ncols] last accepted correction size of the attempt
     double *dt;                // [ncols]
@@ -129,6 +133,8 @@ void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags
 void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
                    double *x, const double *yscale, double *yk2, int max_sweeps, double tol,
                    cudaStream_t s);
+void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
+void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
 cudaError_t init_lureg_kernels(const DevNet &net);
 void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,

@@ -17,6 +17,13 @@
 //   r = b - A x  (FP64, matrix-free from the sparse -J and dA/dB/dC) }
 // until max |d| / (|x| + |yscale| + 1e-10 n_0) <= tol or max sweeps; a
 // column that does not converge is flagged for the FP64 path.
+//
+// Routing.  At large dt the scaled diagonal blocks of a near-steady column
+// reach condition numbers of 1e10..1e16 (c0 -> 0 exposes the conserved and
+// slow chemical modes), beyond what FP32 factors can precondition: refinement
+// diverges.  A column whose refinement failed at step size dt therefore sends
+// every later attempt with a step >= dt straight to the FP64 path (thr64),
+// and tries the mixed path again only after its step has dropped below it.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -38,7 +45,8 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
          const double *__restrict__ rhs, double *__restrict__ x, double *__restrict__ res,
          float *__restrict__ zf, const double *__restrict__ yscale, double *__restrict__ yk2,
          const double *__restrict__ y, int max_sweeps, double tol, int *__restrict__ fallback,
-         int *__restrict__ sweeps_out, int *__restrict__ status, double *__restrict__ err_out) {
+         int *__restrict__ sweeps_out, int *__restrict__ status, double *__restrict__ err_out,
+         double *__restrict__ thr64, int *act32) {
     extern __shared__ __align__(16) unsigned char smr[];
     const int n = net.ni, NNP = block_stride32(n);
     const int c = blockIdx.x;
@@ -181,7 +189,11 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
         }
         if (timed_out) status[c] = VK_ETIMEOUT;
         else {
-            if (!converged) fallback[c] = 1;
+            if (!converged) {
+                fallback[c] = 1;
+                act32[c] = 0;                   // later mixed launches of this attempt skip it
+                thr64[c] = fmin(thr64[c], dt[c]);
+            }
             if (sweeps_out) atomicMax(sweeps_out, sweep + (converged ? 1 : 0));
             if (err_out) err_out[c] = fmax(err_out[c], m_prev);
         }
@@ -190,6 +202,31 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
     if (yk2) {
         for (int e = tid; e < nz * n; e += nth) yk2[base + e] = y[base + e] + x[base + e] / R_ROS;
     }
+}
+
+// fallback[c] = 1: this attempt of column c is solved in FP64 (its step is at or
+// above the size at which its refinement last failed); act32[c] = 1: mixed.
+__global__ void k_route(DevBatch b, const double *__restrict__ dt, const double *__restrict__ thr64,
+                        int *__restrict__ fallback, int *__restrict__ act32) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= b.ncols) return;
+    const int a = b.active ? b.active[c] : 1;
+    const int f64 = a && !(dt[c] < thr64[c]);
+    fallback[c] = f64;
+    act32[c] = a && !f64;
+}
+
+__global__ void k_reset_route(int ncols, double *__restrict__ thr64) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < ncols) thr64[c] = INFINITY;
+}
+
+void launch_route(const DevBatch &b, const Work &w, cudaStream_t s) {
+    k_route<<<(b.ncols + 127) / 128, 128, 0, s>>>(b, w.dt, w.thr64, w.fallback, w.act32);
+}
+
+void launch_reset_route(const Work &w, int ncols, cudaStream_t s) {
+    if (w.thr64) k_reset_route<<<(ncols + 127) / 128, 128, 0, s>>>(ncols, w.thr64);
 }
 
 cudaError_t init_mixed_kernels(int n) {
@@ -204,7 +241,8 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
     size_t sm = 16 + (size_t)2 * block_stride32(n) * sizeof(float) + 2 * n * sizeof(float);
     k_refine<<<b.ncols, 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
                                       rhs, x, w.r, w.zf, yscale, yk2, w.y, max_sweeps, tol,
-                                      w.fallback, w.sweeps, w.status, w.refine_err);
+                                      w.fallback, w.sweeps, w.status, w.refine_err, w.thr64,
+                                      w.act32);
 }
 
 }  // namespace vk

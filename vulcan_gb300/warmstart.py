@@ -8,10 +8,11 @@ at steady state.  It is trained on steady states produced by this package's
 own solver, with the hand-written BF16 kernels of vk_mlp.cu (forward,
 backward, Adam; PyTorch only holds the device memory).
 
-The proposal is projected onto the column's elemental composition
-(generalised iterative scaling per layer, mixing ratios summing to 1), so that
-plain Ros2 from the proposal conserves the same element totals as from
-``const_mix`` and converges to the same steady state.  Plain Ros2 then runs
+The proposal is projected onto the column's element totals (maximum-entropy
+projection: mixing ratios summing to 1 in every layer, column totals equal
+to those of ``const_mix``), so that plain Ros2 from the proposal conserves
+the same element totals as from ``const_mix`` and converges to the same
+steady state.  Plain Ros2 then runs
 to the reference's convergence test; a column whose proposal has a larger
 chemical residual than the const_mix start falls back to const_mix.
 """
@@ -58,50 +59,98 @@ def log_targets(ymix):
     return np.log10(np.clip(ymix, 10.0 ** LOG_FLOOR, None))
 
 
-def project_elements(x, compo, target, iters=100, tol=1e-12):
-    """Closest mixing ratios (in relative entropy) to the proposal x [nz, ni]
-    with sum_i x = 1 and element ratios sum_i compo[i,a] x_i = target[a]:
-    x_i = q_i exp(sum_k lambda_k F_ik), Newton on the multipliers lambda of
-    each layer (F = element counts plus a column of ones)."""
-    act = (target > 0) & (compo.sum(axis=0) > 0)
-    F = np.concatenate([compo[:, act], np.ones((compo.shape[0], 1))], axis=1)
-    T = np.concatenate([target[act], [1.0]])
-    nz, K = x.shape[0], F.shape[1]
-    logq = np.log(np.clip(x, 1e-300, None))
-    logq -= logq.max(axis=1, keepdims=True)
-    lam = np.zeros((nz, K))
+def project_columns(xs, n0s, comp, atom_inis, iters=100, tol=1e-12):
+    """Closest mixing ratios (in relative entropy) to each proposal x [nz, ni]
+    with sum_i x[j, i] = 1 in every layer and the column element totals
+    sum_j n0[j] sum_i comp[i, a] x[j, i] = atom_ini[a] (the reference's
+    atom_ini, op.py:2474-2481, sums number densities over layers).
 
-    def evalf(lm):
-        lx = logq + lm @ F.T
-        xx = np.exp(np.clip(lx, -745.0, 700.0))
-        phi = xx.sum(axis=1) - lm @ T           # convex dual objective
-        return xx, xx @ F - T[None, :], phi
+    x[j, i] = q[j, i] exp(comp[i] . lam + mu[j]); Newton on the convex dual in
+    (lam, mu) with mu eliminated by its diagonal block, Armijo backtracking;
+    all columns at once (layers padded to the longest column)."""
+    comp = np.asarray(comp, dtype=float)
+    nc, ni = len(xs), comp.shape[0]
+    nzs = np.array([x.shape[0] for x in xs])
+    Z = int(nzs.max())
+    lay = np.arange(Z)[None, :] < nzs[:, None]                      # [nc, Z]
+    tot = np.array([n.sum() for n in n0s])
+    w = np.zeros((nc, Z))
+    logq = np.full((nc, Z, ni), -1e4)
+    for c in range(nc):
+        w[c, :nzs[c]] = n0s[c] / tot[c]
+        lq = np.log(np.clip(xs[c], 1e-300, None))
+        logq[c, :nzs[c]] = lq - lq.max(axis=1, keepdims=True)
+    A = np.stack(atom_inis) / tot[:, None]                         # [nc, nel]
+    act = (A > 0) & (comp.sum(axis=0) > 0)[None, :]
+    T = np.where(act, A, 1.0)
+    F = comp
+    K = F.shape[1]
+    eye = np.eye(K)
+    lam = np.zeros((nc, K))
+    mu = -np.log(np.maximum(np.exp(logq).sum(axis=2), 1e-300)) * lay
 
-    xx, g, phi = evalf(lam)
+    def evalf(lm, mm):
+        lx = logq + np.einsum('ia,ca->ci', F, lm)[:, None, :] + mm[:, :, None]
+        xx = np.exp(np.clip(lx, -745.0, 700.0)) * lay[:, :, None]
+        s = xx.sum(axis=2)
+        xf = xx @ F                                               # [nc, Z, K]
+        g_l = np.where(act, np.einsum('cj,cja->ca', w, xf) - A, 0.0)
+        g_m = w * (s - 1.0)
+        phi = (w * s).sum(1) - (lm * A * act).sum(1) - (w * mm).sum(1)
+        return xx, s, xf, g_l, g_m, phi
+
+    def error(g_l, s):
+        return np.maximum(np.max(np.abs(g_l) / T, axis=1),
+                          np.max(np.where(lay, np.abs(s - 1.0), 0.0), axis=1))
+
+    xx, s, xf, g_l, g_m, phi = evalf(lam, mu)
+    done = np.zeros(nc, dtype=bool)
     for _ in range(iters):
-        err = np.max(np.abs(g) / T[None, :], axis=1)
-        todo = err >= tol
-        if not todo.any():
+        err = error(g_l, s)
+        done |= err < tol
+        if done.all():
             break
-        Hm = np.einsum('zi,ik,il->zkl', xx, F, F)
-        d = np.einsum('zkk->zk', Hm)
-        Hm = Hm + (1e-12 * d + 1e-250)[:, :, None] * np.eye(K)[None]
-        step = np.linalg.solve(Hm, g[:, :, None])[:, :, 0]
-        dec = np.einsum('zk,zk->z', g, step)      # directional decrease
-        t = np.ones(nz)
-        acc = ~todo
-        lam_n, xn, gn, phin = lam.copy(), xx.copy(), g.copy(), phi.copy()
-        for _ in range(40):                        # Armijo backtracking per layer
-            cand = lam - t[:, None] * step
-            xc, gc, pc = evalf(cand)
-            ok = (~acc) & (pc <= phi - 1e-4 * t * dec)
-            lam_n[ok], xn[ok], gn[ok], phin[ok] = cand[ok], xc[ok], gc[ok], pc[ok]
+        v = np.einsum('cj,cji->ci', w, xx)
+        Hll = np.einsum('ci,ia,ib->cab', v, F, F, optimize=True)
+        h = w[:, :, None] * xf                                    # [nc, Z, K]
+        d = w * s + (~lay) + 1e-300
+        Sc = Hll - np.einsum('cja,cjb->cab', h, h / d[:, :, None], optimize=True)
+        # inactive elements: identity rows
+        Sc = np.where(act[:, :, None] & act[:, None, :], Sc, 0.0) + (~act)[:, :, None] * eye
+        tr = np.einsum('caa->c', Sc)
+        Sc = Sc + (1e-12 * tr / K + 1e-300)[:, None, None] * eye
+        rhs = g_l - np.einsum('cja,cj->ca', h, g_m / d)
+        dl = np.linalg.solve(Sc, rhs[:, :, None])[:, :, 0] * act
+        dm = (g_m - np.einsum('cja,ca->cj', h, dl)) / d * lay
+        dl[done], dm[done] = 0.0, 0.0
+        dec = (g_l * dl).sum(1) + (g_m * dm).sum(1)
+        t = np.ones(nc)
+        acc = done.copy()
+        new = [v.copy() for v in (xx, s, xf, g_l, g_m, phi)]
+        lam_n, mu_n = lam.copy(), mu.copy()
+        for _ in range(60):
+            cl, cm = lam - t[:, None] * dl, mu - t[:, None] * dm
+            cand = evalf(cl, cm)
+            # Armijo on the dual, or (once its decrease is below rounding of
+            # phi) a halving of the constraint error
+            ok = (~acc) & ((cand[5] <= phi - 1e-4 * t * dec)
+                           | (error(cand[3], cand[1]) < 0.5 * err))
+            for v, cv in zip(new, cand):
+                v[ok] = cv[ok]
+            lam_n[ok], mu_n[ok] = cl[ok], cm[ok]
             acc |= ok
             if acc.all():
                 break
             t = np.where(acc, t, 0.5 * t)
-        lam, xx, g, phi = lam_n, xn, gn, phin
-    return xx
+        done |= ~acc                                  # no decrease possible: at the floor
+        lam, mu = lam_n, mu_n
+        xx, s, xf, g_l, g_m, phi = new
+    return [xx[c, :nzs[c]] for c in range(nc)]
+
+
+def project_column(x, n0, comp, atom_ini, iters=100, tol=1e-12):
+    """project_columns for one column."""
+    return project_columns([x], [n0], comp, [np.asarray(atom_ini, dtype=float)], iters, tol)[0]
 
 
 class MLP:
@@ -245,24 +294,18 @@ class MLP:
         return m
 
 
-def propose(model, specs, net, items):
-    """Warm-start states for column items (from batch.build_items): returns
-    a list of (y, ymix, used_warm) with the proposal projected onto each
-    column's elemental composition."""
-    out = []
-    atoms = net.compo_atoms
-    comp = net.compo.astype(float)
-    for spec, it in zip(specs, items):
-        f = column_features(spec, net)
-        logx = model.predict(f)
-        x = 10.0 ** np.clip(logx, LOG_FLOOR, 0.0)
-        ymix0 = it['ymix']
-        target = ymix0[0] @ comp                        # element ratios of the const_mix start
-        x = project_elements(x, comp, target)
-        y = it['col'].n_0[:, None] * x
-        out.append((y, x))
-    del atoms
-    return out
+def propose(model, specs, net, items, atom_list=('H', 'O', 'C', 'He', 'N')):
+    """Warm-start states for column items (from batch.build_items): returns a
+    list of (y, ymix), each proposal projected onto its column's element
+    totals (those of the const_mix start, which the run then conserves)."""
+    comp = net.compo_for(list(atom_list)).astype(float)
+    feats = [column_features(sp, net) for sp in specs]
+    logx = model.predict(np.concatenate(feats))
+    off = np.concatenate([[0], np.cumsum([f.shape[0] for f in feats])])
+    xs = [10.0 ** np.clip(logx[off[c]:off[c + 1]], LOG_FLOOR, 0.0) for c in range(len(specs))]
+    n0s = [it['col'].n_0 for it in items]
+    xs = project_columns(xs, n0s, comp, [np.asarray(it['atom_ini'], dtype=float) for it in items])
+    return [(n0[:, None] * x, x) for n0, x in zip(n0s, xs)]
 
 
 def chem_residual(h, y, n0, batch):
@@ -302,10 +345,10 @@ def _run_to_steady(net, specs, items, atoms, precision, count_max, timeout_s, ch
 
 
 def generate(net, seeds, ncols, atoms, count_max=4000, timeout_s=900, precision=1, log=print):
-    """Run seeded batches to steady state; return (features, targets) of the
-    converged columns (one sample per layer)."""
+    """Run seeded batches to steady state; return (features, targets, column
+    id) of the converged columns (one sample per layer)."""
     from . import batch as bmod, configs
-    Xs, Ys = [], []
+    Xs, Ys, Cs = [], [], []
     for seed in seeds:
         specs = configs.config2_columns(ncols=ncols, seed=seed)
         items = bmod.build_items(specs, net)
@@ -316,29 +359,26 @@ def generate(net, seeds, ncols, atoms, count_max=4000, timeout_s=900, precision=
             ym = st['ymix'][b.off[c]:b.off[c + 1]]
             Xs.append(column_features(specs[c], net))
             Ys.append(log_targets(ym))
+            Cs.append(np.full(ym.shape[0], seed * 100000 + c))
         log('seed %d: %d/%d converged, median steps %s, %.1f s'
             % (seed, conv.sum(), ncols, np.median(st['count'][conv]) if conv.any() else None,
                st['wall_s']))
-    return np.concatenate(Xs), np.concatenate(Ys)
+    return np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Cs)
 
 
 def warm_items(model, specs, net, items, atoms, precision=1):
     """Items started from the projected MLP proposal where its chemical
-    residual is below that of the const_mix start; returns (items, used_mask)."""
+    residual is below that of the const_mix start; returns (items, used_mask).
+    The element totals (atom_ini) stay those of the const_mix start."""
     from . import batch as bmod
-    from . import column as cm
-    prop = propose(model, specs, net, items)
+    prop = propose(model, specs, net, items, atom_list=atoms)
     h, b = bmod.make_batch_handle(net, items, atoms, precision=precision)
     n0 = np.concatenate([it['col'].n_0 for it in items])
     r_const = chem_residual(h, np.concatenate([it['y'] for it in items]), n0, b)
     r_warm = chem_residual(h, np.concatenate([p[0] for p in prop]), n0, b)
     h.close()
     used = r_warm < r_const
-    out = []
-    for it, (y, x), u, sp in zip(items, prop, used, specs):
-        if u:
-            it = dict(it, y=y, ymix=x, atom_ini=cm.atom_totals(net, y, sp.atom_list))
-        out.append(it)
+    out = [dict(it, y=y, ymix=x) if u else it for it, (y, x), u in zip(items, prop, used)]
     return out, used
 
 
@@ -354,23 +394,34 @@ def main(argv=None):
     ap.add_argument('--ncols', type=int, default=512)
     ap.add_argument('--data', default='warmstart_data.npz')
     ap.add_argument('--model', default='warmstart_model.npz')
-    ap.add_argument('--epochs', type=int, default=40)
+    ap.add_argument('--epochs', type=int, default=100)
+    ap.add_argument('--lr', type=float, default=1e-3)
+    ap.add_argument('--batch', type=int, default=4096)
+    ap.add_argument('--width', type=int, default=512)
+    ap.add_argument('--depth', type=int, default=4)
     ap.add_argument('--count-max', type=int, default=4000)
     ap.add_argument('--timeout', type=float, default=900)
     a = ap.parse_args(argv)
     net = Network.from_npz(a.net) if a.net.endswith('.npz') else Network.from_file(a.net)
     atoms = ['H', 'O', 'C', 'He', 'N']
     if a.cmd == 'generate':
-        X, Y = generate(net, [int(s) for s in a.seeds.split(',')], a.ncols, atoms,
-                        count_max=a.count_max, timeout_s=a.timeout)
-        np.savez_compressed(a.data, X=X, Y=Y)
+        X, Y, cid = generate(net, [int(s) for s in a.seeds.split(',')], a.ncols, atoms,
+                             count_max=a.count_max, timeout_s=a.timeout)
+        np.savez_compressed(a.data, X=X.astype(np.float32), Y=Y.astype(np.float32), col=cid)
         print(json.dumps({'samples': int(X.shape[0]), 'data': os.path.abspath(a.data)}))
     else:
         d = np.load(a.data)
-        m = MLP(d['X'].shape[1], d['Y'].shape[1])
-        hist = m.fit(d['X'], d['Y'], epochs=a.epochs, log=print)
+        X, Y, cid = d['X'].astype(np.float64), d['Y'].astype(np.float64), d['col']
+        cols = np.unique(cid)
+        val = np.isin(cid, cols[::10])               # every tenth column held out
+        m = MLP(X.shape[1], Y.shape[1], width=a.width, depth=a.depth)
+        hist = m.fit(X[~val], Y[~val], epochs=a.epochs, batch=a.batch, lr=a.lr, log=print)
+        err = np.abs(m.predict(X[val]) - Y[val])     # dex
         m.save(a.model)
-        print(json.dumps({'samples': int(d['X'].shape[0]), 'loss_first': hist[0], 'loss_last': hist[-1]}))
+        print(json.dumps({'samples': int(X.shape[0]), 'columns': int(cols.size),
+                          'loss_first': hist[0], 'loss_last': hist[-1],
+                          'val_dex_mean': float(err.mean()), 'val_dex_p99': float(np.percentile(err, 99)),
+                          'val_dex_mean_ymix_gt_1e-10': float(err[Y[val] > -10].mean())}))
 
 
 if __name__ == '__main__':
