@@ -82,3 +82,10 @@ def step_tolerance(e_floor, d_floor):
     """Per-attempt tolerances: 1e-10 (floor metric) and 1e-6 (delta) where the
     step is well conditioned, else 10x the reference's own conditioning floor."""
     return max(1e-10, 10 * e_floor), max(1e-6, 10 * d_floor)
+
+
+def atm_from_column(col):
+    """Oracle atmosphere dict of a column.Column (set-up arrays as built)."""
+    keys = ('M', 'n_0', 'Tco', 'Kzz', 'vz', 'Dzz', 'Ti', 'ms', 'alpha', 'pico', 'dzi', 'Hpi',
+            'g', 'Hp', 'dz', 'zco', 'top_flux', 'bot_flux', 'bot_vdep')
+    return {k: getattr(col, k) for k in keys}

@@ -1,0 +1,100 @@
+"""Synthetic 150-species stress network (ni = 150, 1200 reversible reactions,
+60 frozen photolysis channels, nz = 200): generator checks on the CPU, and on
+the GPU the chemistry and whole Ros2 attempts against the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import atm_from_column, floor_err
+from oracle import ros2 as O
+from vulcan_gb300 import batch, configs, synthnet
+from vulcan_gb300.network import Network
+
+ATOMS = ['H', 'O', 'C', 'He', 'N']
+
+
+@pytest.fixture(scope='module')
+def syn(tmp_path_factory):
+    d = tmp_path_factory.mktemp('syn150')
+    path = synthnet.generate(str(d))
+    net = Network.from_file(path, use_photo=True)
+    npz = os.path.join(str(d), 'net.npz')
+    net.to_npz(npz)
+    return path, net, npz
+
+
+def test_sizes_and_element_balance(syn):
+    path, net, _ = syn
+    assert net.ni == 150
+    kinds = [r.kind for r in net.reactions]
+    assert kinds.count('photo') == 60
+    rev = [r for r in net.reactions if r.kind != 'photo' and r.text != 'He -> He']
+    assert len(rev) == 1200
+    assert sum(r.kind == 'falloff' for r in rev) == 180
+    comp = net.compo_for(ATOMS)
+    si = {s: k for k, s in enumerate(net.species)}
+    for r in net.reactions:
+        a = sum(nu * comp[si[s]] for nu, s in r.reac if s != 'M')
+        b = sum(nu * comp[si[s]] for nu, s in r.prod if s != 'M')
+        np.testing.assert_array_equal(a, b, err_msg=r.text)
+
+
+def test_deterministic(tmp_path, syn):
+    p2 = synthnet.generate(str(tmp_path))
+    assert open(p2).read() == open(syn[0]).read()
+
+
+def test_compiles_for_device_tables(syn):
+    from vulcan_gb300.solver import GPUNetwork
+    g = GPUNetwork(syn[1], ATOMS)
+    rows, cols = g.jac_pattern()
+    assert 150 <= len(rows) <= 150 * 150
+
+
+def _column(net, nz):
+    specs = configs.config4_columns(sorted(net.photo_index()), ncols=2, nz=nz)
+    items = batch.build_items(specs, net)
+    for sp, it in zip(specs, items):
+        pidx = net.photo_index()
+        for key in sp.photo_J:
+            assert it['k'][pidx[key] - 1].max() > 0
+    return specs, items
+
+
+@pytest.mark.gpu
+def test_chem_source_matches_oracle(syn):
+    from vulcan_gb300 import _build
+    _build.build()
+    path, net, npz = syn
+    specs, items = _column(net, 40)
+    h, b = batch.make_batch_handle(net, items, ATOMS)
+    on = O.OracleNet.from_npz(npz, ATOMS)
+    rng = np.random.default_rng(0)
+    y = np.concatenate([it['y'] * (1 + 0.5 * rng.random(it['y'].shape)) + 1e3 for it in items])
+    src = h.chem_source(y)
+    for c, it in enumerate(items):
+        sl = slice(b.off[c], b.off[c + 1])
+        ref = O.chemdf(on, y[sl], it['col'].M, it['k'])
+        scale = np.abs(ref).max(axis=1, keepdims=True)
+        assert np.max(np.abs(src[sl] - ref) / scale) <= 1e-12
+    h.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', [0, 1])
+def test_attempt_matches_oracle(syn, precision):
+    from vulcan_gb300 import _build
+    _build.build()
+    path, net, npz = syn
+    specs, items = _column(net, 30)
+    h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
+    on = O.OracleNet.from_npz(npz, ATOMS)
+    for dt in (1e-10, 1e-6):
+        sol = h.attempt(np.full(b.ncols, dt))['sol']
+        for c, it in enumerate(items):
+            sl = slice(b.off[c], b.off[c + 1])
+            r = O.ros2_attempt(on, it['y'], it['ymix'], dt, it['k'], atm_from_column(it['col']),
+                               O.Flags(), O.Tol())
+            assert floor_err(sol[sl], r.sol, it['col'].n_0) <= 1e-10
+    h.close()

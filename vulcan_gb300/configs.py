@@ -123,3 +123,26 @@ def config2_columns(ncols=512, seed=2, nz_range=(60, 200)):
             const_mix=solar_mix(met=met, c_to_o=c_to_o, with_n=True),
             atom_list=['H', 'O', 'C', 'He', 'N'], conver_ignore=['HC3N']))
     return specs
+
+
+def config4_columns(photo_channels, ncols=128, seed=4, nz=200,
+                    network='SYN150_network.txt'):
+    """Seeded columns on the synthetic 150-species stress network
+    (synthnet.generate): nz = 200, T/Kzz/metallicity drawn like the uneven
+    NCHO batch, frozen J on its 60 photolysis channels."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    pco = log_p_grid(nz)
+    for _ in range(ncols):
+        T_bot = rng.uniform(1200., 3000.)
+        T_top = rng.uniform(500., 1500.)
+        logK = rng.uniform(5., 10.)
+        met = 10.0 ** rng.uniform(-1., 2.)
+        c_to_o = rng.uniform(0.3, 1.2)
+        specs.append(ColumnSpec(
+            network=network, use_photo=True, pco=pco,
+            Tco=linear_logp_T(pco, T_bot, T_top), Kzz=np.full(nz - 1, 10.0 ** logK),
+            const_mix=solar_mix(met=met, c_to_o=c_to_o, with_n=True),
+            atom_list=['H', 'O', 'C', 'He', 'N'], conver_ignore=[],
+            photo_J=photo_J_profile(rng, pco, photo_channels)))
+    return specs

@@ -191,15 +191,16 @@ template <int TY, int RA, int RB>
 __global__ void __launch_bounds__(16 * TY, TY == 16 && RA <= 5 ? 2 : 1)
 k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__restrict__ dB,
        const double *__restrict__ dC, const double *__restrict__ rsc,
-       const double *__restrict__ csc, float *__restrict__ G32, int *__restrict__ status) {
+       const double *__restrict__ csc, float *__restrict__ G32, int *__restrict__ status,
+       int nbuf) {
     extern __shared__ __align__(16) unsigned char smb[];
     const int n = net.ni, nn = n * n, NNP = block_stride32(n);
     const int c = blockIdx.x;
     if (b.active && !b.active[c]) return;
     const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smb);             // [2]
-    float *Dbuf = reinterpret_cast<float *>(smb + 16);             // [2][NNP]
-    float *Gs = Dbuf + 2 * NNP;                                    // [nn]
+    float *Dbuf = reinterpret_cast<float *>(smb + 16);             // [nbuf][NNP]
+    float *Gs = Dbuf + nbuf * NNP;                                 // [nn]
     float *rowv = Gs + nn;
     float *colv = rowv + n;
     float *alpha = colv + n;
@@ -241,14 +242,17 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
             dC_nx = dC[(l + 1) * n + tid];
             dB_nx = dB[(l + 1) * n + tid];
         }
-        const bool ok = mbar_wait(&bar[buf], (j >> 1) & 1);
+        // two buffers: block j in buffer j&1, the j-th use of that barrier;
+        // one buffer (large ni): every block in buffer 0, phase j&1
+        const int bsel = nbuf == 2 ? buf : 0;
+        const bool ok = mbar_wait(&bar[bsel], nbuf == 2 ? (j >> 1) & 1 : j & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) status[c] = VK_ETIMEOUT;
             return;                          // no other copy was issued after this one
         }
-        if (tid == 0 && j + 1 < nz)
+        if (nbuf == 2 && tid == 0 && j + 1 < nz)
             tma_load_1d(Dbuf + (buf ^ 1) * NNP, D32 + (l + 1) * NNP, bytes, &bar[buf ^ 1]);
-        const float *Dj = Dbuf + buf * NNP;
+        const float *Dj = Dbuf + bsel * NNP;
         float M[RA][RB];
 #pragma unroll
         for (int a = 0; a < RA; ++a) {
@@ -266,6 +270,10 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
         }
         for (int t = tid; t < n; t += nth) used[t] = 0;
         __syncthreads();
+        // one buffer: block j is in registers now, so the copy of block j+1
+        // overwrites it while the inversion runs
+        if (nbuf == 1 && tid == 0 && j + 1 < nz)
+            tma_load_1d(Dbuf, D32 + (l + 1) * NNP, bytes, &bar[0]);
         gj_invert_reg<float, TY, RA, RB>(M, n, ty, tx, sh);
         gj_store_natural<float, TY, RA, RB>(M, n, ty, tx, sh, Gs);
         float *Gl = G32 + l * NNP;
@@ -284,10 +292,13 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
 
 // ---------------------------------------------------------------------------
 static size_t smem64(int n) { return (size_t)(n * n + 5 * n) * sizeof(double) + 3 * n * sizeof(int) + 16; }
-static size_t smem32(int n) {
-    return 16 + (size_t)2 * block_stride32(n) * sizeof(float) + (size_t)(n * n + 4 * n) * sizeof(float)
+static size_t smem32(int n, int nbuf) {
+    return 16 + (size_t)nbuf * block_stride32(n) * sizeof(float) + (size_t)(n * n + 4 * n) * sizeof(float)
            + 3 * n * sizeof(int) + 16;
 }
+static int g_smem_optin = 0;         // opt-in shared memory per block of this device
+// double-buffered block stream where it fits, else one buffer (ni above ~120)
+static int lu32_nbuf(int n) { return smem32(n, 2) <= (size_t)g_smem_optin ? 2 : 1; }
 static size_t smem_prep(const DevNet &net) {
     const int n = net.ni;
     return (size_t)(net.nnz + 3 * n) * sizeof(double) + (size_t)n * n * sizeof(float) + n * sizeof(int) + 16;
@@ -306,7 +317,11 @@ cudaError_t init_lureg_kernels(const DevNet &net) {
     const int n = net.ni;
     cudaError_t e = cudaFuncSetAttribute(k_prep32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem_prep(net));
-    size_t s64 = smem64(n), s32 = smem32(n);
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    size_t s64 = smem64(n), s32 = smem32(n, lu32_nbuf(n));
 #define SETATTR(TY, RA, RB)                                                                      \
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu_reg64<TY, RA, RB>,                       \
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s64); \
@@ -332,12 +347,13 @@ void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const 
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s) {
     const int n = net.ni;
     k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs);
-    size_t sm = smem32(n);
+    const int nb = lu32_nbuf(n);
+    size_t sm = smem32(n, nb);
     switch (tiling_of(n)) {
-    case 0: k_lu32<16, 3, 3><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
-    case 1: k_lu32<16, 5, 5><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
-    case 2: k_lu32<16, 7, 7><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
-    default: k_lu32<32, 5, 10><<<b.ncols, 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status); break;
+    case 0: k_lu32<16, 3, 3><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 1: k_lu32<16, 5, 5><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 2: k_lu32<16, 7, 7><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    default: k_lu32<32, 5, 10><<<b.ncols, 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
     }
 }
 
