@@ -41,6 +41,7 @@ sys.path.insert(0, REPO)
 METRIC = "columns-to-steady-state/hr & Ros2 steps/s: learned+mixed vs plain FP64, 1 GB300"
 UNIT = "column-steps/s"
 NCOLS = 512
+C4_NCOLS = 128
 SEED = 2
 ATOMS = ['H', 'O', 'C', 'He', 'N']
 NET = os.path.join(REPO, 'tests', 'golden', 'net_NCHO_thermo.npz')
@@ -155,6 +156,20 @@ def fp64_peak_tflops():
 
 
 # ------------------------------------------------------------ GPU arm
+def _workload(args, ncols=None):
+    """(network, column specs) of the selected workload."""
+    from vulcan_gb300 import configs
+    from vulcan_gb300.network import Network
+    if getattr(args, 'workload', 'c2') == 'c4':
+        from vulcan_gb300 import synthnet
+        net = Network.from_file(synthnet.generate(os.path.join(REPO, '_build', 'syn150')),
+                                use_photo=True)
+        specs = configs.config4_columns(sorted(net.photo_index()), ncols=C4_NCOLS)
+        return net, specs[:ncols or args.ncols or C4_NCOLS]
+    net = Network.from_npz(NET)
+    return net, configs.config2_columns(ncols=NCOLS, seed=SEED)[:ncols or args.ncols or NCOLS]
+
+
 def _setup(args, precision, ncols=None, warm_model=None):
     """Handle over the workload's columns; with warm_model, the columns whose
     learned proposal beats const_mix start from it (returns the mask too)."""
@@ -162,8 +177,7 @@ def _setup(args, precision, ncols=None, warm_model=None):
     from vulcan_gb300.network import Network
     from vulcan_gb300.solver import ctrl_from
     _build.build()
-    net = Network.from_npz(NET)
-    specs = configs.config2_columns(ncols=NCOLS, seed=SEED)[:ncols or args.ncols]
+    net, specs = _workload(args, ncols)
     items = batch.build_items(specs, net)
     used = None
     if warm_model is not None:
@@ -217,6 +231,8 @@ def _measure(args, precision, clocks=None):
     out['bytes_state'] = b.L * net.ni * 8
     out['layers'] = int(b.L)
     out['ni'] = net.ni
+    out['nr'] = net.nr
+    out['npair'] = net.npair
     h.close()
     return out
 
@@ -248,16 +264,23 @@ def run_gpu(args):
         roof[k] = round(roof[k], 4)
     peak64 = fp64_peak_tflops()
     lu64 = float(L) * ni ** 3 * 2.0 / (plain['attempt_ms']['lu'] * 1e-3) / 1e12
-    rate_bytes = float(L) * (782 * 8 + 3 * ni * 8 + 4 * ni * 8)
+    rate_bytes = float(L) * (mixed['nr'] * 8 + 3 * ni * 8 + 4 * ni * 8)
+    if args.workload == 'c4':
+        wl = ('batched Ros2 steps, %d columns of nz=200 on a synthetic 150-species network '
+              '(1200 reversible + 60 frozen photolysis reactions)' % args.ncols)
+        netname = 'synthetic SYN150 (150 species, %d pairs)' % mixed['npair']
+    else:
+        wl = ('batched Ros2 steps, %d uneven NCHO-thermo columns (ni=69, nz 60-200, '
+              'sum nz=%d)' % (args.ncols, L))
+        netname = 'NCHO_thermo (69 species, 391 pairs)'
     out = {
         'metric': METRIC, 'value': round(mixed['value'], 2), 'unit': UNIT, 'n_gpus': 1,
         'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': round(mixed['ms'] / max(args.steps, 1), 3),
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
         'data': 'synthetic (seeded columns; no dataset)',
-        'config': {'workload': 'batched Ros2 steps, %d uneven NCHO-thermo columns (ni=69, nz 60-200, '
-                               'sum nz=%d); FP32 scaled block LU + FP64 refinement' % (args.ncols, L),
-                   'ncols': args.ncols, 'layers': L, 'network': 'NCHO_thermo (69 species, 391 pairs)',
+        'config': {'workload': wl + '; FP32 scaled block LU + FP64 refinement',
+                   'ncols': args.ncols, 'layers': L, 'network': netname,
                    'precision': 'mixed (FP64 rates/residual/error control, FP32 LU)',
                    'l2': 'inputs larger than L2 (state, k, Jacobian, inverses > 3 GB)'},
         'e2e': {'value': round(mixed['e2e'], 2), 'unit': UNIT,
@@ -278,7 +301,7 @@ def run_gpu(args):
                          'frac': round(rate_bytes / (am['rates'] * 1e-3) / 1e9 / hbm, 4)},
     }
     out['clocks'] = clocks.summary()
-    if not args.no_cpu:
+    if not args.no_cpu and args.workload == 'c2':
         out['cpu_baseline'] = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
     print(json.dumps(out))
 
@@ -365,8 +388,7 @@ def run_converge(args):
     res['workload'] = ('%d uneven NCHO-thermo columns to steady state (reference conv criterion, '
                        'count_max %d)' % (args.ncols, args.count_max))
     if 'plain_fp64' in finals:
-        bsz = [it.pco.size for it in __import__('vulcan_gb300.configs', fromlist=['x']).config2_columns(
-            ncols=NCOLS, seed=SEED)[:args.ncols]]
+        bsz = [it.pco.size for it in _workload(args)[1]]
         off = np.concatenate([[0], np.cumsum(bsz)])
         yp, ep = finals['plain_fp64'][0], finals['plain_fp64'][1]
         for name in finals:
@@ -397,8 +419,7 @@ def run_profile(args):
     from vulcan_gb300 import _build, batch, configs
     from vulcan_gb300.network import Network
     _build.build()
-    net = Network.from_npz(NET)
-    specs = configs.config2_columns(ncols=NCOLS, seed=SEED)[:args.ncols]
+    net, specs = _workload(args)
     items = batch.build_items(specs, net)
     prec = 1 if args.precision == 'mixed' else 0
     h, b = batch.make_batch_handle(net, items, ATOMS, precision=prec)
@@ -434,7 +455,10 @@ def main():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--cpu-cols', type=int, default=16)
     ap.add_argument('--cpu-steps', type=int, default=8)
-    ap.add_argument('--ncols', type=int, default=NCOLS)
+    ap.add_argument('--ncols', type=int, default=None,
+                    help='columns (default 512 for c2, 128 for c4)')
+    ap.add_argument('--workload', default='c2', choices=['c2', 'c4'],
+                    help='c2: uneven NCHO-thermo batch; c4: synthetic 150-species network, nz=200')
     ap.add_argument('--profile', action='store_true',
                     help='only run --attempts instrumented attempts (for ncu captures)')
     ap.add_argument('--attempts', type=int, default=2)
@@ -451,6 +475,8 @@ def main():
                     help='learned warm-start weights (converge mode)')
     ap.add_argument('--cpu-workers', type=int, default=min(16, os.cpu_count() or 1))
     args = ap.parse_args()
+    if args.ncols is None:
+        args.ncols = C4_NCOLS if args.workload == 'c4' else NCOLS
     rank = int(os.environ.get('RANK', '0'))
     if args.impl == 'reference':
         if rank == 0:

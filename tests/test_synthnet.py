@@ -14,10 +14,13 @@ from vulcan_gb300.network import Network
 ATOMS = ['H', 'O', 'C', 'He', 'N']
 
 
+BUILD = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), '_build', 'tests')
+
+
 @pytest.fixture(scope='module')
-def syn(tmp_path_factory):
-    d = tmp_path_factory.mktemp('syn150')
-    path = synthnet.generate(str(d))
+def syn():
+    d = os.path.join(BUILD, 'syn150')
+    path = synthnet.generate(d)
     net = Network.from_file(path, use_photo=True)
     npz = os.path.join(str(d), 'net.npz')
     net.to_npz(npz)
@@ -40,8 +43,8 @@ def test_sizes_and_element_balance(syn):
         np.testing.assert_array_equal(a, b, err_msg=r.text)
 
 
-def test_deterministic(tmp_path, syn):
-    p2 = synthnet.generate(str(tmp_path))
+def test_deterministic(syn):
+    p2 = synthnet.generate(os.path.join(BUILD, 'syn150_again'))
     assert open(p2).read() == open(syn[0]).read()
 
 
