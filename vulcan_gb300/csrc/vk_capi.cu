@@ -43,6 +43,9 @@ struct vk_handle {
     double *d_compo = nullptr;
     // batch
     int *d_col_off = nullptr, *d_lay_col = nullptr;
+    int *d_order = nullptr;             // columns by decreasing nz
+    unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
+    int pgrid_max = 0;                  // CTAs of the per-column kernels (0 = one per column)
     double *d_k = nullptr, *d_atm = nullptr, *d_Dzz = nullptr, *d_spf = nullptr;
     vk::Work w{};
     // batched-run state
@@ -72,6 +75,9 @@ struct vk_handle {
         b.ncols = ncols; b.L = L; b.col_off = d_col_off; b.lay_col = d_lay_col;
         b.k = d_k; b.atm = d_atm; b.Dzz = d_Dzz; b.spf = d_spf;
         b.active = nullptr;
+        b.order = d_order;
+        b.queue = d_queue;
+        b.pgrid = (pgrid_max > 0 && pgrid_max < ncols) ? pgrid_max : ncols;
         return b;
     }
 };
@@ -171,6 +177,18 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_jmap, net->jmap));
     const size_t L = (size_t)max_layers, ni = (size_t)h->ni;
     TRY(dalloc(h, &h->d_col_off, max_cols + 1));
+    TRY(dalloc(h, &h->d_order, max_cols));
+    TRY(dalloc(h, &h->d_queue, 1));
+    {
+        // per-column kernels: VK_CTAS_PER_SM resident CTAs per SM take columns
+        // from the queue (unset or 0: one CTA per column)
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const char *env = getenv("VK_CTAS_PER_SM");
+        const int cps = env ? atoi(env) : 0;
+        h->pgrid_max = cps > 0 ? cps * nsm : 0;
+    }
     TRY(dalloc(h, &h->d_lay_col, L));
     TRY(dalloc(h, &h->d_k, L * h->nr));
     TRY(dalloc(h, &h->d_atm, L * VK_ATM_NF));
@@ -263,6 +281,14 @@ extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const doub
     const size_t ni = h->ni;
     cudaStream_t s = h->stream;
     VK_CUDA(h, cudaMemcpyAsync(h->d_col_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    {
+        // longest columns first: the work queue then balances the SMs
+        std::vector<int> order(ncols);
+        for (int c = 0; c < ncols; ++c) order[c] = c;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return nz[a] > nz[b2]; });
+        VK_CUDA(h, cudaMemcpyAsync(h->d_order, order.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaStreamSynchronize(s));
+    }
     VK_CUDA(h, cudaMemcpyAsync(h->d_lay_col, lay_col.data(), L * sizeof(int), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaMemcpyAsync(h->d_k, k, (size_t)L * h->nr * sizeof(double), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaMemcpyAsync(h->d_atm, atm, (size_t)L * VK_ATM_NF * sizeof(double), cudaMemcpyHostToDevice, s));

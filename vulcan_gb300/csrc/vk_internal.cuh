@@ -83,7 +83,26 @@ struct DevBatch {
     const double *Dzz;         // [L][ni]
     const double *spf;         // [ncols][VK_SP_NF][ni]
     const int *active;         // [ncols] non-zero = column takes part (NULL = all)
+    const int *order;          // [ncols] columns by decreasing nz (work-queue order)
+    unsigned *queue;           // [1] next queue position (zeroed before each launch)
+    int pgrid;                 // CTAs of the per-column kernels (<= ncols)
 };
+
+#ifdef __CUDACC__
+// Per-column kernels run as a work queue: each CTA takes the next column in
+// b.order (longest first) until the queue is empty, so the SMs finish
+// together however uneven the columns are.  All threads call it; returns -1
+// when no column is left.
+__device__ __forceinline__ int next_column(const DevBatch &b, int *s_col) {
+    __syncthreads();                 // everyone has read the previous s_col
+    if (threadIdx.x == 0) {
+        const unsigned i = atomicAdd(b.queue, 1u);
+        *s_col = i < (unsigned)b.ncols ? b.order[i] : -1;
+    }
+    __syncthreads();
+    return *s_col;
+}
+#endif
 
 // Launch helpers implemented in vk_kernels.cu (all asynchronous on stream).
 namespace vk {
@@ -137,8 +156,6 @@ void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
 void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
 cudaError_t init_lureg_kernels(const DevNet &net);
-void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
-                     double *z, cudaStream_t s);
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
 
 }  // namespace vk

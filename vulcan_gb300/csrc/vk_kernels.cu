@@ -205,55 +205,56 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
              double *__restrict__ G, double *__restrict__ z, int *__restrict__ status) {
     extern __shared__ double sm[];
     const int n = net.ni, nn = n * n;
-    const int c = blockIdx.x;
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     double *A = sm;
     double *colk = A + nn;
     double *rowk = colk + n;
     double *zp = rowk + n;
     double *bb = zp + n;
     int *perm = reinterpret_cast<int *>(bb + n);
-    __shared__ int s_piv, s_sing;
+    __shared__ int s_piv, s_sing, s_col;
     __shared__ double s_pval;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
-    if (tid == 0) s_sing = 0;
-    const double c0 = 1.0 / (R_ROS * dt[c]);
-    for (int j = 0; j < nz; ++j) {
-        const size_t l = (size_t)l0 + j;
-        const double *cj = dC + l * n;
-        const double *bm = j > 0 ? dB + (l - 1) * n : dB;
-        const double *aj = dA + l * n;
-        for (int e = tid; e < nn; e += nth) {
-            int r = e / n, q = e - r * n;
-            double v = j > 0 ? -cj[r] * A[e] * bm[q] : 0.0;
-            if (r == q) v += c0 - aj[r];
-            A[e] = v;
+    for (int c; (c = next_column(b, &s_col)) >= 0;) {
+        if (b.active && !b.active[c]) continue;
+        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        if (tid == 0) s_sing = 0;
+        const double c0 = 1.0 / (R_ROS * dt[c]);
+        for (int j = 0; j < nz; ++j) {
+            const size_t l = (size_t)l0 + j;
+            const double *cj = dC + l * n;
+            const double *bm = j > 0 ? dB + (l - 1) * n : dB;
+            const double *aj = dA + l * n;
+            for (int e = tid; e < nn; e += nth) {
+                int r = e / n, q = e - r * n;
+                double v = j > 0 ? -cj[r] * A[e] * bm[q] : 0.0;
+                if (r == q) v += c0 - aj[r];
+                A[e] = v;
+            }
+            for (int t = tid; t < n; t += nth)
+                bb[t] = rhs[l * n + t] + (j > 0 ? cj[t] * zp[t] : 0.0);
+            __syncthreads();
+            const double *jl = jv + l * net.nnz;
+            for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
+            __syncthreads();
+            gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
+            double *Gl = G + l * nn;
+            for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
+            for (int r = warp; r < n; r += nwarp) {
+                double s = 0.0;
+                for (int q = lane; q < n; q += 32) s += A[r * n + q] * bb[q];
+                s = warp_sum(s);
+                if (lane == 0) rowk[r] = s;
+            }
+            __syncthreads();
+            for (int t = tid; t < n; t += nth) {
+                zp[t] = rowk[t];
+                z[l * n + t] = rowk[t];
+            }
+            __syncthreads();
         }
-        for (int t = tid; t < n; t += nth)
-            bb[t] = rhs[l * n + t] + (j > 0 ? cj[t] * zp[t] : 0.0);
-        __syncthreads();
-        const double *jl = jv + l * net.nnz;
-        for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
-        __syncthreads();
-        gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
-        double *Gl = G + l * nn;
-        for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
-        for (int r = warp; r < n; r += nwarp) {
-            double s = 0.0;
-            for (int q = lane; q < n; q += 32) s += A[r * n + q] * bb[q];
-            s = warp_sum(s);
-            if (lane == 0) rowk[r] = s;
-        }
-        __syncthreads();
-        for (int t = tid; t < n; t += nth) {
-            zp[t] = rowk[t];
-            z[l * n + t] = rowk[t];
-        }
-        __syncthreads();
+        if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
     }
-    if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
 }
 
 // x_j = z_j + G_j (dB_j o x_{j+1}); optional yk2 = y + x / r.
@@ -263,34 +264,36 @@ k_back_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *_
            double *__restrict__ yk2) {
     extern __shared__ double sm[];
     const int n = net.ni, nn = n * n;
-    const int c = blockIdx.x;
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     double *xs = sm;          // x_{j+1} * dB_j
     double *xn = sm + n;
+    __shared__ int s_col;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
-    for (int j = nz - 1; j >= 0; --j) {
-        const size_t l = (size_t)l0 + j;
-        if (j == nz - 1) {
-            for (int t = tid; t < n; t += nth) xn[t] = z[l * n + t];
-        } else {
-            const double *Gl = G + l * nn;
-            for (int r = warp; r < n; r += nwarp) {
-                double s = 0.0;
-                for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * xs[q];
-                s = warp_sum(s);
-                if (lane == 0) xn[r] = z[l * n + r] + s;
+    for (int c; (c = next_column(b, &s_col)) >= 0;) {
+        if (b.active && !b.active[c]) continue;
+        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        for (int j = nz - 1; j >= 0; --j) {
+            const size_t l = (size_t)l0 + j;
+            if (j == nz - 1) {
+                for (int t = tid; t < n; t += nth) xn[t] = z[l * n + t];
+            } else {
+                const double *Gl = G + l * nn;
+                for (int r = warp; r < n; r += nwarp) {
+                    double s = 0.0;
+                    for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * xs[q];
+                    s = warp_sum(s);
+                    if (lane == 0) xn[r] = z[l * n + r] + s;
+                }
             }
+            __syncthreads();
+            for (int t = tid; t < n; t += nth) {
+                double xv = xn[t];
+                x[l * n + t] = xv;
+                if (yk2) yk2[l * n + t] = y[l * n + t] + xv / R_ROS;
+                if (j > 0) xs[t] = dB[(l - 1) * n + t] * xv;
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int t = tid; t < n; t += nth) {
-            double xv = xn[t];
-            x[l * n + t] = xv;
-            if (yk2) yk2[l * n + t] = y[l * n + t] + xv / R_ROS;
-            if (j > 0) xs[t] = dB[(l - 1) * n + t] * xv;
-        }
-        __syncthreads();
     }
 }
 
@@ -301,46 +304,48 @@ k_solve_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *
             double *__restrict__ zbuf, double *__restrict__ x) {
     extern __shared__ double sm[];
     const int n = net.ni, nn = n * n;
-    const int c = blockIdx.x;
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     double *vin = sm;
     double *vout = sm + n;
+    __shared__ int s_col;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
-    for (int j = 0; j < nz; ++j) {
-        const size_t l = (size_t)l0 + j;
-        for (int t = tid; t < n; t += nth)
-            vin[t] = rhs[l * n + t] + (j > 0 ? dC[l * n + t] * vout[t] : 0.0);
-        __syncthreads();
-        const double *Gl = G + l * nn;
-        for (int r = warp; r < n; r += nwarp) {
-            double s = 0.0;
-            for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
-            s = warp_sum(s);
-            if (lane == 0) { vout[r] = s; zbuf[l * n + r] = s; }
-        }
-        __syncthreads();
-    }
-    for (int j = nz - 1; j >= 0; --j) {
-        const size_t l = (size_t)l0 + j;
-        if (j < nz - 1) {
+    for (int c; (c = next_column(b, &s_col)) >= 0;) {
+        if (b.active && !b.active[c]) continue;
+        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        for (int j = 0; j < nz; ++j) {
+            const size_t l = (size_t)l0 + j;
+            for (int t = tid; t < n; t += nth)
+                vin[t] = rhs[l * n + t] + (j > 0 ? dC[l * n + t] * vout[t] : 0.0);
+            __syncthreads();
             const double *Gl = G + l * nn;
             for (int r = warp; r < n; r += nwarp) {
                 double s = 0.0;
                 for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
                 s = warp_sum(s);
-                if (lane == 0) vout[r] = zbuf[l * n + r] + s;
+                if (lane == 0) { vout[r] = s; zbuf[l * n + r] = s; }
             }
-        } else {
-            for (int t = tid; t < n; t += nth) vout[t] = zbuf[l * n + t];
+            __syncthreads();
         }
-        __syncthreads();
-        for (int t = tid; t < n; t += nth) {
-            x[l * n + t] = vout[t];
-            if (j > 0) vin[t] = dB[(l - 1) * n + t] * vout[t];
+        for (int j = nz - 1; j >= 0; --j) {
+            const size_t l = (size_t)l0 + j;
+            if (j < nz - 1) {
+                const double *Gl = G + l * nn;
+                for (int r = warp; r < n; r += nwarp) {
+                    double s = 0.0;
+                    for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
+                    s = warp_sum(s);
+                    if (lane == 0) vout[r] = zbuf[l * n + r] + s;
+                }
+            } else {
+                for (int t = tid; t < n; t += nth) vout[t] = zbuf[l * n + t];
+            }
+            __syncthreads();
+            for (int t = tid; t < n; t += nth) {
+                x[l * n + t] = vout[t];
+                if (j > 0) vin[t] = dB[(l - 1) * n + t] * vout[t];
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -452,19 +457,22 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
     (void)flags;
     const int n = net.ni;
     size_t sm = (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int);
-    k_lu_fwd_f64<<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
+    cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
+    k_lu_fwd_f64<<<b.pgrid, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
                                           w.status);
 }
 
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
                      const double *z, double *x, const double *y, double *yk2, cudaStream_t s) {
-    k_back_f64<<<b.ncols, 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, z, x, y, yk2);
+    cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
+    k_back_f64<<<b.pgrid, 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, z, x, y, yk2);
 }
 
 void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
                       const double *dC, const double *rhs, double *zbuf, double *x,
                       cudaStream_t s) {
-    k_solve_f64<<<b.ncols, 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, dC, rhs, zbuf, x);
+    cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
+    k_solve_f64<<<b.pgrid, 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, dC, rhs, zbuf, x);
 }
 
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags, double mtol,

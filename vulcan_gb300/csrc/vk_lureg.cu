@@ -1,12 +1,11 @@
-// Block-Thomas factorisations with register-resident Gauss-Jordan inversion.
-//
-//   k_lu_reg64  FP64: D'_j = c0 I + (-J_j) - diag(dA_j) - diag(dC_j) G_{j-1} diag(dB_{j-1}),
-//               G_j = D'_j^-1 stored (natural order) + forward sweep of the first
-//               right-hand side  z_j = G_j (f_j + dC_j o z_{j-1}).
-//   k_lu_reg32  FP32 on the power-of-two row/column-scaled blocks (see vk_mixed.cu):
-//               G~_j = (R_j D'_j S_j)^-1 stored in FP32 with the scales.
-// One CTA per column; each CTA walks its layers in order.  Block sizes up to
-// 160 species are covered by four register tilings (vk_gjreg.cuh).
+// FP32 block-Thomas factorisation with register-resident Gauss-Jordan inversion
+// on the power-of-two row/column-scaled blocks (the mixed path, vk_mixed.cu):
+//   k_prep32  per layer: scales R_j, S_j and the dense scaled block R_j D_j S_j;
+//   k_lu32    per column: G~_j = (R_j D'_j S_j)^-1 stored in FP32, with
+//             D'_j = D_j - diag(dC_j) G_{j-1} diag(dB_{j-1}).
+// Columns come from the work queue (longest first); each CTA walks a column's
+// layers in order.  Block sizes up to 160 species are covered by four
+// register tilings (vk_gjreg.cuh).
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -32,83 +31,6 @@ __device__ __forceinline__ void tile_coords(int &ty, int &tx) {
 }
 
 }  // namespace
-
-template <int TY, int RA, int RB>
-__global__ void __launch_bounds__(16 * TY, TY == 16 ? 2 : 1)
-k_lu_reg64(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
-           const double *__restrict__ dB, const double *__restrict__ dC,
-           const double *__restrict__ dt, const double *__restrict__ rhs,
-           double *__restrict__ G, double *__restrict__ z, int *__restrict__ status) {
-    extern __shared__ double smd[];
-    const int n = net.ni, nn = n * n;
-    const int c = blockIdx.x;
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
-    double *Gs = smd;                  // [n*n] natural-order inverse of the previous layer
-    double *rowv = Gs + nn;
-    double *colv = rowv + n;
-    double *zp = colv + n;
-    double *bb = zp + n;
-    double *zr = bb + n;
-    int *perm = reinterpret_cast<int *>(zr + n);
-    int *kinv = perm + n;
-    int *used = kinv + n;
-    __shared__ int s_piv, s_sing;
-    __shared__ double s_pval;
-    GJShared<double> sh{rowv, colv, perm, kinv, used, &s_piv, &s_pval, &s_sing};
-    int ty, tx;
-    tile_coords<TY>(ty, tx);
-    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const int nwarp = nth >> 5;
-    if (tid == 0) s_sing = 0;
-    const double c0 = 1.0 / (R_ROS * dt[c]);
-    for (int j = 0; j < nz; ++j) {
-        const size_t l = (size_t)l0 + j;
-        const double *jl = jv + l * net.nnz;
-        const double *cj = dC + l * n;
-        const double *aj = dA + l * n;
-        const double *bm = j > 0 ? dB + (l - 1) * n : dB;
-        double M[RA][RB];
-#pragma unroll
-        for (int a = 0; a < RA; ++a) {
-            const int r = ty + TY * a;
-#pragma unroll
-            for (int q = 0; q < RB; ++q) {
-                const int cc = tx + 16 * q;
-                double v = 0.0;
-                if (r < n && cc < n) {
-                    if (j > 0) v = -cj[r] * Gs[r * n + cc] * bm[cc];
-                    if (r == cc) v += c0 - aj[r];
-                    const int e = net.jmap[r * n + cc];
-                    if (e >= 0) v += jl[e];
-                }
-                M[a][q] = v;
-            }
-        }
-        for (int t = tid; t < n; t += nth) {
-            bb[t] = rhs[l * n + t] + (j > 0 ? cj[t] * zp[t] : 0.0);
-            used[t] = 0;
-        }
-        __syncthreads();
-        gj_invert_reg<double, TY, RA, RB>(M, n, ty, tx, sh);
-        gj_store_natural<double, TY, RA, RB>(M, n, ty, tx, sh, Gs);
-        double *Gl = G + l * nn;
-        for (int e = tid; e < nn; e += nth) Gl[e] = Gs[e];
-        for (int r = warp; r < n; r += nwarp) {
-            double s = 0.0;
-            for (int q = lane; q < n; q += 32) s += Gs[r * n + q] * bb[q];
-            for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) zr[r] = s;
-        }
-        __syncthreads();
-        for (int t = tid; t < n; t += nth) {
-            zp[t] = zr[t];
-            z[l * n + t] = zr[t];
-        }
-        __syncthreads();
-    }
-    if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
-}
 
 // Per-layer preparation for the FP32 factorisation (fully parallel over
 // layers): power-of-two row scales (row maxima of D_j) and column scales
@@ -195,9 +117,6 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
        int nbuf) {
     extern __shared__ __align__(16) unsigned char smb[];
     const int n = net.ni, nn = n * n, NNP = block_stride32(n);
-    const int c = blockIdx.x;
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smb);             // [2]
     float *Dbuf = reinterpret_cast<float *>(smb + 16);             // [nbuf][NNP]
     float *Gs = Dbuf + nbuf * NNP;                                 // [nn]
@@ -208,7 +127,7 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
     int *perm = reinterpret_cast<int *>(beta + n);
     int *kinv = perm + n;
     int *used = kinv + n;
-    __shared__ int s_piv, s_sing, s_to;
+    __shared__ int s_piv, s_sing, s_col;
     __shared__ float s_pval;
     GJShared<float> sh{rowv, colv, perm, kinv, used, &s_piv, &s_pval, &s_sing};
     int ty, tx;
@@ -216,82 +135,93 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
     const int tid = threadIdx.x, nth = blockDim.x;
     const uint32_t bytes = (uint32_t)NNP * sizeof(float);
     if (tid == 0) {
-        s_sing = 0;
-        s_to = 0;
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_fence_init();
     }
-    __syncthreads();
-    if (tid == 0) tma_load_1d(Dbuf, D32 + (size_t)l0 * NNP, bytes, &bar[0]);
-    // per-thread copies of this layer's scales (threads t < n own species t)
-    double rs_cur = 0, cs_cur = 0, dB_cur = 0;
-    if (tid < n) {
-        rs_cur = rsc[(size_t)l0 * n + tid];
-        cs_cur = csc[(size_t)l0 * n + tid];
-        dB_cur = dB[(size_t)l0 * n + tid];
-    }
-    for (int j = 0; j < nz; ++j) {
-        const size_t l = (size_t)l0 + j;
-        const int buf = j & 1;
-        // prefetch the scales of the next layer into registers
-        double rs_nx = 0, cs_nx = 0, dC_nx = 0, dB_nx = 0;
-        if (tid < n && j + 1 < nz) {
-            rs_nx = rsc[(l + 1) * n + tid];
-            cs_nx = csc[(l + 1) * n + tid];
-            dC_nx = dC[(l + 1) * n + tid];
-            dB_nx = dB[(l + 1) * n + tid];
+    // u counts the blocks this CTA has consumed over all its columns: block u
+    // sits in buffer u&1 (use u>>1 of that barrier) with two buffers, in
+    // buffer 0 (use u of barrier 0) with one
+    int u = 0;
+    auto buf_of = [&](int uu) { return nbuf == 2 ? (uu & 1) : 0; };
+    for (int c; (c = next_column(b, &s_col)) >= 0;) {
+        if (b.active && !b.active[c]) continue;
+        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        if (tid == 0) {
+            s_sing = 0;
+            tma_load_1d(Dbuf + buf_of(u) * NNP, D32 + (size_t)l0 * NNP, bytes, &bar[buf_of(u)]);
         }
-        // two buffers: block j in buffer j&1, the j-th use of that barrier;
-        // one buffer (large ni): every block in buffer 0, phase j&1
-        const int bsel = nbuf == 2 ? buf : 0;
-        const bool ok = mbar_wait(&bar[bsel], nbuf == 2 ? (j >> 1) & 1 : j & 1);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) status[c] = VK_ETIMEOUT;
-            return;                          // no other copy was issued after this one
+        // per-thread copies of this layer's scales (threads t < n own species t)
+        double rs_cur = 0, cs_cur = 0, dB_cur = 0;
+        if (tid < n) {
+            rs_cur = rsc[(size_t)l0 * n + tid];
+            cs_cur = csc[(size_t)l0 * n + tid];
+            dB_cur = dB[(size_t)l0 * n + tid];
         }
-        if (nbuf == 2 && tid == 0 && j + 1 < nz)
-            tma_load_1d(Dbuf + (buf ^ 1) * NNP, D32 + (l + 1) * NNP, bytes, &bar[buf ^ 1]);
-        const float *Dj = Dbuf + bsel * NNP;
-        float M[RA][RB];
-#pragma unroll
-        for (int a = 0; a < RA; ++a) {
-            const int r = ty + TY * a;
-#pragma unroll
-            for (int q = 0; q < RB; ++q) {
-                const int cc = tx + 16 * q;
-                float v = 0.0f;
-                if (r < n && cc < n) {
-                    v = Dj[r * n + cc];
-                    if (j > 0) v -= alpha[r] * Gs[r * n + cc] * beta[cc];
-                }
-                M[a][q] = v;
+        for (int j = 0; j < nz; ++j) {
+            const size_t l = (size_t)l0 + j;
+            // prefetch the scales of the next layer into registers
+            double rs_nx = 0, cs_nx = 0, dC_nx = 0, dB_nx = 0;
+            if (tid < n && j + 1 < nz) {
+                rs_nx = rsc[(l + 1) * n + tid];
+                cs_nx = csc[(l + 1) * n + tid];
+                dC_nx = dC[(l + 1) * n + tid];
+                dB_nx = dB[(l + 1) * n + tid];
             }
+            const int bsel = buf_of(u);
+            const uint32_t par = nbuf == 2 ? (u >> 1) & 1 : u & 1;
+            const bool ok = mbar_wait(&bar[bsel], par);
+            if (__syncthreads_or(!ok)) {
+                // the copy waited for is the only one in flight: let it land
+                if (tid == 0) {
+                    status[c] = VK_ETIMEOUT;
+                    mbar_wait(&bar[bsel], par);
+                }
+                return;
+            }
+            ++u;
+            if (nbuf == 2 && tid == 0 && j + 1 < nz)
+                tma_load_1d(Dbuf + (bsel ^ 1) * NNP, D32 + (l + 1) * NNP, bytes, &bar[bsel ^ 1]);
+            const float *Dj = Dbuf + bsel * NNP;
+            float M[RA][RB];
+#pragma unroll
+            for (int a = 0; a < RA; ++a) {
+                const int r = ty + TY * a;
+#pragma unroll
+                for (int q = 0; q < RB; ++q) {
+                    const int cc = tx + 16 * q;
+                    float v = 0.0f;
+                    if (r < n && cc < n) {
+                        v = Dj[r * n + cc];
+                        if (j > 0) v -= alpha[r] * Gs[r * n + cc] * beta[cc];
+                    }
+                    M[a][q] = v;
+                }
+            }
+            for (int t = tid; t < n; t += nth) used[t] = 0;
+            __syncthreads();
+            // one buffer: block j is in registers now, so the copy of block j+1
+            // overwrites it while the inversion runs
+            if (nbuf == 1 && tid == 0 && j + 1 < nz)
+                tma_load_1d(Dbuf, D32 + (l + 1) * NNP, bytes, &bar[0]);
+            gj_invert_reg<float, TY, RA, RB>(M, n, ty, tx, sh);
+            gj_store_natural<float, TY, RA, RB>(M, n, ty, tx, sh, Gs);
+            float *Gl = G32 + l * NNP;
+            for (int e = tid; e < nn; e += nth) Gl[e] = Gs[e];
+            if (tid < n && j + 1 < nz) {
+                alpha[tid] = (float)(rs_nx * dC_nx * cs_cur);
+                beta[tid] = (float)(rs_cur * dB_cur * cs_nx);
+                rs_cur = rs_nx;
+                cs_cur = cs_nx;
+                dB_cur = dB_nx;
+            }
+            __syncthreads();
         }
-        for (int t = tid; t < n; t += nth) used[t] = 0;
-        __syncthreads();
-        // one buffer: block j is in registers now, so the copy of block j+1
-        // overwrites it while the inversion runs
-        if (nbuf == 1 && tid == 0 && j + 1 < nz)
-            tma_load_1d(Dbuf, D32 + (l + 1) * NNP, bytes, &bar[0]);
-        gj_invert_reg<float, TY, RA, RB>(M, n, ty, tx, sh);
-        gj_store_natural<float, TY, RA, RB>(M, n, ty, tx, sh, Gs);
-        float *Gl = G32 + l * NNP;
-        for (int e = tid; e < nn; e += nth) Gl[e] = Gs[e];
-        if (tid < n && j + 1 < nz) {
-            alpha[tid] = (float)(rs_nx * dC_nx * cs_cur);
-            beta[tid] = (float)(rs_cur * dB_cur * cs_nx);
-            rs_cur = rs_nx;
-            cs_cur = cs_nx;
-            dB_cur = dB_nx;
-        }
-        __syncthreads();
+        if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
     }
-    if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
 }
 
 // ---------------------------------------------------------------------------
-static size_t smem64(int n) { return (size_t)(n * n + 5 * n) * sizeof(double) + 3 * n * sizeof(int) + 16; }
 static size_t smem32(int n, int nbuf) {
     return 16 + (size_t)nbuf * block_stride32(n) * sizeof(float) + (size_t)(n * n + 4 * n) * sizeof(float)
            + 3 * n * sizeof(int) + 16;
@@ -321,10 +251,8 @@ cudaError_t init_lureg_kernels(const DevNet &net) {
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    size_t s64 = smem64(n), s32 = smem32(n, lu32_nbuf(n));
+    size_t s32 = smem32(n, lu32_nbuf(n));
 #define SETATTR(TY, RA, RB)                                                                      \
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu_reg64<TY, RA, RB>,                       \
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s64); \
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu32<TY, RA, RB>,                           \
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s32);
     VK_LU_TILINGS(SETATTR)
@@ -332,28 +260,17 @@ cudaError_t init_lureg_kernels(const DevNet &net) {
     return e;
 }
 
-void launch_lu_reg64(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
-                     double *z, cudaStream_t s) {
-    const int n = net.ni;
-    size_t sm = smem64(n);
-    switch (tiling_of(n)) {
-    case 0: k_lu_reg64<16, 3, 3><<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    case 1: k_lu_reg64<16, 5, 5><<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    case 2: k_lu_reg64<16, 7, 7><<<b.ncols, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    default: k_lu_reg64<32, 5, 10><<<b.ncols, 512, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    }
-}
-
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s) {
     const int n = net.ni;
     k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs);
     const int nb = lu32_nbuf(n);
     size_t sm = smem32(n, nb);
+    cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
     switch (tiling_of(n)) {
-    case 0: k_lu32<16, 3, 3><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    case 1: k_lu32<16, 5, 5><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    case 2: k_lu32<16, 7, 7><<<b.ncols, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    default: k_lu32<32, 5, 10><<<b.ncols, 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 0: k_lu32<16, 3, 3><<<b.pgrid, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 1: k_lu32<16, 5, 5><<<b.pgrid, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 2: k_lu32<16, 7, 7><<<b.pgrid, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    default: k_lu32<32, 5, 10><<<b.pgrid, 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
     }
 }
 

@@ -49,158 +49,158 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
          double *__restrict__ thr64, int *act32) {
     extern __shared__ __align__(16) unsigned char smr[];
     const int n = net.ni, NNP = block_stride32(n);
-    const int c = blockIdx.x;
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smr);           // [2]
     float *Gbuf = reinterpret_cast<float *>(smr + 16);           // [2][NNP]
     float *vin = Gbuf + 2 * NNP;                                 // [n]
     float *vout = vin + n;                                       // [n]
     __shared__ double red[8];
+    __shared__ int s_col;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
-    const double c0 = 1.0 / (R_ROS * dt[c]);
-    const size_t base = (size_t)l0 * n;
     const uint32_t bytes = (uint32_t)NNP * sizeof(float);
-    const int per_sweep = 2 * nz - 1;            // blocks visited per sweep
-    // visit v (within a sweep) -> layer
-    auto layer_of = [&](int v) { return v < nz ? v : 2 * nz - 2 - v; };
-    int issued = 0, consumed = 0;                // global visit counters
-    auto issue = [&](int v) {                    // thread 0 only
-        const int buf = issued & 1;
-        tma_load_1d(Gbuf + buf * NNP, G32 + ((size_t)l0 + layer_of(v)) * NNP, bytes, &bar[buf]);
-        ++issued;
-    };
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_fence_init();
     }
-    for (int e = tid; e < nz * n; e += nth) {
-        x[base + e] = 0.0;
-        res[base + e] = rhs[base + e];
-    }
-    __syncthreads();
-    if (tid == 0) issue(0);
-    int sweep = 0, converged = 0, timed_out = 0;
-    double m_prev = INFINITY;
-    for (; sweep < max_sweeps && !converged && !timed_out; ++sweep) {
-        double dmax = 0.0;
-        for (int v = 0; v < per_sweep; ++v) {
-            const int j = layer_of(v);
-            const size_t l = (size_t)l0 + j;
-            const bool fwd = v < nz;
-            // right-hand side of this visit
-            if (tid < n) {
-                double vi;
-                if (fwd) {
-                    vi = rsc[l * n + tid] * res[l * n + tid];
-                    if (j > 0) vi += rsc[l * n + tid] * dC[l * n + tid] * csc[(l - 1) * n + tid] * (double)vout[tid];
-                } else {
-                    vi = rsc[l * n + tid] * dB[l * n + tid] * csc[(l + 1) * n + tid] * (double)vout[tid];
+    // copies issued / consumed by this CTA over all its columns (the same
+    // count in every thread; thread 0 issues): copy k lands in buffer k&1
+    int issued = 0, consumed = 0;
+    for (int c; (c = next_column(b, &s_col)) >= 0;) {
+        if (b.active && !b.active[c]) continue;
+        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const double c0 = 1.0 / (R_ROS * dt[c]);
+        const size_t base = (size_t)l0 * n;
+        const int per_sweep = 2 * nz - 1;            // blocks visited per sweep
+        // visit v (within a sweep) -> layer
+        auto layer_of = [&](int v) { return v < nz ? v : 2 * nz - 2 - v; };
+        auto issue = [&](int v) {
+            const int buf = issued & 1;
+            if (tid == 0)
+                tma_load_1d(Gbuf + buf * NNP, G32 + ((size_t)l0 + layer_of(v)) * NNP, bytes, &bar[buf]);
+            ++issued;
+        };
+        for (int e = tid; e < nz * n; e += nth) {
+            x[base + e] = 0.0;
+            res[base + e] = rhs[base + e];
+        }
+        __syncthreads();
+        issue(0);
+        int sweep = 0, converged = 0, timed_out = 0;
+        double m_prev = INFINITY;
+        for (; sweep < max_sweeps && !converged && !timed_out; ++sweep) {
+            double dmax = 0.0;
+            for (int v = 0; v < per_sweep; ++v) {
+                const int j = layer_of(v);
+                const size_t l = (size_t)l0 + j;
+                const bool fwd = v < nz;
+                // right-hand side of this visit
+                if (tid < n) {
+                    double vi;
+                    if (fwd) {
+                        vi = rsc[l * n + tid] * res[l * n + tid];
+                        if (j > 0) vi += rsc[l * n + tid] * dC[l * n + tid] * csc[(l - 1) * n + tid] * (double)vout[tid];
+                    } else {
+                        vi = rsc[l * n + tid] * dB[l * n + tid] * csc[(l + 1) * n + tid] * (double)vout[tid];
+                    }
+                    vin[tid] = (float)vi;
                 }
-                vin[tid] = (float)vi;
-            }
-            const int buf = consumed & 1;
-            const bool ok = mbar_wait(&bar[buf], (consumed >> 1) & 1);
-            ++consumed;
-            if (__syncthreads_or(!ok)) { timed_out = 1; break; }
-            // prefetch the next visit (possibly the first of the next sweep)
-            if (tid == 0) {
+                const int buf = consumed & 1;
+                const bool ok = mbar_wait(&bar[buf], (consumed >> 1) & 1);
+                ++consumed;
+                if (__syncthreads_or(!ok)) {
+                    --consumed;                  // still in flight: drained below
+                    timed_out = 1;
+                    break;
+                }
+                // prefetch the next visit (possibly the first of the next sweep)
                 if (v + 1 < per_sweep) issue(v + 1);
                 else if (sweep + 1 < max_sweeps) issue(0);
-            }
-            const float *G = Gbuf + buf * NNP;
-            if (tid < n) {
-                float s0 = 0.0f, s1 = 0.0f;
-                const float *row = G + tid * n;
-                int q = 0;
-                for (; q + 1 < n; q += 2) {
-                    s0 = fmaf(row[q], vin[q], s0);
-                    s1 = fmaf(row[q + 1], vin[q + 1], s1);
+                const float *G = Gbuf + buf * NNP;
+                if (tid < n) {
+                    float s0 = 0.0f, s1 = 0.0f;
+                    const float *row = G + tid * n;
+                    int q = 0;
+                    for (; q + 1 < n; q += 2) {
+                        s0 = fmaf(row[q], vin[q], s0);
+                        s1 = fmaf(row[q + 1], vin[q + 1], s1);
+                    }
+                    if (q < n) s0 = fmaf(row[q], vin[q], s0);
+                    float sacc = s0 + s1;
+                    if (fwd) {
+                        zf[l * n + tid] = sacc;
+                    } else {
+                        sacc += zf[l * n + tid];
+                    }
+                    vout[tid] = sacc;
                 }
-                if (q < n) s0 = fmaf(row[q], vin[q], s0);
-                float s = s0 + s1;
-                if (fwd) {
-                    zf[l * n + tid] = s;
-                } else {
-                    s += zf[l * n + tid];
+                __syncthreads();
+                // the back sweep starts at the top layer: x~_{nz-1} = z~_{nz-1} (vout)
+                if ((fwd && j == nz - 1) || !fwd) {
+                    if (tid < n) {
+                        const size_t e = l * n + tid;
+                        const double d = csc[e] * (double)vout[tid];
+                        const double xn = x[e] + d;
+                        x[e] = xn;
+                        const double sc = fabs(xn) + (yscale ? fabs(yscale[e]) : 0.0)
+                                          + 1e-10 * b.atm[l * VK_ATM_NF + VK_ATM_N0];
+                        dmax = isfinite(d) ? fmax(dmax, fabs(d) / sc) : INFINITY;
+                    }
                 }
-                vout[tid] = s;
+                __syncthreads();
             }
+            if (timed_out) break;
+            for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+            if (lane == 0) red[warp] = dmax;
             __syncthreads();
-            if (fwd && j == nz - 1) {
-                // back sweep starts at the top layer: x~_{nz-1} = z~_{nz-1} (vout)
-                if (tid < n) {
-                    const size_t e = l * n + tid;
-                    const double d = csc[e] * (double)vout[tid];
-                    const double xn = x[e] + d;
-                    x[e] = xn;
-                    const double sc = fabs(xn) + (yscale ? fabs(yscale[e]) : 0.0)
-                                      + 1e-10 * b.atm[l * VK_ATM_NF + VK_ATM_N0];
-                    dmax = isfinite(d) ? fmax(dmax, fabs(d) / sc) : INFINITY;
-                }
-            } else if (!fwd) {
-                if (tid < n) {
-                    const size_t e = l * n + tid;
-                    const double d = csc[e] * (double)vout[tid];
-                    const double xn = x[e] + d;
-                    x[e] = xn;
-                    const double sc = fabs(xn) + (yscale ? fabs(yscale[e]) : 0.0)
-                                      + 1e-10 * b.atm[l * VK_ATM_NF + VK_ATM_N0];
-                    dmax = isfinite(d) ? fmax(dmax, fabs(d) / sc) : INFINITY;
-                }
+            double m = red[0];
+            for (int w = 1; w < nwarp; ++w) m = fmax(m, red[w]);
+            __syncthreads();
+            // converged; or stagnating at the FP64 residual's noise floor (the
+            // correction stopped shrinking while already below 1e-6 of |x|+|y|)
+            converged = (m <= tol) || (sweep >= 1 && m > 0.25 * m_prev && m <= 1e-6);
+            if (!(m <= m_prev) && sweep >= 2) break;        // diverging: leave to the FP64 path
+            m_prev = m;
+            if (converged) break;
+            // residual r = b - A x  (FP64, matrix-free; every (layer, species) at once)
+            for (int q = tid; q < nz * n; q += nth) {
+                const int j = q / n, sp = q - j * n;
+                const size_t l = (size_t)l0 + j;
+                const size_t e = base + q;
+                const double *jl = jv + l * net.nnz;
+                double ax = (c0 - dA[e]) * x[e];
+                for (int k = net.jrowptr[sp]; k < net.jrowptr[sp + 1]; ++k) ax += jl[k] * x[l * n + net.jcol[k]];
+                if (j > 0) ax -= dC[e] * x[e - n];
+                if (j < nz - 1) ax -= dB[e] * x[e + n];
+                res[e] = rhs[e] - ax;
             }
             __syncthreads();
         }
-        if (timed_out) break;
-        for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-        if (lane == 0) red[warp] = dmax;
-        __syncthreads();
-        double m = red[0];
-        for (int w = 1; w < nwarp; ++w) m = fmax(m, red[w]);
-        __syncthreads();
-        // converged; or stagnating at the FP64 residual's noise floor (the
-        // correction stopped shrinking while already below 1e-6 of |x|+|y|)
-        converged = (m <= tol) || (sweep >= 1 && m > 0.25 * m_prev && m <= 1e-6);
-        if (!(m <= m_prev) && sweep >= 2) break;        // diverging: leave to the FP64 path
-        m_prev = m;
-        if (converged) break;
-        // residual r = b - A x  (FP64, matrix-free; every (layer, species) at once)
-        for (int q = tid; q < nz * n; q += nth) {
-            const int j = q / n, s = q - j * n;
-            const size_t l = (size_t)l0 + j;
-            const size_t e = base + q;
-            const double *jl = jv + l * net.nnz;
-            double ax = (c0 - dA[e]) * x[e];
-            for (int k = net.jrowptr[s]; k < net.jrowptr[s + 1]; ++k) ax += jl[k] * x[l * n + net.jcol[k]];
-            if (j > 0) ax -= dC[e] * x[e - n];
-            if (j < nz - 1) ax -= dB[e] * x[e + n];
-            res[e] = rhs[e] - ax;
-        }
-        __syncthreads();
-    }
-    // every issued copy must land before the CTA exits
-    if (tid == 0) {
+        // every issued copy lands before the column ends (bounded waits); a
+        // copy that never lands ends this CTA's work with a timeout
+        int lost = 0;
         while (consumed < issued) {
-            const int buf = consumed & 1;
-            mbar_wait(&bar[buf], (consumed >> 1) & 1);
+            lost |= !mbar_wait(&bar[consumed & 1], (consumed >> 1) & 1);
             ++consumed;
         }
-        if (timed_out) status[c] = VK_ETIMEOUT;
-        else {
-            if (!converged) {
-                fallback[c] = 1;
-                act32[c] = 0;                   // later mixed launches of this attempt skip it
-                thr64[c] = fmin(thr64[c], dt[c]);
+        if (__syncthreads_or(lost)) timed_out = 1;
+        if (tid == 0) {
+            if (timed_out) status[c] = VK_ETIMEOUT;
+            else {
+                if (!converged) {
+                    fallback[c] = 1;
+                    act32[c] = 0;                   // later mixed launches of this attempt skip it
+                    thr64[c] = fmin(thr64[c], dt[c]);
+                }
+                if (sweeps_out) atomicMax(sweeps_out, sweep + (converged ? 1 : 0));
+                if (err_out) err_out[c] = fmax(err_out[c], m_prev);
             }
-            if (sweeps_out) atomicMax(sweeps_out, sweep + (converged ? 1 : 0));
-            if (err_out) err_out[c] = fmax(err_out[c], m_prev);
         }
-    }
-    __syncthreads();
-    if (yk2) {
-        for (int e = tid; e < nz * n; e += nth) yk2[base + e] = y[base + e] + x[base + e] / R_ROS;
+        if (timed_out) return;
+        __syncthreads();
+        if (yk2) {
+            for (int e = tid; e < nz * n; e += nth) yk2[base + e] = y[base + e] + x[base + e] / R_ROS;
+        }
     }
 }
 
@@ -239,7 +239,8 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
                    cudaStream_t s) {
     const int n = net.ni;
     size_t sm = 16 + (size_t)2 * block_stride32(n) * sizeof(float) + 2 * n * sizeof(float);
-    k_refine<<<b.ncols, 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
+    cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
+    k_refine<<<b.pgrid, 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
                                       rhs, x, w.r, w.zf, yscale, yk2, w.y, max_sweeps, tol,
                                       w.fallback, w.sweeps, w.status, w.refine_err, w.thr64,
                                       w.act32);
