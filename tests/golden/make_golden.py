@@ -45,8 +45,13 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c1': (0, 1, 2, 10, 29),
         'c2': (0, 1, 2, 10, 29),
         'c2long': (400, 800, 1200, 1600, 1999),
-        'c2conv': (0,)}
-NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000}
+        'c2conv': (0,),
+        'c2tight': (0,)}
+NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000}
+# convergence criterion tightened from the reference defaults (yconv_cri 0.01,
+# yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
+# must reproduce, whatever path it takes there
+EXTRA_CFG = {'c2tight': 'yconv_cri = 0.001\nyconv_min = 0.001\n'}
 
 DRIVER = r'''
 import os, sys, time, json
@@ -191,7 +196,7 @@ MPL_STUB = {
 }
 
 
-def cfg_overrides(spec, nz, count_max, use_photo):
+def cfg_overrides(spec, nz, count_max, use_photo, extra=''):
     mix = {k: float(v) for k, v in spec.const_mix.items()}
     return textwrap.dedent(f'''
         # ---- overrides appended by the golden-fixture generator ----
@@ -236,7 +241,7 @@ def cfg_overrides(spec, nz, count_max, use_photo):
         conver_ignore = {spec.conver_ignore!r}
         count_max = {count_max}
         out_name = 'golden.vul'
-        ''')
+        ''') + extra
 
 
 def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
@@ -259,7 +264,7 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
     env = dict(os.environ, PYTHONPATH=os.path.join(dst, '_mplstub'), OMP_NUM_THREADS='1')
     # code generation (photo reactions included when the workload has J rates)
     with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
-        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, spec.use_photo))
+        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, spec.use_photo, EXTRA_CFG.get(tag, '')))
     subprocess.run([sys.executable, 'make_chem_funs.py'], cwd=dst, env=env,
                    stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     with open(os.path.join(dst, 'chem_funs.py')) as f:
@@ -267,7 +272,7 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
             raise RuntimeError('reference code generation failed for ' + tag)
     # run time: photochemistry (radiative transfer) off, J frozen in k
     with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
-        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, False))
+        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, False, EXTRA_CFG.get(tag, '')))
     keys = sorted(spec.photo_J) if spec.photo_J else []
     np.savez(os.path.join(dst, 'golden_inputs.npz'), Tco=spec.Tco, Kzz=spec.Kzz,
              photo_J=np.array([spec.photo_J[k] for k in keys]) if keys else np.zeros((0, nz)))
@@ -286,7 +291,7 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
 def make(tag, ref_root, workdir, full_dir=None):
     if tag == 'c0':
         spec = configs.config0()
-    elif tag in ('c2', 'c2long', 'c2conv'):
+    elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]
     elif tag == 'c1':
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
@@ -310,7 +315,7 @@ def make(tag, ref_root, workdir, full_dir=None):
     np.savez_compressed(out, **d)
     net.to_npz(os.path.join(HERE, 'net_%s.npz' % spec.network.replace('_network.txt', '')
                             + ('_photo' if spec.use_photo and 'photo' not in spec.network else '')))
-    if full_dir and tag != 'c2conv':
+    if full_dir and tag not in ('c2conv', 'c2tight'):
         os.makedirs(full_dir, exist_ok=True)
         shutil.copy(os.path.join(dst, 'golden_full.npz'),
                     os.path.join(full_dir, 'golden_full_%s.npz' % tag))

@@ -239,18 +239,10 @@ def test_run_watchdog_returns_timeout():
     assert np.isfinite(st['y']).all()
 
 
-@pytest.mark.parametrize('precision', [0, 1])
-def test_device_run_reaches_reference_steady_state(precision):
-    """vk_run from the reference's initial state to its convergence criterion
-    (op.py conv / stop) lands on the reference's steady state.
-
-    Trajectories part at the late stiff steps' conditioning floor, so the
-    comparison is between converged states: the reference stops once the
-    relative change over its window is below yconv_cri (1 %), which bounds how
-    far either run can sit from the true steady state."""
+def _run_to_steady(tag, precision, **cfg):
     from vulcan_gb300 import configs
     from vulcan_gb300.solver import ctrl_from
-    g, net, gn, h, b = make_handle('c2conv', precision=precision)
+    g, net, gn, h, b = make_handle(tag, precision=precision)
     h.set_atom_ini(g['atom_ini'][None, :])
     mask = np.zeros(net.ni, dtype=np.int32)
     for sp in g['conver_ignore']:
@@ -258,15 +250,41 @@ def test_device_run_reaches_reference_steady_state(precision):
             mask[net.species.index(str(sp))] = 1
     h.set_conv_ignore(mask)
     h.set_clock(dt=1e-10, t=0.0, count=0)
-    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    ctrl = ctrl_from(cfg, gs=configs.GS, Rp=configs.RP)
+    ctrl.count_max = 20000
     h.run(ctrl, max_steps=20000, timeout_s=900)
-    st = h.state()
-    assert st['end_case'][0] == 1                      # converged, like the reference
-    assert 0.5 * g['final_count'] <= st['count'][0] <= 2.0 * g['final_count']
+    return g, h.state()
+
+
+@pytest.mark.parametrize('precision', [0, 1])
+def test_device_run_converges_like_reference(precision):
+    """vk_run from the reference's initial state stops by the reference's own
+    convergence test (op.py:1018-1085, default criterion).  That test allows
+    10 % drift over the last half of the run time once t is large
+    (yconv_min = 0.1 with the slope clause), so runs that part at the late
+    steps' conditioning floor stop at different points; the step count is
+    compared, the state is compared under the tight criterion below."""
+    g, st = _run_to_steady('c2conv', precision)
+    assert st['end_case'][0] == 1
+    assert 0.4 * g['final_count'] <= st['count'][0] <= 2.5 * g['final_count']
+
+
+@pytest.mark.parametrize('precision', [0, 1])
+def test_device_run_reaches_reference_steady_state(precision):
+    """With the criterion tightened to yconv_cri = yconv_min = 1e-3 in both
+    (fixture c2tight, recorded from the reference with those vulcan_cfg
+    values), the device run lands on the reference's steady state:
+    median relative difference <= 1e-3 over species with ymix > 1e-20."""
+    import os
+    from conftest import GOLDEN
+    if not os.path.exists(os.path.join(GOLDEN, 'golden_c2tight.npz')):
+        pytest.skip('golden_c2tight.npz not recorded')
+    g, st = _run_to_steady('c2tight', precision, yconv_cri=1e-3, yconv_min=1e-3)
+    assert st['end_case'][0] == 1
     ref = g['final_ymix']
     sel = ref > 1e-20
     rel = np.abs(st['ymix'][sel] - ref[sel]) / ref[sel]
     print('steady state: count %d (ref %d), rel median %.3g p99 %.3g max %.3g'
           % (st['count'][0], g['final_count'], np.median(rel), np.percentile(rel, 99), rel.max()))
     assert np.median(rel) <= 1e-3
-    assert np.percentile(rel, 99) <= 5e-2
+    assert np.percentile(rel, 99) <= 2e-2

@@ -13,6 +13,11 @@ __device__ __forceinline__ void gj_invert_f64(double *A, int n, double *colk, do
                               int *s_piv, double *s_pval, int *s_sing) {
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nn = n * n;
+    // rank-1 update mapping: thread t owns column t % n of rows t / n + R q
+    // (R = nth / n row groups); needs nth >= n, else a flat loop
+    const int R = nth / n;
+    const int my_col = R ? tid % n : 0, my_row0 = R ? tid / n : 0;
+    const bool mapped = R > 0 && tid < R * n;
     for (int k = 0; k < n; ++k) {
         if (warp == 0) {
             double best = -1.0;
@@ -46,10 +51,22 @@ __device__ __forceinline__ void gj_invert_f64(double *A, int n, double *colk, do
             colk[t] = (t == k) ? pval : ((t == p) ? A[k * n + k] : A[t * n + k]);
         }
         __syncthreads();
-        for (int e = tid; e < nn; e += nth) {
-            int i = e / n, jj = e - i * n;
-            if (i == k) A[e] = rowk[jj];
-            else A[e] = (jj == k ? 0.0 : A[e]) - colk[i] * rowk[jj];
+        if (R > 0) {
+            if (mapped) {
+                const double rj = rowk[my_col];
+                const bool is_k = my_col == k;
+                for (int i = my_row0; i < n; i += R) {
+                    double *a = A + i * n + my_col;
+                    if (i == k) *a = rj;
+                    else *a = (is_k ? 0.0 : *a) - colk[i] * rj;
+                }
+            }
+        } else {
+            for (int e = tid; e < nn; e += nth) {
+                int i = e / n, jj = e - i * n;
+                if (i == k) A[e] = rowk[jj];
+                else A[e] = (jj == k ? 0.0 : A[e]) - colk[i] * rowk[jj];
+            }
         }
         __syncthreads();
     }
