@@ -167,7 +167,16 @@ def _workload(args, ncols=None):
         specs = configs.config4_columns(sorted(net.photo_index()), ncols=C4_NCOLS)
         return net, specs[:ncols or args.ncols or C4_NCOLS]
     net = Network.from_npz(NET)
-    return net, configs.config2_columns(ncols=NCOLS, seed=SEED)[:ncols or args.ncols or NCOLS]
+    n = ncols or args.ncols or NCOLS
+    from vulcan_gb300 import replicas
+    rank, ws, _ = replicas.world()
+    if ws > 1 and not getattr(args, 'converge', False):
+        # replicas: every rank integrates its own n columns (weak scaling),
+        # a balanced share of n * world_size seeded columns
+        allspecs = configs.config2_columns(ncols=n * ws, seed=SEED)
+        part = replicas.column_shards([sp.pco.size for sp in allspecs], ws)[rank]
+        return net, [allspecs[i] for i in part]
+    return net, configs.config2_columns(ncols=NCOLS, seed=SEED)[:n]
 
 
 def _setup(args, precision, ncols=None, warm_model=None):
@@ -190,44 +199,56 @@ def _setup(args, precision, ncols=None, warm_model=None):
     return net, items, h, b, ctrl
 
 
-def _measure(args, precision, clocks=None):
-    """Warm-up, then args.steps timed steps of every column (state resident)."""
+def _measure(args, precision, clocks=None, dist=None):
+    """Warm-up, then args.steps timed steps of every column (state resident).
+    With several ranks: barrier on both sides, steps summed, time the max."""
+    from vulcan_gb300 import replicas
     net, items, h, b, ctrl = _setup(args, precision)
     h.run(ctrl, max_steps=args.warmup, timeout_s=1800)
     st0, c0 = h.state(), h.counters()
     if clocks is not None:
         clocks.__enter__()
         time.sleep(0.3)
+    replicas.barrier(dist)
     try:
         h.run(ctrl, max_steps=args.steps, timeout_s=3600)
     finally:
         if clocks is not None:
             clocks.__exit__()
+    replicas.barrier(dist)
     tm = h.timing()
     st1, c1 = h.state(), h.counters()
     steps = int((st1['count'] - st0['count']).sum())
     attempts = int((c1[:, 0] - c0[:, 0]).sum())
     ms_dev = tm['rates']                  # device time of the whole run (CUDA events)
-    out = dict(value=steps / (ms_dev * 1e-3), ms=ms_dev, steps=steps, attempts=attempts,
+    steps_all, sec_max = replicas.reduce_run(dist, steps, ms_dev * 1e-3)
+    out = dict(value=steps_all / sec_max, ms=sec_max * 1e3, steps=steps, attempts=attempts,
                launches=tm['launches'], fallbacks=int((c1[:, 4] - c0[:, 4]).sum()))
     # per-kernel device times of one attempt from the current state
     h.set_state(st1['y'], st1['ymix'])
     for _ in range(2):
         h.attempt(st1['dt'])
     out['attempt_ms'] = {k: round(v, 3) for k, v in h.timing().items() if k != 'launches'}
-    # e2e: host state in, one step, host state out -- through the public API
-    y_host = np.ascontiguousarray(st1['y'])
-    ym_host = np.ascontiguousarray(st1['ymix'])
+    # e2e: host state in (pinned), one step, host state out (pinned) -- through
+    # the public API, every step
+    import torch
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = {k: pin(st1[k]) for k in ('y', 'ymix', 'dt', 't', 'delta')}
+    host['count'] = pin(st1['count'])
+    host['end_case'] = pin(st1['end_case'])
     h.set_clock(dt=st1['dt'], t=st1['t'], count=st1['count'])
+    replicas.barrier(dist)
     n_e2e, t0 = 0, time.perf_counter()
     for _ in range(max(2, min(args.steps, 5))):
-        c_before = h.state()['count']
-        h.set_state(y_host, ym_host)
+        c_before = host['count'].copy()
+        h.set_state(host['y'], host['ymix'])
         h.run(ctrl, max_steps=1, timeout_s=600)
-        s = h.state()
-        y_host, ym_host = s['y'], s['ymix']
-        n_e2e += int((s['count'] - c_before).sum())
-    out['e2e'] = n_e2e / (time.perf_counter() - t0)
+        h.state(out=host)
+        n_e2e += int((host['count'] - c_before).sum())
+    sec = time.perf_counter() - t0
+    replicas.barrier(dist)
+    e2e_steps, e2e_sec = replicas.reduce_run(dist, n_e2e, sec)
+    out['e2e'] = e2e_steps / e2e_sec
     out['bytes_state'] = b.L * net.ni * 8
     out['layers'] = int(b.L)
     out['ni'] = net.ni
@@ -238,11 +259,16 @@ def _measure(args, precision, clocks=None):
 
 
 def run_gpu(args):
+    from vulcan_gb300 import replicas
+    dist = replicas.init()
+    rank, ws, _ = replicas.world()
     hbm, hbm_kind = peaks()
     clocks = Clocks(os.path.join(REPO, 'gpurun_out', 'bench_clocks.csv')
                     if os.path.isdir(os.path.join(REPO, 'gpurun_out')) else '/tmp/bench_clocks.csv')
-    mixed = _measure(args, 1, clocks)
-    plain = _measure(args, 0)
+    mixed = _measure(args, 1, clocks if rank == 0 else None, dist)
+    plain = _measure(args, 0, None, dist)
+    if rank != 0:
+        return
     ni, L = mixed['ni'], mixed['layers']
     # roofline of the dominant kernel of the headline path
     am = mixed['attempt_ms']
@@ -274,7 +300,7 @@ def run_gpu(args):
               'sum nz=%d)' % (args.ncols, L))
         netname = 'NCHO_thermo (69 species, 391 pairs)'
     out = {
-        'metric': METRIC, 'value': round(mixed['value'], 2), 'unit': UNIT, 'n_gpus': 1,
+        'metric': METRIC, 'value': round(mixed['value'], 2), 'unit': UNIT, 'n_gpus': ws,
         'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': round(mixed['ms'] / max(args.steps, 1), 3),
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
@@ -301,7 +327,7 @@ def run_gpu(args):
                          'frac': round(rate_bytes / (am['rates'] * 1e-3) / 1e9 / hbm, 4)},
     }
     out['clocks'] = clocks.summary()
-    if not args.no_cpu and args.workload == 'c2':
+    if not args.no_cpu and args.workload == 'c2' and ws == 1:
         out['cpu_baseline'] = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
     print(json.dumps(out))
 

@@ -245,16 +245,26 @@ class Ros2Handle:
     def run(self, ctrl, max_steps=0, timeout_s=0.0):
         check(lib().vk_run(self.h, C.byref(ctrl), int(max_steps), float(timeout_s)), self.h)
 
-    def state(self):
+    def state(self, out=None):
+        """Device state copied to host arrays: new ones, or the (e.g. pinned)
+        C-contiguous arrays of ``out`` (keys y, ymix, dt, t, count, end_case,
+        delta; float64, counts int32)."""
         b = self.batch
-        y = np.empty((b.L, self.ni))
-        ymix = np.empty((b.L, self.ni))
-        dt, t, delta = np.empty(b.ncols), np.empty(b.ncols), np.empty(b.ncols)
-        count = np.empty(b.ncols, dtype=np.int32)
-        end = np.empty(b.ncols, dtype=np.int32)
-        check(lib().vk_get_state(self.h, ptr(y), ptr(ymix), ptr(dt), ptr(t), ptr(count, C.c_int),
-                                 ptr(end, C.c_int), ptr(delta)), self.h)
-        return dict(y=y, ymix=ymix, dt=dt, t=t, count=count, end_case=end, delta=delta)
+        if out is None:
+            out = dict(y=np.empty((b.L, self.ni)), ymix=np.empty((b.L, self.ni)),
+                       dt=np.empty(b.ncols), t=np.empty(b.ncols), delta=np.empty(b.ncols),
+                       count=np.empty(b.ncols, dtype=np.int32),
+                       end_case=np.empty(b.ncols, dtype=np.int32))
+        for k, n in (('y', b.L * self.ni), ('ymix', b.L * self.ni), ('dt', b.ncols),
+                     ('t', b.ncols), ('delta', b.ncols), ('count', b.ncols), ('end_case', b.ncols)):
+            a = out[k]
+            want = np.int32 if k in ('count', 'end_case') else np.float64
+            if a.dtype != want or a.size != n or not a.flags.c_contiguous:
+                raise ValueError('state(out): %s must be C-contiguous %s of %d' % (k, want.__name__, n))
+        check(lib().vk_get_state(self.h, ptr(out['y']), ptr(out['ymix']), ptr(out['dt']),
+                                 ptr(out['t']), ptr(out['count'], C.c_int),
+                                 ptr(out['end_case'], C.c_int), ptr(out['delta'])), self.h)
+        return out
 
     def refine_stats(self):
         """(most sweeps any column needed, columns redone in FP64) of the last attempt."""
