@@ -258,6 +258,21 @@ def _measure(args, precision, clocks=None, dist=None):
     return out
 
 
+def profile_traffic(kernel):
+    """DRAM bytes per layer of `kernel` from the committed ncu summaries
+    (a line 'roofline-traffic <kernel> bytes_per_layer=<B>' in profiles/*.md),
+    or None."""
+    import glob
+    import re
+    for path in sorted(glob.glob(os.path.join(REPO, 'profiles', '*.md'))):
+        with open(path) as f:
+            for line in f:
+                m = re.match(r'\s*roofline-traffic\s+(\S+)\s+bytes_per_layer=([0-9.eE+]+)', line)
+                if m and m.group(1) == kernel:
+                    return float(m.group(2))
+    return None
+
+
 def run_gpu(args):
     from vulcan_gb300 import replicas
     dist = replicas.init()
@@ -285,7 +300,9 @@ def run_gpu(args):
         roof = {'bound': 'hbm', 'kernel': 'k_refine', 'achieved': by / (am['solve'] * 1e-3) / 1e9,
                 'peak': hbm, 'unit': 'GB/s', 'peak_source': hbm_kind}
     roof['frac'] = roof['achieved'] / roof['peak']
-    roof['traffic'] = None
+    tpl = profile_traffic(roof['kernel'].split()[0])
+    # DRAM bytes per launch: the ncu capture's bytes per layer x this launch's layers
+    roof['traffic'] = round(tpl * L) if tpl else None
     for k in ('achieved', 'peak', 'frac'):
         roof[k] = round(roof[k], 4)
     peak64 = fp64_peak_tflops()
@@ -369,7 +386,8 @@ def run_converge(args):
         paths = paths[1:]
         res['learned_mixed'] = {'skipped': 'no warm-start weights at %s' % args.weights}
     if args.precision_only:
-        paths = [p for p in paths if p[0] == args.precision_only]
+        keep = args.precision_only.split(',')
+        paths = [p for p in paths if p[0] in keep]
     for name, prec in paths:
         t0 = time.perf_counter()
         if name == 'learned_mixed':
@@ -495,7 +513,7 @@ def main():
     ap.add_argument('--count-max', type=int, default=30000)
     ap.add_argument('--chunk', type=int, default=500)
     ap.add_argument('--precision-only', default=None,
-                    choices=['learned_mixed', 'mixed', 'plain_fp64'])
+                    help='comma-separated subset of learned_mixed,mixed,plain_fp64 (converge mode)')
     ap.add_argument('--weights', default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                                       'vulcan_gb300', 'warmstart_weights.npz'),
                     help='learned warm-start weights (converge mode)')

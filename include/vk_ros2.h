@@ -171,6 +171,9 @@ VK_API int  vk_set_clock(vk_handle *h, const double *dt, const double *t, const 
  * because mixed-precision refinement did not converge, accepted steps. */
 #define VK_NCOUNTERS 6
 VK_API int  vk_get_counters(vk_handle *h, int *counters);
+/* Diagnostic: longdy and longdydt of each column's last steady-state test
+ * (the reference keeps them as var.longdy / var.longdydt, op.py:1046-1049). */
+VK_API int  vk_get_conv(vk_handle *h, double *longdy, double *longdydt);
 
 /* Device time of the last call in ms: after vk_ros2_attempt the rate +
  * Jacobian kernel, the block factorisation, the solves (including the second

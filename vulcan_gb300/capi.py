@@ -34,7 +34,7 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
-           'vk_mlp_backward', 'vk_mlp_adam')
+           'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv')
 
 
 class VkNetworkDesc(C.Structure):
@@ -99,6 +99,7 @@ def lib(path=None):
         'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
         'vk_set_clock': (i, [vp, pd, pd, pi]),
         'vk_get_counters': (i, [vp, pi]),
+        'vk_get_conv': (i, [vp, pd, pd]),
         'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
         'vk_chem_source': (i, [vp, pd, pd]),
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),

@@ -180,13 +180,14 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &h->d_order, max_cols));
     TRY(dalloc(h, &h->d_queue, 1));
     {
-        // per-column kernels: VK_CTAS_PER_SM resident CTAs per SM take columns
-        // from the queue (unset or 0: one CTA per column)
+        // per-column kernels: k resident CTAs per SM take columns from the queue
+        // (k = VK_CTAS_PER_SM, default 2, the fastest FP64 LU measured on GB300;
+        // 0 = one CTA per column)
         int dev = 0, nsm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         const char *env = getenv("VK_CTAS_PER_SM");
-        const int cps = env ? atoi(env) : 0;
+        const int cps = env ? atoi(env) : 2;
         h->pgrid_max = cps > 0 ? cps * nsm : 0;
     }
     TRY(dalloc(h, &h->d_lay_col, L));
@@ -547,6 +548,17 @@ extern "C" int vk_get_counters(vk_handle *h, int *counters) {
     if (rc) return rc;
     if (!counters) return fail(h, VK_EINVAL, "counters is NULL");
     VK_CUDA(h, cudaMemcpy(counters, h->rs.counters, (size_t)h->ncols * VK_NCOUNTERS * sizeof(int), cudaMemcpyDeviceToHost));
+    return VK_OK;
+}
+
+// Diagnostic: the last steady-state test's longdy and longdydt per column
+// (Integration.conv, op.py:1046-1049); zero before a column's first test.
+extern "C" int vk_get_conv(vk_handle *h, double *longdy, double *longdydt) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!h->rs_ready) return fail(h, VK_EINVAL, "no vk_run yet");
+    if (longdy) VK_CUDA(h, cudaMemcpy(longdy, h->rs.longdy, h->ncols * sizeof(double), cudaMemcpyDeviceToHost));
+    if (longdydt) VK_CUDA(h, cudaMemcpy(longdydt, h->rs.longdydt, h->ncols * sizeof(double), cudaMemcpyDeviceToHost));
     return VK_OK;
 }
 

@@ -266,6 +266,13 @@ class Ros2Handle:
                                  ptr(out['end_case'], C.c_int), ptr(out['delta'])), self.h)
         return out
 
+    def conv_stats(self):
+        """(longdy, longdydt) of each column's last steady-state test."""
+        b = self.batch
+        ld, ldt = np.zeros(b.ncols), np.zeros(b.ncols)
+        check(lib().vk_get_conv(self.h, ptr(ld), ptr(ldt)), self.h)
+        return ld, ldt
+
     def refine_stats(self):
         """(most sweeps any column needed, columns redone in FP64) of the last attempt."""
         a, b = C.c_int(), C.c_int()

@@ -24,7 +24,11 @@ Choices (all seeded):
     5 % unimolecular A -> B + C;
   * k = A T^B exp(-C/T): two-body A log-U[1e-14, 1e-9] cm^3 s^-1, C U[0, 40000]
     K; three-body k0 = 1e-20 A (cm^6 s^-1) and k_inf = A; unimolecular
-    A log-U[1e8, 1e13] s^-1; B = 0;
+    A log-U[1e8, 1e13] s^-1; B = 0.  C is then raised where needed so that
+    the reverse rate k/Keq (the reference's rev_rate, op.py:287-309) stays
+    below the collision limit (1e-9 cm^3 s^-1 for two-body reverses, 1e13
+    s^-1 for first-order ones) over 400-3500 K, as the endothermic direction
+    of a real reaction is the slow one;
   * Gibbs data: constant heat capacity cp/R = 2.5 + 0.5 n_atoms, enthalpy of
     formation b1 = sum of per-element terms + U[-6000, 6000] K, entropy
     offset b2 U[10, 40] + 2 n_atoms, the same in both NASA-9 ranges;
@@ -68,6 +72,28 @@ def make_species(rng, ni=150):
     return names
 
 
+CORR = 1.38064852E-16 / 1.0e6          # k_B / P0 (the reference's gibbs_text corr)
+T_GRID = np.linspace(400.0, 3500.0, 64)
+K2_MAX = 1e-9                             # two-body collision limit (cm^3 s^-1)
+K1_MAX = 1e13                             # first-order limit (s^-1)
+
+
+def _g_rt(a3, b1, b2, T):
+    """g/RT of the constant-cp species model: h/RT - s/R."""
+    return a3 * (1.0 - np.log(T)) + b1 / T - b2
+
+
+def _min_ea(lnA, reac, prod, g, extra_order=0):
+    """Smallest activation temperature C (K) keeping the reverse rate below its
+    limit over T_GRID; reac/prod are species index lists (M excluded)."""
+    dg = sum(g[p] for p in prod) - sum(g[r] for r in reac)          # [T]
+    lnK = -dg + (len(reac) - len(prod)) * np.log(CORR * T_GRID)
+    order = len(prod) + extra_order                                # reverse order (with M)
+    ln_lim = np.log(K2_MAX if order >= 2 else K1_MAX)
+    # ln k_r = lnA - C/T - lnK <= ln_lim  <=>  C >= T (lnA - lnK - ln_lim)
+    return float(max(0.0, np.max(T_GRID * (lnA - lnK - ln_lim))))
+
+
 def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
     """Write the network, NASA-9 and composition files; returns the network
     file path.  Deterministic in (seed, ni, n_rev, n_photo)."""
@@ -75,6 +101,16 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
     sp = make_species(rng, ni)
     names = list(sp)
     comp = np.array([sp[s] for s in names])
+    # thermo: constant cp, seeded formation enthalpy and entropy offset
+    h_el = {'H': -1500.0, 'O': -12000.0, 'C': 8000.0, 'N': 2000.0}
+    thermo = []
+    for cv in comp:
+        nat = max(int(cv.sum()), 1)
+        a3 = 2.5 + 0.5 * nat
+        b1 = sum(h_el[e] * k for e, k in zip(('H', 'O', 'C', 'N'), cv)) + rng.uniform(-6000, 6000)
+        b2 = rng.uniform(10, 40) + 2.0 * nat
+        thermo.append((a3, b1, b2))
+    g = [_g_rt(a3, b1, b2, T_GRID) for a3, b1, b2 in thermo]
     idx = {tuple(v): k for k, v in enumerate(comp.tolist())}
     # composition sums of unordered pairs (allowing A + A)
     pairs = {}
@@ -104,7 +140,7 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
             continue
         seen.add(k1)
         A = 10.0 ** rng.uniform(-14, -9)
-        Ea = rng.uniform(0, 40000)
+        Ea = max(rng.uniform(0, 40000), _min_ea(np.log(A), [a, b], [c, d], g))
         lines['bi'].append(('%s + %s -> %s + %s' % (names[a], names[b], names[c], names[d]),
                             '%.4E 0.0 %.1f' % (A, Ea)))
     # species that are the sum of a pair (three-body association, unimolecular split)
@@ -118,7 +154,9 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
             continue
         seen.add(k1)
         A = 10.0 ** rng.uniform(-14, -9)
-        Ea = rng.uniform(0, 40000)
+        # high-pressure limit k_inf = A exp(-Ea/T) bounds the fall-off rate; its
+        # reverse C + M -> A + B + M is two-body in the reference's units
+        Ea = max(rng.uniform(0, 40000), _min_ea(np.log(A), [a, b], [c], g, extra_order=1))
         lines['ter'].append(('%s + %s + M -> %s + M' % (names[a], names[b], names[c]),
                              '%.4E 0.0 %.1f %.4E 0.0 %.1f' % (1e-20 * A, Ea, A, Ea)))
     while len(lines['uni']) < n_uni:
@@ -128,7 +166,7 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
             continue
         seen.add(k1)
         A = 10.0 ** rng.uniform(8, 13)
-        Ea = rng.uniform(0, 40000)
+        Ea = max(rng.uniform(0, 40000), _min_ea(np.log(A), [a], [b, c], g))
         lines['uni'].append(('%s -> %s + %s' % (names[a], names[b], names[c]),
                              '%.4E 0.0 %.1f' % (A, Ea)))
     photo = []
@@ -166,16 +204,10 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
     net_path = os.path.join(out_dir, '%s_network.txt' % name)
     with open(net_path, 'w') as f:
         f.write('\n'.join(out) + '\n')
-    # --- thermo: constant cp, seeded formation enthalpy and entropy offset
-    h_el = {'H': -1500.0, 'O': -12000.0, 'C': 8000.0, 'N': 2000.0}
+    # --- thermo files (He: monatomic constants)
     allsp = names + ['He']
     allcomp = np.vstack([comp, [0, 0, 0, 0]])
-    for s, cv in zip(allsp, allcomp):
-        nat = max(int(cv.sum()), 1)
-        a3 = 2.5 + 0.5 * nat if s != 'He' else 2.5
-        b1 = (sum(h_el[e] * k for e, k in zip(('H', 'O', 'C', 'N'), cv))
-              + rng.uniform(-6000, 6000)) if s != 'He' else -745.0
-        b2 = rng.uniform(10, 40) + 2.0 * nat if s != 'He' else 0.9
+    for s, (a3, b1, b2) in zip(allsp, thermo + [(2.5, -745.0, 0.9)]):
         row = [0.0, 0.0, a3, 0.0, 0.0, 0.0, 0.0, 0.0, b1, b2]
         with open(os.path.join(out_dir, 'NASA9', s + '.txt'), 'w') as f:
             f.write(' '.join('%.8E' % v for v in row) + '\n')

@@ -367,19 +367,19 @@ def generate(net, seeds, ncols, atoms, count_max=4000, timeout_s=900, precision=
 
 
 def warm_items(model, specs, net, items, atoms, precision=1):
-    """Items started from the projected MLP proposal where its chemical
-    residual is below that of the const_mix start; returns (items, used_mask).
-    The element totals (atom_ini) stay those of the const_mix start."""
-    from . import batch as bmod
+    """Items started from the projected MLP proposal (element totals, and so
+    atom_ini, those of the const_mix start); returns (items, used_mask).
+    The solver judges the proposal: its step control and convergence test are
+    the reference's, and a column that does not converge from it can be rerun
+    from const_mix (fallback_items)."""
     prop = propose(model, specs, net, items, atom_list=atoms)
-    h, b = bmod.make_batch_handle(net, items, atoms, precision=precision)
-    n0 = np.concatenate([it['col'].n_0 for it in items])
-    r_const = chem_residual(h, np.concatenate([it['y'] for it in items]), n0, b)
-    r_warm = chem_residual(h, np.concatenate([p[0] for p in prop]), n0, b)
-    h.close()
-    used = r_warm < r_const
-    out = [dict(it, y=y, ymix=x) if u else it for it, (y, x), u in zip(items, prop, used)]
-    return out, used
+    out = [dict(it, y=y, ymix=x) for it, (y, x) in zip(items, prop)]
+    return out, np.ones(len(items), dtype=bool)
+
+
+def fallback_items(items_const, end_case):
+    """const_mix items of the columns whose warm-started run did not converge."""
+    return [it for it, e in zip(items_const, end_case) if e != 1]
 
 
 def main(argv=None):
