@@ -210,7 +210,11 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
     double *rowk = colk + n;
     double *zp = rowk + n;
     double *bb = zp + n;
-    int *perm = reinterpret_cast<int *>(bb + n);
+    double *colk2 = bb + n;
+    double *rowk2 = colk2 + n;
+    double *c2 = rowk2 + n;
+    double *tmp = c2 + n;
+    int *perm = reinterpret_cast<int *>(tmp + n);
     __shared__ int s_piv, s_sing, s_col;
     __shared__ double s_pval;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
@@ -237,7 +241,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
             const double *jl = jv + l * net.nnz;
             for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
             __syncthreads();
-            gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
+            gj_invert_f64_x2(A, n, colk, rowk, colk2, rowk2, c2, tmp, perm, &s_piv, &s_pval, &s_sing);
             double *Gl = G + l * nn;
             for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
             for (int r = warp; r < n; r += nwarp) {
@@ -416,13 +420,15 @@ void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flag
 
 // ---------------------------------------------------------------------------
 static size_t rates_smem(const DevNet &net);
+// block, colk, rowk, zp, bb, colk2, rowk2, c2, tmp (doubles) + perm (ints)
+static size_t lu_fwd_smem(int n) { return (size_t)(n * n + 8 * n) * sizeof(double) + (size_t)n * sizeof(int); }
 
 // Opt the kernels into the dynamic shared memory this network needs; called
 // once per handle, outside any stream capture.
 cudaError_t init_kernels(const DevNet &net) {
     size_t sr = rates_smem(net);
     const int n = net.ni;
-    size_t sl = (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int);
+    size_t sl = lu_fwd_smem(n);
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_rates<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
     if ((e = cudaFuncSetAttribute(k_rates<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
@@ -456,7 +462,7 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
                        const double *rhs, double *z, int flags, cudaStream_t s) {
     (void)flags;
     const int n = net.ni;
-    size_t sm = (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int);
+    size_t sm = lu_fwd_smem(n);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
     k_lu_fwd_f64<<<b.pgrid, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
                                           w.status);
