@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import atm_from_column, floor_err
+from helpers import GOLDEN, atm_from_column, floor_err
 from oracle import ros2 as O
 from vulcan_gb300 import batch, configs, synthnet
 from vulcan_gb300.network import Network
@@ -100,4 +100,59 @@ def test_attempt_matches_oracle(syn, precision):
             r = O.ros2_attempt(on, it['y'], it['ymix'], dt, it['k'], atm_from_column(it['col']),
                                O.Flags(), O.Tol())
             assert floor_err(sol[sl], r.sol, it['col'].n_0) <= 1e-10
+    h.close()
+
+
+def _lhs_check(net, items, npz, precision=0):
+    from vulcan_gb300.solver import GPUNetwork
+    h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
+    on = O.OracleNet.from_npz(npz, ATOMS)
+    h.attempt(np.full(b.ncols, 1e-10))
+    jv, dA, dB, dC = h.lhs()
+    rows, cols = GPUNetwork(net, ATOMS).jac_pattern()
+    it = items[0]
+    nz = it['col'].nz
+    J = O.neg_jac_blocks(on, it['y'], it['col'].M, it['k'])
+    for l in (0, 1, nz // 2, nz - 1):
+        ref = J[l][rows, cols]
+        assert np.max(np.abs(jv[l] - ref)) <= 1e-13 * np.abs(J[l]).max(), 'layer %d' % l
+    A, B, C, Ai, Bi, Ci = O.diff_coeffs(it['y'], atm_from_column(it['col']), O.Flags())
+    for got, e, m, sl in ((dA, A, Ai, slice(None)), (dB, B, Bi, slice(0, -1)),
+                          (dC, C, Ci, slice(1, None))):
+        ref = e[:, None] + m
+        mag = np.abs(e[:, None]) + np.abs(m)
+        assert np.all(np.abs(got[:nz][sl] - ref[sl]) <= 1e-13 * mag[sl])
+    h.close()
+
+
+@pytest.mark.gpu
+def test_lhs_matches_oracle(syn):
+    """Sparse -J and transport coefficients of the 150-species network."""
+    from vulcan_gb300 import _build
+    _build.build()
+    path, net, npz = syn
+    specs, items = _column(net, 30)
+    _lhs_check(net, items[:1], npz)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('precision', [0, 1])
+def test_attempt_matches_oracle_ncho_items(precision):
+    """The same item -> oracle path on an NCHO-thermo column (ni = 69): the
+    seeded set-up (batch.build_items) against the oracle at small dt."""
+    from vulcan_gb300 import _build
+    _build.build()
+    net = Network.from_npz(os.path.join(GOLDEN, 'net_NCHO_thermo.npz'))
+    specs = configs.config2_columns(ncols=2, seed=7, nz_range=(40, 60))
+    items = batch.build_items(specs, net)
+    npz = os.path.join(GOLDEN, 'net_NCHO_thermo.npz')
+    on = O.OracleNet.from_npz(npz, ATOMS)
+    h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
+    for dt in (1e-10, 1e-6):
+        sol = h.attempt(np.full(b.ncols, dt))['sol']
+        for c, it in enumerate(items):
+            sl = slice(b.off[c], b.off[c + 1])
+            r = O.ros2_attempt(on, it['y'], it['ymix'], dt, it['k'], atm_from_column(it['col']),
+                               O.Flags(), O.Tol())
+            assert floor_err(sol[sl], r.sol, it['col'].n_0) <= 1e-10, (dt, c)
     h.close()

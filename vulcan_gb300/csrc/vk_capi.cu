@@ -556,7 +556,6 @@ extern "C" int vk_get_counters(vk_handle *h, int *counters) {
 extern "C" int vk_get_conv(vk_handle *h, double *longdy, double *longdydt) {
     int rc = need_batch(h);
     if (rc) return rc;
-    if (!h->rs_ready) return fail(h, VK_EINVAL, "no vk_run yet");
     if (longdy) VK_CUDA(h, cudaMemcpy(longdy, h->rs.longdy, h->ncols * sizeof(double), cudaMemcpyDeviceToHost));
     if (longdydt) VK_CUDA(h, cudaMemcpy(longdydt, h->rs.longdydt, h->ncols * sizeof(double), cudaMemcpyDeviceToHost));
     return VK_OK;
