@@ -45,7 +45,8 @@ struct vk_handle {
     int *d_col_off = nullptr, *d_lay_col = nullptr;
     int *d_order = nullptr;             // columns by decreasing nz
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
-    int pgrid_max = 0;                  // CTAs of the per-column kernels (0 = one per column)
+    int nsm = 0;                        // SMs of the device
+    int cps = 0;                        // VK_CTAS_PER_SM override (0: kernel defaults)
     double *d_k = nullptr, *d_atm = nullptr, *d_Dzz = nullptr, *d_spf = nullptr;
     vk::Work w{};
     // batched-run state
@@ -77,7 +78,8 @@ struct vk_handle {
         b.active = nullptr;
         b.order = d_order;
         b.queue = d_queue;
-        b.pgrid = (pgrid_max > 0 && pgrid_max < ncols) ? pgrid_max : ncols;
+        b.nsm = nsm;
+        b.cps = cps;
         return b;
     }
 };
@@ -180,15 +182,13 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &h->d_order, max_cols));
     TRY(dalloc(h, &h->d_queue, 1));
     {
-        // per-column kernels: k resident CTAs per SM take columns from the queue
-        // (k = VK_CTAS_PER_SM, default 2, the fastest FP64 LU measured on GB300;
-        // 0 = one CTA per column)
-        int dev = 0, nsm = 0;
+        // per-column kernels: k resident CTAs per SM take columns from the queue;
+        // k = VK_CTAS_PER_SM when set, else each kernel's measured best
+        int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev);
         const char *env = getenv("VK_CTAS_PER_SM");
-        const int cps = env ? atoi(env) : 2;
-        h->pgrid_max = cps > 0 ? cps * nsm : 0;
+        h->cps = env ? atoi(env) : 0;
     }
     TRY(dalloc(h, &h->d_lay_col, L));
     TRY(dalloc(h, &h->d_k, L * h->nr));

@@ -85,8 +85,18 @@ struct DevBatch {
     const int *active;         // [ncols] non-zero = column takes part (NULL = all)
     const int *order;          // [ncols] columns by decreasing nz (work-queue order)
     unsigned *queue;           // [1] next queue position (zeroed before each launch)
-    int pgrid;                 // CTAs of the per-column kernels (<= ncols)
+    int nsm;                   // SMs of the device
+    int cps;                   // resident CTAs per SM of the per-column kernels
+                               // (0: each kernel's own default)
 };
+
+// Grid of a per-column kernel: cps CTAs per SM (the batch's override, else
+// the kernel's default), never more than the columns.
+inline int column_grid(const DevBatch &b, int cps_default) {
+    const int cps = b.cps > 0 ? b.cps : cps_default;
+    const long long g = (long long)cps * b.nsm;
+    return (g > 0 && g < b.ncols) ? (int)g : b.ncols;
+}
 
 #ifdef __CUDACC__
 // Per-column kernels run as a work queue: each CTA takes the next column in

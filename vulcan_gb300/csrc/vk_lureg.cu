@@ -110,7 +110,7 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
 // The dense scaled block of layer j+1 streams into shared memory by TMA while
 // layer j is inverted (register-resident Gauss-Jordan).
 template <int TY, int RA, int RB>
-__global__ void __launch_bounds__(16 * TY, TY == 16 && RA <= 5 ? 2 : 1)
+__global__ void __launch_bounds__(16 * TY, TY == 16 && RA <= 5 ? 3 : 1)
 k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__restrict__ dB,
        const double *__restrict__ dC, const double *__restrict__ rsc,
        const double *__restrict__ csc, float *__restrict__ G32, int *__restrict__ status,
@@ -267,10 +267,10 @@ void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaSt
     size_t sm = smem32(n, nb);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
     switch (tiling_of(n)) {
-    case 0: k_lu32<16, 3, 3><<<b.pgrid, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    case 1: k_lu32<16, 5, 5><<<b.pgrid, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    case 2: k_lu32<16, 7, 7><<<b.pgrid, 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    default: k_lu32<32, 5, 10><<<b.pgrid, 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 0: k_lu32<16, 3, 3><<<column_grid(b, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 1: k_lu32<16, 5, 5><<<column_grid(b, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 2: k_lu32<16, 7, 7><<<column_grid(b, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    default: k_lu32<32, 5, 10><<<column_grid(b, 1), 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
     }
 }
 
