@@ -179,9 +179,10 @@ def _workload(args, ncols=None):
     return net, configs.config2_columns(ncols=NCOLS, seed=SEED)[:n]
 
 
-def _setup(args, precision, ncols=None, warm_model=None):
-    """Handle over the workload's columns; with warm_model, the columns whose
-    learned proposal beats const_mix start from it (returns the mask too)."""
+def _setup(args, precision, ncols=None, warm_model=None, start='const_mix'):
+    """Handle over the workload's columns, started from const_mix, from
+    thermochemical equilibrium (start='eq') or from the learned proposal
+    (warm_model; returns the mask of warm-started columns too)."""
     from vulcan_gb300 import _build, batch, configs
     from vulcan_gb300.network import Network
     from vulcan_gb300.solver import ctrl_from
@@ -192,6 +193,9 @@ def _setup(args, precision, ncols=None, warm_model=None):
     if warm_model is not None:
         from vulcan_gb300 import warmstart
         items, used = warmstart.warm_items(warm_model, specs, net, items, ATOMS, precision)
+    elif start == 'eq':
+        from vulcan_gb300 import warmstart
+        items = warmstart.eq_items(specs, net, items, ATOMS)
     h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
     ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
     if warm_model is not None:
@@ -377,7 +381,7 @@ def run_converge(args):
     from vulcan_gb300 import capi
     res = {}
     finals = {}
-    paths = [('learned_mixed', 1), ('mixed', 1), ('plain_fp64', 0)]
+    paths = [('learned_mixed', 1), ('eq_mixed', 1), ('mixed', 1), ('plain_fp64', 0)]
     model = None
     if os.path.exists(args.weights):
         from vulcan_gb300 import warmstart
@@ -394,6 +398,9 @@ def run_converge(args):
             net, items, h, b, ctrl, used = _setup(args, prec, warm_model=model)
             res_extra = {'warm_started': int(used.sum()),
                          'proposal_s': round(time.perf_counter() - t0, 2)}
+        elif name == 'eq_mixed':
+            net, items, h, b, ctrl = _setup(args, prec, start='eq')
+            res_extra = {'proposal_s': round(time.perf_counter() - t0, 2)}
         else:
             net, items, h, b, ctrl = _setup(args, prec)
             res_extra = {}
@@ -513,7 +520,7 @@ def main():
     ap.add_argument('--count-max', type=int, default=30000)
     ap.add_argument('--chunk', type=int, default=500)
     ap.add_argument('--precision-only', default=None,
-                    help='comma-separated subset of learned_mixed,mixed,plain_fp64 (converge mode)')
+                    help='comma-separated subset of learned_mixed,eq_mixed,mixed,plain_fp64 (converge mode)')
     ap.add_argument('--weights', default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                                       'vulcan_gb300', 'warmstart_weights.npz'),
                     help='learned warm-start weights (converge mode)')

@@ -27,6 +27,7 @@ from .capi import check, lib
 
 LOG_FLOOR = -30.0
 N_TP = 16
+N_BASE_FEATURES = 3 + 4 + N_TP
 
 
 def column_features(spec, net, atom_list=('H', 'O', 'C', 'N', 'He')):
@@ -53,6 +54,31 @@ def column_features(spec, net, atom_list=('H', 'O', 'C', 'N', 'He')):
     f[:, 3:3 + len(ab)] = ab
     f[:, 3 + len(ab):] = tp[None, :]
     return f
+
+
+def const_mix_abundances(spec, net, atom_list=('H', 'O', 'C', 'He', 'N')):
+    """Element counts per molecule of the column's const_mix start."""
+    comp = net.compo_for(list(atom_list))
+    x0 = np.zeros(net.ni)
+    for sp, v in spec.const_mix.items():
+        x0[net.species.index(sp)] = v
+    return (x0 / x0.sum()) @ comp
+
+
+def eq_mix(spec, net, atom_list=('H', 'O', 'C', 'He', 'N')):
+    """Thermochemical equilibrium of every layer of the column [nz, ni]."""
+    from . import eqchem
+    return eqchem.equilibrium(net, spec.Tco, spec.pco, const_mix_abundances(spec, net, atom_list),
+                              list(atom_list))
+
+
+def features_eq(spec, net, x_eq=None):
+    """[nz, 23 + ni]: column_features plus the layer's log10 equilibrium
+    mixing ratios (the steady state is equilibrium at depth and quenched
+    above, so the network learns the departure from it)."""
+    if x_eq is None:
+        x_eq = eq_mix(spec, net)
+    return np.concatenate([column_features(spec, net), log_targets(x_eq)], axis=1)
 
 
 def log_targets(ymix):
@@ -299,7 +325,8 @@ def propose(model, specs, net, items, atom_list=('H', 'O', 'C', 'He', 'N')):
     list of (y, ymix), each proposal projected onto its column's element
     totals (those of the const_mix start, which the run then conserves)."""
     comp = net.compo_for(list(atom_list)).astype(float)
-    feats = [column_features(sp, net) for sp in specs]
+    with_eq = model.dims[0] > N_BASE_FEATURES
+    feats = [features_eq(sp, net) if with_eq else column_features(sp, net) for sp in specs]
     logx = model.predict(np.concatenate(feats))
     off = np.concatenate([[0], np.cumsum([f.shape[0] for f in feats])])
     xs = [10.0 ** np.clip(logx[off[c]:off[c + 1]], LOG_FLOOR, 0.0) for c in range(len(specs))]
@@ -357,7 +384,7 @@ def generate(net, seeds, ncols, atoms, count_max=4000, timeout_s=900, precision=
         conv = st['end_case'] == 1
         for c in np.nonzero(conv)[0]:
             ym = st['ymix'][b.off[c]:b.off[c + 1]]
-            Xs.append(column_features(specs[c], net))
+            Xs.append(features_eq(specs[c], net))
             Ys.append(log_targets(ym))
             Cs.append(np.full(ym.shape[0], seed * 100000 + c))
         log('seed %d: %d/%d converged, median steps %s, %.1f s'
@@ -375,6 +402,17 @@ def warm_items(model, specs, net, items, atoms, precision=1):
     prop = propose(model, specs, net, items, atom_list=atoms)
     out = [dict(it, y=y, ymix=x) for it, (y, x) in zip(items, prop)]
     return out, np.ones(len(items), dtype=bool)
+
+
+def eq_items(specs, net, items, atoms):
+    """Items started from thermochemical equilibrium (the reference's
+    ini_mix = 'EQ' seam), projected onto the const_mix start's element
+    totals."""
+    comp = net.compo_for(list(atoms)).astype(float)
+    xs = [eq_mix(sp, net, atoms) for sp in specs]
+    n0s = [it['col'].n_0 for it in items]
+    xs = project_columns(xs, n0s, comp, [np.asarray(it['atom_ini'], dtype=float) for it in items])
+    return [dict(it, y=n0[:, None] * x, ymix=x) for it, n0, x in zip(items, n0s, xs)]
 
 
 def fallback_items(items_const, end_case):
