@@ -90,3 +90,17 @@ def atm_from_column(col):
     keys = ('M', 'n_0', 'Tco', 'Kzz', 'vz', 'Dzz', 'Ti', 'ms', 'alpha', 'pico', 'dzi', 'Hpi',
             'g', 'Hp', 'dz', 'zco', 'top_flux', 'bot_flux', 'bot_vdep')
     return {k: getattr(col, k) for k in keys}
+
+
+def item_floor(on, it, dt, samples=3, eps=4e-16):
+    """Conditioning floor of an attempt from a column item (batch.build_items):
+    the oracle's result and its spread when the Jacobian changes at the
+    rounding level (see reference_floor).  Returns (oracle result, floor)."""
+    args = (on, it['y'], it['ymix'], dt, it['k'], atm_from_column(it['col']), O.Flags(),
+            O.Tol(), 'banded')
+    r0 = O.ros2_attempt(*args)
+    e = 0.0
+    for seed in range(samples):
+        r = O.ros2_attempt(*args, perturb=(eps, seed))
+        e = max(e, floor_err(r.sol, r0.sol, it['col'].n_0))
+    return r0, e

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import GOLDEN, atm_from_column, floor_err
+from helpers import GOLDEN, atm_from_column, floor_err, item_floor
 from oracle import ros2 as O
 from vulcan_gb300 import batch, configs, synthnet
 from vulcan_gb300.network import Network
@@ -97,9 +97,10 @@ def test_attempt_matches_oracle(syn, precision):
         sol = h.attempt(np.full(b.ncols, dt))['sol']
         for c, it in enumerate(items):
             sl = slice(b.off[c], b.off[c + 1])
-            r = O.ros2_attempt(on, it['y'], it['ymix'], dt, it['k'], atm_from_column(it['col']),
-                               O.Flags(), O.Tol())
-            assert floor_err(sol[sl], r.sol, it['col'].n_0) <= 1e-10
+            r, fl = item_floor(on, it, dt)
+            # these first attempts from const_mix are rejected steps (delta ~ 1):
+            # 1e-10 where the step is well conditioned, else 10x its floor
+            assert floor_err(sol[sl], r.sol, it['col'].n_0) <= max(1e-10, 10 * fl), (dt, c, fl)
     h.close()
 
 
@@ -152,7 +153,6 @@ def test_attempt_matches_oracle_ncho_items(precision):
         sol = h.attempt(np.full(b.ncols, dt))['sol']
         for c, it in enumerate(items):
             sl = slice(b.off[c], b.off[c + 1])
-            r = O.ros2_attempt(on, it['y'], it['ymix'], dt, it['k'], atm_from_column(it['col']),
-                               O.Flags(), O.Tol())
-            assert floor_err(sol[sl], r.sol, it['col'].n_0) <= 1e-10, (dt, c)
+            r, fl = item_floor(on, it, dt)
+            assert floor_err(sol[sl], r.sol, it['col'].n_0) <= max(1e-10, 10 * fl), (dt, c, fl)
     h.close()

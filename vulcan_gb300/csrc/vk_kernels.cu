@@ -210,11 +210,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
     double *rowk = colk + n;
     double *zp = rowk + n;
     double *bb = zp + n;
-    double *colk2 = bb + n;
-    double *rowk2 = colk2 + n;
-    double *c2 = rowk2 + n;
-    double *tmp = c2 + n;
-    int *perm = reinterpret_cast<int *>(tmp + n);
+    int *perm = reinterpret_cast<int *>(bb + n);
     __shared__ int s_piv, s_sing, s_col;
     __shared__ double s_pval;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
@@ -241,7 +237,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
             const double *jl = jv + l * net.nnz;
             for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
             __syncthreads();
-            gj_invert_f64_x2(A, n, colk, rowk, colk2, rowk2, c2, tmp, perm, &s_piv, &s_pval, &s_sing);
+            gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
             double *Gl = G + l * nn;
             for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
             for (int r = warp; r < n; r += nwarp) {
@@ -420,8 +416,8 @@ void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flag
 
 // ---------------------------------------------------------------------------
 static size_t rates_smem(const DevNet &net);
-// block, colk, rowk, zp, bb, colk2, rowk2, c2, tmp (doubles) + perm (ints)
-static size_t lu_fwd_smem(int n) { return (size_t)(n * n + 8 * n) * sizeof(double) + (size_t)n * sizeof(int); }
+// block, colk, rowk, zp, bb (doubles) + perm (ints)
+static size_t lu_fwd_smem(int n) { return (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int); }
 
 // Opt the kernels into the dynamic shared memory this network needs; called
 // once per handle, outside any stream capture.

@@ -28,10 +28,12 @@ Choices (all seeded):
     the reverse rate k/Keq (the reference's rev_rate, op.py:287-309) stays
     below the collision limit (1e-9 cm^3 s^-1 for two-body reverses, 1e13
     s^-1 for first-order ones) over 400-3500 K, as the endothermic direction
-    of a real reaction is the slow one;
+    of a real reaction is the slow one; a draw that would need C > 1.5e5 K is
+    rejected (its rates would underflow at 400 K);
   * Gibbs data: constant heat capacity cp/R = 2.5 + 0.5 n_atoms, enthalpy of
-    formation b1 = sum of per-element terms + U[-6000, 6000] K, entropy
-    offset b2 U[10, 40] + 2 n_atoms, the same in both NASA-9 ranges;
+    formation b1 = sum of per-element terms - 25000 K per bond (n_atoms - 1)
+    + U[-6000, 6000] K, entropy offset b2 U[10, 40] + 2 n_atoms, the same in
+    both NASA-9 ranges;
   * photolysis: 60 channels A -> B + C of species with >= 2 atoms, J frozen
     per column (configs.photo_J_profile).
 """
@@ -76,6 +78,10 @@ CORR = 1.38064852E-16 / 1.0e6          # k_B / P0 (the reference's gibbs_text co
 T_GRID = np.linspace(400.0, 3500.0, 64)
 K2_MAX = 1e-9                             # two-body collision limit (cm^3 s^-1)
 K1_MAX = 1e13                             # first-order limit (s^-1)
+BOND = 25000.0                            # formation enthalpy per bond (K): associations
+                                          # are exothermic, exchanges thermoneutral
+EA_MAX = 1.5e5                            # larger barriers: the draw is rejected (k would
+                                          # underflow at 400 K and k0/k_inf become 0/0)
 
 
 def _g_rt(a3, b1, b2, T):
@@ -107,7 +113,8 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
     for cv in comp:
         nat = max(int(cv.sum()), 1)
         a3 = 2.5 + 0.5 * nat
-        b1 = sum(h_el[e] * k for e, k in zip(('H', 'O', 'C', 'N'), cv)) + rng.uniform(-6000, 6000)
+        b1 = (sum(h_el[e] * k for e, k in zip(('H', 'O', 'C', 'N'), cv)) - BOND * (nat - 1)
+              + rng.uniform(-6000, 6000))
         b2 = rng.uniform(10, 40) + 2.0 * nat
         thermo.append((a3, b1, b2))
     g = [_g_rt(a3, b1, b2, T_GRID) for a3, b1, b2 in thermo]
@@ -141,32 +148,49 @@ def generate(out_dir, seed=4, ni=150, n_rev=1200, n_photo=60, name='SYN150'):
         seen.add(k1)
         A = 10.0 ** rng.uniform(-14, -9)
         Ea = max(rng.uniform(0, 40000), _min_ea(np.log(A), [a, b], [c, d], g))
+        if Ea > EA_MAX:
+            seen.discard(k1)
+            continue
         lines['bi'].append(('%s + %s -> %s + %s' % (names[a], names[b], names[c], names[d]),
                             '%.4E 0.0 %.1f' % (A, Ea)))
     # species that are the sum of a pair (three-body association, unimolecular split)
     assoc = [(pr, idx[s]) for s, prs in pairs.items() if s in idx for pr in prs]
-    order = rng.permutation(len(assoc))
-    it = iter(order)
+    tries = 0
+
+    def draw():
+        nonlocal tries
+        tries += 1
+        if tries > 10 ** 6:
+            raise RuntimeError('could not draw enough association / split reactions')
+        return assoc[rng.integers(len(assoc))]
+
     while len(lines['ter']) < n_ter:
-        (a, b), c = assoc[next(it)]
+        (a, b), c = draw()
         k1 = key((a, b, -1), (c, -1))
         if k1 in seen:
             continue
         seen.add(k1)
         A = 10.0 ** rng.uniform(-14, -9)
-        # high-pressure limit k_inf = A exp(-Ea/T) bounds the fall-off rate; its
-        # reverse C + M -> A + B + M is two-body in the reference's units
-        Ea = max(rng.uniform(0, 40000), _min_ea(np.log(A), [a, b], [c], g, extra_order=1))
+        # the fall-off rate k0 / (1 + k0 M / k_inf) never exceeds k0 = 1e-20 A exp(-Ea/T)
+        # (cm^6 s^-1, the rate law carries M); its reverse C + M -> A + B + M is
+        # two-body in (C, M)
+        Ea = max(rng.uniform(0, 40000), _min_ea(np.log(1e-20 * A), [a, b], [c], g, extra_order=1))
+        if Ea > EA_MAX:
+            seen.discard(k1)
+            continue
         lines['ter'].append(('%s + %s + M -> %s + M' % (names[a], names[b], names[c]),
                              '%.4E 0.0 %.1f %.4E 0.0 %.1f' % (1e-20 * A, Ea, A, Ea)))
     while len(lines['uni']) < n_uni:
-        (b, c), a = assoc[next(it)]
+        (b, c), a = draw()
         k1 = key((a,), (b, c))
         if k1 in seen:
             continue
         seen.add(k1)
         A = 10.0 ** rng.uniform(8, 13)
         Ea = max(rng.uniform(0, 40000), _min_ea(np.log(A), [a], [b, c], g))
+        if Ea > EA_MAX:
+            seen.discard(k1)
+            continue
         lines['uni'].append(('%s -> %s + %s' % (names[a], names[b], names[c]),
                              '%.4E 0.0 %.1f' % (A, Ea)))
     photo = []
