@@ -46,8 +46,10 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c2': (0, 1, 2, 10, 29),
         'c2long': (400, 800, 1200, 1600, 1999),
         'c2conv': (0,),
-        'c2tight': (0,)}
-NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000}
+        'c2tight': (0,),
+        'c2slow': (0,)}
+NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
+          'c2slow': 4000}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -293,6 +295,10 @@ def make(tag, ref_root, workdir, full_dir=None):
         spec = configs.config0()
     elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]
+    elif tag == 'c2slow':
+        # a column of the 512-column batch that has not converged after 4000 steps
+        # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
+        spec = configs.config2_columns(ncols=512, seed=2)[60]
     elif tag == 'c1':
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
                                 use_photo=True)
@@ -315,7 +321,7 @@ def make(tag, ref_root, workdir, full_dir=None):
     np.savez_compressed(out, **d)
     net.to_npz(os.path.join(HERE, 'net_%s.npz' % spec.network.replace('_network.txt', '')
                             + ('_photo' if spec.use_photo and 'photo' not in spec.network else '')))
-    if full_dir and tag not in ('c2conv', 'c2tight'):
+    if full_dir and tag not in ('c2conv', 'c2tight', 'c2slow'):
         os.makedirs(full_dir, exist_ok=True)
         shutil.copy(os.path.join(dst, 'golden_full.npz'),
                     os.path.join(full_dir, 'golden_full_%s.npz' % tag))
