@@ -153,3 +153,109 @@ __device__ __forceinline__ void gj_store_natural(const T (&M)[RA][RB], int n, in
 }
 
 }  // namespace vk
+
+namespace vk {
+
+// gj_invert_reg with one block barrier per pivot step.  The pivot row reaches
+// the threads of each column group by warp shuffles (the TY owners of a column
+// are consecutive lanes, so every thread finds row p of its own columns at lane
+// p % TY of its group); only the pivot column goes through shared memory, in
+// two buffers by parity of k (colv2[2n]), written together with the search of
+// the next pivot right after each update -- so the next step needs one
+// barrier.  Same pivots and the same FMA per element as gj_invert_reg.
+// s_piv2 holds two pivot slots (parity of k).
+template <typename T, int TY, int RA, int RB>
+__device__ __forceinline__ void gj_invert_reg1(T (&M)[RA][RB], int n, int ty, int tx,
+                                               const GJShared<T> &sh, T *colv2, int *s_piv2) {
+    int rr[RA], cc[RB];
+#pragma unroll
+    for (int a = 0; a < RA; ++a) rr[a] = ty + TY * a;
+#pragma unroll
+    for (int b = 0; b < RB; ++b) cc[b] = tx + 16 * b;
+    const unsigned gmask = TY == 32 ? 0xffffffffu : (0xffffu << (threadIdx.x & 16));
+    // pivot search of column k among this thread's unused rows, reduced over
+    // the column group; lane ty == 0 records it (all owners know bi after)
+    auto search = [&](int k) {
+        const int kb = k >> 4;
+        T best = T(-1);
+        int bi = n;
+#pragma unroll
+        for (int a = 0; a < RA; ++a) {
+            if (rr[a] < n && !sh.used[rr[a]]) {
+                T v = gj_abs(pick_col(M[a], kb));
+                if (v > best) { best = v; bi = rr[a]; }
+            }
+        }
+#pragma unroll
+        for (int o = TY >> 1; o; o >>= 1) {
+            T ob = __shfl_xor_sync(gmask, best, o, TY);
+            int oi = __shfl_xor_sync(gmask, bi, o, TY);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (ty == 0) {
+            if (bi >= n || !(best >= T(0)) || isinf((double)best)) {
+                *sh.s_sing = 2;
+                for (int r = 0; r < n; ++r)
+                    if (!sh.used[r]) { bi = r; break; }
+            } else if (!(best > T(0))) {
+                if (*sh.s_sing == 0) *sh.s_sing = 1;
+            }
+            s_piv2[k & 1] = bi;
+            sh.perm[k] = bi;
+            sh.kinv[bi] = k;
+            sh.used[bi] = 1;
+        }
+        // the column (before elimination) for every row
+        T *cv = colv2 + (k & 1) * n;
+#pragma unroll
+        for (int a = 0; a < RA; ++a)
+            if (rr[a] < n) cv[rr[a]] = pick_col(M[a], kb);
+    };
+    if (tx == 0) search(0);
+    for (int k = 0; k < n; ++k) {
+        __syncthreads();
+        const int kx = k & 15, kb = k >> 4;
+        const int p = s_piv2[k & 1];
+        const T *cv = colv2 + (k & 1) * n;
+        const T pinv = T(1) / cv[p];
+        // pivot row of this thread's columns from its column group (lane p % TY)
+        const int pa = p / TY, pl = p - pa * TY;
+        T rp[RB];
+#pragma unroll
+        for (int b = 0; b < RB; ++b) {
+            T mine = T(0);
+#pragma unroll
+            for (int a = 0; a < RA; ++a)
+                if (a == pa) mine = M[a][b];
+            // every lane runs this: full mask, segments of TY lanes
+            const T v = __shfl_sync(0xffffffffu, mine, pl, TY);
+            rp[b] = cc[b] < n ? v * pinv : T(0);
+        }
+        T fr[RA];
+#pragma unroll
+        for (int a = 0; a < RA; ++a) {
+            fr[a] = rr[a] < n ? cv[rr[a]] : T(0);
+            if (rr[a] == p) {
+#pragma unroll
+                for (int b = 0; b < RB; ++b) M[a][b] = rp[b];
+            } else {
+#pragma unroll
+                for (int b = 0; b < RB; ++b) M[a][b] -= fr[a] * rp[b];
+            }
+        }
+        if (tx == kx) {
+#pragma unroll
+            for (int a = 0; a < RA; ++a) {
+                const T v = rr[a] == p ? pinv : -fr[a] * pinv;
+#pragma unroll
+                for (int b = 0; b < RB; ++b)
+                    if (b == kb) M[a][b] = v;
+            }
+        }
+        // next pivot: its column owners search their updated registers now
+        if (k + 1 < n && tx == ((k + 1) & 15)) search(k + 1);
+    }
+    __syncthreads();
+}
+
+}  // namespace vk

@@ -127,9 +127,10 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
     int *perm = reinterpret_cast<int *>(beta + n);
     int *kinv = perm + n;
     int *used = kinv + n;
-    __shared__ int s_piv, s_sing, s_col;
+    __shared__ int s_piv, s_sing, s_col, s_piv2[2];
     __shared__ float s_pval;
     GJShared<float> sh{rowv, colv, perm, kinv, used, &s_piv, &s_pval, &s_sing};
+    float *colv2 = rowv;                                           // [2][n] (rowv, colv)
     int ty, tx;
     tile_coords<TY>(ty, tx);
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -204,7 +205,7 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
             // overwrites it while the inversion runs
             if (nbuf == 1 && tid == 0 && j + 1 < nz)
                 tma_load_1d(Dbuf, D32 + (l + 1) * NNP, bytes, &bar[0]);
-            gj_invert_reg<float, TY, RA, RB>(M, n, ty, tx, sh);
+            gj_invert_reg1<float, TY, RA, RB>(M, n, ty, tx, sh, colv2, s_piv2);
             gj_store_natural<float, TY, RA, RB>(M, n, ty, tx, sh, Gs);
             float *Gl = G32 + l * NNP;
             for (int e = tid; e < nn; e += nth) Gl[e] = Gs[e];
