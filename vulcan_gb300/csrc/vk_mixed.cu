@@ -58,6 +58,8 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
     const uint32_t bytes = (uint32_t)NNP * sizeof(float);
+    const int tpr = 2 * n <= nth ? 2 : 1;          // lanes per matvec row
+    const int mrow = tid / tpr, mhalf = tid - mrow * tpr;
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -117,22 +119,27 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 if (v + 1 < per_sweep) issue(v + 1);
                 else if (sweep + 1 < max_sweeps) issue(0);
                 const float *G = Gbuf + buf * NNP;
-                if (tid < n) {
+                // matvec: tpr adjacent lanes per row, interleaved columns
+                float sacc = 0.0f;
+                if (mrow < n) {
                     float s0 = 0.0f, s1 = 0.0f;
-                    const float *row = G + tid * n;
-                    int q = 0;
-                    for (; q + 1 < n; q += 2) {
+                    const float *row = G + mrow * n;
+                    int q = mhalf;
+                    for (; q + tpr < n; q += 2 * tpr) {
                         s0 = fmaf(row[q], vin[q], s0);
-                        s1 = fmaf(row[q + 1], vin[q + 1], s1);
+                        s1 = fmaf(row[q + tpr], vin[q + tpr], s1);
                     }
                     if (q < n) s0 = fmaf(row[q], vin[q], s0);
-                    float sacc = s0 + s1;
+                    sacc = s0 + s1;
+                }
+                if (tpr == 2) sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
+                if (mrow < n && mhalf == 0) {
                     if (fwd) {
-                        zf[l * n + tid] = sacc;
+                        zf[l * n + mrow] = sacc;
                     } else {
-                        sacc += zf[l * n + tid];
+                        sacc += zf[l * n + mrow];
                     }
-                    vout[tid] = sacc;
+                    vout[mrow] = sacc;
                 }
                 __syncthreads();
                 // the back sweep starts at the top layer: x~_{nz-1} = z~_{nz-1} (vout)
