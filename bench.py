@@ -406,6 +406,8 @@ def run_converge(args):
             res_extra = {}
             t0 = time.perf_counter()
         ctrl.count_max = args.count_max
+        if args.yconv:
+            ctrl.yconv_cri = ctrl.yconv_min = args.yconv
         curve = []
         dev_s = 0.0
         while True:
@@ -436,8 +438,9 @@ def run_converge(args):
         finals[name] = (st['ymix'], st['end_case'], st['count'])
         h.close()
     res['metric'] = METRIC
-    res['workload'] = ('%d uneven NCHO-thermo columns to steady state (reference conv criterion, '
-                       'count_max %d)' % (args.ncols, args.count_max))
+    res['workload'] = ('%d uneven NCHO-thermo columns to steady state (%s, count_max %d)'
+                       % (args.ncols, 'reference conv criterion' if not args.yconv else
+                          'yconv_cri = yconv_min = %g' % args.yconv, args.count_max))
     if 'plain_fp64' in finals:
         bsz = [it.pco.size for it in _workload(args)[1]]
         off = np.concatenate([[0], np.cumsum(bsz)])
@@ -519,6 +522,8 @@ def main():
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
     ap.add_argument('--count-max', type=int, default=30000)
     ap.add_argument('--chunk', type=int, default=500)
+    ap.add_argument('--yconv', type=float, default=None,
+                    help='converge mode: yconv_cri = yconv_min = this (tighter than the defaults)')
     ap.add_argument('--precision-only', default=None,
                     help='comma-separated subset of learned_mixed,eq_mixed,mixed,plain_fp64 (converge mode)')
     ap.add_argument('--weights', default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
