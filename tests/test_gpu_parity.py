@@ -288,3 +288,31 @@ def test_device_run_reaches_reference_steady_state(precision):
           % (st['count'][0], g['final_count'], np.median(rel), np.percentile(rel, 99), rel.max()))
     assert np.median(rel) <= 1e-3
     assert np.percentile(rel, 99) <= 2e-2
+
+
+@pytest.mark.parametrize('precision', [0, 1])
+def test_slow_column_stalls_like_reference(precision):
+    """A column that the reference itself does not bring to steady state in
+    4000 steps (fixture c2slow: count_max reached at t = 7e6 s with dt ~ 1e3 s,
+    the stall the device batch shows on a quarter of the uneven columns):
+    the device run stalls the same way -- the stragglers of a batch come from
+    the reference algorithm, not from this implementation."""
+    from vulcan_gb300 import configs
+    from vulcan_gb300.solver import ctrl_from
+    g, net, gn, h, b = make_handle('c2slow', precision=precision)
+    h.set_atom_ini(g['atom_ini'][None, :])
+    mask = np.zeros(net.ni, dtype=np.int32)
+    for sp in g['conver_ignore']:
+        if str(sp) in net.species:
+            mask[net.species.index(str(sp))] = 1
+    h.set_conv_ignore(mask)
+    h.set_clock(dt=1e-10, t=0.0, count=0)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    ctrl.count_max = int(g['final_count']) - 1
+    h.run(ctrl, max_steps=10 * int(g['final_count']), timeout_s=900)
+    st = h.state()
+    assert g['end_case'] == 3
+    assert st['end_case'][0] == 3 and st['count'][0] == g['final_count']
+    assert 0.2 * g['final_t'] <= st['t'][0] <= 5.0 * g['final_t']
+    dt_ref = np.median(g['traj_dt_used'][-500:])
+    assert 0.05 * dt_ref <= st['dt'][0] <= 20 * dt_ref
