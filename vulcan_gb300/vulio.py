@@ -1,0 +1,89 @@
+"""`.vul` output and `vulcan_ini` restart, the reference's file seam.
+
+The reference saves a run as a pickle (protocol 4) of
+``{'variable': var_save, 'atm': vars(atm), 'parameter': vars(para)}``
+(op.Output.save_out, op.py:3216-3256), with ``var_save`` holding
+``species``, ``nr`` and the fields of store.Variables.var_save (store.py:83):
+``k`` (dict reaction index -> [nz]), ``y``, ``ymix``, ``y_ini``, ``t``, ``dt``,
+``longdy``, ``longdydt``, ``atom_ini``, ``atom_sum``, ``atom_loss``,
+``atom_conden`` (dicts over atom_list), ``aflux_change`` and ``Rf`` (dict
+reaction index -> text).  Downstream scripts (the reference's plot_py/) read
+``variable['ymix']``, ``variable['species']``, ``atm['pco']`` and friends.
+
+``ini_mix = 'vulcan_ini'`` (build_atm.py:166-181) starts a run from the ``y``
+of such a file, species matched by name; :func:`read_vul_y` does the same.
+"""
+from __future__ import annotations
+
+import pickle
+
+import numpy as np
+
+ATM_KEYS = ('pco', 'pico', 'Tco', 'Kzz', 'vz', 'M', 'n_0', 'mu', 'g', 'Hp', 'dz', 'zco',
+            'dzi', 'Dzz', 'ms', 'alpha', 'Ti', 'Hpi', 'top_flux', 'bot_flux', 'bot_vdep',
+            'pref_indx', 'gs', 'Rp')
+
+
+def vul_dict(net, item, y, ymix, t, dt, count, end_case, atom_list, longdy=0.0, longdydt=0.0,
+             delta=0.0):
+    """The save_out dictionary of one column (state arrays [nz, ni])."""
+    from .column import atom_totals
+    col = item['col']
+    k = item['k']
+    atom_sum = atom_totals(net, y, atom_list)
+    atom_ini = np.asarray(item['atom_ini'], dtype=float)
+    var = {'species': list(net.species), 'nr': net.nr,
+           'k': {i + 1: np.array(k[i]) for i in range(k.shape[0])},
+           'y': np.array(y), 'ymix': np.array(ymix),
+           'y_ini': np.array(item.get('y_ini', item['y'])),
+           't': float(t), 'dt': float(dt), 'longdy': float(longdy), 'longdydt': float(longdydt),
+           'atom_ini': {a: float(v) for a, v in zip(atom_list, atom_ini)},
+           'atom_sum': {a: float(v) for a, v in zip(atom_list, atom_sum)},
+           'atom_loss': {a: float((s - i) / i) for a, s, i in zip(atom_list, atom_sum, atom_ini)},
+           'atom_conden': {a: 0.0 for a in atom_list},
+           'aflux_change': 0.0,
+           'Rf': {r.index: r.text for r in net.reactions}}
+    atm = {key: np.array(getattr(col, key)) if hasattr(getattr(col, key, None), '__len__')
+           else getattr(col, key) for key in ATM_KEYS if hasattr(col, key)}
+    para = {'count': int(count), 'end_case': int(end_case), 'delta': float(delta),
+            'solver_str': 'Ros2GPU'}
+    return {'variable': var, 'atm': atm, 'parameter': para}
+
+
+def write_vul(path, data):
+    with open(path, 'wb') as f:
+        pickle.dump(data, f, protocol=4)
+
+
+def write_batch(paths, net, items, state, atom_list, conv=None):
+    """One .vul per column of a batch state (Ros2Handle.state()); ``paths``
+    lists the file names; ``conv`` = (longdy, longdydt) per column."""
+    off = np.concatenate([[0], np.cumsum([it['col'].nz for it in items])])
+    for c, (path, it) in enumerate(zip(paths, items)):
+        sl = slice(off[c], off[c + 1])
+        ld = conv[0][c] if conv is not None else 0.0
+        ldt = conv[1][c] if conv is not None else 0.0
+        write_vul(path, vul_dict(net, it, state['y'][sl], state['ymix'][sl], state['t'][c],
+                                 state['dt'][c], state['count'][c], state['end_case'][c],
+                                 atom_list, ld, ldt, state['delta'][c]))
+
+
+def read_vul_y(path, species, nz=None):
+    """y [nz, len(species)] from a .vul file, species matched by name (a
+    species the file does not hold stays 0 and is listed in the second
+    return value), as ini_mix = 'vulcan_ini' does."""
+    with open(path, 'rb') as f:
+        d = pickle.load(f)
+    v = d['variable']
+    src = v['species']
+    y_src = np.asarray(v['y'])
+    if nz is not None and y_src.shape[0] != nz:
+        raise ValueError('%s has %d layers, the run %d' % (path, y_src.shape[0], nz))
+    y = np.zeros((y_src.shape[0], len(species)))
+    missing = []
+    for i, sp in enumerate(species):
+        if sp in src:
+            y[:, i] = y_src[:, src.index(sp)]
+        else:
+            missing.append(sp)
+    return y, missing
