@@ -106,7 +106,8 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
     }
 }
 
-// FP32 block-Thomas factorisation of the scaled system, one CTA per column.
+// FP32 block-Thomas factorisation of the scaled system, one column at a time
+// per CTA (columns from the work queue).
 // The dense scaled block of layer j+1 streams into shared memory by TMA while
 // layer j is inverted (register-resident Gauss-Jordan).
 template <int TY, int RA, int RB>

@@ -12,7 +12,7 @@
 //     D~'_j = R_j D_j S_j - L~_j G~_{j-1} U~_{j-1}
 // is inverted in FP32 and G~_j is stored in FP32 (half the bytes of FP64).
 //
-// k_refine (one CTA per column) solves A x = b: x = 0, r = b; repeat
+// k_refine (one column at a time per CTA) solves A x = b: x = 0, r = b; repeat
 // { d = S M~^-1 R r  (FP32 forward/back sweeps with G~);  x += d (FP64);
 //   r = b - A x  (FP64, matrix-free from the sparse -J and dA/dB/dC) }
 // until max |d| / (|x| + |yscale| + 1e-10 n_0) <= tol or max sweeps; a
@@ -33,7 +33,8 @@
 namespace vk {
 
 
-// Iterative refinement of A x = b with the FP32 factors (one CTA per column).
+// Iterative refinement of A x = b with the FP32 factors (one column at a time
+// per CTA, columns from the work queue).
 // The inverse blocks G~_j stream into shared memory by TMA (double-buffered)
 // in the order the sweeps visit them: forward 0..nz-1, back nz-2..0.
 // yscale (may be NULL) widens the convergence floor: k1/k2 enter sol next to y.

@@ -2,19 +2,20 @@
 
 Not part of the reference (its initial state is ``ini_mix``, build_atm.py:141;
 ``const_mix`` :192-198 is the fallback here).  The network maps per-layer
-inputs -- log P, T, log Kzz, the column's elemental abundances and a
-16-point summary of the column's T-P profile -- to the ni log10 mixing ratios
-at steady state.  It is trained on steady states produced by this package's
-own solver, with the hand-written BF16 kernels of vk_mlp.cu (forward,
-backward, Adam; PyTorch only holds the device memory).
+inputs -- log P, T, log Kzz, the column's elemental abundances, a 16-point
+summary of the column's T-P profile and the layer's log10 thermochemical
+equilibrium mixing ratios (eqchem.py) -- to the ni log10 mixing ratios at
+steady state.  It is trained on steady states produced by this package's own
+solver, with the hand-written BF16 kernels of vk_mlp.cu (forward, backward,
+Adam; PyTorch only holds the device memory).
 
 The proposal is projected onto the column's element totals (maximum-entropy
 projection: mixing ratios summing to 1 in every layer, column totals equal
 to those of ``const_mix``), so that plain Ros2 from the proposal conserves
-the same element totals as from ``const_mix`` and converges to the same
-steady state.  Plain Ros2 then runs
-to the reference's convergence test; a column whose proposal has a larger
-chemical residual than the const_mix start falls back to const_mix.
+the same element totals as from ``const_mix``.  Plain Ros2 then runs to the
+reference's convergence test -- the solver, not the network, decides the
+answer -- and a column that does not converge from its proposal can be rerun
+from const_mix (fallback_items).
 """
 from __future__ import annotations
 
