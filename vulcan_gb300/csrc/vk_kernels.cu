@@ -97,8 +97,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
     const int j = l - l0;
     double *ys = sm;                       // [3][ni] layers j-1, j, j+1
-    double *sums = ys + 3 * ni;            // [4]
-    double *v = sums + 4;                  // [max(npair, nw)]
+    double *sums = ys + 3 * ni;            // [8] column sums, ysum ratios, 2/(r dt)
+    double *v = sums + 8;                  // [max(npair, nw)]
     double *kM = v + (net.npair > net.nw ? net.npair : net.nw);   // [2*npair] (JAC only)
     const int tid = threadIdx.x, nth = blockDim.x;
     for (int t = tid; t < 3 * ni; t += nth) {
@@ -107,11 +107,25 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     }
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
-    if (warp < 3) {
-        double s = 0;
-        for (int i = lane; i < ni; i += 32) s += ys[warp * ni + i];
-        s = warp_sum(s);
-        if (lane == 0) sums[warp] = s;
+    const bool has_up = j + 1 < nz, has_dn = j > 0;
+    if (warp == 0) {
+        // layer sums and the state-dependent ysum ratios of the transport
+        // operator, once per layer (FP64 divisions are costly on this chip)
+        double s3[3];
+#pragma unroll
+        for (int w = 0; w < 3; ++w) {
+            double s = 0;
+            for (int i = lane; i < ni; i += 32) s += ys[w * ni + i];
+            s3[w] = warp_sum(s);
+        }
+        if (lane == 0) {
+            const double ysm = s3[0], ys0 = s3[1], ysp = s3[2];
+            sums[0] = has_up ? (ysp + ys0) / (2. * ys0) : 0.0;
+            sums[1] = has_dn ? (ys0 + ysm) / (2. * ys0) : 0.0;
+            sums[2] = has_up ? (ysp + ys0) / (2. * ysp) : 0.0;
+            sums[3] = has_dn ? (ys0 + ysm) / (2. * ysm) : 0.0;
+            sums[4] = k1 ? 2. / (R_ROS * dt[c]) : 0.0;
+        }
     }
     const double *yl = ys + ni;
     const double *al = b.atm + (size_t)l * VK_ATM_NF;
@@ -129,13 +143,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     }
     __syncthreads();
     // ysum ratios of the transport operator (state dependent part)
-    const double ysm = sums[0], ys0 = sums[1], ysp = sums[2];
-    const bool has_up = j + 1 < nz, has_dn = j > 0;
-    const double qU0 = has_up ? (ysp + ys0) / (2. * ys0) : 0.0;
-    const double qD0 = has_dn ? (ys0 + ysm) / (2. * ys0) : 0.0;
-    const double qUp = has_up ? (ysp + ys0) / (2. * ysp) : 0.0;
-    const double qDm = has_dn ? (ys0 + ysm) / (2. * ysm) : 0.0;
-    const double hinv = k1 ? 2. / (R_ROS * dt[c]) : 0.0;
+    const double qU0 = sums[0], qD0 = sums[1], qUp = sums[2], qDm = sums[3];
+    const double hinv = sums[4];
     const double *gl = geo + (size_t)l * GEO_NF * ni;
     const double *spf = b.spf + (size_t)c * VK_SP_NF * ni;
     // production - loss gather (generated chemdf order) + transport
@@ -434,7 +443,7 @@ cudaError_t init_kernels(const DevNet &net) {
 
 static size_t rates_smem(const DevNet &net) {
     int m = net.npair > net.nw ? net.npair : net.nw;
-    return (size_t)(3 * net.ni + 4 + m + 2 * net.npair) * sizeof(double);
+    return (size_t)(3 * net.ni + 8 + m + 2 * net.npair) * sizeof(double);
 }
 
 void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
