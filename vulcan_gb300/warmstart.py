@@ -449,8 +449,10 @@ def main(argv=None):
         np.savez_compressed(a.data, X=X.astype(np.float32), Y=Y.astype(np.float32), col=cid)
         print(json.dumps({'samples': int(X.shape[0]), 'data': os.path.abspath(a.data)}))
     else:
-        d = np.load(a.data)
-        X, Y, cid = d['X'].astype(np.float64), d['Y'].astype(np.float64), d['col']
+        parts = [np.load(f) for f in a.data.split(',')]      # several generate outputs
+        X = np.concatenate([d['X'] for d in parts]).astype(np.float64)
+        Y = np.concatenate([d['Y'] for d in parts]).astype(np.float64)
+        cid = np.concatenate([d['col'] for d in parts])
         cols = np.unique(cid)
         val = np.isin(cid, cols[::10])               # every tenth column held out
         m = MLP(X.shape[1], Y.shape[1], width=a.width, depth=a.depth)
