@@ -518,7 +518,8 @@ def run_profile(args):
 
 
 def run_reference(args):
-    res = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
+    # one bounded sample: cpu_cols columns x the run's timed steps, all host cores
+    res = cpu_baseline(args.cpu_cols, max(args.cpu_steps, args.steps), args.cpu_workers)
     out = {'metric': METRIC, 'value': round(res['value'], 3), 'unit': UNIT, 'n_gpus': args.gpus,
            'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
