@@ -183,6 +183,25 @@ VK_API int  vk_get_conv(vk_handle *h, double *longdy, double *longdydt);
 VK_API int  vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double *ms_solve,
                    double *ms_stage, int *launches);
 
+/* ---- rate constants on the device ----
+ * Replaces the host's op.ReadRate.read_rate / rev_rate (op.py:63-309) for
+ * batches whose temperature varies by column.  Per reaction pair: kind
+ * (VK_K_*), rev = 1 when the reverse rate is k_f / Keq (pairs before
+ * '# reverse stops'), params = A B C A_inf B_inf C_inf; nasa9 [ni][20] with
+ * the T < 1000 K range first (chem_funs gibbs_sp).  vk_compute_k fills the
+ * device k of every layer from the atmosphere's TCO and M; forward slots of
+ * VK_K_NONE pairs (photolysis, ionisation, condensation) keep the uploaded
+ * values (frozen J). */
+#define VK_K_NONE           0
+#define VK_K_ARRHENIUS      1
+#define VK_K_FALLOFF        2
+#define VK_K_SPECIAL_OH_CH3 3
+VK_API int  vk_set_rate_params(vk_handle *h, const int *kind, const int *rev, const double *params,
+                               const double *nasa9);
+VK_API int  vk_compute_k(vk_handle *h);
+/* Diagnostic: the device rate constants [L][nr] back to the host. */
+VK_API int  vk_get_k(vk_handle *h, double *k);
+
 /* ---- learned warm start: BF16 MLP kernels ----
  * No counterpart in the reference (its initial state comes from ini_mix,
  * build_atm.py:141-279).  Device pointers owned by the caller; BF16 weights

@@ -1,0 +1,55 @@
+"""Rate constants on the device (vk_compute_k) against the host restatement
+of the reference's read_rate / rev_rate (network.Network.rate_constants)."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, network
+from vulcan_gb300 import batch, configs, synthnet
+from vulcan_gb300.network import Network
+
+pytestmark = pytest.mark.gpu
+ATOMS = ['H', 'O', 'C', 'He', 'N']
+
+
+@pytest.fixture(scope='module', autouse=True)
+def built():
+    from vulcan_gb300 import _build
+    _build.build()
+
+
+def _check(net, specs, atoms):
+    items = batch.build_items(specs, net)
+    h, b = batch.make_batch_handle(net, items, atoms)
+    host = np.concatenate([it['k'].T for it in items])           # [L, nr]
+    h.set_rate_params(net)
+    h.compute_k()
+    dev = h.k()
+    h.close()
+    # exp / pow / log of two math libraries: a few ulp, more where exp's
+    # argument is large (reverse rates through Keq = exp(-dg))
+    np.testing.assert_allclose(dev, host, rtol=2e-12, atol=1e-290)
+    return items, dev
+
+
+def test_thermo_network_columns_of_different_temperature():
+    net = network('c2')
+    _check(net, configs.config2_columns(ncols=6, seed=5, nz_range=(30, 60)), ATOMS)
+
+
+def test_special_and_photo_slots():
+    """NCHO photo network: the OH + CH3 + M pressure-dependent form, and the
+    photolysis forward slots keep the uploaded frozen J."""
+    net = Network.from_npz(os.path.join(GOLDEN, 'net_NCHO_photo.npz'))
+    spec = configs.config1(sorted(net.photo_index()), nz=40)
+    items, dev = _check(net, [spec], ATOMS)
+    pidx = net.photo_index()
+    for key, J in spec.photo_J.items():
+        np.testing.assert_array_equal(dev[:, pidx[key] - 1], J)
+
+
+def test_synthetic_150_species():
+    d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), '_build', 'tests', 'syn150')
+    net = Network.from_file(synthnet.generate(d), use_photo=True)
+    _check(net, configs.config4_columns(sorted(net.photo_index()), ncols=2, nz=40), ATOMS)

@@ -34,7 +34,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
-           'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv')
+           'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
+           'vk_compute_k', 'vk_get_k')
 
 
 class VkNetworkDesc(C.Structure):
@@ -100,6 +101,9 @@ def lib(path=None):
         'vk_set_clock': (i, [vp, pd, pd, pi]),
         'vk_get_counters': (i, [vp, pi]),
         'vk_get_conv': (i, [vp, pd, pd]),
+        'vk_set_rate_params': (i, [vp, pi, pi, pd, pd]),
+        'vk_compute_k': (i, [vp]),
+        'vk_get_k': (i, [vp, pd]),
         'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
         'vk_chem_source': (i, [vp, pd, pd]),
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),

@@ -44,6 +44,8 @@ struct vk_handle {
     // batch
     int *d_col_off = nullptr, *d_lay_col = nullptr;
     int *d_order = nullptr;             // columns by decreasing nz
+    int *d_kkind = nullptr, *d_krev = nullptr;   // rate-constant parameters (vk_set_rate_params)
+    double *d_kpar = nullptr, *d_nasa9 = nullptr;
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
     int nsm = 0;                        // SMs of the device
     int cps = 0;                        // VK_CTAS_PER_SM override (0: kernel defaults)
@@ -548,6 +550,49 @@ extern "C" int vk_get_counters(vk_handle *h, int *counters) {
     if (rc) return rc;
     if (!counters) return fail(h, VK_EINVAL, "counters is NULL");
     VK_CUDA(h, cudaMemcpy(counters, h->rs.counters, (size_t)h->ncols * VK_NCOUNTERS * sizeof(int), cudaMemcpyDeviceToHost));
+    return VK_OK;
+}
+
+extern "C" int vk_set_rate_params(vk_handle *h, const int *kind, const int *rev, const double *params,
+                                  const double *nasa9) {
+    if (!h) return fail(h, VK_EINVAL, "handle is NULL");
+    if (!kind || !rev || !params || !nasa9) return fail(h, VK_EINVAL, "rate parameter array is NULL");
+    for (int p = 0; p < h->npair; ++p)
+        if (kind[p] < VK_K_NONE || kind[p] > VK_K_SPECIAL_OH_CH3)
+            return fail(h, VK_EINVAL, "unknown rate kind for pair " + std::to_string(p));
+    if (!h->d_kkind) {
+        int rc = dalloc(h, &h->d_kkind, h->npair);
+        if (!rc) rc = dalloc(h, &h->d_krev, h->npair);
+        if (!rc) rc = dalloc(h, &h->d_kpar, (size_t)h->npair * 6);
+        if (!rc) rc = dalloc(h, &h->d_nasa9, (size_t)h->ni * 20);
+        if (rc) {                          // the handle frees what was allocated
+            h->d_kkind = nullptr;
+            return rc;
+        }
+    }
+    VK_CUDA(h, cudaMemcpy(h->d_kkind, kind, h->npair * sizeof(int), cudaMemcpyHostToDevice));
+    VK_CUDA(h, cudaMemcpy(h->d_krev, rev, h->npair * sizeof(int), cudaMemcpyHostToDevice));
+    VK_CUDA(h, cudaMemcpy(h->d_kpar, params, (size_t)h->npair * 6 * sizeof(double), cudaMemcpyHostToDevice));
+    VK_CUDA(h, cudaMemcpy(h->d_nasa9, nasa9, (size_t)h->ni * 20 * sizeof(double), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" int vk_compute_k(vk_handle *h) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!h->d_kkind) return fail(h, VK_EINVAL, "no rate parameters (call vk_set_rate_params)");
+    vk::launch_rate_consts(h->net(), h->batch(), h->d_kkind, h->d_krev, h->d_kpar, h->d_nasa9,
+                           h->d_k, h->stream);
+    VK_CUDA(h, cudaGetLastError());
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
+extern "C" int vk_get_k(vk_handle *h, double *k) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!k) return fail(h, VK_EINVAL, "k is NULL");
+    VK_CUDA(h, cudaMemcpy(k, h->d_k, (size_t)h->L * h->nr * sizeof(double), cudaMemcpyDeviceToHost));
     return VK_OK;
 }
 

@@ -9,6 +9,7 @@
 #include "../../include/vk_ros2.h"
 
 #define VK_MAXF 4              // distinct species on one side of a reaction
+#define VK_CORR (1.38064852E-16 / 1.0e6)   // k_B / P0 (1 bar), the reference's gibbs corr
 #define VK_MAX_NI 160          // largest species count a diagonal block may have
 #define VK_MAX_NATOM 16
 
@@ -162,6 +163,8 @@ void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags
 void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,
                    double *x, const double *yscale, double *yk2, int max_sweeps, double tol,
                    cudaStream_t s);
+void launch_rate_consts(const DevNet &net, const DevBatch &b, const int *kind, const int *rev,
+                        const double *params, const double *nasa9, double *k, cudaStream_t s);
 void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
 void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);

@@ -366,6 +366,27 @@ class Network:
             elif r.text == 'H + C2H5 + M -> C2H6 + M':
                 k[2 * p][Tco <= 200] = 2.49E-27
 
+    def rate_params(self):
+        """Per-pair tables for vk_set_rate_params: (kind, rev, params [npair, 6],
+        nasa9 [ni, 20]); kind 1 Arrhenius (two-body, k0-only three-body), 2
+        fall-off, 3 the OH + CH3 + M form, 0 photolysis / ionisation /
+        condensation (forward slot as uploaded); rev = 1 where the reverse rate
+        is k_f / Keq (before '# reverse stops', not condensation)."""
+        codes = {'arrhenius': 1, 'k0': 1, 'falloff': 2}
+        kind = np.zeros(self.npair, dtype=np.int32)
+        rev = np.zeros(self.npair, dtype=np.int32)
+        params = np.zeros((self.npair, 6))
+        for p, r in enumerate(self.reactions):
+            if r.kind == 'special':
+                if r.text != SPECIAL_OH_CH3:
+                    raise ValueError('no rate form for special reaction ' + r.text)
+                kind[p] = 3
+            else:
+                kind[p] = codes.get(r.kind, 0)
+            rev[p] = int(r.index + 1 < self.stop_rev_indx and r.kind != 'conden')
+            params[p] = (r.A, r.B, r.C, r.A_inf, r.B_inf, r.C_inf)
+        return kind, rev, params, np.ascontiguousarray(self.nasa9, dtype=np.float64)
+
     def photo_index(self):
         """{(species, branch): forward k index} for photolysis reactions."""
         return {(r.photo_sp, r.photo_br): r.index for r in self.reactions

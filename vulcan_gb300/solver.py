@@ -266,6 +266,22 @@ class Ros2Handle:
                                  ptr(out['end_case'], C.c_int), ptr(out['delta'])), self.h)
         return out
 
+    def set_rate_params(self, net):
+        """Upload the network's rate parameters for compute_k (Network.rate_params)."""
+        kind, rev, params, nasa9 = net.rate_params()
+        check(lib().vk_set_rate_params(self.h, ptr(kind, C.c_int), ptr(rev, C.c_int),
+                                       ptr(np.ascontiguousarray(params)), ptr(nasa9)), self.h)
+
+    def compute_k(self):
+        """Rate constants of every layer from its temperature and M, on the device."""
+        check(lib().vk_compute_k(self.h), self.h)
+
+    def k(self):
+        """Device rate constants, [L, nr]."""
+        out = np.empty((self.batch.L, self.gnet.net.nr))
+        check(lib().vk_get_k(self.h, ptr(out)), self.h)
+        return out
+
     def conv_stats(self):
         """(longdy, longdydt) of each column's last steady-state test."""
         b = self.batch
