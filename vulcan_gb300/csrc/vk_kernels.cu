@@ -23,7 +23,6 @@
 #include "vk_internal.cuh"
 #include "vk_geo.cuh"
 #include "vk_gj.cuh"
-#include "vk_gjreg.cuh"
 
 namespace vk {
 
@@ -207,13 +206,11 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
 // (c) block-Thomas factorisation + forward sweep, FP64, one column at a time
 // per CTA (work queue).  The diagonal block
 //   D'_j = c0 I - J_j - diag(dA_j) - diag(dC_j) G_{j-1} diag(dB_{j-1})
-// is built in shared memory and inverted by Gauss-Jordan elimination with
-// partial pivoting (largest |a|, lowest row on ties): RA = 0 in shared memory
-// (any ni), RA = 3 / 5 with the block held in registers (16 x 16 threads,
-// ni <= 48 / 80; vk_gjreg.cuh, one barrier per pivot).  Both give the same
-// pivots and the same FMA per element.
-template <int RA>
-__global__ void __launch_bounds__(256, RA > 0 ? 2 : 1)
+// is built and inverted in place in shared memory by Gauss-Jordan elimination
+// with partial pivoting (largest |a|, lowest row on ties).  (A variant with the
+// block in registers, as the FP32 path has, measured 92.9 ms against 76.4 ms
+// per attempt at 512 columns: FP64 throughput, not barriers, bounds this one.)
+__global__ void __launch_bounds__(256)
 k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
              const double *__restrict__ dB, const double *__restrict__ dC,
              const double *__restrict__ dt, const double *__restrict__ rhs,
@@ -226,9 +223,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
     double *zp = rowk + n;
     double *bb = zp + n;
     int *perm = reinterpret_cast<int *>(bb + n);
-    int *kinv = perm + n;
-    int *used = kinv + n;
-    __shared__ int s_piv, s_sing, s_col, s_piv2[2];
+    __shared__ int s_piv, s_sing, s_col;
     __shared__ double s_pval;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
@@ -254,24 +249,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
             const double *jl = jv + l * net.nnz;
             for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
             __syncthreads();
-            if constexpr (RA == 0) {
-                gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
-            } else {
-                const int ty = tid & 15, tx = tid >> 4;
-                double M[RA][RA];
-#pragma unroll
-                for (int a = 0; a < RA; ++a)
-#pragma unroll
-                    for (int q = 0; q < RA; ++q) {
-                        const int r = ty + 16 * a, cc = tx + 16 * q;
-                        M[a][q] = (r < n && cc < n) ? A[r * n + cc] : 0.0;
-                    }
-                for (int t = tid; t < n; t += nth) used[t] = 0;
-                __syncthreads();
-                GJShared<double> sh{rowk, colk, perm, kinv, used, &s_piv, &s_pval, &s_sing};
-                gj_invert_reg1<double, 16, RA, RA>(M, n, ty, tx, sh, colk, s_piv2);
-                gj_store_natural<double, 16, RA, RA>(M, n, ty, tx, sh, A);
-            }
+            gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
             double *Gl = G + l * nn;
             for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
             for (int r = warp; r < n; r += nwarp) {
@@ -450,10 +428,8 @@ void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flag
 
 // ---------------------------------------------------------------------------
 static size_t rates_smem(const DevNet &net);
-// block, colk, rowk, zp, bb (doubles) + perm, kinv, used (ints)
-static size_t lu_fwd_smem(int n) { return (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)3 * n * sizeof(int); }
-// register tiling of the FP64 Gauss-Jordan: 3 or 5 rows/columns per thread, 0 = shared memory
-static int lu_fwd_ra(int n) { return n <= 48 ? 3 : (n <= 80 ? 5 : 0); }
+// block, colk, rowk, zp, bb (doubles) + perm (ints)
+static size_t lu_fwd_smem(int n) { return (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int); }
 
 // Opt the kernels into the dynamic shared memory this network needs; called
 // once per handle, outside any stream capture.
@@ -464,9 +440,7 @@ cudaError_t init_kernels(const DevNet &net) {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_rates<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
     if ((e = cudaFuncSetAttribute(k_rates<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
-    if ((e = cudaFuncSetAttribute(k_lu_fwd_f64<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
-    if ((e = cudaFuncSetAttribute(k_lu_fwd_f64<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
-    if ((e = cudaFuncSetAttribute(k_lu_fwd_f64<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
+    if ((e = cudaFuncSetAttribute(k_lu_fwd_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
     return cudaSuccess;
 }
 
@@ -498,12 +472,8 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
     const int n = net.ni;
     size_t sm = lu_fwd_smem(n);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    const int g = column_grid(b, 2);
-    switch (lu_fwd_ra(n)) {
-    case 3: k_lu_fwd_f64<3><<<g, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    case 5: k_lu_fwd_f64<5><<<g, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    default: k_lu_fwd_f64<0><<<g, 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z, w.status); break;
-    }
+    k_lu_fwd_f64<<<column_grid(b, 2), 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
+                                                    w.status);
 }
 
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
