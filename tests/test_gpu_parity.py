@@ -239,7 +239,14 @@ def test_run_watchdog_returns_timeout():
     assert np.isfinite(st['y']).all()
 
 
-def _run_to_steady(tag, precision, **cfg):
+def g_count_max(tag, budget=12000):
+    """count_max the reference ran with (the fixture generator's step budget
+    minus one; a run that hit it ended at count_max + 1)."""
+    g = golden(tag)
+    return budget - 1 if g['end_case'] == 1 else g['final_count'] - 1
+
+
+def _run_to_steady(tag, precision, count_max=20000, **cfg):
     from vulcan_gb300 import configs
     from vulcan_gb300.solver import ctrl_from
     g, net, gn, h, b = make_handle(tag, precision=precision)
@@ -251,8 +258,8 @@ def _run_to_steady(tag, precision, **cfg):
     h.set_conv_ignore(mask)
     h.set_clock(dt=1e-10, t=0.0, count=0)
     ctrl = ctrl_from(cfg, gs=configs.GS, Rp=configs.RP)
-    ctrl.count_max = 20000
-    h.run(ctrl, max_steps=20000, timeout_s=900)
+    ctrl.count_max = count_max
+    h.run(ctrl, max_steps=count_max + 10, timeout_s=900)
     return g, h.state()
 
 
@@ -279,7 +286,14 @@ def test_device_run_reaches_reference_steady_state(precision):
     from conftest import GOLDEN
     if not os.path.exists(os.path.join(GOLDEN, 'golden_c2tight.npz')):
         pytest.skip('golden_c2tight.npz not recorded')
-    g, st = _run_to_steady('c2tight', precision, yconv_cri=1e-3, yconv_min=1e-3)
+    g, st = _run_to_steady('c2tight', precision, yconv_cri=1e-3, yconv_min=1e-3,
+                           count_max=int(g_count_max('c2tight')))
+    if g['end_case'] != 1:
+        # the reference did not meet the tight criterion within its step budget:
+        # neither may the device run, and both must have run to that budget
+        assert st['end_case'][0] == g['end_case']
+        assert st['count'][0] == g['final_count']
+        return
     assert st['end_case'][0] == 1
     ref = g['final_ymix']
     sel = ref > 1e-20
