@@ -167,8 +167,9 @@ VK_API int  vk_get_state(vk_handle *h, double *y, double *ymix, double *dt, doub
 VK_API int  vk_set_clock(vk_handle *h, const double *dt, const double *t, const int *count);
 
 /* Cumulative counters per column: [ncols][VK_NCOUNTERS] = attempts, delta
- * rejections, negativity rejections, loss rejections, attempts redone in FP64
- * because mixed-precision refinement did not converge, accepted steps. */
+ * rejections, negativity rejections, loss rejections, attempts solved in FP64
+ * on a mixed-precision handle (routed there because refinement had failed at
+ * that step size, or redone after it failed), accepted steps. */
 #define VK_NCOUNTERS 6
 VK_API int  vk_get_counters(vk_handle *h, int *counters);
 /* Diagnostic: longdy and longdydt of each column's last steady-state test
