@@ -156,6 +156,47 @@ __device__ __forceinline__ void gj_store_natural(const T (&M)[RA][RB], int n, in
 
 namespace vk {
 
+// Column kb / row pa of the register tile for a CTA-uniform runtime index:
+// a switch on the index (one uniform branch) instead of a select per element.
+#define VK_TILE_CASE(B, BODY) \
+    case B:                   \
+        if constexpr (B < LIM) { BODY(B); } \
+        break;
+#define VK_TILE_SWITCH(IDX, BODY)                                                     \
+    switch (IDX) {                                                                    \
+        VK_TILE_CASE(0, BODY) VK_TILE_CASE(1, BODY) VK_TILE_CASE(2, BODY)             \
+        VK_TILE_CASE(3, BODY) VK_TILE_CASE(4, BODY) VK_TILE_CASE(5, BODY)             \
+        VK_TILE_CASE(6, BODY) VK_TILE_CASE(7, BODY) VK_TILE_CASE(8, BODY)             \
+        VK_TILE_CASE(9, BODY)                                                         \
+    default: break;                                                                   \
+    }
+
+template <typename T, int RA, int RB>
+__device__ __forceinline__ void tile_get_col(const T (&M)[RA][RB], int kb, T (&out)[RA]) {
+    constexpr int LIM = RB;
+    static_assert(RB <= 10, "tile switch covers 10 columns");
+#define VK_BODY(B) _Pragma("unroll") for (int a = 0; a < RA; ++a) out[a] = M[a][B]
+    VK_TILE_SWITCH(kb, VK_BODY)
+#undef VK_BODY
+}
+
+template <typename T, int RA, int RB>
+__device__ __forceinline__ void tile_set_col(T (&M)[RA][RB], int kb, const T (&v)[RA]) {
+    constexpr int LIM = RB;
+#define VK_BODY(B) _Pragma("unroll") for (int a = 0; a < RA; ++a) M[a][B] = v[a]
+    VK_TILE_SWITCH(kb, VK_BODY)
+#undef VK_BODY
+}
+
+template <typename T, int RA, int RB>
+__device__ __forceinline__ void tile_get_row(const T (&M)[RA][RB], int pa, T (&out)[RB]) {
+    constexpr int LIM = RA;
+    static_assert(RA <= 10, "tile switch covers 10 rows");
+#define VK_BODY(A) _Pragma("unroll") for (int b = 0; b < RB; ++b) out[b] = M[A][b]
+    VK_TILE_SWITCH(pa, VK_BODY)
+#undef VK_BODY
+}
+
 // gj_invert_reg with one block barrier per pivot step.  The pivot row reaches
 // the threads of each column group by warp shuffles (the TY owners of a column
 // are consecutive lanes, so every thread finds row p of its own columns at lane
@@ -177,12 +218,14 @@ __device__ __forceinline__ void gj_invert_reg1(T (&M)[RA][RB], int n, int ty, in
     // the column group; lane ty == 0 records it (all owners know bi after)
     auto search = [&](int k) {
         const int kb = k >> 4;
+        T colk[RA];
+        tile_get_col(M, kb, colk);
         T best = T(-1);
         int bi = n;
 #pragma unroll
         for (int a = 0; a < RA; ++a) {
             if (rr[a] < n && !sh.used[rr[a]]) {
-                T v = gj_abs(pick_col(M[a], kb));
+                T v = gj_abs(colk[a]);
                 if (v > best) { best = v; bi = rr[a]; }
             }
         }
@@ -209,7 +252,7 @@ __device__ __forceinline__ void gj_invert_reg1(T (&M)[RA][RB], int n, int ty, in
         T *cv = colv2 + (k & 1) * n;
 #pragma unroll
         for (int a = 0; a < RA; ++a)
-            if (rr[a] < n) cv[rr[a]] = pick_col(M[a], kb);
+            if (rr[a] < n) cv[rr[a]] = colk[a];
     };
     if (tx == 0) search(0);
     for (int k = 0; k < n; ++k) {
@@ -221,14 +264,11 @@ __device__ __forceinline__ void gj_invert_reg1(T (&M)[RA][RB], int n, int ty, in
         // pivot row of this thread's columns from its column group (lane p % TY)
         const int pa = p / TY, pl = p - pa * TY;
         T rp[RB];
+        tile_get_row(M, pa, rp);
 #pragma unroll
         for (int b = 0; b < RB; ++b) {
-            T mine = T(0);
-#pragma unroll
-            for (int a = 0; a < RA; ++a)
-                if (a == pa) mine = M[a][b];
             // every lane runs this: full mask, segments of TY lanes
-            const T v = __shfl_sync(0xffffffffu, mine, pl, TY);
+            const T v = __shfl_sync(0xffffffffu, rp[b], pl, TY);
             rp[b] = cc[b] < n ? v * pinv : T(0);
         }
         T fr[RA];
@@ -244,13 +284,10 @@ __device__ __forceinline__ void gj_invert_reg1(T (&M)[RA][RB], int n, int ty, in
             }
         }
         if (tx == kx) {
+            T pc[RA];
 #pragma unroll
-            for (int a = 0; a < RA; ++a) {
-                const T v = rr[a] == p ? pinv : -fr[a] * pinv;
-#pragma unroll
-                for (int b = 0; b < RB; ++b)
-                    if (b == kb) M[a][b] = v;
-            }
+            for (int a = 0; a < RA; ++a) pc[a] = rr[a] == p ? pinv : -fr[a] * pinv;
+            tile_set_col(M, kb, pc);
         }
         // next pivot: its column owners search their updated registers now
         if (k + 1 < n && tx == ((k + 1) & 15)) search(k + 1);
