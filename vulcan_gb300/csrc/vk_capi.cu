@@ -33,6 +33,7 @@ struct vk_handle {
     // network tables
     PairDesc *d_pairs = nullptr;
     int *d_src_ptr = nullptr;
+    int *d_src_order = nullptr;
     int2 *d_src = nullptr;
     double *d_src_nu = nullptr, *d_jterm_nu = nullptr;
     WDesc *d_w = nullptr;
@@ -68,6 +69,7 @@ struct vk_handle {
         DevNet n;
         n.ni = ni; n.npair = npair; n.nr = nr; n.nw = nw; n.nnz = nnz; n.natom = natom;
         n.pairs = d_pairs; n.src_ptr = d_src_ptr; n.src = d_src; n.w = d_w;
+        n.src_order = d_src_order;
         n.src_nu = d_src_nu; n.jterm_nu = d_jterm_nu;
         n.jptr = d_jptr; n.jterm = d_jterm; n.jpos = d_jpos; n.compo = d_compo;
         n.jrow = d_jrow; n.jcol = d_jcol; n.jrowptr = d_jrowptr; n.jmap = d_jmap;
@@ -167,6 +169,17 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     for (auto &e : h->ev) TRY(cudaEventCreate(&e) == cudaSuccess ? VK_OK : fail(h, VK_ECUDA, "cudaEventCreate"));
     TRY(upload(h, &h->d_pairs, net->pairs));
     TRY(upload(h, &h->d_src_ptr, net->src_ptr));
+    {
+        // the source gather runs one thread per species in the reference's
+        // summation order; sorting species by term count gives every warp
+        // chains of similar length (FP64 issue is per warp, idle lanes cost)
+        std::vector<int> order(h->ni);
+        for (int i = 0; i < h->ni; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b2) {
+            return net->src_ptr[a + 1] - net->src_ptr[a] > net->src_ptr[b2 + 1] - net->src_ptr[b2];
+        });
+        TRY(upload(h, &h->d_src_order, order));
+    }
     TRY(upload(h, &h->d_src, net->src));
     TRY(upload(h, &h->d_src_nu, net->src_nu));
     TRY(upload(h, &h->d_jterm_nu, net->jterm_nu));

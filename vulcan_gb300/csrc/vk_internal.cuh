@@ -62,6 +62,7 @@ struct DevNet {
     int ni, npair, nr, nw, nnz, natom;
     const PairDesc *pairs;
     const int *src_ptr;
+    const int *src_order;      // [ni] species by decreasing production/loss term count
     const int2 *src;
     const double *src_nu;
     const WDesc *w;

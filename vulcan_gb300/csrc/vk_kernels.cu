@@ -147,8 +147,10 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     const double hinv = sums[4];
     const double *gl = geo + (size_t)l * GEO_NF * ni;
     const double *spf = b.spf + (size_t)c * VK_SP_NF * ni;
-    // production - loss gather (generated chemdf order) + transport
-    for (int s = tid; s < ni; s += nth) {
+    // production - loss gather (generated chemdf order) + transport; species
+    // in decreasing order of term count so a warp's lanes end together
+    for (int si = tid; si < ni; si += nth) {
+        const int s = net.src_order[si];
         double acc = 0.0;
         for (int e = net.src_ptr[s]; e < net.src_ptr[s + 1]; ++e) {
             const int2 t = net.src[e];
