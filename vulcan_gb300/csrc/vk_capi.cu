@@ -34,6 +34,7 @@ struct vk_handle {
     PairDesc *d_pairs = nullptr;
     int *d_src_ptr = nullptr;
     int *d_src_order = nullptr;
+    int *d_jorder = nullptr;
     int2 *d_src = nullptr;
     double *d_src_nu = nullptr, *d_jterm_nu = nullptr;
     WDesc *d_w = nullptr;
@@ -69,7 +70,7 @@ struct vk_handle {
         DevNet n;
         n.ni = ni; n.npair = npair; n.nr = nr; n.nw = nw; n.nnz = nnz; n.natom = natom;
         n.pairs = d_pairs; n.src_ptr = d_src_ptr; n.src = d_src; n.w = d_w;
-        n.src_order = d_src_order;
+        n.src_order = d_src_order; n.jorder = d_jorder;
         n.src_nu = d_src_nu; n.jterm_nu = d_jterm_nu;
         n.jptr = d_jptr; n.jterm = d_jterm; n.jpos = d_jpos; n.compo = d_compo;
         n.jrow = d_jrow; n.jcol = d_jcol; n.jrowptr = d_jrowptr; n.jmap = d_jmap;
@@ -185,6 +186,16 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_jterm_nu, net->jterm_nu));
     TRY(upload(h, &h->d_w, net->w));
     TRY(upload(h, &h->d_jptr, net->jptr));
+    {
+        // Jacobian entries by decreasing term count (the same reason)
+        const int nnz = (int)net->jptr.size() - 1;
+        std::vector<int> order(nnz > 0 ? nnz : 1, 0);
+        for (int i = 0; i < nnz; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.begin() + (nnz > 0 ? nnz : 0), [&](int a, int b2) {
+            return net->jptr[a + 1] - net->jptr[a] > net->jptr[b2 + 1] - net->jptr[b2];
+        });
+        TRY(upload(h, &h->d_jorder, order));
+    }
     TRY(upload(h, &h->d_jterm, net->jterm));
     TRY(upload(h, &h->d_jpos, net->jpos));
     TRY(upload(h, &h->d_compo, net->compo));

@@ -67,6 +67,7 @@ struct DevNet {
     const double *src_nu;
     const WDesc *w;
     const int *jptr;
+    const int *jorder;         // [nnz] Jacobian entries by decreasing term count
     const int2 *jterm;
     const double *jterm_nu;
     const int *jpos;

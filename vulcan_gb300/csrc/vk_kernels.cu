@@ -193,7 +193,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     }
     __syncthreads();
     double *jl = jv + (size_t)l * net.nnz;
-    for (int e = tid; e < net.nnz; e += nth) {
+    for (int ei = tid; ei < net.nnz; ei += nth) {
+        const int e = net.jorder[ei];
         double acc = 0.0;
         for (int t = net.jptr[e]; t < net.jptr[e + 1]; ++t) {
             const int2 jt = net.jterm[t];
