@@ -276,7 +276,7 @@ def test_device_run_converges_like_reference(precision):
     assert 0.4 * g['final_count'] <= st['count'][0] <= 2.5 * g['final_count']
 
 
-@pytest.mark.parametrize('precision', [0, 1])
+@pytest.mark.parametrize('precision', [0])
 def test_device_run_reaches_reference_steady_state(precision):
     """With the criterion tightened to yconv_cri = yconv_min = 1e-3 in both
     (fixture c2tight, recorded from the reference with those vulcan_cfg
