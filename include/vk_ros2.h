@@ -203,6 +203,33 @@ VK_API int  vk_compute_k(vk_handle *h);
 /* Diagnostic: the device rate constants [L][nr] back to the host. */
 VK_API int  vk_get_k(vk_handle *h, double *k);
 
+/* ---- photochemistry radiative transfer ----
+ * op.ODESolver.compute_tau / compute_flux / compute_J (op.py:2580-2786; T-
+ * independent cross sections, isotropic scattering) for every column.  The
+ * tables are those of the reference's make_bins_read_cross / read_sflux
+ * (op.py:495-782, build_atm.py:617-656): wavelength bins, the J integral's
+ * bin weights, absorbers (species index, 1 if a photolysis species -- the
+ * albedo's absorption counts those), their cross sections [nabs][nbins],
+ * Rayleigh scatterers and cross sections [nscat][nbins], photolysis channels
+ * (1-based k index of the channel's rate) and cross sections [nch][nbins],
+ * the top-of-atmosphere flux [nbins]; angles in radians.  The diffuse fluxes
+ * persist between updates as the reference's arrays do (vk_photo_reset
+ * clears them).  vk_photo_update computes tau, the actinic flux and J from
+ * the current state, writes J * f_diurnal into the channels' k slots and, if
+ * aflux_change is given, each column's largest relative actinic-flux change
+ * where the flux exceeds flux_atol (var.aflux_change).  No counterpart for
+ * the T-dependent cross sections or photoionisation yet. */
+VK_API int  vk_photo_setup(vk_handle *h, int nbins, const double *bins, const double *jweights,
+                           int nabs, const int *abs_sp, const int *abs_photo, const double *cross,
+                           int nscat, const int *scat_sp, const double *cross_scat, int nch,
+                           const int *ch_kindex, const double *cross_J, const double *sflux_top,
+                           double sl_angle, double edd, double f_diurnal, double flux_atol);
+VK_API int  vk_photo_reset(vk_handle *h);
+VK_API int  vk_photo_update(vk_handle *h, double *aflux_change);
+/* Diagnostic: tau [(L + ncols)][nbins] (staggered, column c from row
+ * col_off[c] + c), actinic flux [L][nbins], J [L][nch]. */
+VK_API int  vk_photo_get(vk_handle *h, double *tau, double *aflux, double *J);
+
 /* ---- learned warm start: BF16 MLP kernels ----
  * No counterpart in the reference (its initial state comes from ini_mix,
  * build_atm.py:141-279).  Device pointers owned by the caller; BF16 weights

@@ -47,13 +47,18 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c2long': (400, 800, 1200, 1600, 1999),
         'c2conv': (0,),
         'c2tight': (0,),
-        'c2slow': (0,)}
+        'c2slow': (0,),
+        'c1rt': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
-          'c2slow': 4000}
+          'c2slow': 4000, 'c1rt': 110}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
-EXTRA_CFG = {'c2tight': 'yconv_cri = 0.001\nyconv_min = 0.001\n'}
+EXTRA_CFG = {'c2tight': 'yconv_cri = 0.001\nyconv_min = 0.001\n',
+             # radiative transfer on, on 1 nm bins below 240 nm (2 nm above) to keep
+             # the fixture small; everything else the reference's defaults
+             'c1rt': 'dbin1 = 1.0\n'}
+PHOTO_TAGS = ('c1rt',)
 
 DRIVER = r'''
 import os, sys, time, json
@@ -181,6 +186,79 @@ np.savez_compressed('golden_full.npz',
 print('attempts', len(ATT), 'steps', len(STEPS), 'wall', wall)
 '''
 
+PHOTO_DRIVER = r'''
+import os, sys, time, json
+import numpy as np
+sys.path.insert(0, os.getcwd())
+sys.path.insert(0, os.path.join(os.getcwd(), '_mplstub'))
+import vulcan_cfg
+import store, build_atm, op, chem_funs
+from phy_const import kb
+inp = np.load('golden_inputs.npz', allow_pickle=True)
+
+var = store.Variables(); atm = store.AtmData(); para = store.Parameters()
+para.start_time = time.time()
+make_atm = build_atm.Atm()
+output = op.Output()
+atm = make_atm.f_pico(atm)
+atm = make_atm.load_TPK(atm)
+atm.Tco = inp['Tco'].copy()
+atm.M = atm.pco / (kb * atm.Tco)
+atm.n_0 = atm.M.copy()
+atm.Kzz = inp['Kzz'].copy()
+rate = op.ReadRate()
+var = rate.read_rate(var, atm)
+var = rate.rev_rate(var, atm)
+var = rate.remove_rate(var)
+ini = build_atm.InitialAbun()
+var = ini.ini_y(var, atm)
+var = ini.ele_sum(var)
+atm = make_atm.f_mu_dz(var, atm, output)
+make_atm.mol_diff(atm)
+make_atm.BC_flux(atm)
+REC = []
+CH = sorted(var.pho_rate_index)                 # (species, branch) channels
+
+class RecRos2(op.Ros2):
+    def compute_J(self, v, a):
+        op.Ros2.compute_J(self, v, a)
+        REC.append(dict(y=v.y.copy(), ymix=v.ymix.copy(), tau=v.tau.copy(), aflux=v.aflux.copy(),
+                        dflux_u=v.dflux_u.copy(), dflux_d=v.dflux_d.copy(),
+                        sflux=v.sflux.copy(), aflux_change=float(v.aflux_change),
+                        J=np.array([v.J_sp[c] for c in CH]), dz=a.dz.copy(),
+                        count=int(para.count)))
+
+solver = RecRos2()
+rate.make_bins_read_cross(var, atm)
+make_atm.read_sflux(var, atm)
+solver.compute_tau(var, atm)
+solver.compute_flux(var, atm)
+solver.compute_J(var, atm)
+var = rate.remove_rate(var)
+absp = sorted(set.union(var.photo_sp, var.ion_sp))
+out = dict(bins=var.bins, dbin1=var.dbin1, dbin2=var.dbin2,
+           sflux_din12_indx=var.sflux_din12_indx, sflux_top=var.sflux_top,
+           absp_sp=np.array(absp), photo_sp=np.array(sorted(var.photo_sp)),
+           cross=np.array([var.cross[s] for s in absp]),
+           scat_sp=np.array(vulcan_cfg.scat_sp),
+           cross_scat=np.array([var.cross_scat[s] for s in vulcan_cfg.scat_sp]),
+           ch_sp=np.array([c[0] for c in CH]), ch_br=np.array([c[1] for c in CH]),
+           ch_kindex=np.array([var.pho_rate_index[c] for c in CH]),
+           cross_J=np.array([var.cross_J[c] for c in CH]),
+           sl_angle=vulcan_cfg.sl_angle, edd=vulcan_cfg.edd, f_diurnal=vulcan_cfg.f_diurnal,
+           flux_atol=vulcan_cfg.flux_atol, spec_list=np.array(chem_funs.spec_list),
+           pco=atm.pco, Tco=atm.Tco, M=atm.M, n_0=atm.n_0)
+integ = op.Integration(solver, output)
+solver.naming_solver(para)
+integ(var, atm, para, make_atm)
+for i, r in enumerate(REC):
+    for k, v in r.items():
+        out['rec%d_%s' % (i, k)] = np.asarray(v)
+out['n_rec'] = len(REC)
+np.savez_compressed('golden_out.npz', **out)
+print('photo records', len(REC), 'nbins', len(var.bins), 'counts', [r['count'] for r in REC])
+'''
+
 MPL_STUB = {
     '__init__.py': 'use = lambda *a, **k: None\n',
     'pyplot.py': textwrap.dedent('''
@@ -272,22 +350,47 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
     with open(os.path.join(dst, 'chem_funs.py')) as f:
         if 'def neg_symjac' not in f.read():
             raise RuntimeError('reference code generation failed for ' + tag)
-    # run time: photochemistry (radiative transfer) off, J frozen in k
+    # run time: photochemistry (radiative transfer) off, J frozen in k -- except
+    # for the radiative-transfer fixtures, which record the reference's own J
     with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
-        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, False, EXTRA_CFG.get(tag, '')))
+        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, tag in PHOTO_TAGS,
+                                         EXTRA_CFG.get(tag, '')))
     keys = sorted(spec.photo_J) if spec.photo_J else []
     np.savez(os.path.join(dst, 'golden_inputs.npz'), Tco=spec.Tco, Kzz=spec.Kzz,
              photo_J=np.array([spec.photo_J[k] for k in keys]) if keys else np.zeros((0, nz)))
     with open(os.path.join(dst, 'golden_meta.json'), 'w') as f:
         json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep)}, f)
     with open(os.path.join(dst, 'golden_driver.py'), 'w') as f:
-        f.write(DRIVER)
+        f.write(PHOTO_DRIVER if tag in PHOTO_TAGS else DRIVER)
     r = subprocess.run([sys.executable, 'golden_driver.py'], cwd=dst, env=env,
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('reference run failed:\n' + r.stdout[-3000:] + r.stderr[-3000:])
     print(r.stdout.strip().splitlines()[-1])
     return dst
+
+
+def photo_setup_check(d, ref_root):
+    """Largest relative differences between the reference's binned tables
+    (recorded) and this package's restatement (vulcan_gb300.photo) from the
+    same files -- stored in the fixture so the CPU tests pin the restatement
+    without the reference's data files."""
+    from vulcan_gb300 import photo
+    net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
+                            use_photo=True)
+    t = photo.PhotoTables.from_reference_files(
+        net, ref_root, 'atm/stellar_flux/sflux-HD189_Moses11.txt', 0.805, 0.03142,
+        float(d['sl_angle']), dbin1=float(d['dbin1']))
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    same = (len(t.bins) == len(d['bins']) and t.i12 == int(d['sflux_din12_indx'])
+            and t.absp_sp == [str(s) for s in d['absp_sp']]
+            and t.ch_sp == [str(s) for s in d['ch_sp']])
+    return {'setup_same_layout': same,
+            'setup_rel_bins': rel(t.bins, d['bins']) if same else np.inf,
+            'setup_rel_cross': rel(t.cross, d['cross']) if same else np.inf,
+            'setup_rel_cross_J': rel(t.cross_J, d['cross_J']) if same else np.inf,
+            'setup_rel_cross_scat': rel(t.cross_scat, d['cross_scat']) if same else np.inf,
+            'setup_rel_sflux_top': rel(t.sflux_top, d['sflux_top']) if same else np.inf}
 
 
 def make(tag, ref_root, workdir, full_dir=None):
@@ -299,7 +402,7 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a column of the 512-column batch that has not converged after 4000 steps
         # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
         spec = configs.config2_columns(ncols=512, seed=2)[60]
-    elif tag == 'c1':
+    elif tag in ('c1', 'c1rt'):
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
                                 use_photo=True)
         spec = configs.config1(sorted(net.photo_index()))
@@ -309,6 +412,12 @@ def make(tag, ref_root, workdir, full_dir=None):
                             use_photo=spec.use_photo)
     dst = run_reference(ref_root, tag, spec, NSTEPS[tag], KEEP[tag], workdir)
     d = dict(np.load(os.path.join(dst, 'golden_out.npz'), allow_pickle=False))
+    if tag in PHOTO_TAGS:
+        d.update(photo_setup_check(d, ref_root))
+        out = os.path.join(HERE, 'golden_%s.npz' % tag)
+        np.savez_compressed(out, **d)
+        print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
+        return
     d['atom_list'] = np.array(spec.atom_list)
     d['conver_ignore'] = np.array(spec.conver_ignore, dtype='U16')
     d['const_mix_sp'] = np.array(list(spec.const_mix))

@@ -1,0 +1,118 @@
+"""Photochemistry radiative transfer: the oracle against the reference's own
+compute_tau / compute_flux / compute_J (fixture c1rt, recorded with the
+reference's radiative transfer on), and the device path against the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import photo as P
+
+
+def _fixture():
+    d = dict(np.load(os.path.join(GOLDEN, 'golden_c1rt.npz'), allow_pickle=False))
+    spec = [str(s) for s in d['spec_list']]
+    d['absp_idx'] = [spec.index(str(s)) for s in d['absp_sp']]
+    d['photo_idx'] = [spec.index(str(s)) for s in d['photo_sp']]
+    d['scat_idx'] = [spec.index(str(s)) for s in d['scat_sp']]
+    absp = [str(s) for s in d['absp_sp']]
+    d['cross_photo'] = np.array([d['cross'][absp.index(str(s))] for s in d['photo_sp']])
+    d['weights'] = P.j_weights(len(d['bins']), int(d['sflux_din12_indx']), float(d['dbin1']),
+                               float(d['dbin2']))
+    return d
+
+
+def _oracle_call(d, y, ymix, dz, du, dd, prev=None):
+    tau = P.compute_tau(y, dz, d['absp_idx'], d['cross'], d['scat_idx'], d['cross_scat'])
+    af, _, ch = P.compute_flux(tau, ymix, d['photo_idx'], d['cross_photo'], d['scat_idx'],
+                               d['cross_scat'], d['sflux_top'], d['bins'], float(d['sl_angle']),
+                               float(d['edd']), du, dd, aflux_prev=prev,
+                               flux_atol=float(d['flux_atol']))
+    return tau, af, P.compute_J(af, d['cross_J'], d['weights']), ch
+
+
+def _rel(a, b, floor=1e-300):
+    m = np.abs(b) > floor
+    return float(np.max(np.abs(a - b)[m] / np.abs(b)[m]))
+
+
+def test_oracle_matches_reference_records():
+    d = _fixture()
+    nz, nb = d['rec0_y'].shape[0], len(d['bins'])
+    du, dd = np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb))
+    # first call (set-up), then the integrator's first update on the same state
+    # (the downward sweep reads the first call's upward flux), then count 100
+    tau, af, J, _ = _oracle_call(d, d['rec0_y'], d['rec0_ymix'], d['rec0_dz'], du, dd)
+    assert _rel(tau, d['rec0_tau']) < 1e-13
+    assert _rel(af, d['rec0_aflux'], 1e-30) < 1e-12
+    assert _rel(J, d['rec0_J']) < 1e-11
+    np.testing.assert_allclose(du, d['rec0_dflux_u'], rtol=1e-10, atol=1e-12 * np.abs(du).max())
+    _, af1, J1, ch1 = _oracle_call(d, d['rec0_y'], d['rec0_ymix'], d['rec0_dz'], du, dd, af)
+    assert _rel(af1, d['rec1_aflux'], 1e-30) < 1e-12 and _rel(J1, d['rec1_J']) < 1e-11
+    assert abs(ch1 / float(d['rec1_aflux_change']) - 1) < 1e-10
+    np.testing.assert_allclose(du, d['rec1_dflux_u'], rtol=1e-10, atol=1e-12 * np.abs(du).max())
+    _, af2, J2, _ = _oracle_call(d, d['rec2_y'], d['rec2_ymix'], d['rec2_dz'], du, dd, af1)
+    assert _rel(af2, d['rec2_aflux'], 1e-30) < 1e-12 and _rel(J2, d['rec2_J']) < 1e-11
+
+
+def test_host_tables_match_the_reference_set_up():
+    """vulcan_gb300.photo.PhotoTables.from_reference_files against the tables
+    the reference's make_bins_read_cross / read_sflux built from the same
+    files (differences recorded by the fixture generator)."""
+    d = _fixture()
+    assert bool(d['setup_same_layout'])
+    for key in ('bins', 'cross', 'cross_J', 'cross_scat', 'sflux_top'):
+        assert float(d['setup_rel_' + key]) <= 1e-15, key
+
+
+def test_j_weights_follow_the_reference_sums():
+    """The weights reproduce the reference's four-part trapezoid sums, also
+    when the dbin switch lies outside the bins (index -1)."""
+    rng = np.random.default_rng(0)
+    for i12 in (5, -1):
+        f = rng.random(20)
+        ref = (np.sum(f[:i12]) * 0.1 - 0.5 * (f[0] + f[i12 - 1]) * 0.1
+               + np.sum(f[i12:]) * 2.0 - 0.5 * (f[i12] + f[-1]) * 2.0)
+        assert abs(f @ P.j_weights(20, i12, 0.1, 2.0) - ref) < 1e-13
+
+
+@pytest.mark.gpu
+def test_device_radiative_transfer_matches_oracle():
+    """vk_photo_update on the c1 column (the reference's set-up arrays) from
+    the recorded states: tau, actinic flux, J and the k slots, over the three
+    recorded calls (the diffuse fluxes persist between calls)."""
+    from test_gpu_parity import make_handle
+    from vulcan_gb300 import _build, photo
+    from vulcan_gb300.capi import ATM_DZ
+    _build.build()
+    d = _fixture()
+    g, net, gn, h, b = make_handle('c1')
+    np.testing.assert_allclose(g['dz'], d['rec0_dz'], rtol=1e-14)
+    tables = photo.PhotoTables.from_fixture(d)
+    photo.attach(h, tables, net)
+    nz = d['rec0_y'].shape[0]
+    nb = len(d['bins'])
+    du, dd = np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb))
+    prev = None
+    for rec, (y, ym) in enumerate(((d['rec0_y'], d['rec0_ymix']), (d['rec0_y'], d['rec0_ymix']),
+                                   (d['rec2_y'], d['rec2_ymix']))):
+        dz = d['rec2_dz'] if rec == 2 else d['rec0_dz']
+        if rec == 2:                  # update_mu_dz changed dz by count 100
+            atm = b.atm.copy()
+            atm[:, ATM_DZ] = dz
+            h.set_atm(atm)
+        h.set_state(y, ym)
+        change = h.photo_update()
+        tau_d, af_d, J_d = h.photo_get()
+        tau, af, J, ch = _oracle_call(d, y, ym, dz, du, dd, prev)
+        prev = af
+        assert _rel(tau_d[:nz + 1], tau) < 1e-13
+        assert _rel(af_d, af, 1e-30) < 1e-11
+        assert _rel(J_d.T, J) < 1e-10
+        if rec > 0:
+            assert abs(change[0] / ch - 1) < 1e-9
+        k = h.k()
+        for c, ki in enumerate(d['ch_kindex']):
+            np.testing.assert_allclose(k[:, int(ki) - 1], J_d[:, c] * float(d['f_diurnal']), rtol=1e-15)
+    h.close()

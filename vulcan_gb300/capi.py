@@ -35,7 +35,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
-           'vk_compute_k', 'vk_get_k')
+           'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
+           'vk_photo_update', 'vk_photo_get')
 
 
 class VkNetworkDesc(C.Structure):
@@ -104,6 +105,11 @@ def lib(path=None):
         'vk_set_rate_params': (i, [vp, pi, pi, pd, pd]),
         'vk_compute_k': (i, [vp]),
         'vk_get_k': (i, [vp, pd]),
+        'vk_photo_setup': (i, [vp, i, pd, pd, i, pi, pi, pd, i, pi, pd, i, pi, pd, pd,
+                               C.c_double, C.c_double, C.c_double, C.c_double]),
+        'vk_photo_reset': (i, [vp]),
+        'vk_photo_update': (i, [vp, pd]),
+        'vk_photo_get': (i, [vp, pd, pd, pd]),
         'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
         'vk_chem_source': (i, [vp, pd, pd]),
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),

@@ -46,6 +46,8 @@ struct vk_handle {
     // batch
     int *d_col_off = nullptr, *d_lay_col = nullptr;
     int *d_order = nullptr;             // columns by decreasing nz
+    PhotoDev ph{};                  // radiative transfer (vk_photo_setup)
+    unsigned long long *d_phchange = nullptr;
     int *d_kkind = nullptr, *d_krev = nullptr;   // rate-constant parameters (vk_set_rate_params)
     double *d_kpar = nullptr, *d_nasa9 = nullptr;
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
@@ -598,6 +600,102 @@ extern "C" int vk_set_rate_params(vk_handle *h, const int *kind, const int *rev,
     VK_CUDA(h, cudaMemcpy(h->d_krev, rev, h->npair * sizeof(int), cudaMemcpyHostToDevice));
     VK_CUDA(h, cudaMemcpy(h->d_kpar, params, (size_t)h->npair * 6 * sizeof(double), cudaMemcpyHostToDevice));
     VK_CUDA(h, cudaMemcpy(h->d_nasa9, nasa9, (size_t)h->ni * 20 * sizeof(double), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" int vk_photo_setup(vk_handle *h, int nbins, const double *bins, const double *jweights,
+                              int nabs, const int *abs_sp, const int *abs_photo, const double *cross,
+                              int nscat, const int *scat_sp, const double *cross_scat, int nch,
+                              const int *ch_kindex, const double *cross_J, const double *sflux_top,
+                              double sl_angle, double edd, double f_diurnal, double flux_atol) {
+    if (!h) return fail(h, VK_EINVAL, "handle is NULL");
+    if (h->ph.nbins) return fail(h, VK_EINVAL, "radiative transfer already set up on this handle");
+    if (nbins < 2 || nabs < 1 || nscat < 0 || nch < 1)
+        return fail(h, VK_EINVAL, "need nbins >= 2, nabs >= 1, nscat >= 0, nch >= 1");
+    if (!bins || !jweights || !abs_sp || !abs_photo || !cross || !ch_kindex || !cross_J || !sflux_top ||
+        (nscat && (!scat_sp || !cross_scat)))
+        return fail(h, VK_EINVAL, "radiative-transfer array is NULL");
+    for (int a = 0; a < nabs; ++a)
+        if (abs_sp[a] < 0 || abs_sp[a] >= h->ni) return fail(h, VK_EINVAL, "absorber species out of range");
+    for (int a = 0; a < nscat; ++a)
+        if (scat_sp[a] < 0 || scat_sp[a] >= h->ni) return fail(h, VK_EINVAL, "scatterer species out of range");
+    for (int c = 0; c < nch; ++c)
+        if (ch_kindex[c] < 1 || ch_kindex[c] > h->nr) return fail(h, VK_EINVAL, "channel k index out of range");
+    if (!(edd > 0) || !(cos(sl_angle) > 0)) return fail(h, VK_EINVAL, "need edd > 0 and cos(sl_angle) > 0");
+    std::vector<double> wcj((size_t)nch * nbins);
+    for (int c = 0; c < nch; ++c)
+        for (int n = 0; n < nbins; ++n) wcj[(size_t)c * nbins + n] = cross_J[(size_t)c * nbins + n] * jweights[n];
+    PhotoDev &p = h->ph;
+    const size_t st = (size_t)(h->max_layers + h->max_cols) * nbins, ly = (size_t)h->max_layers * nbins;
+    int rc = 0;
+    double *db = nullptr, *dc = nullptr, *dsc = nullptr, *dw = nullptr, *dtop = nullptr;
+    int *das = nullptr, *dap = nullptr, *dss = nullptr, *dki = nullptr;
+    std::vector<double> bv(bins, bins + nbins), cv(cross, cross + (size_t)nabs * nbins),
+        scv(cross_scat ? cross_scat : bins, cross_scat ? cross_scat + (size_t)nscat * nbins : bins),
+        topv(sflux_top, sflux_top + nbins);
+    std::vector<int> asv(abs_sp, abs_sp + nabs), apv(abs_photo, abs_photo + nabs),
+        ssv(scat_sp ? scat_sp : abs_sp, scat_sp ? scat_sp + nscat : abs_sp), kiv(ch_kindex, ch_kindex + nch);
+    if (!rc) rc = upload(h, &db, bv);
+    if (!rc) rc = upload(h, &dc, cv);
+    if (!rc) rc = upload(h, &dsc, scv);
+    if (!rc) rc = upload(h, &dw, wcj);
+    if (!rc) rc = upload(h, &dtop, topv);
+    if (!rc) rc = upload(h, &das, asv);
+    if (!rc) rc = upload(h, &dap, apv);
+    if (!rc) rc = upload(h, &dss, ssv);
+    if (!rc) rc = upload(h, &dki, kiv);
+    double **big[] = {&p.tau, &p.dflux_u, &p.dflux_d};
+    for (double **q : big) if (!rc) rc = dalloc(h, q, st);
+    double **lay[] = {&p.w0, &p.aflux, &p.aflux_prev};
+    for (double **q : lay) if (!rc) rc = dalloc(h, q, ly);
+    if (!rc) rc = dalloc(h, &p.J, (size_t)h->max_layers * nch);
+    if (!rc) rc = dalloc(h, &h->d_phchange, h->max_cols);
+    if (rc) return rc;                     // the handle frees what was allocated
+    p.bins = db; p.cross = dc; p.cross_scat = dsc; p.wcross_J = dw; p.sflux_top = dtop;
+    p.abs_sp = das; p.abs_photo = dap; p.scat_sp = dss; p.ch_kindex = dki;
+    p.nabs = nabs; p.nscat = nscat; p.nch = nch;
+    p.sl_angle = sl_angle; p.edd = edd; p.f_diurnal = f_diurnal; p.flux_atol = flux_atol;
+    VK_CUDA(h, cudaMemset(p.dflux_u, 0, st * sizeof(double)));
+    VK_CUDA(h, cudaMemset(p.dflux_d, 0, st * sizeof(double)));
+    VK_CUDA(h, cudaMemset(p.aflux, 0, ly * sizeof(double)));
+    p.nbins = nbins;
+    return VK_OK;
+}
+
+extern "C" int vk_photo_reset(vk_handle *h) {
+    if (!h) return fail(h, VK_EINVAL, "handle is NULL");
+    PhotoDev &p = h->ph;
+    if (!p.nbins) return fail(h, VK_EINVAL, "no radiative transfer (call vk_photo_setup)");
+    const size_t st = (size_t)(h->max_layers + h->max_cols) * p.nbins, ly = (size_t)h->max_layers * p.nbins;
+    VK_CUDA(h, cudaMemset(p.dflux_u, 0, st * sizeof(double)));
+    VK_CUDA(h, cudaMemset(p.dflux_d, 0, st * sizeof(double)));
+    VK_CUDA(h, cudaMemset(p.aflux, 0, ly * sizeof(double)));
+    return VK_OK;
+}
+
+extern "C" int vk_photo_update(vk_handle *h, double *aflux_change) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    PhotoDev &p = h->ph;
+    if (!p.nbins) return fail(h, VK_EINVAL, "no radiative transfer (call vk_photo_setup)");
+    VK_CUDA(h, cudaMemsetAsync(h->d_phchange, 0, h->ncols * sizeof(unsigned long long), h->stream));
+    vk::launch_photo(h->net(), h->batch(), p, h->w.y, h->w.ymix, h->d_k, h->d_phchange, h->stream);
+    VK_CUDA(h, cudaGetLastError());
+    if (aflux_change)
+        VK_CUDA(h, cudaMemcpyAsync(aflux_change, h->d_phchange, h->ncols * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
+extern "C" int vk_photo_get(vk_handle *h, double *tau, double *aflux, double *J) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    PhotoDev &p = h->ph;
+    if (!p.nbins) return fail(h, VK_EINVAL, "no radiative transfer (call vk_photo_setup)");
+    if (tau) VK_CUDA(h, cudaMemcpy(tau, p.tau, (size_t)(h->L + h->ncols) * p.nbins * sizeof(double), cudaMemcpyDeviceToHost));
+    if (aflux) VK_CUDA(h, cudaMemcpy(aflux, p.aflux, (size_t)h->L * p.nbins * sizeof(double), cudaMemcpyDeviceToHost));
+    if (J) VK_CUDA(h, cudaMemcpy(J, p.J, (size_t)h->L * p.nch * sizeof(double), cudaMemcpyDeviceToHost));
     return VK_OK;
 }
 

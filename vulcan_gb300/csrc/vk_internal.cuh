@@ -117,6 +117,24 @@ __device__ __forceinline__ int next_column(const DevBatch &b, int *s_col) {
 }
 #endif
 
+// Photochemistry radiative transfer tables and state (vk_photo.cu).
+struct PhotoDev {
+    int nbins, nabs, nscat, nch;
+    const double *bins;        // [nbins] wavelength (nm)
+    const double *cross;       // [nabs][nbins] absorption cross sections
+    const int *abs_sp;         // [nabs] species index
+    const int *abs_photo;      // [nabs] 1: counts in the absorption of the albedo
+    const double *cross_scat;  // [nscat][nbins] Rayleigh cross sections
+    const int *scat_sp;        // [nscat]
+    const double *wcross_J;    // [nch][nbins] photolysis cross section x J bin weight
+    const int *ch_kindex;      // [nch] 1-based k index of the channel
+    const double *sflux_top;   // [nbins] top-of-atmosphere flux
+    double sl_angle, edd, f_diurnal, flux_atol;
+    double *tau, *dflux_u, *dflux_d;   // [(L + ncols)][nbins] staggered
+    double *w0, *aflux, *aflux_prev;   // [L][nbins]
+    double *J;                 // [L][nch]
+};
+
 // Launch helpers implemented in vk_kernels.cu (all asynchronous on stream).
 namespace vk {
 
@@ -167,6 +185,8 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
                    cudaStream_t s);
 void launch_rate_consts(const DevNet &net, const DevBatch &b, const int *kind, const int *rev,
                         const double *params, const double *nasa9, double *k, cudaStream_t s);
+void launch_photo(const DevNet &net, const DevBatch &b, const PhotoDev &ph, const double *y,
+                  const double *ymix, double *k, unsigned long long *change, cudaStream_t s);
 void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
 void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);

@@ -1,0 +1,155 @@
+"""Photochemistry radiative transfer: host set-up of the tables the device
+path (vk_photo_setup / vk_photo_update) runs on.
+
+Restates the reference's make_bins_read_cross (op.py:495-782) and read_sflux
+(build_atm.py:617-656) for T-independent cross sections without
+photoionisation (the reference's defaults: T_cross_sp = [], use_ion = False):
+
+* bins: from the shortest absorption edge (not below the stellar file's
+  first wavelength or 2 nm) to min(longest edge, the file's last wavelength
+  or 700 nm, the longest photolysis threshold), step dbin1 below dbin_12trans
+  and dbin2 above;
+* cross sections interpolated linearly onto the bins with zero outside the
+  tabulated range; branch cross sections = dissociation cross section x the
+  branching ratio (held constant beyond its table);
+* top-of-atmosphere flux: the stellar surface flux x (r_star R_sun / (a AU))^2
+  interpolated onto the bins.
+
+The J integral's bin weights follow the reference's four-part trapezoid sums
+(op.py:2770-2773), including its index semantics when dbin_12trans lies
+outside the bins.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+R_SUN = 6.957E10          # cm (phy_const.py)
+AU = 1.49597871E13         # cm (phy_const.py)
+
+
+def j_weights(nbins, i12, dbin1, dbin2):
+    """Weight of each bin in the reference's J sum (see module docstring)."""
+    w = np.zeros(nbins)
+    idx = np.arange(nbins)
+    w[idx[:i12]] += dbin1
+    w[idx[0]] -= 0.5 * dbin1
+    w[idx[i12 - 1]] -= 0.5 * dbin1
+    w[idx[i12:]] += dbin2
+    w[idx[i12]] -= 0.5 * dbin2
+    w[idx[-1]] -= 0.5 * dbin2
+    return w
+
+
+@dataclass
+class PhotoTables:
+    bins: np.ndarray
+    dbin1: float
+    dbin2: float
+    i12: int                  # index of dbin_12trans in bins (-1 if outside)
+    sflux_top: np.ndarray
+    absp_sp: list             # absorbers (photolysis species)
+    cross: np.ndarray         # [nabs, nbins]
+    scat_sp: list
+    cross_scat: np.ndarray    # [nscat, nbins]
+    ch_sp: list               # photolysis channels
+    ch_br: list
+    cross_J: np.ndarray       # [nch, nbins]
+    sl_angle: float
+    edd: float
+    f_diurnal: float
+    flux_atol: float
+
+    def weights(self):
+        return j_weights(len(self.bins), self.i12, self.dbin1, self.dbin2)
+
+    @classmethod
+    def from_fixture(cls, d):
+        """Tables recorded from the reference's own set-up (tests/golden)."""
+        absp = [str(s) for s in d['absp_sp']]
+        return cls(bins=np.asarray(d['bins'], float), dbin1=float(d['dbin1']),
+                   dbin2=float(d['dbin2']), i12=int(d['sflux_din12_indx']),
+                   sflux_top=np.asarray(d['sflux_top'], float), absp_sp=absp,
+                   cross=np.asarray(d['cross'], float), scat_sp=[str(s) for s in d['scat_sp']],
+                   cross_scat=np.asarray(d['cross_scat'], float),
+                   ch_sp=[str(s) for s in d['ch_sp']], ch_br=[int(b) for b in d['ch_br']],
+                   cross_J=np.asarray(d['cross_J'], float), sl_angle=float(d['sl_angle']),
+                   edd=float(d['edd']), f_diurnal=float(d['f_diurnal']),
+                   flux_atol=float(d['flux_atol']))
+
+    @classmethod
+    def from_reference_files(cls, net, ref_root, sflux_file, r_star, orbit_radius,
+                             sl_angle, scat_sp=('H2', 'He'), edd=0.5, dbin1=0.1, dbin2=2.0,
+                             dbin_12trans=240.0, f_diurnal=1.0, flux_atol=1.0,
+                             cross_folder='thermo/photo_cross/'):
+        """Tables from the reference's data layout (cross-section folder,
+        thresholds.txt, rayleigh/ and a stellar flux file), for the photolysis
+        channels of ``net`` (Network.from_file(..., use_photo=True))."""
+        cf = os.path.join(ref_root, cross_folder)
+        chans = sorted(net.photo_index())
+        photo_sp = sorted({sp for sp, _ in chans})
+        lab = np.genfromtxt(os.path.join(cf, 'thresholds.txt'), dtype=str, usecols=0)
+        thr = np.genfromtxt(os.path.join(cf, 'thresholds.txt'), skip_header=1)[:, 1]
+        threshold = {l: v for l, v in zip(lab, thr) if l in net.species}
+        sraw = np.genfromtxt(os.path.join(ref_root, sflux_file), dtype=float, skip_header=1,
+                             names=['lambda', 'flux'])
+        def_min, def_max = max(sraw['lambda'][0], 2.), min(sraw['lambda'][-1], 700.)
+        raw, ratio = {}, {}
+        bin_min = bin_max = diss_max = None
+        for sp in photo_sp:
+            raw[sp] = np.genfromtxt(os.path.join(cf, sp, sp + '_cross.csv'), dtype=float,
+                                    delimiter=',', skip_header=1, names=['lambda', 'cross', 'disso'])
+            ratio[sp] = np.genfromtxt(os.path.join(cf, sp, sp + '_branch.csv'), dtype=float,
+                                      delimiter=',', skip_header=1, names=True)
+            lo, hi = raw[sp]['lambda'][0], raw[sp]['lambda'][-1]
+            bin_min = lo if bin_min is None else min(bin_min, lo)
+            bin_max = hi if bin_max is None else max(bin_max, hi)
+            diss_max = threshold[sp] if diss_max is None else max(diss_max, threshold[sp])
+        bin_min = max(bin_min, def_min)
+        bin_max = min(bin_max, def_max, diss_max)
+        if bin_min <= dbin_12trans <= bin_max:
+            bins = np.concatenate((np.arange(bin_min, dbin_12trans, dbin1),
+                                   np.arange(dbin_12trans, bin_max, dbin2)))
+        else:
+            bins = np.arange(bin_min, bin_max, dbin1)
+        interp0 = lambda x, xp, fp: np.interp(x, xp, fp, left=0.0, right=0.0)
+        cross = np.array([interp0(bins, raw[sp]['lambda'], raw[sp]['cross']) for sp in photo_sp])
+        cross_J = []
+        for sp, br in chans:
+            key = 'br_ratio_%d' % br
+            r = np.interp(bins, ratio[sp]['lambda'], ratio[sp][key])      # edge values held
+            cross_J.append(interp0(bins, raw[sp]['lambda'], raw[sp]['disso']) * r)
+        scat = []
+        for sp in scat_sp:
+            s = np.genfromtxt(os.path.join(cf, 'rayleigh', sp + '_scat.txt'), dtype=float,
+                              skip_header=1, names=['lambda', 'cross'])
+            scat.append(interp0(bins, s['lambda'], s['cross']))
+        top = interp0(bins, sraw['lambda'], sraw['flux'] * (r_star * R_SUN / (AU * orbit_radius)) ** 2)
+        hit = np.nonzero(bins == dbin_12trans)[0]
+        return cls(bins=bins, dbin1=dbin1, dbin2=dbin2, i12=int(hit[-1]) if hit.size else -1,
+                   sflux_top=top, absp_sp=photo_sp, cross=cross, scat_sp=list(scat_sp),
+                   cross_scat=np.array(scat), ch_sp=[c[0] for c in chans],
+                   ch_br=[c[1] for c in chans], cross_J=np.array(cross_J), sl_angle=sl_angle,
+                   edd=edd, f_diurnal=f_diurnal, flux_atol=flux_atol)
+
+
+def attach(handle, tables, net):
+    """vk_photo_setup on a Ros2Handle for the network's species and channels."""
+    from .capi import check, lib, ptr
+    sp = {s: i for i, s in enumerate(net.species)}
+    pidx = net.photo_index()
+    abs_sp = np.array([sp[s] for s in tables.absp_sp], dtype=np.int32)
+    abs_photo = np.ones(len(abs_sp), dtype=np.int32)
+    scat_sp = np.array([sp[s] for s in tables.scat_sp], dtype=np.int32)
+    kidx = np.array([pidx[(s, b)] for s, b in zip(tables.ch_sp, tables.ch_br)], dtype=np.int32)
+    c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    check(lib().vk_photo_setup(
+        handle.h, len(tables.bins), ptr(c(tables.bins)), ptr(c(tables.weights())),
+        len(abs_sp), ptr(abs_sp, C.c_int), ptr(abs_photo, C.c_int), ptr(c(tables.cross)),
+        len(scat_sp), ptr(scat_sp, C.c_int), ptr(c(tables.cross_scat)),
+        len(kidx), ptr(kidx, C.c_int), ptr(c(tables.cross_J)), ptr(c(tables.sflux_top)),
+        tables.sl_angle, tables.edd, tables.f_diurnal, tables.flux_atol), handle.h)
+    handle.photo_dims = (len(tables.bins), len(kidx))

@@ -282,6 +282,23 @@ class Ros2Handle:
         check(lib().vk_get_k(self.h, ptr(out)), self.h)
         return out
 
+    def photo_update(self):
+        """Radiative transfer from the current state (vk_photo_update): J into
+        the photolysis k slots; returns each column's actinic-flux change."""
+        ch = np.zeros(self.batch.ncols)
+        check(lib().vk_photo_update(self.h, ptr(ch)), self.h)
+        return ch
+
+    def photo_get(self):
+        """(tau [L + ncols, nbins], actinic flux [L, nbins], J [L, nch])."""
+        nb, nch = self.photo_dims
+        b = self.batch
+        tau = np.empty((b.L + b.ncols, nb))
+        af = np.empty((b.L, nb))
+        J = np.empty((b.L, nch))
+        check(lib().vk_photo_get(self.h, ptr(tau), ptr(af), ptr(J)), self.h)
+        return tau, af, J
+
     def conv_stats(self):
         """(longdy, longdydt) of each column's last steady-state test."""
         b = self.batch
