@@ -105,6 +105,9 @@ typedef struct vk_ctrl {
     int max_attempts;       /* attempt cap per step (device guard)            */
     int flags;              /* VK_F_* */
     double gs, Rp;          /* gravity update (update_mu_dz)                  */
+    double flux_cri;        /* steady state also needs the actinic-flux change
+                               of the last vk_photo_update below this
+                               (op.py:1054; 0 change without photochemistry) */
 } vk_ctrl;
 
 /* ---- network ---- */
@@ -215,9 +218,11 @@ VK_API int  vk_get_k(vk_handle *h, double *k);
  * the top-of-atmosphere flux [nbins]; angles in radians.  The diffuse fluxes
  * persist between updates as the reference's arrays do (vk_photo_reset
  * clears them).  vk_photo_update computes tau, the actinic flux and J from
- * the current state, writes J * f_diurnal into the channels' k slots and, if
- * aflux_change is given, each column's largest relative actinic-flux change
- * where the flux exceeds flux_atol (var.aflux_change).  No counterpart for
+ * the current state of the columns with col_mask[c] != 0 (NULL: all), writes
+ * J * f_diurnal into the channels' k slots and each column's largest
+ * relative actinic-flux change where the flux exceeds flux_atol
+ * (var.aflux_change) into the run state -- the steady-state test of vk_run
+ * requires it below vk_ctrl.flux_cri -- and into aflux_change if given.  No counterpart for
  * the T-dependent cross sections or photoionisation yet. */
 VK_API int  vk_photo_setup(vk_handle *h, int nbins, const double *bins, const double *jweights,
                            int nabs, const int *abs_sp, const int *abs_photo, const double *cross,
@@ -225,7 +230,7 @@ VK_API int  vk_photo_setup(vk_handle *h, int nbins, const double *bins, const do
                            const int *ch_kindex, const double *cross_J, const double *sflux_top,
                            double sl_angle, double edd, double f_diurnal, double flux_atol);
 VK_API int  vk_photo_reset(vk_handle *h);
-VK_API int  vk_photo_update(vk_handle *h, double *aflux_change);
+VK_API int  vk_photo_update(vk_handle *h, const int *col_mask, double *aflux_change);
 /* Diagnostic: tau [(L + ncols)][nbins] (staggered, column c from row
  * col_off[c] + c), actinic flux [L][nbins], J [L][nch]. */
 VK_API int  vk_photo_get(vk_handle *h, double *tau, double *aflux, double *J);

@@ -116,3 +116,31 @@ def test_device_radiative_transfer_matches_oracle():
         for c, ki in enumerate(d['ch_kindex']):
             np.testing.assert_allclose(k[:, int(ki) - 1], J_d[:, c] * float(d['f_diurnal']), rtol=1e-15)
     h.close()
+
+
+@pytest.mark.gpu
+def test_device_run_with_photo_tracks_reference():
+    """vk_run with the reference's photochemistry schedule from the c1rt
+    set-up: J recomputed at count 0 (twice, as the reference's set-up and its
+    first loop iteration do), the state after 100 steps and the J of the
+    update at count 100 against the reference's records."""
+    from helpers import floor_err
+    from test_gpu_parity import make_handle
+    from vulcan_gb300 import _build, batch, configs, photo
+    from vulcan_gb300.solver import ctrl_from
+    _build.build()
+    d = _fixture()
+    g, net, gn, h, b = make_handle('c1')
+    h.set_atom_ini(g['atom_ini'][None, :])
+    h.set_clock(dt=1e-10, t=0.0, count=0)
+    photo.attach(h, photo.PhotoTables.from_fixture(d), net)
+    h.photo_update()                                   # the set-up call
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    st = batch.run_with_photo(h, ctrl, max_steps=100)
+    assert st['count'][0] == 100
+    assert floor_err(st['y'], d['rec2_y'], g['n_0']) <= 1e-8
+    h.photo_update()                                   # the update at count 100
+    _, _, J = h.photo_get()
+    m = d['rec2_J'] > 1e-300
+    assert float(np.max(np.abs(J.T - d['rec2_J'])[m] / d['rec2_J'][m])) <= 1e-6
+    h.close()

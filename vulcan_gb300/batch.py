@@ -58,3 +58,37 @@ def run_batch(net, specs, atom_list, max_steps=0, timeout_s=0.0, cfg=None,
     st['counters'] = h.counters()
     st['batch'] = b
     return st
+
+
+def run_with_photo(h, ctrl, max_steps, ini_frq=100, final_frq=5, chunk=5, timeout_s=0.0):
+    """vk_run with the reference's photochemistry schedule (Integration.__call__,
+    op.py:811-830): before a step whose count is a multiple of the column's
+    update_photo_frq, recompute its J from the current state
+    (vk_photo_update); a column's frequency switches from ini_frq to final_frq
+    once longdy < 10 yconv_min and longdydt < 1e-6.  Runs chunks of ``chunk``
+    steps (a divisor of both frequencies) until every column has ended or
+    max_steps steps were taken; returns the final state."""
+    from . import capi
+    if ini_frq % chunk or final_frq % chunk:
+        raise ValueError('chunk must divide both photo update frequencies')
+    n = h.batch.ncols
+    final = np.zeros(n, dtype=bool)
+    done_steps = 0
+    while done_steps < max_steps:
+        st = h.state()
+        live = st['end_case'] == 0
+        if not live.any():
+            break
+        ld, ldt = h.conv_stats()
+        final |= (ld < ctrl.yconv_min * 10.) & (ldt < 1.e-6)
+        frq = np.where(final, final_frq, ini_frq)
+        due = live & (st['count'] % frq == 0)
+        if due.any():
+            h.photo_update(due.astype(np.int32))
+        try:
+            h.run(ctrl, max_steps=chunk, timeout_s=timeout_s)
+        except capi.VkError as e:
+            if e.code != capi.VK_ETIMEOUT:
+                raise
+        done_steps += chunk
+    return h.state()

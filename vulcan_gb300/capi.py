@@ -55,7 +55,7 @@ class VkCtrl(C.Structure):
         'yconv_cri', 'slope_cri', 'yconv_min', 'st_factor', 'trun_min', 'runtime')] + \
         [(n, C.c_int) for n in ('conv_step', 'count_min', 'count_max', 'update_frq',
                                 'max_attempts', 'flags')] + \
-        [('gs', C.c_double), ('Rp', C.c_double)]
+        [('gs', C.c_double), ('Rp', C.c_double), ('flux_cri', C.c_double)]
 
 
 class VkError(RuntimeError):
@@ -108,7 +108,7 @@ def lib(path=None):
         'vk_photo_setup': (i, [vp, i, pd, pd, i, pi, pi, pd, i, pi, pd, i, pi, pd, pd,
                                C.c_double, C.c_double, C.c_double, C.c_double]),
         'vk_photo_reset': (i, [vp]),
-        'vk_photo_update': (i, [vp, pd]),
+        'vk_photo_update': (i, [vp, pi, pd]),
         'vk_photo_get': (i, [vp, pd, pd, pd]),
         'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
         'vk_chem_source': (i, [vp, pd, pd]),

@@ -47,7 +47,7 @@ struct vk_handle {
     int *d_col_off = nullptr, *d_lay_col = nullptr;
     int *d_order = nullptr;             // columns by decreasing nz
     PhotoDev ph{};                  // radiative transfer (vk_photo_setup)
-    unsigned long long *d_phchange = nullptr;
+    int *d_phmask = nullptr;            // [max_cols] columns of a masked photo update
     int *d_kkind = nullptr, *d_krev = nullptr;   // rate-constant parameters (vk_set_rate_params)
     double *d_kpar = nullptr, *d_nasa9 = nullptr;
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
@@ -254,7 +254,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     vk::RunState &r = h->rs;
     r.y = w.y; r.ymix = w.ymix; r.dt = w.dt; r.delta = w.delta; r.atm = h->d_atm;
     TRY(dalloc(h, &r.y_prev, L * ni));
-    double **cd[] = {&r.t, &r.longdy, &r.longdydt};
+    double **cd[] = {&r.t, &r.longdy, &r.longdydt, &r.aflux_change};
     for (double **p : cd) TRY(dalloc(h, p, max_cols));
     int **ci[] = {&r.count, &r.end_case, &r.active, &r.natt, &r.steps_call, &r.pref};
     for (int **p : ci) TRY(dalloc(h, p, max_cols));
@@ -330,6 +330,13 @@ extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const doub
     {
         vk::RunState &r = h->rs;
         VK_CUDA(h, cudaMemsetAsync(r.t, 0, ncols * sizeof(double), s));
+        VK_CUDA(h, cudaMemsetAsync(r.aflux_change, 0, ncols * sizeof(double), s));
+        {
+            // the reference starts longdy = longdydt = 1 (store.Variables)
+            std::vector<double> one(ncols, 1.0);
+            VK_CUDA(h, cudaMemcpy(r.longdy, one.data(), ncols * sizeof(double), cudaMemcpyHostToDevice));
+            VK_CUDA(h, cudaMemcpy(r.longdydt, one.data(), ncols * sizeof(double), cudaMemcpyHostToDevice));
+        }
         VK_CUDA(h, cudaMemsetAsync(r.count, 0, ncols * sizeof(int), s));
         VK_CUDA(h, cudaMemsetAsync(r.end_case, 0, ncols * sizeof(int), s));
         VK_CUDA(h, cudaMemsetAsync(r.counters, 0, ncols * VK_NCOUNTERS * sizeof(int), s));
@@ -649,7 +656,7 @@ extern "C" int vk_photo_setup(vk_handle *h, int nbins, const double *bins, const
     double **lay[] = {&p.w0, &p.aflux, &p.aflux_prev};
     for (double **q : lay) if (!rc) rc = dalloc(h, q, ly);
     if (!rc) rc = dalloc(h, &p.J, (size_t)h->max_layers * nch);
-    if (!rc) rc = dalloc(h, &h->d_phchange, h->max_cols);
+    if (!rc) rc = dalloc(h, &h->d_phmask, h->max_cols);
     if (rc) return rc;                     // the handle frees what was allocated
     p.bins = db; p.cross = dc; p.cross_scat = dsc; p.wcross_J = dw; p.sflux_top = dtop;
     p.abs_sp = das; p.abs_photo = dap; p.scat_sp = dss; p.ch_kindex = dki;
@@ -673,18 +680,26 @@ extern "C" int vk_photo_reset(vk_handle *h) {
     return VK_OK;
 }
 
-extern "C" int vk_photo_update(vk_handle *h, double *aflux_change) {
+extern "C" int vk_photo_update(vk_handle *h, const int *col_mask, double *aflux_change) {
     int rc = need_batch(h);
     if (rc) return rc;
     PhotoDev &p = h->ph;
     if (!p.nbins) return fail(h, VK_EINVAL, "no radiative transfer (call vk_photo_setup)");
-    VK_CUDA(h, cudaMemsetAsync(h->d_phchange, 0, h->ncols * sizeof(unsigned long long), h->stream));
-    vk::launch_photo(h->net(), h->batch(), p, h->w.y, h->w.ymix, h->d_k, h->d_phchange, h->stream);
+    cudaStream_t s = h->stream;
+    DevBatch b = h->batch();
+    if (col_mask) {
+        VK_CUDA(h, cudaMemcpyAsync(h->d_phmask, col_mask, h->ncols * sizeof(int), cudaMemcpyHostToDevice, s));
+        b.active = h->d_phmask;
+    }
+    // the change is accumulated as the bit pattern of a non-negative double
+    unsigned long long *chg = reinterpret_cast<unsigned long long *>(h->rs.aflux_change);
+    vk::launch_photo_clear(b, chg, s);
+    vk::launch_photo(h->net(), b, p, h->w.y, h->w.ymix, h->d_k, chg, s);
     VK_CUDA(h, cudaGetLastError());
     if (aflux_change)
-        VK_CUDA(h, cudaMemcpyAsync(aflux_change, h->d_phchange, h->ncols * sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+        VK_CUDA(h, cudaMemcpyAsync(aflux_change, h->rs.aflux_change, h->ncols * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+    VK_CUDA(h, cudaStreamSynchronize(s));
     return VK_OK;
 }
 
@@ -736,7 +751,7 @@ static vk::RunCtrl to_run_ctrl(const vk_ctrl *c, int max_steps) {
     r.dt_min = c->dt_min; r.dt_max = c->dt_max; r.dt_var_min = c->dt_var_min; r.dt_var_max = c->dt_var_max;
     r.yconv_cri = c->yconv_cri; r.slope_cri = c->slope_cri; r.yconv_min = c->yconv_min;
     r.st_factor = c->st_factor; r.trun_min = c->trun_min; r.runtime = c->runtime;
-    r.gs = c->gs; r.Rp = c->Rp;
+    r.gs = c->gs; r.Rp = c->Rp; r.flux_cri = c->flux_cri;
     r.conv_step = c->conv_step; r.count_min = c->count_min; r.count_max = c->count_max;
     r.update_frq = c->update_frq; r.max_attempts = c->max_attempts; r.flags = c->flags;
     r.max_steps = max_steps > 0 ? max_steps : INT_MAX;

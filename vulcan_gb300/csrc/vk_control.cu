@@ -127,8 +127,9 @@ __device__ int conv_test(const DevNet &net, const DevBatch &b, const RunState &r
         double longdydt = longdy / dtt;
         rs.longdy[c] = longdy;
         rs.longdydt[c] = longdydt;
-        ok = (longdy < cc.yconv_cri && longdydt < cc.slope_cri) ||
-             (longdy < cc.yconv_min && longdydt < slope_min);
+        ok = ((longdy < cc.yconv_cri && longdydt < cc.slope_cri) ||
+              (longdy < cc.yconv_min && longdydt < slope_min)) &&
+             rs.aflux_change[c] < cc.flux_cri;
     }
     return ok;
 }

@@ -8,6 +8,7 @@ struct RunState {
     double *y, *ymix, *y_prev;          // [L][ni]
     double *atm;                        // [L][VK_ATM_NF], same storage as DevBatch::atm
     double *dt, *t, *delta, *longdy, *longdydt;   // [ncols]
+    double *aflux_change;               // [ncols] last radiative-transfer flux change (0: none)
     int *count, *end_case, *active, *natt, *steps_call, *pref;  // [ncols]
     int *counters;                      // [ncols][VK_NCOUNTERS]
     double *atom_ini, *loss, *loss_prev;  // [ncols][VK_MAX_NATOM]
@@ -20,7 +21,7 @@ struct RunCtrl {
     double rtol, atol, mtol, mtol_conv, pos_cut, nega_cut, loss_eps;
     double dt_min, dt_max, dt_var_min, dt_var_max;
     double yconv_cri, slope_cri, yconv_min, st_factor, trun_min, runtime;
-    double gs, Rp;
+    double gs, Rp, flux_cri;
     int conv_step, count_min, count_max, update_frq, max_attempts, flags, max_steps;
 };
 

@@ -187,6 +187,7 @@ void launch_rate_consts(const DevNet &net, const DevBatch &b, const int *kind, c
                         const double *params, const double *nasa9, double *k, cudaStream_t s);
 void launch_photo(const DevNet &net, const DevBatch &b, const PhotoDev &ph, const double *y,
                   const double *ymix, double *k, unsigned long long *change, cudaStream_t s);
+void launch_photo_clear(const DevBatch &b, unsigned long long *change, cudaStream_t s);
 void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
 void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);

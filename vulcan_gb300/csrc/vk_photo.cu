@@ -146,6 +146,16 @@ k_photo_J(DevNet net, DevBatch b, PhotoDev ph, double *k, unsigned long long *ch
     if (lane == 0 && m > 0.0) atomicMax(change + c, (unsigned long long)__double_as_longlong(m));
 }
 
+// zero the change of the columns this update covers
+__global__ void k_photo_clear(DevBatch b, unsigned long long *change) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < b.ncols && (!b.active || b.active[c])) change[c] = 0ull;
+}
+
+void launch_photo_clear(const DevBatch &b, unsigned long long *change, cudaStream_t s) {
+    k_photo_clear<<<(b.ncols + 127) / 128, 128, 0, s>>>(b, change);
+}
+
 void launch_photo(const DevNet &net, const DevBatch &b, const PhotoDev &ph, const double *y,
                   const double *ymix, double *k, unsigned long long *change, cudaStream_t s) {
     dim3 g1((ph.nbins + 127) / 128, b.ncols);

@@ -145,7 +145,7 @@ def ctrl_from(cfg=None, flags=capi.VK_F_MOLDIFF, gs=2140., Rp=1.138 * 7.1492E9,
     c = capi.VkCtrl()
     for k in ('rtol', 'atol', 'mtol', 'mtol_conv', 'pos_cut', 'nega_cut', 'loss_eps',
               'dt_min', 'dt_max', 'dt_var_min', 'dt_var_max', 'yconv_cri', 'slope_cri',
-              'yconv_min', 'st_factor', 'trun_min', 'runtime'):
+              'yconv_min', 'st_factor', 'trun_min', 'runtime', 'flux_cri'):
         setattr(c, k, float(v[k]))
     for k in ('conv_step', 'count_min', 'count_max', 'update_frq'):
         setattr(c, k, int(v[k]))
@@ -282,11 +282,13 @@ class Ros2Handle:
         check(lib().vk_get_k(self.h, ptr(out)), self.h)
         return out
 
-    def photo_update(self):
-        """Radiative transfer from the current state (vk_photo_update): J into
-        the photolysis k slots; returns each column's actinic-flux change."""
+    def photo_update(self, mask=None):
+        """Radiative transfer from the current state (vk_photo_update) of all
+        columns or those with mask != 0: J into the photolysis k slots; returns
+        each column's actinic-flux change (kept by the run's steady-state test)."""
         ch = np.zeros(self.batch.ncols)
-        check(lib().vk_photo_update(self.h, ptr(ch)), self.h)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.int32)
+        check(lib().vk_photo_update(self.h, ptr(m, C.c_int), ptr(ch)), self.h)
         return ch
 
     def photo_get(self):
