@@ -282,8 +282,10 @@ def run_gpu(args):
     dist = replicas.init()
     rank, ws, _ = replicas.world()
     hbm, hbm_kind = peaks()
-    clocks = Clocks(os.path.join(REPO, 'gpurun_out', 'bench_clocks.csv')
-                    if os.path.isdir(os.path.join(REPO, 'gpurun_out')) else '/tmp/bench_clocks.csv')
+    # nvidia-smi samples of the timed region (VK_BENCH_CLOCKS overrides the file)
+    clocks_csv = os.environ.get('VK_BENCH_CLOCKS', os.path.join(REPO, '_build', 'bench_clocks.csv'))
+    os.makedirs(os.path.dirname(clocks_csv), exist_ok=True)
+    clocks = Clocks(clocks_csv)
     mixed = _measure(args, 1, clocks if rank == 0 else None, dist)
     plain = _measure(args, 0, None, dist)
     if rank != 0:

@@ -638,10 +638,13 @@ extern "C" int vk_photo_setup(vk_handle *h, int nbins, const double *bins, const
     double *db = nullptr, *dc = nullptr, *dsc = nullptr, *dw = nullptr, *dtop = nullptr;
     int *das = nullptr, *dap = nullptr, *dss = nullptr, *dki = nullptr;
     std::vector<double> bv(bins, bins + nbins), cv(cross, cross + (size_t)nabs * nbins),
-        scv(cross_scat ? cross_scat : bins, cross_scat ? cross_scat + (size_t)nscat * nbins : bins),
-        topv(sflux_top, sflux_top + nbins);
+        topv(sflux_top, sflux_top + nbins), scv;
     std::vector<int> asv(abs_sp, abs_sp + nabs), apv(abs_photo, abs_photo + nabs),
-        ssv(scat_sp ? scat_sp : abs_sp, scat_sp ? scat_sp + nscat : abs_sp), kiv(ch_kindex, ch_kindex + nch);
+        kiv(ch_kindex, ch_kindex + nch), ssv;
+    if (nscat) {
+        scv.assign(cross_scat, cross_scat + (size_t)nscat * nbins);
+        ssv.assign(scat_sp, scat_sp + nscat);
+    }
     if (!rc) rc = upload(h, &db, bv);
     if (!rc) rc = upload(h, &dc, cv);
     if (!rc) rc = upload(h, &dsc, scv);
