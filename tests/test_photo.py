@@ -144,3 +144,38 @@ def test_device_run_with_photo_tracks_reference():
     m = d['rec2_J'] > 1e-300
     assert float(np.max(np.abs(J.T - d['rec2_J'])[m] / d['rec2_J'][m])) <= 1e-6
     h.close()
+
+
+def test_photo_schedule_follows_the_reference():
+    """batch.run_with_photo on a stand-in handle: J before the steps whose
+    count is a multiple of update_photo_frq (100, then 5 once longdy < 10
+    yconv_min and longdydt < 1e-6), per column."""
+    from types import SimpleNamespace
+    from vulcan_gb300 import batch
+
+    class FakeHandle:
+        def __init__(self):
+            self.batch = SimpleNamespace(ncols=2)
+            self.count = np.zeros(2, dtype=int)
+            self.updates = []
+
+        def state(self):
+            return {'count': self.count.copy(), 'end_case': np.where(self.count >= 300, 1, 0)}
+
+        def conv_stats(self):
+            # column 1 is near steady state from count 150 on
+            ld = np.array([1.0, 1e-3 if self.count[1] >= 150 else 1.0])
+            return ld, ld * 1e-9
+
+        def photo_update(self, mask=None):
+            self.updates.append((self.count.copy(), np.asarray(mask).copy()))
+
+        def run(self, ctrl, max_steps=0, timeout_s=0.0):
+            self.count += max_steps * (self.count < 300)
+
+    h = FakeHandle()
+    batch.run_with_photo(h, SimpleNamespace(yconv_min=0.1), max_steps=300)
+    col0 = [int(c[0]) for c, m in h.updates if m[0]]
+    col1 = [int(c[1]) for c, m in h.updates if m[1]]
+    assert col0 == [0, 100, 200]
+    assert col1[:2] == [0, 100] and col1[2:] == list(range(150, 300, 5))
