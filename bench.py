@@ -500,6 +500,48 @@ def run_converge(args):
     print(json.dumps(res))
 
 
+def run_photo(args):
+    """Radiative transfer throughput: vk_photo_update over --ncols columns of
+    the NCHO photochemistry workload (nz = 150) on the reference's binned
+    tables recorded in tests/golden (1 nm bins below 240 nm), against the
+    numpy oracle of the same call on one column (host, one core)."""
+    from vulcan_gb300 import _build, batch, configs, photo
+    from vulcan_gb300.network import Network
+    _build.build()
+    net = Network.from_npz(os.path.join(REPO, 'tests', 'golden', 'net_NCHO_photo.npz'))
+    d = dict(np.load(os.path.join(REPO, 'tests', 'golden', 'golden_c1rt.npz'), allow_pickle=False))
+    tables = photo.PhotoTables.from_fixture(d)
+    spec = configs.config1(sorted(net.photo_index()))
+    items = batch.build_items([spec] * args.ncols, net)
+    h, b = batch.make_batch_handle(net, items, ATOMS)
+    photo.attach(h, tables, net)
+    for _ in range(2):
+        h.photo_update()
+    reps = 10
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        h.photo_update()
+    sec = (time.perf_counter() - t0) / reps
+    h.close()
+    from oracle import photo as P
+    spec_list = [str(x) for x in d['spec_list']]
+    ai = [spec_list.index(str(x)) for x in d['absp_sp']]
+    si = [spec_list.index(str(x)) for x in d['scat_sp']]
+    pi = [spec_list.index(str(x)) for x in d['photo_sp']]
+    nz, nb = d['rec0_y'].shape[0], len(d['bins'])
+    t0 = time.perf_counter()
+    tau = P.compute_tau(d['rec0_y'], d['rec0_dz'], ai, d['cross'], si, d['cross_scat'])
+    af, _, _ = P.compute_flux(tau, d['rec0_ymix'], pi, d['cross'], si, d['cross_scat'],
+                              d['sflux_top'], d['bins'], float(d['sl_angle']), float(d['edd']),
+                              np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb)))
+    P.compute_J(af, d['cross_J'], tables.weights())
+    cpu = time.perf_counter() - t0
+    print(json.dumps({'photo': True, 'ncols': args.ncols, 'layers': int(b.L), 'nbins': nb,
+                      'channels': len(tables.ch_sp), 'update_ms': round(sec * 1e3, 3),
+                      'columns_per_s': round(args.ncols / sec, 1),
+                      'oracle_one_column_ms': round(cpu * 1e3, 1)}))
+
+
 def run_profile(args):
     """Fixed kernel sequence for profiling: set-up, then --attempts attempts of
     every column of the first --ncols columns of the workload."""
@@ -550,6 +592,8 @@ def main():
     ap.add_argument('--profile', action='store_true',
                     help='only run --attempts instrumented attempts (for ncu captures)')
     ap.add_argument('--attempts', type=int, default=2)
+    ap.add_argument('--photo', action='store_true',
+                    help='radiative-transfer update throughput (photochemistry workload)')
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
@@ -577,6 +621,9 @@ def main():
         return
     if args.profile:
         run_profile(args)
+        return
+    if args.photo:
+        run_photo(args)
         return
     if args.converge:
         run_converge(args)
