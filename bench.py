@@ -306,8 +306,9 @@ def run_gpu(args):
         roof = {'bound': 'hbm', 'kernel': 'k_refine', 'achieved': by / (am['solve'] * 1e-3) / 1e9,
                 'peak': hbm, 'unit': 'GB/s', 'peak_source': hbm_kind}
     roof['frac'] = roof['achieved'] / roof['peak']
-    tpl = profile_traffic(roof['kernel'].split()[0])
-    # DRAM bytes per launch: the ncu capture's bytes per layer x this launch's layers
+    # DRAM bytes per launch: the ncu capture's bytes per layer (captured on the
+    # 69-species workload) x this launch's layers; none for other networks
+    tpl = profile_traffic(roof['kernel'].split()[0]) if args.workload == 'c2' else None
     roof['traffic'] = round(tpl * L) if tpl else None
     for k in ('achieved', 'peak', 'frac'):
         roof[k] = round(roof[k], 4)
