@@ -1,14 +1,14 @@
 // Register-resident Gauss-Jordan inversion of one n x n block per CTA.
 //
-// Thread layout: TX = 16 column groups x TY row groups (TY = blockDim/16),
+// Thread layout: 16 column groups x TY row groups (TY = blockDim/16),
 // tid = tx * TY + ty.  Thread (ty, tx) owns rows r = ty + TY*a (a < RA) and
 // columns c = tx + 16*b (b < RB) and keeps those elements in registers for the
 // whole inversion.  Pivoting is implicit (no row exchanges): step k picks, among
 // rows not yet used, the row p with the largest |A[p][k]| (lowest p on ties) --
 // the same pivot sequence as partial pivoting with row swaps -- and eliminates
-// column k from every other row.  The TY owners of column k are consecutive
-// threads, so the pivot search is one shuffle reduction; each step needs two
-// barriers.  On return the registers hold the inverse with permuted labels:
+// column k from every other row.  The TY owners of a column are consecutive
+// lanes, so the pivot search is one shuffle reduction.  On return the
+// registers hold the inverse with permuted labels:
 //     inverse[kinv[r]][perm[c]] = M[r][c],
 // perm[k] = pivot row of step k, kinv = its inverse (both in shared memory).
 #pragma once
@@ -31,108 +31,6 @@ struct GJShared {
 
 template <typename T>
 __device__ __forceinline__ T gj_abs(T v) { return v < T(0) ? -v : v; }
-
-// M_row[kb] with a runtime kb, without indexing the register array dynamically.
-template <typename T, int RB>
-__device__ __forceinline__ T pick_col(const T (&row)[RB], int kb) {
-    T v = T(0);
-#pragma unroll
-    for (int b = 0; b < RB; ++b)
-        if (b == kb) v = row[b];
-    return v;
-}
-
-template <typename T, int TY, int RA, int RB>
-__device__ __forceinline__ void gj_invert_reg(T (&M)[RA][RB], int n, int ty, int tx,
-                                              const GJShared<T> &sh) {
-    int rr[RA], cc[RB];
-#pragma unroll
-    for (int a = 0; a < RA; ++a) rr[a] = ty + TY * a;
-#pragma unroll
-    for (int b = 0; b < RB; ++b) cc[b] = tx + 16 * b;
-    for (int k = 0; k < n; ++k) {
-        const int kx = k & 15, kb = k >> 4;
-        if (tx == kx) {
-            // pivot search among this thread's unused rows of column k
-            T best = T(-1);
-            int bi = n;
-#pragma unroll
-            for (int a = 0; a < RA; ++a) {
-                if (rr[a] < n && !sh.used[rr[a]]) {
-                    T v = gj_abs(pick_col(M[a], kb));
-                    if (v > best) { best = v; bi = rr[a]; }
-                }
-            }
-            // the TY owners of column k are consecutive lanes (a half or a full warp)
-            const unsigned mask = TY == 32 ? 0xffffffffu : (0xffffu << (threadIdx.x & 16));
-#pragma unroll
-            for (int o = TY >> 1; o; o >>= 1) {
-                T ob = __shfl_xor_sync(mask, best, o, TY);
-                int oi = __shfl_xor_sync(mask, bi, o, TY);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (ty == 0) {
-                if (bi >= n || !(best >= T(0)) || isinf((double)best)) {
-                    *sh.s_sing = 2;
-                    for (int r = 0; r < n; ++r)
-                        if (!sh.used[r]) { bi = r; break; }
-                } else if (!(best > T(0))) {
-                    if (*sh.s_sing == 0) *sh.s_sing = 1;
-                }
-                *sh.s_piv = bi;
-                sh.perm[k] = bi;
-                sh.kinv[bi] = k;
-                sh.used[bi] = 1;      // visible to the next search after two barriers
-            }
-        }
-        __syncthreads();
-        const int p = *sh.s_piv;
-        // broadcast the pivot row and the pivot column
-        if ((p % TY) == ty) {
-            const int pa = p / TY;
-#pragma unroll
-            for (int a = 0; a < RA; ++a) {
-                if (a != pa) continue;
-#pragma unroll
-                for (int b = 0; b < RB; ++b)
-                    if (cc[b] < n) sh.rowv[cc[b]] = M[a][b];
-            }
-        }
-        if (tx == kx) {
-#pragma unroll
-            for (int a = 0; a < RA; ++a)
-                if (rr[a] < n) sh.colv[rr[a]] = pick_col(M[a], kb);
-        }
-        __syncthreads();
-        const T pinv = T(1) / sh.colv[p];
-        T rp[RB];
-#pragma unroll
-        for (int b = 0; b < RB; ++b) rp[b] = cc[b] < n ? sh.rowv[cc[b]] * pinv : T(0);
-        T fr[RA];
-#pragma unroll
-        for (int a = 0; a < RA; ++a) {
-            fr[a] = rr[a] < n ? sh.colv[rr[a]] : T(0);
-            if (rr[a] == p) {
-#pragma unroll
-                for (int b = 0; b < RB; ++b) M[a][b] = rp[b];
-            } else {
-#pragma unroll
-                for (int b = 0; b < RB; ++b) M[a][b] -= fr[a] * rp[b];
-            }
-        }
-        // pivot column of the inverse: 1/piv on the pivot row, -f/piv elsewhere
-        if (tx == kx) {
-#pragma unroll
-            for (int a = 0; a < RA; ++a) {
-                const T v = rr[a] == p ? pinv : -fr[a] * pinv;
-#pragma unroll
-                for (int b = 0; b < RB; ++b)
-                    if (b == kb) M[a][b] = v;
-            }
-        }
-    }
-    __syncthreads();
-}
 
 // Registers (permuted inverse) -> shared memory in natural order.
 template <typename T, int TY, int RA, int RB>
@@ -197,14 +95,13 @@ __device__ __forceinline__ void tile_get_row(const T (&M)[RA][RB], int pa, T (&o
 #undef VK_BODY
 }
 
-// gj_invert_reg with one block barrier per pivot step.  The pivot row reaches
-// the threads of each column group by warp shuffles (the TY owners of a column
-// are consecutive lanes, so every thread finds row p of its own columns at lane
-// p % TY of its group); only the pivot column goes through shared memory, in
-// two buffers by parity of k (colv2[2n]), written together with the search of
-// the next pivot right after each update -- so the next step needs one
-// barrier.  Same pivots and the same FMA per element as gj_invert_reg.
-// s_piv2 holds two pivot slots (parity of k).
+// Gauss-Jordan on the register tile with one block barrier per pivot step.
+// The pivot row reaches the threads of each column group by warp shuffles
+// (every thread finds row p of its own columns at lane p % TY of its group);
+// only the pivot column goes through shared memory, in two buffers by parity
+// of k (colv2[2n]), written together with the search of the next pivot right
+// after each update -- so the next step needs one barrier.  s_piv2 holds two
+// pivot slots (parity of k).
 template <typename T, int TY, int RA, int RB>
 __device__ __forceinline__ void gj_invert_reg1(T (&M)[RA][RB], int n, int ty, int tx,
                                                const GJShared<T> &sh, T *colv2, int *s_piv2) {
