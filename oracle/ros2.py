@@ -20,7 +20,6 @@ Follows, function by function (paths relative to the reference project):
 """
 from __future__ import annotations
 
-import math
 from dataclasses import dataclass, field
 
 import numpy as np

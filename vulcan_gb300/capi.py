@@ -8,7 +8,6 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-import numpy as np
 
 from ._build import LIB
 

@@ -23,7 +23,6 @@ import ctypes as C
 
 import numpy as np
 
-from . import column as colmod
 from .capi import check, lib
 
 LOG_FLOOR = -30.0
