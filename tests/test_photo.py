@@ -179,3 +179,101 @@ def test_photo_schedule_follows_the_reference():
     col1 = [int(c[1]) for c, m in h.updates if m[1]]
     assert col0 == [0, 100, 200]
     assert col1[:2] == [0, 100] and col1[2:] == list(range(150, 300, 5))
+
+
+def _dropin(d, net, g, T_cross_sp=()):
+    """Ros2GPU over a stand-in op module whose own radiative transfer records
+    its calls, with the c1 column's set-up arrays as var/atm."""
+    import types
+    from helpers import column_from_golden
+    from vulcan_gb300.solver import make_ros2gpu
+    calls = []
+
+    class FakeRos2:
+        def compute_tau(self, var, atm):
+            calls.append('tau')
+
+        def compute_flux(self, var, atm):
+            calls.append('flux')
+
+        def compute_J(self, var, atm):
+            calls.append('J')
+
+    op = types.SimpleNamespace(Ros2=FakeRos2)
+    cfg = types.SimpleNamespace(
+        network=None, use_photo=True, atom_list=[str(a) for a in g['atom_list']],
+        use_moldiff=True, use_topflux=False, use_botflux=False, T_cross_sp=list(T_cross_sp),
+        use_ion=False, scat_sp=[str(s) for s in d['scat_sp']], sl_angle=float(d['sl_angle']),
+        edd=float(d['edd']), f_diurnal=float(d['f_diurnal']), flux_atol=float(d['flux_atol']),
+        remove_list=[])
+    cls = make_ros2gpu(op, cfg, net.species)
+    cls._vk_net_cls = types.SimpleNamespace(from_file=lambda path, use_photo: net)
+    chans = list(zip([str(s) for s in d['ch_sp']], [int(b) for b in d['ch_br']]))
+    absp = [str(s) for s in d['absp_sp']]
+    var = types.SimpleNamespace(
+        y=d['rec0_y'].copy(), ymix=d['rec0_ymix'].copy(), dt=1e-10,
+        k={i: g['k'][i - 1].copy() for i in range(1, net.nr + 1)},
+        bins=d['bins'], dbin1=float(d['dbin1']), dbin2=float(d['dbin2']),
+        sflux_din12_indx=int(d['sflux_din12_indx']), sflux_top=d['sflux_top'],
+        photo_sp=set(str(s) for s in d['photo_sp']),
+        pho_rate_index={c: int(ki) for c, ki in zip(chans, d['ch_kindex'])},
+        cross={sp: d['cross'][i] for i, sp in enumerate(absp)},
+        cross_scat={str(sp): d['cross_scat'][i] for i, sp in enumerate(d['scat_sp'])},
+        cross_J={c: d['cross_J'][i] for i, c in enumerate(chans)},
+        aflux=np.zeros((d['rec0_y'].shape[0], len(d['bins']))))
+    col = column_from_golden(g)
+    atm = types.SimpleNamespace(**{k: getattr(col, k) for k in (
+        'M', 'n_0', 'Tco', 'g', 'dzi', 'Kzz', 'vz', 'Ti', 'Hpi', 'Hp', 'pico', 'dz', 'Dzz',
+        'ms', 'alpha', 'top_flux', 'bot_flux', 'bot_vdep', 'pref_indx')})
+    return cls(), var, atm, chans, calls
+
+
+def test_dropin_radiative_transfer_dispatch():
+    """Ros2GPU keeps the reference's own compute_tau / compute_flux /
+    compute_J where the device path does not apply (T-dependent cross
+    sections); otherwise compute_tau and compute_flux leave var alone and the
+    device work happens in compute_J."""
+    from helpers import golden, network
+    d = _fixture()
+    s, var, atm, _, calls = _dropin(d, network('c1'), golden('c1'), T_cross_sp=['CO2'])
+    for f in (s.compute_tau, s.compute_flux, s.compute_J):
+        f(var, atm)
+    assert calls == ['tau', 'flux', 'J']
+    s, var, atm, _, calls = _dropin(d, network('c1'), golden('c1'))
+    s.compute_tau(var, atm)
+    s.compute_flux(var, atm)
+    assert calls == [] and not hasattr(var, 'tau')
+
+
+@pytest.mark.gpu
+def test_dropin_radiative_transfer_matches_reference():
+    """Ros2GPU.compute_tau / compute_flux / compute_J in the reference's call
+    order on the c1 column: var.tau, var.aflux, var.J_sp and the photolysis
+    k against the reference's records of its set-up call and its first
+    update (whose aflux_change reads the set-up call's flux).  The absorbers
+    are summed in this process's set order, not the recording's, so the
+    actinic flux is held to 1e-10 here (1.6e-11 seen); the kernel's own
+    parity on identical tables is test_device_radiative_transfer_matches_oracle."""
+    from helpers import golden, network
+    from vulcan_gb300 import _build
+    _build.build()
+    d = _fixture()
+    g = golden('c1')
+    s, var, atm, chans, calls = _dropin(d, network('c1'), g)
+    nz = d['rec0_y'].shape[0]
+    for rec in ('rec0', 'rec1'):
+        for f in (s.compute_tau, s.compute_flux, s.compute_J):
+            f(var, atm)
+        if rec == 'rec0':
+            assert _rel(var.tau, d['rec0_tau']) < 1e-13
+        assert _rel(var.aflux, d[rec + '_aflux'], 1e-30) < 1e-10
+        J = np.array([var.J_sp[c] for c in chans])
+        assert _rel(J, d[rec + '_J']) < 1e-10
+        for c, ki in var.pho_rate_index.items():
+            np.testing.assert_array_equal(var.k[ki], var.J_sp[c] * float(d['f_diurnal']))
+        for sp in var.photo_sp:
+            tot = sum(var.J_sp[c] for c in chans if c[0] == sp)
+            np.testing.assert_allclose(var.J_sp[(sp, 0)], tot, rtol=1e-14)
+    assert abs(var.aflux_change / float(d['rec1_aflux_change']) - 1) < 1e-9
+    assert var.tau.shape == (nz + 1, len(d['bins'])) and calls == []
+    s._vk_h.close()

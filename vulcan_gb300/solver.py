@@ -397,6 +397,69 @@ class Ros2GPUMixin:
         para.delta = float(out['delta'][0])
         return var, para
 
+    # ---- photochemistry: the reference calls compute_tau, compute_flux and
+    # compute_J in that order (vulcan.py:172-174 before the loop,
+    # op.py:826-828 inside it); the device does all three in compute_J
+    # (vk_photo_update), on the tables the reference's own set-up left in var
+    # (make_bins_read_cross, read_sflux).  The diffuse fluxes persist on the
+    # device between calls, as var.dflux_u / var.dflux_d do in the reference.
+    # Temperature-dependent cross sections and photoionisation keep the
+    # reference's own methods (the device path does not implement them).
+    def _vk_photo_gpu(self):
+        cfg = self._vk_cfg
+        return not getattr(cfg, 'T_cross_sp', []) and not getattr(cfg, 'use_ion', False)
+
+    def compute_tau(self, var, atm):
+        if not self._vk_photo_gpu():
+            return super().compute_tau(var, atm)
+
+    def compute_flux(self, var, atm):
+        if not self._vk_photo_gpu():
+            return super().compute_flux(var, atm)
+
+    def compute_J(self, var, atm):
+        if not self._vk_photo_gpu():
+            return super().compute_J(var, atm)
+        from . import photo
+        cfg = self._vk_cfg
+        if getattr(self, '_vk_h', None) is None:
+            self._vk_setup(var, atm)
+        h = self._vk_h
+        h.set_columns(self._vk_pack(var, atm))
+        net = self._vk_gnet.net
+        if getattr(h, 'photo_dims', None) is None:
+            chans = sorted(var.pho_rate_index)
+            # absorbers in the order the reference's compute_tau sums them
+            ps = var.photo_sp if isinstance(var.photo_sp, set) else set(var.photo_sp)
+            absp = list(set.union(ps, getattr(var, 'ion_sp', set())))
+            t = photo.PhotoTables(
+                bins=np.asarray(var.bins, float), dbin1=float(var.dbin1), dbin2=float(var.dbin2),
+                i12=int(var.sflux_din12_indx), sflux_top=np.asarray(var.sflux_top, float),
+                absp_sp=absp, cross=np.array([var.cross[sp] for sp in absp]),
+                scat_sp=list(cfg.scat_sp), cross_scat=np.array([var.cross_scat[sp] for sp in cfg.scat_sp]),
+                ch_sp=[c[0] for c in chans], ch_br=[c[1] for c in chans],
+                cross_J=np.array([var.cross_J[c] for c in chans]), sl_angle=float(cfg.sl_angle),
+                edd=float(cfg.edd), f_diurnal=float(cfg.f_diurnal), flux_atol=float(cfg.flux_atol))
+            photo.attach(h, t, net)
+            self._vk_photo_chans = chans
+        change = h.photo_update()
+        tau, aflux, J = h.photo_get()
+        nz = var.y.shape[0]
+        var.tau = tau[:nz + 1]
+        if hasattr(var, 'aflux'):
+            var.prev_aflux = var.aflux
+        var.aflux = aflux
+        var.sflux = var.sflux_top * np.exp(-1. * var.tau / np.cos(cfg.sl_angle))
+        var.aflux_change = float(change[0])
+        remove = set(getattr(cfg, 'remove_list', []))
+        var.J_sp = {(sp, 0): np.zeros(nz) for sp in var.photo_sp}
+        for ch, (sp, br) in enumerate(self._vk_photo_chans):
+            var.J_sp[(sp, br)] = J[:, ch].copy()
+            var.J_sp[(sp, 0)] += J[:, ch]
+            i = var.pho_rate_index[(sp, br)]
+            if i not in remove:
+                var.k[i] = J[:, ch] * cfg.f_diurnal
+
 
 class _AtmView:
     """Adapter: a reference AtmData object seen as a column.Column."""
