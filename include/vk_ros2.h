@@ -222,13 +222,27 @@ VK_API int  vk_get_k(vk_handle *h, double *k);
  * J * f_diurnal into the channels' k slots and each column's largest
  * relative actinic-flux change where the flux exceeds flux_atol
  * (var.aflux_change) into the run state -- the steady-state test of vk_run
- * requires it below vk_ctrl.flux_cri -- and into aflux_change if given.  No counterpart for
- * the T-dependent cross sections or photoionisation yet. */
+ * requires it below vk_ctrl.flux_cri -- and into aflux_change if given.  No
+ * counterpart for photoionisation yet. */
 VK_API int  vk_photo_setup(vk_handle *h, int nbins, const double *bins, const double *jweights,
                            int nabs, const int *abs_sp, const int *abs_photo, const double *cross,
                            int nscat, const int *scat_sp, const double *cross_scat, int nch,
                            const int *ch_kindex, const double *cross_J, const double *sflux_top,
                            double sl_angle, double edd, double f_diurnal, double flux_atol);
+/* Temperature-dependent cross sections (vulcan_cfg.T_cross_sp): per-layer
+ * tables replacing, in the optical depth, the absorption cross section of
+ * some absorbers and, in J, the photolysis cross section of some channels --
+ * var.cross_T / var.cross_J_T of op.ReadRate.make_bins_read_cross
+ * (op.py:640-745) as compute_tau (op.py:2591-2592) and compute_J
+ * (op.py:2770-2774) read them; the single-scattering albedo keeps the
+ * T-independent cross sections (op.py:2623-2624).  abs_slot[i] / ch_slot[i]:
+ * position in vk_photo_setup's absorber / channel list (each at most once);
+ * cross_T [nabs_t][L][nbins] and cross_J_T [nch_t][L][nbins] over the layers
+ * of the current batch (call after vk_set_columns, again when the columns
+ * change).  Replaces earlier tables; nabs_t = nch_t = 0 removes them. */
+VK_API int  vk_photo_set_cross_T(vk_handle *h, int nabs_t, const int *abs_slot,
+                                 const double *cross_T, int nch_t, const int *ch_slot,
+                                 const double *cross_J_T);
 VK_API int  vk_photo_reset(vk_handle *h);
 VK_API int  vk_photo_update(vk_handle *h, const int *col_mask, double *aflux_change);
 /* Diagnostic: tau [(L + ncols)][nbins] (staggered, column c from row

@@ -14,14 +14,17 @@ import numpy as np
 HC = 1.98644582E-9        # erg nm (phy_const.py)
 
 
-def compute_tau(y, dz, absp_idx, cross, scat_idx, cross_scat):
+def compute_tau(y, dz, absp_idx, cross, scat_idx, cross_scat, cross_T=None):
     """tau [nz+1, nbins]: absorbers (photo and ion species) and Rayleigh
-    scatterers summed layer by layer from the top (op.py:2580-2599)."""
+    scatterers summed layer by layer from the top (op.py:2580-2599).
+    cross_T {absorber position: [nz, nbins]}: the per-layer cross sections
+    of the temperature-dependent absorbers (op.py:2591-2592)."""
     nz = y.shape[0]
+    cross_T = cross_T or {}
     tau = np.zeros((nz + 1, cross.shape[1]))
     for j in range(nz - 1, -1, -1):
         for a, s in enumerate(absp_idx):
-            tau[j] += y[j, s] * dz[j] * cross[a]
+            tau[j] += y[j, s] * dz[j] * (cross_T[a][j] if a in cross_T else cross[a])
         for a, s in enumerate(scat_idx):
             tau[j] += y[j, s] * dz[j] * cross_scat[a]
         tau[j] += tau[j + 1]
@@ -92,7 +95,12 @@ def j_weights(nbins, i12, dbin1, dbin2):
     return w
 
 
-def compute_J(aflux, cross_J, weights):
-    """J [nch, nz] of every photolysis channel (op.py:2751-2786, T-independent
-    cross sections): sum over bins of aflux x cross_J x weights."""
-    return (aflux[None, :, :] * cross_J[:, None, :] * weights[None, None, :]).sum(axis=2)
+def compute_J(aflux, cross_J, weights, cross_J_T=None):
+    """J [nch, nz] of every photolysis channel (op.py:2751-2786): sum over
+    bins of aflux x cross_J x weights; cross_J_T {channel position: [nz,
+    nbins]} replaces cross_J by per-layer cross sections for the channels of
+    temperature-dependent species (op.py:2770-2774)."""
+    J = (aflux[None, :, :] * cross_J[:, None, :] * weights[None, None, :]).sum(axis=2)
+    for c, cj in (cross_J_T or {}).items():
+        J[c] = (aflux * cj * weights[None, :]).sum(axis=1)
+    return J

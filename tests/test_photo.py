@@ -1,6 +1,8 @@
 """Photochemistry radiative transfer: the oracle against the reference's own
-compute_tau / compute_flux / compute_J (fixture c1rt, recorded with the
-reference's radiative transfer on), and the device path against the oracle."""
+compute_tau / compute_flux / compute_J (fixtures c1rt and, with
+temperature-dependent cross sections for CO2, H2O and NH3, c1rtT, recorded
+with the reference's radiative transfer on), and the device path against
+the oracle."""
 import os
 
 import numpy as np
@@ -10,8 +12,8 @@ from conftest import GOLDEN
 from oracle import photo as P
 
 
-def _fixture():
-    d = dict(np.load(os.path.join(GOLDEN, 'golden_c1rt.npz'), allow_pickle=False))
+def _fixture(tag='c1rt'):
+    d = dict(np.load(os.path.join(GOLDEN, 'golden_%s.npz' % tag), allow_pickle=False))
     spec = [str(s) for s in d['spec_list']]
     d['absp_idx'] = [spec.index(str(s)) for s in d['absp_sp']]
     d['photo_idx'] = [spec.index(str(s)) for s in d['photo_sp']]
@@ -20,16 +22,26 @@ def _fixture():
     d['cross_photo'] = np.array([d['cross'][absp.index(str(s))] for s in d['photo_sp']])
     d['weights'] = P.j_weights(len(d['bins']), int(d['sflux_din12_indx']), float(d['dbin1']),
                                float(d['dbin2']))
+    # temperature-dependent tables keyed by absorber / channel position
+    chans = list(zip([str(s) for s in d['ch_sp']], [int(b) for b in d['ch_br']]))
+    d['chans'] = chans
+    d['cross_T_at'], d['cross_J_T_at'] = {}, {}
+    if 'T_cross_sp' in d:
+        for i, sp in enumerate(d['T_cross_sp']):
+            d['cross_T_at'][absp.index(str(sp))] = d['cross_T'][i]
+        for i, c in enumerate(zip([str(s) for s in d['chT_sp']], [int(b) for b in d['chT_br']])):
+            d['cross_J_T_at'][chans.index(c)] = d['cross_J_T'][i]
     return d
 
 
 def _oracle_call(d, y, ymix, dz, du, dd, prev=None):
-    tau = P.compute_tau(y, dz, d['absp_idx'], d['cross'], d['scat_idx'], d['cross_scat'])
+    tau = P.compute_tau(y, dz, d['absp_idx'], d['cross'], d['scat_idx'], d['cross_scat'],
+                        d['cross_T_at'])
     af, _, ch = P.compute_flux(tau, ymix, d['photo_idx'], d['cross_photo'], d['scat_idx'],
                                d['cross_scat'], d['sflux_top'], d['bins'], float(d['sl_angle']),
                                float(d['edd']), du, dd, aflux_prev=prev,
                                flux_atol=float(d['flux_atol']))
-    return tau, af, P.compute_J(af, d['cross_J'], d['weights']), ch
+    return tau, af, P.compute_J(af, d['cross_J'], d['weights'], d['cross_J_T_at']), ch
 
 
 def _rel(a, b, floor=1e-300):
@@ -37,8 +49,9 @@ def _rel(a, b, floor=1e-300):
     return float(np.max(np.abs(a - b)[m] / np.abs(b)[m]))
 
 
-def test_oracle_matches_reference_records():
-    d = _fixture()
+@pytest.mark.parametrize('tag', ['c1rt', 'c1rtT'])
+def test_oracle_matches_reference_records(tag):
+    d = _fixture(tag)
     nz, nb = d['rec0_y'].shape[0], len(d['bins'])
     du, dd = np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb))
     # first call (set-up), then the integrator's first update on the same state
@@ -54,6 +67,11 @@ def test_oracle_matches_reference_records():
     np.testing.assert_allclose(du, d['rec1_dflux_u'], rtol=1e-10, atol=1e-12 * np.abs(du).max())
     _, af2, J2, _ = _oracle_call(d, d['rec2_y'], d['rec2_ymix'], d['rec2_dz'], du, dd, af1)
     assert _rel(af2, d['rec2_aflux'], 1e-30) < 1e-12 and _rel(J2, d['rec2_J']) < 1e-11
+    if d['cross_J_T_at']:             # the per-layer tables change J well above rounding
+        e = dict(d, cross_T_at={}, cross_J_T_at={})
+        du, dd = np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb))
+        _, _, J0, _ = _oracle_call(e, d['rec0_y'], d['rec0_ymix'], d['rec0_dz'], du, dd)
+        assert _rel(J0, d['rec0_J']) > 1e-3
 
 
 def test_host_tables_match_the_reference_set_up():
@@ -62,6 +80,7 @@ def test_host_tables_match_the_reference_set_up():
     files (differences recorded by the fixture generator)."""
     d = _fixture()
     assert bool(d['setup_same_layout'])
+    assert bool(_fixture('c1rtT')['setup_same_layout'])
     for key in ('bins', 'cross', 'cross_J', 'cross_scat', 'sflux_top'):
         assert float(d['setup_rel_' + key]) <= 1e-15, key
 
@@ -77,20 +96,33 @@ def test_j_weights_follow_the_reference_sums():
         assert abs(f @ P.j_weights(20, i12, 0.1, 2.0) - ref) < 1e-13
 
 
+def _attach(h, d, net):
+    """The fixture's tables on a handle whose batch is the c1 column."""
+    from vulcan_gb300 import photo
+    photo.attach(h, photo.PhotoTables.from_fixture(d), net)
+    if 'T_cross_sp' in d:
+        photo.attach_cross_T(
+            h, {str(sp): d['cross_T'][i] for i, sp in enumerate(d['T_cross_sp'])},
+            {(str(sp), int(br)): d['cross_J_T'][i]
+             for i, (sp, br) in enumerate(zip(d['chT_sp'], d['chT_br']))})
+
+
 @pytest.mark.gpu
-def test_device_radiative_transfer_matches_oracle():
+@pytest.mark.parametrize('tag', ['c1rt', 'c1rtT'])
+def test_device_radiative_transfer_matches_oracle(tag):
     """vk_photo_update on the c1 column (the reference's set-up arrays) from
     the recorded states: tau, actinic flux, J and the k slots, over the three
-    recorded calls (the diffuse fluxes persist between calls)."""
+    recorded calls (the diffuse fluxes persist between calls); c1rtT with
+    per-layer cross sections (vk_photo_set_cross_T)."""
     from test_gpu_parity import make_handle
-    from vulcan_gb300 import _build, photo
+    from vulcan_gb300 import _build
     from vulcan_gb300.capi import ATM_DZ
     _build.build()
-    d = _fixture()
+    d = _fixture(tag)
     g, net, gn, h, b = make_handle('c1')
     np.testing.assert_allclose(g['dz'], d['rec0_dz'], rtol=1e-14)
-    tables = photo.PhotoTables.from_fixture(d)
-    photo.attach(h, tables, net)
+    np.testing.assert_array_equal(g['Tco'], d['Tco'])
+    _attach(h, d, net)
     nz = d['rec0_y'].shape[0]
     nb = len(d['bins'])
     du, dd = np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb))
@@ -119,21 +151,23 @@ def test_device_radiative_transfer_matches_oracle():
 
 
 @pytest.mark.gpu
-def test_device_run_with_photo_tracks_reference():
+@pytest.mark.parametrize('tag', ['c1rt', 'c1rtT'])
+def test_device_run_with_photo_tracks_reference(tag):
     """vk_run with the reference's photochemistry schedule from the c1rt
-    set-up: J recomputed at count 0 (twice, as the reference's set-up and its
-    first loop iteration do), the state after 100 steps and the J of the
-    update at count 100 against the reference's records."""
+    (c1rtT: T-dependent cross sections) set-up: J recomputed at count 0
+    (twice, as the reference's set-up and its first loop iteration do), the
+    state after 100 steps and the J of the update at count 100 against the
+    reference's records."""
     from helpers import floor_err
     from test_gpu_parity import make_handle
-    from vulcan_gb300 import _build, batch, configs, photo
+    from vulcan_gb300 import _build, batch, configs
     from vulcan_gb300.solver import ctrl_from
     _build.build()
-    d = _fixture()
+    d = _fixture(tag)
     g, net, gn, h, b = make_handle('c1')
     h.set_atom_ini(g['atom_ini'][None, :])
     h.set_clock(dt=1e-10, t=0.0, count=0)
-    photo.attach(h, photo.PhotoTables.from_fixture(d), net)
+    _attach(h, d, net)
     h.photo_update()                                   # the set-up call
     ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
     st = batch.run_with_photo(h, ctrl, max_steps=100)
@@ -181,7 +215,7 @@ def test_photo_schedule_follows_the_reference():
     assert col1[:2] == [0, 100] and col1[2:] == list(range(150, 300, 5))
 
 
-def _dropin(d, net, g, T_cross_sp=()):
+def _dropin(d, net, g, use_ion=False):
     """Ros2GPU over a stand-in op module whose own radiative transfer records
     its calls, with the c1 column's set-up arrays as var/atm."""
     import types
@@ -202,8 +236,9 @@ def _dropin(d, net, g, T_cross_sp=()):
     op = types.SimpleNamespace(Ros2=FakeRos2)
     cfg = types.SimpleNamespace(
         network=None, use_photo=True, atom_list=[str(a) for a in g['atom_list']],
-        use_moldiff=True, use_topflux=False, use_botflux=False, T_cross_sp=list(T_cross_sp),
-        use_ion=False, scat_sp=[str(s) for s in d['scat_sp']], sl_angle=float(d['sl_angle']),
+        use_moldiff=True, use_topflux=False, use_botflux=False,
+        T_cross_sp=[str(sp) for sp in d.get('T_cross_sp', [])],
+        use_ion=use_ion, scat_sp=[str(s) for s in d['scat_sp']], sl_angle=float(d['sl_angle']),
         edd=float(d['edd']), f_diurnal=float(d['f_diurnal']), flux_atol=float(d['flux_atol']),
         remove_list=[])
     cls = make_ros2gpu(op, cfg, net.species)
@@ -221,6 +256,10 @@ def _dropin(d, net, g, T_cross_sp=()):
         cross_scat={str(sp): d['cross_scat'][i] for i, sp in enumerate(d['scat_sp'])},
         cross_J={c: d['cross_J'][i] for i, c in enumerate(chans)},
         aflux=np.zeros((d['rec0_y'].shape[0], len(d['bins']))))
+    if 'T_cross_sp' in d:
+        var.cross_T = {str(sp): d['cross_T'][i] for i, sp in enumerate(d['T_cross_sp'])}
+        var.cross_J_T = {(str(sp), int(br)): d['cross_J_T'][i]
+                         for i, (sp, br) in enumerate(zip(d['chT_sp'], d['chT_br']))}
     col = column_from_golden(g)
     atm = types.SimpleNamespace(**{k: getattr(col, k) for k in (
         'M', 'n_0', 'Tco', 'g', 'dzi', 'Kzz', 'vz', 'Ti', 'Hpi', 'Hp', 'pico', 'dz', 'Dzz',
@@ -230,12 +269,12 @@ def _dropin(d, net, g, T_cross_sp=()):
 
 def test_dropin_radiative_transfer_dispatch():
     """Ros2GPU keeps the reference's own compute_tau / compute_flux /
-    compute_J where the device path does not apply (T-dependent cross
-    sections); otherwise compute_tau and compute_flux leave var alone and the
-    device work happens in compute_J."""
+    compute_J where the device path does not apply (photoionisation);
+    otherwise compute_tau and compute_flux leave var alone and the device
+    work happens in compute_J."""
     from helpers import golden, network
     d = _fixture()
-    s, var, atm, _, calls = _dropin(d, network('c1'), golden('c1'), T_cross_sp=['CO2'])
+    s, var, atm, _, calls = _dropin(d, network('c1'), golden('c1'), use_ion=True)
     for f in (s.compute_tau, s.compute_flux, s.compute_J):
         f(var, atm)
     assert calls == ['tau', 'flux', 'J']
@@ -246,18 +285,20 @@ def test_dropin_radiative_transfer_dispatch():
 
 
 @pytest.mark.gpu
-def test_dropin_radiative_transfer_matches_reference():
+@pytest.mark.parametrize('tag', ['c1rt', 'c1rtT'])
+def test_dropin_radiative_transfer_matches_reference(tag):
     """Ros2GPU.compute_tau / compute_flux / compute_J in the reference's call
     order on the c1 column: var.tau, var.aflux, var.J_sp and the photolysis
     k against the reference's records of its set-up call and its first
     update (whose aflux_change reads the set-up call's flux).  The absorbers
     are summed in this process's set order, not the recording's, so the
     actinic flux is held to 1e-10 here (1.6e-11 seen); the kernel's own
-    parity on identical tables is test_device_radiative_transfer_matches_oracle."""
+    parity on identical tables is test_device_radiative_transfer_matches_oracle.
+    c1rtT: CO2, H2O and NH3 with the reference's per-layer cross sections."""
     from helpers import golden, network
     from vulcan_gb300 import _build
     _build.build()
-    d = _fixture()
+    d = _fixture(tag)
     g = golden('c1')
     s, var, atm, chans, calls = _dropin(d, network('c1'), g)
     nz = d['rec0_y'].shape[0]

@@ -35,7 +35,7 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
-           'vk_photo_update', 'vk_photo_get')
+           'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T')
 
 
 class VkNetworkDesc(C.Structure):
@@ -109,6 +109,7 @@ def lib(path=None):
         'vk_photo_reset': (i, [vp]),
         'vk_photo_update': (i, [vp, pi, pd]),
         'vk_photo_get': (i, [vp, pd, pd, pd]),
+        'vk_photo_set_cross_T': (i, [vp, i, pi, pd, i, pi, pd]),
         'vk_get_timing': (i, [vp, pd, pd, pd, pd, pi]),
         'vk_chem_source': (i, [vp, pd, pd]),
         'vk_get_lhs': (i, [vp, pd, pd, pd, pd]),

@@ -48,6 +48,10 @@ struct vk_handle {
     int *d_order = nullptr;             // columns by decreasing nz
     PhotoDev ph{};                  // radiative transfer (vk_photo_setup)
     int *d_phmask = nullptr;            // [max_cols] columns of a masked photo update
+    std::vector<double> ph_jw;          // J bin weights (host copy, weights cross_J_T)
+    int *d_abs_tslot = nullptr, *d_ch_tslot = nullptr;   // vk_photo_set_cross_T
+    double *d_crossT = nullptr, *d_wcrossJT = nullptr;
+    int tcap_abs = 0, tcap_ch = 0;      // table rows allocated
     int *d_kkind = nullptr, *d_krev = nullptr;   // rate-constant parameters (vk_set_rate_params)
     double *d_kpar = nullptr, *d_nasa9 = nullptr;
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
@@ -119,6 +123,16 @@ static int dalloc(vk_handle *h, T **p, size_t count) {
     }
     h->allocs.push_back((void *)*p);
     return VK_OK;
+}
+
+static void dfree(vk_handle *h, void *p) {
+    if (!p) return;
+    for (size_t i = 0; i < h->allocs.size(); ++i)
+        if (h->allocs[i] == p) {
+            h->allocs.erase(h->allocs.begin() + (long)i);
+            break;
+        }
+    cudaFree(p);
 }
 
 template <typename T>
@@ -664,11 +678,78 @@ extern "C" int vk_photo_setup(vk_handle *h, int nbins, const double *bins, const
     p.bins = db; p.cross = dc; p.cross_scat = dsc; p.wcross_J = dw; p.sflux_top = dtop;
     p.abs_sp = das; p.abs_photo = dap; p.scat_sp = dss; p.ch_kindex = dki;
     p.nabs = nabs; p.nscat = nscat; p.nch = nch;
+    p.abs_tslot = nullptr; p.cross_T = nullptr; p.ch_tslot = nullptr; p.wcross_J_T = nullptr;
+    p.lstride = h->max_layers;
+    h->ph_jw.assign(jweights, jweights + nbins);
     p.sl_angle = sl_angle; p.edd = edd; p.f_diurnal = f_diurnal; p.flux_atol = flux_atol;
     VK_CUDA(h, cudaMemset(p.dflux_u, 0, st * sizeof(double)));
     VK_CUDA(h, cudaMemset(p.dflux_d, 0, st * sizeof(double)));
     VK_CUDA(h, cudaMemset(p.aflux, 0, ly * sizeof(double)));
     p.nbins = nbins;
+    return VK_OK;
+}
+
+extern "C" int vk_photo_set_cross_T(vk_handle *h, int nabs_t, const int *abs_slot,
+                                    const double *cross_T, int nch_t, const int *ch_slot,
+                                    const double *cross_J_T) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    PhotoDev &p = h->ph;
+    if (!p.nbins) return fail(h, VK_EINVAL, "no radiative transfer (call vk_photo_setup)");
+    if (nabs_t < 0 || nabs_t > p.nabs || nch_t < 0 || nch_t > p.nch)
+        return fail(h, VK_EINVAL, "nabs_t / nch_t out of range");
+    if ((nabs_t && (!abs_slot || !cross_T)) || (nch_t && (!ch_slot || !cross_J_T)))
+        return fail(h, VK_EINVAL, "T-dependent cross-section array is NULL");
+    std::vector<int> at(p.nabs, -1), ct(p.nch, -1);
+    for (int i = 0; i < nabs_t; ++i) {
+        if (abs_slot[i] < 0 || abs_slot[i] >= p.nabs || at[abs_slot[i]] >= 0)
+            return fail(h, VK_EINVAL, "absorber slot out of range or repeated");
+        at[abs_slot[i]] = i;
+    }
+    for (int i = 0; i < nch_t; ++i) {
+        if (ch_slot[i] < 0 || ch_slot[i] >= p.nch || ct[ch_slot[i]] >= 0)
+            return fail(h, VK_EINVAL, "channel slot out of range or repeated");
+        ct[ch_slot[i]] = i;
+    }
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));   // no update reads the tables meanwhile
+    p.abs_tslot = nullptr; p.cross_T = nullptr; p.ch_tslot = nullptr; p.wcross_J_T = nullptr;
+    if (!nabs_t && !nch_t) return VK_OK;
+    const size_t NB = (size_t)p.nbins, LS = (size_t)h->max_layers, L = (size_t)h->L;
+    if (!h->d_abs_tslot) {
+        rc = dalloc(h, &h->d_abs_tslot, (size_t)p.nabs);
+        if (!rc) rc = dalloc(h, &h->d_ch_tslot, (size_t)p.nch);
+        if (rc) return rc;
+    }
+    if (nabs_t > h->tcap_abs) {
+        dfree(h, h->d_crossT);
+        h->d_crossT = nullptr;
+        h->tcap_abs = 0;
+        if ((rc = dalloc(h, &h->d_crossT, (size_t)nabs_t * LS * NB))) return rc;
+        h->tcap_abs = nabs_t;
+    }
+    if (nch_t > h->tcap_ch) {
+        dfree(h, h->d_wcrossJT);
+        h->d_wcrossJT = nullptr;
+        h->tcap_ch = 0;
+        if ((rc = dalloc(h, &h->d_wcrossJT, (size_t)nch_t * LS * NB))) return rc;
+        h->tcap_ch = nch_t;
+    }
+    VK_CUDA(h, cudaMemcpy(h->d_abs_tslot, at.data(), at.size() * sizeof(int), cudaMemcpyHostToDevice));
+    VK_CUDA(h, cudaMemcpy(h->d_ch_tslot, ct.data(), ct.size() * sizeof(int), cudaMemcpyHostToDevice));
+    for (int i = 0; i < nabs_t; ++i)
+        VK_CUDA(h, cudaMemcpy(h->d_crossT + i * LS * NB, cross_T + i * L * NB, L * NB * sizeof(double),
+                              cudaMemcpyHostToDevice));
+    std::vector<double> w(L * NB);
+    for (int i = 0; i < nch_t; ++i) {
+        const double *src = cross_J_T + i * L * NB;
+        for (size_t l = 0; l < L; ++l)
+            for (size_t n = 0; n < NB; ++n) w[l * NB + n] = src[l * NB + n] * h->ph_jw[n];
+        VK_CUDA(h, cudaMemcpy(h->d_wcrossJT + i * LS * NB, w.data(), L * NB * sizeof(double),
+                              cudaMemcpyHostToDevice));
+    }
+    p.abs_tslot = h->d_abs_tslot; p.cross_T = h->d_crossT;
+    p.ch_tslot = h->d_ch_tslot; p.wcross_J_T = h->d_wcrossJT;
+    p.lstride = (int)LS;
     return VK_OK;
 }
 

@@ -133,6 +133,12 @@ struct PhotoDev {
     double *tau, *dflux_u, *dflux_d;   // [(L + ncols)][nbins] staggered
     double *w0, *aflux, *aflux_prev;   // [L][nbins]
     double *J;                 // [L][nch]
+    // temperature-dependent cross sections (vk_photo_set_cross_T); NULL: none
+    const int *abs_tslot;      // [nabs] row of cross_T, or -1
+    const double *cross_T;     // [nabs_t][lstride][nbins]
+    const int *ch_tslot;       // [nch] row of wcross_J_T, or -1
+    const double *wcross_J_T;  // [nch_t][lstride][nbins] x J bin weight
+    int lstride;               // layer stride of the per-layer tables
 };
 
 // Launch helpers implemented in vk_kernels.cu (all asynchronous on stream).

@@ -6,6 +6,9 @@
 // compute_J (op.py:2751-2786, T-independent cross sections) on the binned
 // cross sections the host set-up provides (make_bins_read_cross, read_sflux).
 //
+// compute_tau's T-dependent branch (op.py:2591-2592) and compute_J's
+// (op.py:2770-2774) read per-layer tables where vk_photo_set_cross_T gave them.
+//
 //   k_photo_flux  one thread per (column, wavelength bin): tau from the top,
 //                 single-scattering albedo, the downward then upward sweeps of
 //                 the diffuse fluxes (the downward sweep reads the previous
@@ -52,7 +55,9 @@ k_photo_flux(DevNet net, DevBatch b, PhotoDev ph, const double *__restrict__ y,
         for (int a = 0; a < ph.nabs; ++a) {
             const double cr = ph.cross[(size_t)a * NB + n];
             const int s = ph.abs_sp[a];
-            t += y[l * ni + s] * dz * cr;
+            const int ts = ph.abs_tslot ? ph.abs_tslot[a] : -1;
+            const double crt = ts < 0 ? cr : ph.cross_T[((size_t)ts * ph.lstride + l) * NB + n];
+            t += y[l * ni + s] * dz * crt;
             if (ph.abs_photo[a]) tabs += ymix[l * ni + s] * cr;
         }
         for (int a = 0; a < ph.nscat; ++a) {
@@ -123,7 +128,9 @@ k_photo_J(DevNet net, DevBatch b, PhotoDev ph, double *k, unsigned long long *ch
     const double *af = ph.aflux + (size_t)l * NB;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;
     for (int ch = 0; ch < ph.nch; ++ch) {
-        const double *wj = ph.wcross_J + (size_t)ch * NB;
+        const int ts = ph.ch_tslot ? ph.ch_tslot[ch] : -1;
+        const double *wj = ts < 0 ? ph.wcross_J + (size_t)ch * NB
+                                  : ph.wcross_J_T + ((size_t)ts * ph.lstride + l) * NB;
         double s = 0.0;
         for (int n = tid; n < NB; n += blockDim.x) s += af[n] * wj[n];
         for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

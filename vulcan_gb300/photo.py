@@ -3,7 +3,9 @@ path (vk_photo_setup / vk_photo_update) runs on.
 
 Restates the reference's make_bins_read_cross (op.py:495-782) and read_sflux
 (build_atm.py:617-656) for T-independent cross sections without
-photoionisation (the reference's defaults: T_cross_sp = [], use_ion = False):
+photoionisation (the reference's defaults: T_cross_sp = [], use_ion = False);
+per-layer temperature-dependent tables (T_cross_sp) are uploaded as given
+(attach_cross_T), e.g. the reference's own var.cross_T / var.cross_J_T:
 
 * bins: from the shortest absorption edge (not below the stellar file's
   first wavelength or 2 nm) to min(longest edge, the file's last wavelength
@@ -153,3 +155,29 @@ def attach(handle, tables, net):
         len(kidx), ptr(kidx, C.c_int), ptr(c(tables.cross_J)), ptr(c(tables.sflux_top)),
         tables.sl_angle, tables.edd, tables.f_diurnal, tables.flux_atol), handle.h)
     handle.photo_dims = (len(tables.bins), len(kidx))
+    handle.photo_tables = tables
+
+
+def attach_cross_T(handle, cross_T, cross_J_T):
+    """vk_photo_set_cross_T for the handle's current batch: cross_T {absorber:
+    [L, nbins]} and cross_J_T {(species, branch): [L, nbins]} -- the
+    reference's var.cross_T / var.cross_J_T (op.py:640-745), the layers of the
+    batch's columns stacked in batch order.  Empty dicts remove the tables."""
+    from .capi import check, lib, ptr
+    t = handle.photo_tables
+    L, nb = handle.batch.L, len(t.bins)
+    chans = list(zip(t.ch_sp, t.ch_br))
+    aslot = np.array([t.absp_sp.index(sp) for sp in cross_T], dtype=np.int32)
+    cslot = np.array([chans.index(tuple(c)) for c in cross_J_T], dtype=np.int32)
+
+    def stack(tab):
+        if not tab:
+            return None
+        a = np.ascontiguousarray(np.array([tab[key] for key in tab], dtype=np.float64))
+        if a.shape[1:] != (L, nb):
+            raise ValueError('per-layer cross sections must be [L, nbins] = [%d, %d]' % (L, nb))
+        return a
+
+    ct, cj = stack(cross_T), stack(cross_J_T)
+    check(lib().vk_photo_set_cross_T(handle.h, len(aslot), ptr(aslot, C.c_int), ptr(ct),
+                                     len(cslot), ptr(cslot, C.c_int), ptr(cj)), handle.h)

@@ -403,11 +403,11 @@ class Ros2GPUMixin:
     # (vk_photo_update), on the tables the reference's own set-up left in var
     # (make_bins_read_cross, read_sflux).  The diffuse fluxes persist on the
     # device between calls, as var.dflux_u / var.dflux_d do in the reference.
-    # Temperature-dependent cross sections and photoionisation keep the
-    # reference's own methods (the device path does not implement them).
+    # Temperature-dependent cross sections (T_cross_sp) use the reference's
+    # per-layer var.cross_T / var.cross_J_T.  Photoionisation keeps the
+    # reference's own methods (the device path does not implement it).
     def _vk_photo_gpu(self):
-        cfg = self._vk_cfg
-        return not getattr(cfg, 'T_cross_sp', []) and not getattr(cfg, 'use_ion', False)
+        return not getattr(self._vk_cfg, 'use_ion', False)
 
     def compute_tau(self, var, atm):
         if not self._vk_photo_gpu():
@@ -442,6 +442,10 @@ class Ros2GPUMixin:
                 edd=float(cfg.edd), f_diurnal=float(cfg.f_diurnal), flux_atol=float(cfg.flux_atol))
             photo.attach(h, t, net)
             self._vk_photo_chans = chans
+            tsp = set(getattr(cfg, 'T_cross_sp', []))
+            if tsp:
+                photo.attach_cross_T(h, {sp: var.cross_T[sp] for sp in absp if sp in tsp},
+                                     {c: var.cross_J_T[c] for c in chans if c[0] in tsp})
         change = h.photo_update()
         tau, aflux, J = h.photo_get()
         nz = var.y.shape[0]
