@@ -202,6 +202,14 @@ VK_API int  vk_get_timing(vk_handle *h, double *ms_rates, double *ms_lu, double 
 #define VK_K_SPECIAL_OH_CH3 3
 VK_API int  vk_set_rate_params(vk_handle *h, const int *kind, const int *rev, const double *params,
                                const double *nasa9);
+/* Low-temperature caps (use_lowT_limit_rates; op.ReadRate.lim_lowT_rates,
+ * op.py:320-342): per pair, kind VK_K_NONE (no cap), VK_K_ARRHENIUS or
+ * VK_K_FALLOFF with params [6] as in vk_set_rate_params; where the layer's
+ * T <= t_max, vk_compute_k takes the cap's form as the forward rate and
+ * forms the reverse rate from it (the reference's order).  kind = NULL
+ * removes the caps. */
+VK_API int  vk_set_rate_caps(vk_handle *h, const int *kind, const double *t_max,
+                             const double *params);
 VK_API int  vk_compute_k(vk_handle *h);
 /* Diagnostic: the device rate constants [L][nr] back to the host. */
 VK_API int  vk_get_k(vk_handle *h, double *k);

@@ -49,9 +49,10 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c2tight': (0,),
         'c2slow': (0,),
         'c1rt': (0,),
-        'c1rtT': (0,)}
+        'c1rtT': (0,),
+        'lowT': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
-          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110}
+          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -63,6 +64,8 @@ EXTRA_CFG = {'c2tight': 'yconv_cri = 0.001\nyconv_min = 0.001\n',
              # species the reference ships T tables for in this network
              'c1rtT': "dbin1 = 1.0\nT_cross_sp = ['CO2', 'H2O', 'NH3']\n"}
 PHOTO_TAGS = ('c1rt', 'c1rtT')
+# rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
+RATE_TAGS = ('lowT',)
 
 DRIVER = r'''
 import os, sys, time, json
@@ -269,6 +272,33 @@ np.savez_compressed('golden_out.npz', **out)
 print('photo records', len(REC), 'nbins', len(var.bins), 'counts', [r['count'] for r in REC])
 '''
 
+RATE_DRIVER = r'''
+import os, sys
+import numpy as np
+sys.path.insert(0, os.getcwd())
+sys.path.insert(0, os.path.join(os.getcwd(), '_mplstub'))
+import vulcan_cfg
+import store, build_atm, op, chem_funs
+from phy_const import kb
+inp = np.load('golden_inputs.npz', allow_pickle=True)
+var = store.Variables(); atm = store.AtmData()
+make_atm = build_atm.Atm()
+atm = make_atm.f_pico(atm)
+atm = make_atm.load_TPK(atm)
+atm.Tco = inp['Tco'].copy()
+atm.M = atm.pco / (kb * atm.Tco)
+atm.n_0 = atm.M.copy()
+rate = op.ReadRate()
+var = rate.read_rate(var, atm)
+k_plain = np.array([np.array(var.k[i], dtype=float) for i in range(1, chem_funs.nr + 1, 2)])   # forward
+var = rate.lim_lowT_rates(var, atm)
+var = rate.rev_rate(var, atm)
+var = rate.remove_rate(var)
+np.savez_compressed('golden_out.npz', Tco=atm.Tco, M=atm.M, pco=atm.pco, k_plain=k_plain,
+                    k=np.array([var.k[i] for i in range(1, chem_funs.nr + 1)]))
+print('rate constants', chem_funs.nr, 'layers', atm.Tco.size)
+'''
+
 MPL_STUB = {
     '__init__.py': 'use = lambda *a, **k: None\n',
     'pyplot.py': textwrap.dedent('''
@@ -371,7 +401,7 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
     with open(os.path.join(dst, 'golden_meta.json'), 'w') as f:
         json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep)}, f)
     with open(os.path.join(dst, 'golden_driver.py'), 'w') as f:
-        f.write(PHOTO_DRIVER if tag in PHOTO_TAGS else DRIVER)
+        f.write(PHOTO_DRIVER if tag in PHOTO_TAGS else RATE_DRIVER if tag in RATE_TAGS else DRIVER)
     r = subprocess.run([sys.executable, 'golden_driver.py'], cwd=dst, env=env,
                        capture_output=True, text=True)
     if r.returncode != 0:
@@ -432,6 +462,10 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a column of the 512-column batch that has not converged after 4000 steps
         # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
         spec = configs.config2_columns(ncols=512, seed=2)[60]
+    elif tag == 'lowT':
+        # a cold column (150 -> 450 K) crossing the three low-temperature caps
+        spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]
+        spec.Tco = configs.linear_logp_T(spec.pco, 450., 150.)
     elif tag in ('c1', 'c1rt', 'c1rtT'):
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
                                 use_photo=True)
@@ -442,6 +476,11 @@ def make(tag, ref_root, workdir, full_dir=None):
                             use_photo=spec.use_photo)
     dst = run_reference(ref_root, tag, spec, NSTEPS[tag], KEEP[tag], workdir)
     d = dict(np.load(os.path.join(dst, 'golden_out.npz'), allow_pickle=False))
+    if tag in RATE_TAGS:
+        out = os.path.join(HERE, 'golden_%s.npz' % tag)
+        np.savez_compressed(out, **d)
+        print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
+        return
     if tag in PHOTO_TAGS:
         d = slim_photo(d)
         d.update(photo_setup_check(d, ref_root))

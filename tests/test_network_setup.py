@@ -86,3 +86,21 @@ def test_column_helper_consistent():
     g = golden('c0')
     col = column_from_golden(g)
     assert col.nz == g['pco'].size
+
+
+def test_low_temperature_caps_bit_exact():
+    """use_lowT_limit_rates: the reference's read_rate, lim_lowT_rates,
+    rev_rate on a 150-450 K column (fixture lowT); the three capped forward
+    rates and their reverses, every other rate unchanged."""
+    g = golden('lowT')
+    net = network('c2')
+    k = net.rate_constants(g['Tco'], g['M'], use_lowT_limit_rates=True)
+    np.testing.assert_array_equal(k, g['k'])
+    plain = net.rate_constants(g['Tco'], g['M'])
+    np.testing.assert_array_equal(plain[0::2], g['k_plain'])
+    capped = np.nonzero(np.any(k != plain, axis=1))[0]
+    texts = {net.reactions[p].text for p in set(capped // 2)}
+    assert texts == {'H + CH3 + M -> CH4 + M', 'H + C2H4 + M -> C2H5 + M',
+                     'H + C2H5 + M -> C2H6 + M'}
+    kind, t_max, params = net.rate_caps()
+    assert int((kind > 0).sum()) == 3 and set(t_max[kind > 0]) == {277.5, 300., 200.}

@@ -35,7 +35,7 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
-           'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T')
+           'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps')
 
 
 class VkNetworkDesc(C.Structure):
@@ -103,6 +103,7 @@ def lib(path=None):
         'vk_get_conv': (i, [vp, pd, pd]),
         'vk_set_rate_params': (i, [vp, pi, pi, pd, pd]),
         'vk_compute_k': (i, [vp]),
+        'vk_set_rate_caps': (i, [vp, pi, pd, pd]),
         'vk_get_k': (i, [vp, pd]),
         'vk_photo_setup': (i, [vp, i, pd, pd, i, pi, pi, pd, i, pi, pd, i, pi, pd, pd,
                                C.c_double, C.c_double, C.c_double, C.c_double]),

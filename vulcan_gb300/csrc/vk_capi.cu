@@ -54,6 +54,9 @@ struct vk_handle {
     int tcap_abs = 0, tcap_ch = 0;      // table rows allocated
     int *d_kkind = nullptr, *d_krev = nullptr;   // rate-constant parameters (vk_set_rate_params)
     double *d_kpar = nullptr, *d_nasa9 = nullptr;
+    int *d_capk = nullptr;              // low-temperature caps (vk_set_rate_caps)
+    double *d_capT = nullptr, *d_capp = nullptr;
+    int caps_on = 0;
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
     int nsm = 0;                        // SMs of the device
     int cps = 0;                        // VK_CTAS_PER_SM override (0: kernel defaults)
@@ -624,6 +627,34 @@ extern "C" int vk_set_rate_params(vk_handle *h, const int *kind, const int *rev,
     return VK_OK;
 }
 
+extern "C" int vk_set_rate_caps(vk_handle *h, const int *kind, const double *t_max,
+                                const double *params) {
+    if (!h) return fail(h, VK_EINVAL, "handle is NULL");
+    if (!kind) {
+        h->caps_on = 0;
+        return VK_OK;
+    }
+    if (!t_max || !params) return fail(h, VK_EINVAL, "t_max or params is NULL");
+    for (int p = 0; p < h->npair; ++p)
+        if (kind[p] != VK_K_NONE && kind[p] != VK_K_ARRHENIUS && kind[p] != VK_K_FALLOFF)
+            return fail(h, VK_EINVAL, "cap kind must be VK_K_NONE, VK_K_ARRHENIUS or VK_K_FALLOFF");
+    if (!h->d_capk) {
+        int rc = dalloc(h, &h->d_capk, (size_t)h->npair);
+        if (!rc) rc = dalloc(h, &h->d_capT, (size_t)h->npair);
+        if (!rc) rc = dalloc(h, &h->d_capp, (size_t)h->npair * 6);
+        if (rc) {                          // the handle frees what was allocated
+            h->d_capk = nullptr;
+            return rc;
+        }
+    }
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    VK_CUDA(h, cudaMemcpy(h->d_capk, kind, h->npair * sizeof(int), cudaMemcpyHostToDevice));
+    VK_CUDA(h, cudaMemcpy(h->d_capT, t_max, h->npair * sizeof(double), cudaMemcpyHostToDevice));
+    VK_CUDA(h, cudaMemcpy(h->d_capp, params, (size_t)h->npair * 6 * sizeof(double), cudaMemcpyHostToDevice));
+    h->caps_on = 1;
+    return VK_OK;
+}
+
 extern "C" int vk_photo_setup(vk_handle *h, int nbins, const double *bins, const double *jweights,
                               int nabs, const int *abs_sp, const int *abs_photo, const double *cross,
                               int nscat, const int *scat_sp, const double *cross_scat, int nch,
@@ -802,8 +833,9 @@ extern "C" int vk_compute_k(vk_handle *h) {
     int rc = need_batch(h);
     if (rc) return rc;
     if (!h->d_kkind) return fail(h, VK_EINVAL, "no rate parameters (call vk_set_rate_params)");
-    vk::launch_rate_consts(h->net(), h->batch(), h->d_kkind, h->d_krev, h->d_kpar, h->d_nasa9,
-                           h->d_k, h->stream);
+    vk::launch_rate_consts(h->net(), h->batch(), h->d_kkind, h->d_krev,
+                           h->caps_on ? h->d_capk : nullptr, h->d_capT, h->d_capp, h->d_kpar,
+                           h->d_nasa9, h->d_k, h->stream);
     VK_CUDA(h, cudaGetLastError());
     VK_CUDA(h, cudaStreamSynchronize(h->stream));
     return VK_OK;

@@ -190,6 +190,7 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
                    double *x, const double *yscale, double *yk2, int max_sweeps, double tol,
                    cudaStream_t s);
 void launch_rate_consts(const DevNet &net, const DevBatch &b, const int *kind, const int *rev,
+                        const int *cap_kind, const double *cap_T, const double *cap_params,
                         const double *params, const double *nasa9, double *k, cudaStream_t s);
 void launch_photo(const DevNet &net, const DevBatch &b, const PhotoDev &ph, const double *y,
                   const double *ymix, double *k, unsigned long long *change, cudaStream_t s);

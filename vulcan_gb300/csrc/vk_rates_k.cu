@@ -6,6 +6,8 @@
 //            k0 / (1 + k0 M / k_inf)               (fall-off three-body)
 //            the pressure-dependent OH + CH3 + M form (op.py:197-207)
 //            photolysis / ionisation / condensation: the slot is left as uploaded
+//            low-temperature caps (op.py:320-342), where set: at T <= T_max the
+//            cap's Arrhenius or fall-off form replaces the forward rate
 //   reverse  k_f / Keq,  Keq = exp(-(sum_p nu g_p - sum_r nu g_r)) (kB T / P0)^(n_r - n_p)
 //            with g/RT from two-range NASA-9 polynomials switched at 1000 K
 //            (chem_funs Gibbs / gibbs_sp), for pairs before '# reverse stops'.
@@ -46,7 +48,9 @@ __device__ double special_oh_ch3(double T, double M) {
 
 __global__ void __launch_bounds__(128)
 k_rate_consts(DevNet net, DevBatch b, const int *__restrict__ kind, const int *__restrict__ rev,
-              const double *__restrict__ params, const double *__restrict__ nasa9, double *k) {
+              const int *__restrict__ cap_kind, const double *__restrict__ cap_T,
+              const double *__restrict__ cap_params, const double *__restrict__ params,
+              const double *__restrict__ nasa9, double *k) {
     extern __shared__ double gs[];                       // [ni] g/RT of this layer
     const int l = blockIdx.x;
     const double *al = b.atm + (size_t)l * VK_ATM_NF;
@@ -69,6 +73,15 @@ k_rate_consts(DevNet net, DevBatch b, const int *__restrict__ kind, const int *_
         case VK_K_SPECIAL_OH_CH3: kf = special_oh_ch3(T, M); break;
         default: kf = kl[2 * p];                         // photolysis etc.: as uploaded
         }
+        if (cap_kind && cap_kind[p] != VK_K_NONE && T <= cap_T[p]) {
+            const double *cp = cap_params + (size_t)p * 6;
+            double c = arrhenius(cp[0], cp[1], cp[2], T);
+            if (cap_kind[p] == VK_K_FALLOFF) {
+                const double cinf = arrhenius(cp[3], cp[4], cp[5], T);
+                c = c / (1. + c * M / cinf);
+            }
+            kf = c;
+        }
         kl[2 * p] = kf;
         if (rev[p]) {
             const PairDesc *pd = net.pairs + p;
@@ -86,8 +99,10 @@ k_rate_consts(DevNet net, DevBatch b, const int *__restrict__ kind, const int *_
 }
 
 void launch_rate_consts(const DevNet &net, const DevBatch &b, const int *kind, const int *rev,
+                        const int *cap_kind, const double *cap_T, const double *cap_params,
                         const double *params, const double *nasa9, double *k, cudaStream_t s) {
-    k_rate_consts<<<b.L, 128, net.ni * sizeof(double), s>>>(net, b, kind, rev, params, nasa9, k);
+    k_rate_consts<<<b.L, 128, net.ni * sizeof(double), s>>>(net, b, kind, rev, cap_kind, cap_T,
+                                                            cap_params, params, nasa9, k);
 }
 
 }  // namespace vk

@@ -39,6 +39,15 @@ NAVO = 6.02214086E+23
 CORR = KB / 1.0e6          # gibbs_text.txt:1  (P0 = 1 bar)
 
 SPECIAL_OH_CH3 = 'OH + CH3 + M -> CH3OH + M'
+# use_lowT_limit_rates (op.ReadRate.lim_lowT_rates, op.py:320-342): reaction
+# -> (T_max, form, (A, B, C, A_inf, B_inf, C_inf)); at T <= T_max the forward
+# rate becomes A T^B exp(-C/T) ('arrhenius') or the fall-off of that k0 and
+# k_inf = A_inf T^B_inf exp(-C_inf/T) ('falloff') -- Moses et al. 2005 values
+LOWT_CAPS = {
+    'H + CH3 + M -> CH4 + M': (277.5, 'falloff', (6e-29, 0., 0., 2.06E-10, -0.4, 0.)),
+    'H + C2H4 + M -> C2H5 + M': (300., 'arrhenius', (3.7E-30, 0., 0., 0., 0., 0.)),
+    'H + C2H5 + M -> C2H6 + M': (200., 'arrhenius', (2.49E-27, 0., 0., 0., 0., 0.)),
+}
 
 
 @dataclass
@@ -353,18 +362,33 @@ class Network:
         return k
 
     def _lim_lowT(self, k, Tco, M):
-        """Low-temperature caps of op.ReadRate.lim_lowT_rates (op.py:320-342)."""
+        """Low-temperature caps of op.ReadRate.lim_lowT_rates (op.py:320-342),
+        applied to the forward rates before the reverse rates are formed
+        (vulcan.py:130-136 order)."""
         for p, r in enumerate(self.reactions):
-            if r.text == 'H + CH3 + M -> CH4 + M':
-                m = Tco <= 277.5
-                k0 = 6e-29
-                kinf = 2.06E-10 * Tco ** -0.4
-                lim = k0 / (1. + k0 * M / kinf)
-                k[2 * p][m] = lim[m]
-            elif r.text == 'H + C2H4 + M -> C2H5 + M':
-                k[2 * p][Tco <= 300] = 3.7E-30
-            elif r.text == 'H + C2H5 + M -> C2H6 + M':
-                k[2 * p][Tco <= 200] = 2.49E-27
+            cap = LOWT_CAPS.get(r.text)
+            if cap is None:
+                continue
+            t_max, kind, (A, B, C, A2, B2, C2) = cap
+            m = Tco <= t_max
+            k0 = A * Tco ** B * np.exp(-C / Tco)
+            if kind == 'falloff':
+                kinf = A2 * Tco ** B2 * np.exp(-C2 / Tco)
+                k0 = k0 / (1. + k0 * M / kinf)
+            k[2 * p][m] = k0[m]
+
+    def rate_caps(self):
+        """Per-pair tables for vk_set_rate_caps: (kind [npair], T_max [npair],
+        params [npair, 6]) of the low-temperature caps (LOWT_CAPS)."""
+        codes = {'arrhenius': 1, 'falloff': 2}
+        kind = np.zeros(self.npair, dtype=np.int32)
+        t_max = np.zeros(self.npair)
+        params = np.zeros((self.npair, 6))
+        for p, r in enumerate(self.reactions):
+            cap = LOWT_CAPS.get(r.text)
+            if cap is not None:
+                t_max[p], kind[p], params[p] = cap[0], codes[cap[1]], cap[2]
+        return kind, t_max, params
 
     def rate_params(self):
         """Per-pair tables for vk_set_rate_params: (kind, rev, params [npair, 6],

@@ -266,11 +266,18 @@ class Ros2Handle:
                                  ptr(out['end_case'], C.c_int), ptr(out['delta'])), self.h)
         return out
 
-    def set_rate_params(self, net):
-        """Upload the network's rate parameters for compute_k (Network.rate_params)."""
+    def set_rate_params(self, net, use_lowT_limit_rates=False):
+        """Upload the network's rate parameters for compute_k (Network.rate_params)
+        and, with use_lowT_limit_rates, its low-temperature caps (Network.rate_caps)."""
         kind, rev, params, nasa9 = net.rate_params()
         check(lib().vk_set_rate_params(self.h, ptr(kind, C.c_int), ptr(rev, C.c_int),
                                        ptr(np.ascontiguousarray(params)), ptr(nasa9)), self.h)
+        if use_lowT_limit_rates:
+            ck, ct, cp = net.rate_caps()
+            check(lib().vk_set_rate_caps(self.h, ptr(ck, C.c_int), ptr(ct),
+                                         ptr(np.ascontiguousarray(cp))), self.h)
+        else:
+            check(lib().vk_set_rate_caps(self.h, None, None, None), self.h)
 
     def compute_k(self):
         """Rate constants of every layer from its temperature and M, on the device."""
