@@ -425,12 +425,21 @@ def photo_setup_check(d, ref_root):
     same = (len(t.bins) == len(d['bins']) and t.i12 == int(d['sflux_din12_indx'])
             and t.absp_sp == [str(s) for s in d['absp_sp']]
             and t.ch_sp == [str(s) for s in d['ch_sp']])
-    return {'setup_same_layout': same,
-            'setup_rel_bins': rel(t.bins, d['bins']) if same else np.inf,
-            'setup_rel_cross': rel(t.cross, d['cross']) if same else np.inf,
-            'setup_rel_cross_J': rel(t.cross_J, d['cross_J']) if same else np.inf,
-            'setup_rel_cross_scat': rel(t.cross_scat, d['cross_scat']) if same else np.inf,
-            'setup_rel_sflux_top': rel(t.sflux_top, d['sflux_top']) if same else np.inf}
+    out = {'setup_same_layout': same,
+           'setup_rel_bins': rel(t.bins, d['bins']) if same else np.inf,
+           'setup_rel_cross': rel(t.cross, d['cross']) if same else np.inf,
+           'setup_rel_cross_J': rel(t.cross_J, d['cross_J']) if same else np.inf,
+           'setup_rel_cross_scat': rel(t.cross_scat, d['cross_scat']) if same else np.inf,
+           'setup_rel_sflux_top': rel(t.sflux_top, d['sflux_top']) if same else np.inf}
+    if 'T_cross_sp' in d and same:
+        # the per-layer tables of photo.TCross for the recorded temperatures
+        tsp = [str(s) for s in d['T_cross_sp']]
+        ct, cj = photo.TCross.from_reference_files(t, ref_root, tsp).for_column(d['Tco'])
+        out['setup_rel_cross_T'] = max(rel(ct[sp], d['cross_T'][i]) for i, sp in enumerate(tsp))
+        out['setup_rel_cross_J_T'] = max(
+            rel(cj[(str(sp), int(br))], d['cross_J_T'][i])
+            for i, (sp, br) in enumerate(zip(d['chT_sp'], d['chT_br'])))
+    return out
 
 
 def slim_photo(d):
@@ -513,7 +522,18 @@ def main():
     ap.add_argument('--ref', default='/root/reference')
     ap.add_argument('--full-dir', default=None,
                     help='also keep every recorded attempt here (not committed)')
+    ap.add_argument('--setup-only', action='store_true',
+                    help='radiative-transfer fixtures: recompute only the host set-up '
+                         'comparisons of an existing fixture (no reference run)')
     a = ap.parse_args()
+    if a.setup_only:
+        for t in a.tags:
+            path = os.path.join(HERE, 'golden_%s.npz' % t)
+            d = dict(np.load(path, allow_pickle=False))
+            d.update(photo_setup_check(d, a.ref))
+            np.savez_compressed(path, **d)
+            print('updated', path)
+        return
     with tempfile.TemporaryDirectory() as w:
         for t in a.tags:
             make(t, a.ref, w, a.full_dir)

@@ -80,9 +80,90 @@ def test_host_tables_match_the_reference_set_up():
     files (differences recorded by the fixture generator)."""
     d = _fixture()
     assert bool(d['setup_same_layout'])
-    assert bool(_fixture('c1rtT')['setup_same_layout'])
     for key in ('bins', 'cross', 'cross_J', 'cross_scat', 'sflux_top'):
         assert float(d['setup_rel_' + key]) <= 1e-15, key
+    # T-dependent per-layer tables (photo.TCross) for the c1 column's
+    # 973-2535 K: CO2 above its hottest table for the upper layers and
+    # between tables below, H2O between tables, NH3 above its hottest
+    t = _fixture('c1rtT')
+    assert bool(t['setup_same_layout'])
+    for key in ('cross', 'cross_J', 'cross_T', 'cross_J_T'):
+        assert float(t['setup_rel_' + key]) <= 1e-15, key
+
+
+def _tcross(temps, base=2e-18):
+    """photo.TCross over synthetic tables: one absorber with two branches
+    (ratios 0.25 / 0.75), tables at ``temps`` of constant cross section
+    1e-18 x T/100 over 100-200 nm (disso = 0.5 x cross), bins 50-250 nm."""
+    from vulcan_gb300 import photo
+    bins = np.arange(50., 250., 10.)
+    inside = (bins >= 100.) & (bins <= 200.)
+    t = photo.PhotoTables(bins=bins, dbin1=10., dbin2=10., i12=-1, sflux_top=np.ones_like(bins),
+                          absp_sp=['X'], cross=np.full((1, bins.size), base), scat_sp=[],
+                          cross_scat=np.zeros((0, bins.size)), ch_sp=['X', 'X'], ch_br=[1, 2],
+                          cross_J=np.array([np.full(bins.size, base * 0.25),
+                                            np.full(bins.size, base * 0.75)]),
+                          sl_angle=0.5, edd=0.5, f_diurnal=1.0, flux_atol=1.0)
+    lam = np.linspace(100., 200., 11)
+    raw = {T: (lam, np.full(11, 1e-18 * T / 100.), np.full(11, 0.5e-18 * T / 100.))
+           for T in temps}
+    raw[300] = (lam, np.full(11, base), np.full(11, base))
+    ratio = {('X', 1): np.full(bins.size, 0.25), ('X', 2): np.full(bins.size, 0.75)}
+    return photo.TCross(t, {'X': raw}, ratio), inside, bins
+
+
+def test_tcross_cases():
+    """The reference's three temperature cases (op.py:649-747) on synthetic
+    tables: log-linear in T between two tables inside their common
+    wavelengths; the nearest table at or beyond either end; the
+    T-independent values outside a table's wavelengths or where the end
+    table is the 300 K one."""
+    base = 2e-18
+    tc, inside, bins = _tcross([100, 500], base)
+    ct, cj = tc.for_column(np.array([200., 50., 900., 100.]))
+    c = ct['X']
+    # 200 K between 100 K (1e-18) and 300 K (base): log-linear at a half
+    want = 10 ** (np.log10(1e-18) + 0.5 * (np.log10(base) - np.log10(1e-18)))
+    np.testing.assert_allclose(c[0][inside], want, rtol=1e-14)
+    assert np.all(c[0][~inside] == base)
+    # disso between 0.5e-18 and base, times the branch ratio
+    wj = 10 ** (np.log10(0.5e-18) + 0.5 * (np.log10(base) - np.log10(0.5e-18)))
+    np.testing.assert_allclose(cj[('X', 2)][0][inside], 0.75 * wj, rtol=1e-14)
+    assert np.all(cj[('X', 1)][0][~inside] == base * 0.25)
+    # 50 K: below every table -> the 100 K table; 900 K: above -> 500 K table
+    assert np.all(c[1][inside] == 1e-18) and np.all(c[1][~inside] == base)
+    assert np.all(c[2][inside] == 5e-18) and np.all(cj[('X', 1)][2][inside] == 0.25 * 2.5e-18)
+    # exactly at the lowest table: between it and the next (the reference's <= / >)
+    np.testing.assert_allclose(c[3][inside], 1e-18, rtol=1e-14)
+    # the 300 K table at an end: T-independent values
+    tc, inside, _ = _tcross([500], base)
+    ct, cj = tc.for_column(np.array([250.]))
+    assert np.all(ct['X'][0] == base) and np.all(cj[('X', 2)][0] == base * 0.75)
+    tc, inside, _ = _tcross([100], base)
+    ct, _ = tc.for_column(np.array([400.]))
+    assert np.all(ct['X'][0] == base)
+
+
+def test_tcross_zero_cross_sections():
+    """A zero table value is log10 -100: both tables zero gives 0, one zero
+    gives a vanishing interpolant (the reference's -100 convention)."""
+    tc, inside, bins = _tcross([100], 2e-18)
+    tc.raw['X'][100] = (tc.raw['X'][100][0], np.zeros(11), np.zeros(11))
+    ct, cj = tc.for_column(np.array([200.]))
+    v = ct['X'][0][inside]
+    assert np.all((v > 0) & (v < 1e-50))
+    tc.raw['X'][300] = (tc.raw['X'][300][0], np.zeros(11), np.zeros(11))
+    ct, cj = tc.for_column(np.array([200.]))
+    assert np.all(ct['X'][0][inside] == 0) and np.all(cj[('X', 1)][0][inside] == 0)
+
+
+def test_tcross_batch_layout():
+    tc, inside, bins = _tcross([100, 500])
+    Ts = [np.array([200., 900.]), np.array([50., 250., 600.])]
+    ct, cj = tc.for_columns(Ts)
+    assert ct['X'].shape == (5, bins.size) and cj[('X', 1)].shape == (5, bins.size)
+    one, _ = tc.for_column(Ts[1])
+    np.testing.assert_array_equal(ct['X'][2:], one['X'])
 
 
 def test_j_weights_follow_the_reference_sums():

@@ -4,8 +4,9 @@ path (vk_photo_setup / vk_photo_update) runs on.
 Restates the reference's make_bins_read_cross (op.py:495-782) and read_sflux
 (build_atm.py:617-656) for T-independent cross sections without
 photoionisation (the reference's defaults: T_cross_sp = [], use_ion = False);
-per-layer temperature-dependent tables (T_cross_sp) are uploaded as given
-(attach_cross_T), e.g. the reference's own var.cross_T / var.cross_J_T:
+the per-layer temperature-dependent tables of T_cross_sp come from TCross (the
+same function's T branch) or as given, e.g. the reference's own var.cross_T /
+var.cross_J_T, and are uploaded by attach_cross_T:
 
 * bins: from the shortest absorption edge (not below the stellar file's
   first wavelength or 2 nm) to min(longest edge, the file's last wavelength
@@ -136,6 +137,112 @@ class PhotoTables:
                    cross_scat=np.array(scat), ch_sp=[c[0] for c in chans],
                    ch_br=[c[1] for c in chans], cross_J=np.array(cross_J), sl_angle=sl_angle,
                    edd=edd, f_diurnal=f_diurnal, flux_atol=flux_atol)
+
+
+class TCross:
+    """Temperature-dependent cross sections (vulcan_cfg.T_cross_sp) of one
+    column, restating the T branch of make_bins_read_cross (files op.py:542-557,
+    per-layer tables op.py:640-747).  A species' tables are its
+    ``<sp>_cross_<T>K.csv`` files plus the room-temperature file as 300 K.
+    For a layer at T:
+
+    * T between two tabulated temperatures (Tlow <= T < Thigh): inside the
+      wavelengths both tables cover, log10 of the cross section linear in T
+      (log10 0 taken as -100, a result of -100 giving 0), the branch ratio as
+      for the T-independent channels; outside, the T-independent values;
+    * T at or below every tabulated temperature: the lowest table (its own
+      wavelength range) unless that is the 300 K one, which means the
+      T-independent values; likewise above every temperature with the highest.
+    """
+
+    def __init__(self, tables, raw, ratio):
+        self.tables = tables
+        self.raw = raw            # sp -> {T: (lambda, cross, disso)}
+        self.ratio = ratio        # (sp, branch) -> branch ratio on the bins
+
+    @classmethod
+    def from_reference_files(cls, tables, ref_root, T_cross_sp,
+                             cross_folder='thermo/photo_cross/'):
+        import re
+        read = lambda path: np.genfromtxt(path, dtype=float, delimiter=',', skip_header=1,
+                                          usecols=(0, 1, 2)).T
+        raw, ratio = {}, {}
+        for sp in T_cross_sp:
+            if sp not in tables.absp_sp:
+                continue
+            d = os.path.join(ref_root, cross_folder, sp)
+            tabs = {}
+            for name in os.listdir(d):
+                m = re.fullmatch(re.escape(sp) + r'_cross_(\d+)K\.csv', name)
+                if m:
+                    tabs[int(m.group(1))] = read(os.path.join(d, name))
+            tabs[300] = read(os.path.join(d, sp + '_cross.csv'))
+            raw[sp] = tabs
+            br = np.genfromtxt(os.path.join(d, sp + '_branch.csv'), dtype=float, delimiter=',',
+                               skip_header=1, names=True)
+            for s, b in zip(tables.ch_sp, tables.ch_br):
+                if s == sp:
+                    key = 'br_ratio_%d' % b
+                    ratio[(s, b)] = np.interp(tables.bins, br['lambda'], br[key])
+        return cls(tables, raw, ratio)
+
+    def for_column(self, Tco):
+        """(cross_T {sp: [nz, nbins]}, cross_J_T {(sp, branch): [nz, nbins]})."""
+        t = self.tables
+        bins = t.bins
+        interp0 = lambda tab, col: np.interp(bins, tab[0], tab[col], left=0.0, right=0.0)
+        cross_T, cross_J_T = {}, {}
+        for sp, tabs in self.raw.items():
+            base = t.cross[t.absp_sp.index(sp)]
+            chans = [(i, (s, b)) for i, (s, b) in enumerate(zip(t.ch_sp, t.ch_br)) if s == sp]
+            Ts = np.array(sorted(tabs), dtype=float)
+            ct = np.zeros((len(Tco), len(bins)))
+            cj = {c: np.zeros((len(Tco), len(bins))) for _, c in chans}
+            for lev, Tz in enumerate(Tco):
+                lo, hi = Ts[Ts <= Tz], Ts[Ts > Tz]
+                if lo.size and hi.size:
+                    A, B = tabs[int(lo.max())], tabs[int(hi.min())]
+                    inside = (bins >= max(A[0][0], B[0][0])) & (bins <= min(A[0][-1], B[0][-1]))
+                    frac = lambda la, lb: (lb - la) / (hi.min() - lo.max()) * (Tz - lo.max()) + la
+                    with np.errstate(divide='ignore'):
+                        v = frac(_log10_floor(interp0(A, 1)), _log10_floor(interp0(B, 1)))
+                        vj = frac(_log10_floor(interp0(A, 2)), _log10_floor(interp0(B, 2)))
+                    row = np.where(v == -100, 0.0, 10 ** v)
+                    rowj = np.where(vj == -100, 0.0, 10 ** vj)
+                    ct[lev] = np.where(inside, row, base)
+                    for i, c in chans:
+                        cj[c][lev] = np.where(inside, rowj * self.ratio[c], t.cross_J[i])
+                else:
+                    edge = Ts.min() if not (Ts < Tz).any() else Ts.max()
+                    if edge == 300:
+                        ct[lev] = base
+                        for i, c in chans:
+                            cj[c][lev] = t.cross_J[i]
+                        continue
+                    E = tabs[int(edge)]
+                    inside = (bins >= E[0][0]) & (bins <= E[0][-1])
+                    ct[lev] = np.where(inside, interp0(E, 1), base)
+                    for i, c in chans:
+                        cj[c][lev] = np.where(inside, interp0(E, 2) * self.ratio[c], t.cross_J[i])
+            cross_T[sp] = ct
+            cross_J_T.update(cj)
+        return cross_T, cross_J_T
+
+    def for_columns(self, Tcos):
+        """for_column of every column of a batch, layers stacked in batch
+        order (the [L, nbins] tables attach_cross_T uploads)."""
+        parts = [self.for_column(T) for T in Tcos]
+        cross_T = {sp: np.concatenate([p[0][sp] for p in parts]) for sp in parts[0][0]}
+        cross_J_T = {c: np.concatenate([p[1][c] for p in parts]) for c in parts[0][1]}
+        return cross_T, cross_J_T
+
+
+def _log10_floor(x):
+    """log10 with -inf replaced by -100, as the reference does before
+    interpolating in temperature."""
+    v = np.log10(x)
+    v[np.isinf(v)] = -100.
+    return v
 
 
 def attach(handle, tables, net):
