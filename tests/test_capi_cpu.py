@@ -79,3 +79,29 @@ def test_null_handle_errors(lib):
     from vulcan_gb300 import capi
     assert lib.vk_set_columns(None, 1, None, None, None, None, None, None, None) == capi.VK_EINVAL
     assert lib.vk_last_error(None)
+
+
+NO_HANDLE = ('vk_network_compile', 'vk_network_free', 'vk_network_last_error', 'vk_destroy',
+             'vk_last_error')
+
+
+def test_every_entry_point_rejects_null_arguments(lib):
+    """Each status-returning entry point answers VK_EINVAL to a NULL handle
+    (zero sizes for the handle-free ones) before touching the device."""
+    from vulcan_gb300 import capi
+    checked = 0
+    for name in capi.EXPORTS:
+        if name in NO_HANDLE:
+            continue
+        f = getattr(lib, name)
+        args = []
+        for t in f.argtypes:
+            if t in (C.c_int, C.c_longlong):
+                args.append(0)
+            elif t in (C.c_double, C.c_float):
+                args.append(0.0)
+            else:
+                args.append(None)
+        assert f(*args) == capi.VK_EINVAL, name
+        checked += 1
+    assert checked == len(capi.EXPORTS) - len(NO_HANDLE)
