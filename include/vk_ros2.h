@@ -215,8 +215,9 @@ VK_API int  vk_compute_k(vk_handle *h);
 VK_API int  vk_get_k(vk_handle *h, double *k);
 
 /* ---- photochemistry radiative transfer ----
- * op.ODESolver.compute_tau / compute_flux / compute_J (op.py:2580-2786; T-
- * independent cross sections, isotropic scattering) for every column.  The
+ * op.ODESolver.compute_tau / compute_flux / compute_J (op.py:2580-2786;
+ * isotropic scattering; T-dependent cross sections through
+ * vk_photo_set_cross_T below) for every column.  The
  * tables are those of the reference's make_bins_read_cross / read_sflux
  * (op.py:495-782, build_atm.py:617-656): wavelength bins, the J integral's
  * bin weights, absorbers (species index, 1 if a photolysis species -- the

@@ -3,11 +3,10 @@
 //
 // Restates op.ODESolver.compute_tau (op.py:2580-2599), compute_flux
 // (op.py:2603-2739, isotropic scattering, ag0 = 0 in phy_const.py) and
-// compute_J (op.py:2751-2786, T-independent cross sections) on the binned
-// cross sections the host set-up provides (make_bins_read_cross, read_sflux).
-//
-// compute_tau's T-dependent branch (op.py:2591-2592) and compute_J's
-// (op.py:2770-2774) read per-layer tables where vk_photo_set_cross_T gave them.
+// compute_J (op.py:2751-2786) on the binned cross sections the host set-up
+// provides (make_bins_read_cross, read_sflux).  The T-dependent branches of
+// compute_tau (op.py:2591-2592) and compute_J (op.py:2770-2774) read
+// per-layer tables where vk_photo_set_cross_T gave them.
 //
 //   k_photo_flux  one thread per (column, wavelength bin): tau from the top,
 //                 single-scattering albedo, the downward then upward sweeps of
