@@ -108,7 +108,7 @@ class Clocks:
             self.f = open(self.path, 'w')
             self.p = subprocess.Popen(['nvidia-smi', '--query-gpu=' + q, '--format=csv,noheader,nounits',
                                        '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
-        except Exception:
+        except OSError:         # no nvidia-smi: no clock record
             self.p = None
         return self
 
@@ -121,7 +121,7 @@ class Clocks:
     def summary(self):
         try:
             rows = [l.split(',') for l in open(self.path).read().strip().splitlines()]
-        except Exception:
+        except OSError:
             return None
         rows = [[x.strip() for x in r] for r in rows if len(r) >= 9]
         if not rows:
