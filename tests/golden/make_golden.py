@@ -50,9 +50,12 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c2slow': (0,),
         'c1rt': (0,),
         'c1rtT': (0,),
-        'lowT': (0,)}
+        'lowT': (0,),
+        'c0bc': (0, 1, 2, 10, 29),
+        'c0nomol': (0, 1, 2, 10, 29)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
-          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1}
+          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1, 'c0bc': 30,
+          'c0nomol': 30}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -63,6 +66,20 @@ EXTRA_CFG = {'c2tight': 'yconv_cri = 0.001\nyconv_min = 0.001\n',
              # the same with temperature-dependent cross sections for the three
              # species the reference ships T tables for in this network
              'c1rtT': "dbin1 = 1.0\nT_cross_sp = ['CO2', 'H2O', 'NH3']\n"}
+# boundary options on the c0 column: constant top and bottom fluxes with
+# deposition velocities, diffusion-limited escape of H (update_phi_esc), with
+# and without molecular diffusion (the no-moldiff Jacobian's escape term is
+# not part of the device path, so c0nomol leaves diff_esc empty)
+BC_CFG = ("use_topflux = True\nuse_botflux = True\n"
+          "top_BC_flux_file = 'atm/BC_top_golden.txt'\n"
+          "bot_BC_flux_file = 'atm/BC_bot_golden.txt'\n")
+EXTRA_CFG['c0bc'] = BC_CFG + "diff_esc = ['H']\n"
+EXTRA_CFG['c0nomol'] = BC_CFG + "use_moldiff = False\n"
+# fluxes large enough to stand out in the transport terms they enter
+BC_FILES = {'atm/BC_top_golden.txt': '#species flux [cm-2 s-1]\nCO2  1.0E+12\nH2O  4.0E+11\n',
+            'atm/BC_bot_golden.txt': ('#species flux [cm-2 s-1]   v_dep [cm s-1]\n'
+                                      'CH4  1.0E+14  0.\nCO  0.  1.0E-02\nH2O  2.0E+14  1.0E-03\n')}
+BC_TAGS = ('c0bc', 'c0nomol')
 PHOTO_TAGS = ('c1rt', 'c1rtT')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
 RATE_TAGS = ('lowT',)
@@ -106,6 +123,9 @@ var = ini.ele_sum(var)
 atm = make_atm.f_mu_dz(var, atm, output)
 make_atm.mol_diff(atm)
 make_atm.BC_flux(atm)
+NZ = len(atm.pco)
+if not vulcan_cfg.use_moldiff:         # no interface T / Hp without molecular diffusion
+    atm.Ti, atm.Hpi = np.zeros(NZ - 1), np.zeros(NZ - 1)
 for key, J in zip(meta['photo_keys'], inp['photo_J']):
     var.k[var.pho_rate_index[(key[0], int(key[1]))]] = J.copy()
 nr = chem_funs.nr
@@ -116,7 +136,10 @@ setup = dict(pico=atm.pico, M=atm.M, n_0=atm.n_0, mu=atm.mu, g=atm.g.copy(),
              Kzz=atm.Kzz, vz=atm.vz, Tco=atm.Tco, pco=atm.pco, k=K,
              y_ini=var.y.copy(), ymix_ini=var.ymix.copy(),
              atom_ini=np.array([var.atom_ini[a] for a in vulcan_cfg.atom_list]),
-             pref_indx=atm.pref_indx)
+             pref_indx=atm.pref_indx, top_flux=atm.top_flux.copy(), bot_flux=atm.bot_flux.copy(),
+             bot_vdep=atm.bot_vdep.copy(), use_moldiff=bool(vulcan_cfg.use_moldiff),
+             use_topflux=bool(vulcan_cfg.use_topflux), use_botflux=bool(vulcan_cfg.use_botflux),
+             diff_esc=np.array(list(vulcan_cfg.diff_esc), dtype='U8'))
 # chemistry pins at the initial state
 setup['chemdf0'] = chem_funs.chemdf(var.y, atm.M, var.k)
 ATT, STEPS = [], []
@@ -125,7 +148,7 @@ class RecRos2(op.Ros2):
     def solver(self, v, a, p):
         snap = dict(y=v.y.copy(), ymix=v.ymix.copy(), dt=float(v.dt),
                     dzi=a.dzi.copy(), Hpi=a.Hpi.copy(), g=a.g.copy(), Hp=a.Hp.copy(),
-                    count=int(p.count), t=float(v.t))
+                    count=int(p.count), t=float(v.t), top_flux=a.top_flux.copy())
         del SB[:]
         v, p = op.Ros2.solver(self, v, a, p)
         snap.update(k1=SB[0], k2=SB[1], sol=v.y.copy(), delta=float(p.delta))
@@ -145,6 +168,28 @@ class RecRos2(op.Ros2):
         return v
 
 solver = RecRos2()
+if vulcan_cfg.use_topflux or vulcan_cfg.use_botflux or not vulcan_cfg.use_moldiff:
+    # the reference's own transport RHS and LHS at the initial state, with the
+    # functions its Ros2.solver picks for these options (op.py:2870-2888); the
+    # LHS with every rate constant zero and dt = 1e10 s, so that its blocks are
+    # the transport Jacobian (the chemistry part is pinned by negjac_blocks)
+    mol = vulcan_cfg.use_moldiff
+    setup['diffdf0'] = (solver.diffdf if mol else solver.diffdf_no_mol)(var.y, atm)
+    k_keep, dt_keep = var.k, var.dt
+    var.k = {i: np.zeros_like(v) for i, v in var.k.items()}
+    var.dt = 1e10
+    lhs = (solver.lhs_jac_tot if mol else solver.lhs_jac_no_mol)(var, atm)
+    var.k, var.dt = k_keep, dt_keep
+    ni_, nz_ = chem_funs.ni, len(atm.pco)
+    lays = [0, 1, nz_ // 2, nz_ - 1]
+    setup['lhs_layers'] = np.array(lays)
+    setup['lhs_D'] = np.array([lhs[l*ni_:(l+1)*ni_, l*ni_:(l+1)*ni_] for l in lays])
+    setup['lhs_U'] = np.array([np.diag(lhs[l*ni_:(l+1)*ni_, (l+1)*ni_:(l+2)*ni_])
+                               if l < nz_ - 1 else np.zeros(ni_) for l in lays])
+    setup['lhs_L'] = np.array([np.diag(lhs[l*ni_:(l+1)*ni_, (l-1)*ni_:l*ni_])
+                               if l > 0 else np.zeros(ni_) for l in lays])
+    setup['lhs_dt'] = 1e10
+    del lhs
 integ = op.Integration(solver, output)
 solver.naming_solver(para)
 # chemistry Jacobian pins (a few diagonal blocks of neg_symjac at the start)
@@ -159,7 +204,7 @@ integ(var, atm, para, make_atm)
 wall = time.time() - t0
 keep = meta['keep']
 att_keys = ['y', 'ymix', 'dt', 'dzi', 'Hpi', 'g', 'Hp', 'count', 't', 'k1', 'k2',
-            'sol', 'delta', 'y_clip', 'atom_loss', 'ok']
+            'sol', 'delta', 'y_clip', 'atom_loss', 'ok', 'top_flux']
 out = dict(setup)
 sel = [i for i in keep if i < len(ATT)]
 out['att_index'] = np.array(sel)
@@ -374,6 +419,10 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
             os.chmod(os.path.join(root, d), 0o755)
         for f in files:
             os.chmod(os.path.join(root, f), 0o644)
+    if tag in BC_TAGS:
+        for name, text in BC_FILES.items():
+            with open(os.path.join(dst, name), 'w') as f:
+                f.write(text)
     stub = os.path.join(dst, '_mplstub', 'matplotlib')
     os.makedirs(stub)
     for name, src in MPL_STUB.items():
@@ -463,7 +512,7 @@ def slim_photo(d):
 
 
 def make(tag, ref_root, workdir, full_dir=None):
-    if tag == 'c0':
+    if tag in ('c0', 'c0bc', 'c0nomol'):
         spec = configs.config0()
     elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]

@@ -11,7 +11,8 @@ from vulcan_gb300.network import Network
 
 NETS = {'c0': 'net_CHO_thermo.npz', 'c1': 'net_NCHO_photo.npz', 'c2': 'net_NCHO_thermo.npz',
         'c2long': 'net_NCHO_thermo.npz', 'c2conv': 'net_NCHO_thermo.npz',
-        'c2tight': 'net_NCHO_thermo.npz', 'c2slow': 'net_NCHO_thermo.npz'}
+        'c2tight': 'net_NCHO_thermo.npz', 'c2slow': 'net_NCHO_thermo.npz',
+        'c0bc': 'net_CHO_thermo.npz', 'c0nomol': 'net_CHO_thermo.npz'}
 
 
 def golden(tag):
@@ -27,14 +28,28 @@ def oracle_net(tag, g):
 
 
 def base_atm(g):
+    ni = g['ms'].size
     return dict(M=g['M'], n_0=g['n_0'], Tco=g['Tco'], Kzz=g['Kzz'], vz=g['vz'], Dzz=g['Dzz'],
                 Ti=g['Ti'], ms=g['ms'], alpha=g['alpha'], pico=g['pico'], dzi=g['dzi'],
-                Hpi=g['Hpi'], g=g['g'], Hp=g['Hp'], dz=g['dz'], zco=g['zco'])
+                Hpi=g['Hpi'], g=g['g'], Hp=g['Hp'], dz=g['dz'], zco=g['zco'],
+                top_flux=g.get('top_flux', np.zeros(ni)), bot_flux=g.get('bot_flux', np.zeros(ni)),
+                bot_vdep=g.get('bot_vdep', np.zeros(ni)))
 
 
 def attempt_atm(g, n):
-    return dict(base_atm(g), dzi=g['att_dzi'][n], Hpi=g['att_Hpi'][n], g=g['att_g'][n],
-                Hp=g['att_Hp'][n])
+    a = dict(base_atm(g), dzi=g['att_dzi'][n], Hpi=g['att_Hpi'][n], g=g['att_g'][n],
+             Hp=g['att_Hp'][n])
+    if 'att_top_flux' in g:           # diffusion-limited escape updates the top fluxes
+        a['top_flux'] = g['att_top_flux'][n]
+    return a
+
+
+def fixture_flags(g):
+    """Transport options a fixture was recorded with (the reference's
+    defaults where the fixture predates the keys)."""
+    return O.Flags(use_moldiff=bool(g.get('use_moldiff', True)),
+                   use_topflux=bool(g.get('use_topflux', False)),
+                   use_botflux=bool(g.get('use_botflux', False)))
 
 
 def column_from_golden(g, n=None):

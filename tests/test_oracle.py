@@ -115,3 +115,52 @@ def test_reference_does_not_meet_tight_criterion():
     assert g['final_t'] > 1e12
     dt = g['traj_dt_used']
     assert dt[1000:].min() < 1e-3 * dt[1000:].max()
+
+
+
+@pytest.mark.parametrize('tag', ['c0bc', 'c0nomol'])
+def test_transport_options_match_reference(tag):
+    """Constant top and bottom fluxes with deposition velocities on the c0
+    column, with molecular diffusion (c0bc: diffdf, lhs_jac_tot) and without
+    (c0nomol: diffdf_no_mol, lhs_jac_no_mol): the reference's own transport
+    RHS at the initial state, and its LHS blocks with the chemistry switched
+    off (k = 0, dt = 1e10 s) so that they hold the transport Jacobian."""
+    import dataclasses
+    from helpers import base_atm, fixture_flags
+    g = golden(tag)
+    flags = fixture_flags(g)
+    assert flags.use_topflux and flags.use_botflux and flags.use_moldiff == (tag == 'c0bc')
+    atm = base_atm(g)
+    d = O.diffdf(g['y_ini'], atm, flags)
+    np.testing.assert_array_equal(d, g['diffdf0'])
+    # the fluxes are not lost in the rounding of the other terms
+    plain = O.diffdf(g['y_ini'], atm, dataclasses.replace(flags, use_topflux=False,
+                                                          use_botflux=False))
+    assert np.max(np.abs(plain - d) / np.maximum(np.abs(d), 1e-300)) > 1e-3
+    on = oracle_net(tag, g)
+    kz = np.zeros_like(g['k'])
+    D, U, L = O.lhs_blocks(on, g['y_ini'], g['M'], kz, float(g['lhs_dt']), atm, flags)
+    D0, _, _ = O.lhs_blocks(on, g['y_ini'], g['M'], kz, float(g['lhs_dt']), atm,
+                            dataclasses.replace(flags, use_botflux=False))
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+    for i, l in enumerate(g['lhs_layers']):
+        assert rel(D[l], g['lhs_D'][i]) <= 1e-15
+        assert rel(U[l], g['lhs_U'][i]) <= 1e-15 and rel(L[l], g['lhs_L'][i]) <= 1e-15
+    # the deposition velocity's Jacobian term is visible in the bottom block
+    assert rel(D0[0], g['lhs_D'][0]) > 1e-5
+
+
+@pytest.mark.parametrize('tag,n', _attempts('c0bc') + _attempts('c0nomol'))
+def test_transport_option_attempts_match_reference(tag, n):
+    """The recorded attempts of the same runs (30 steps; top fluxes as the
+    reference's update_phi_esc left them, H escaping in c0bc), banded and
+    block-Thomas."""
+    from helpers import fixture_flags
+    g = golden(tag)
+    on = oracle_net(tag, g)
+    args = (on, g['att_y'][n], g['att_ymix'][n], float(g['att_dt'][n]), g['k'],
+            attempt_atm(g, n), fixture_flags(g), O.Tol())
+    for solve in ('banded', 'block'):
+        r = O.ros2_attempt(*args, solve)
+        assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
+        assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve

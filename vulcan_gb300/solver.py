@@ -354,8 +354,14 @@ def _unsupported(cfg):
             bad.append(key)
     if getattr(cfg, 'use_fix_sp_bot', {}):
         bad.append('use_fix_sp_bot')
+    if getattr(cfg, 'use_fix_H2He', False):        # turns use_fix_sp_bot on (op.py:2935-2941)
+        bad.append('use_fix_H2He')
     if getattr(cfg, 'non_gas_sp', []):
         bad.append('non_gas_sp')
+    if getattr(cfg, 'diff_esc', []) and not getattr(cfg, 'use_moldiff', True):
+        # lhs_jac_no_mol's escape term (op.py:2102-2107); with molecular
+        # diffusion the escape only enters through the top flux, as here
+        bad.append('diff_esc with use_moldiff = False')
     return bad
 
 
