@@ -18,7 +18,15 @@ For each workload it
   4. stores the compiled network (our parser's tables) beside the reference's
      own view of it (species order, nr) and the atmosphere arrays.
 
-Usage:  python tests/golden/make_golden.py [c0|c1|c2 ...] [--ref /root/reference]
+Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow (Ros2 attempts and
+trajectories); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
+with and without molecular diffusion, plus the reference's transport RHS and
+LHS blocks); c1rt, c1rtT (the reference's radiative transfer, T-independent
+and T-dependent cross sections); lowT (rate constants with the
+low-temperature caps).
+
+Usage:  python tests/golden/make_golden.py [tag ...] [--ref /root/reference]
+        python tests/golden/make_golden.py --setup-only c1rt c1rtT
 """
 from __future__ import annotations
 
