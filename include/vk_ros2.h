@@ -11,12 +11,16 @@
  *                       and make_chem_funs.py:653-717 (symbolic Jacobian)
  *   vk_set_columns      store.py:21-180 data contract (var.y, var.k, atm.*)
  *   vk_ros2_attempt     op.py:2860-3007   Ros2.solver (one Rosenbrock attempt)
- *   vk_one_step         op.py:3091-3103   Ros2.one_step (+ clip/loss/step_ok/
- *                       step_reject, op.py:2447-2534)
- *   vk_run              op.py:808-936     Integration.__call__ (accept/reject,
+ *   vk_run              op.py:808-936     Integration.__call__ for a batch of
+ *                       columns: Ros2.one_step op.py:3091-3103 with clip /
+ *                       loss / step_ok / step_reject op.py:2447-2534,
  *                       step_size op.py:3105-3125, update_mu_dz op.py:944-984,
- *                       conv/stop op.py:1018-1085) for a batch of columns
+ *                       conv / stop op.py:1018-1085 (max_steps = 1: one step)
  *   vk_get_state        var.y / var.ymix / var.dt / para.delta read-back
+ *   vk_compute_k        op.py:63-342      ReadRate read_rate / rev_rate /
+ *                       lim_lowT_rates on the device
+ *   vk_photo_*          op.py:2580-2786   compute_tau / compute_flux /
+ *                       compute_J on the device
  */
 #ifndef VK_ROS2_H
 #define VK_ROS2_H
