@@ -105,3 +105,22 @@ def test_every_entry_point_rejects_null_arguments(lib):
         assert f(*args) == capi.VK_EINVAL, name
         checked += 1
     assert checked == len(capi.EXPORTS) - len(NO_HANDLE)
+
+
+def test_c_client_builds_and_runs(lib, tmp_path):
+    """A plain C program compiled against include/vk_ros2.h and linked to
+    the library: network compile, table sizes, Jacobian pattern, error paths."""
+    import shutil
+    import subprocess
+    from vulcan_gb300 import capi
+    cc = shutil.which('gcc') or shutil.which('cc')
+    if cc is None:
+        pytest.skip('no C compiler')
+    libdir = os.path.dirname(capi.LIB)
+    exe = str(tmp_path / 'c_abi_client')
+    subprocess.run([cc, '-std=c99', '-Wall', '-Werror', '-I', os.path.join(REPO, 'include'),
+                    os.path.join(REPO, 'tests', 'c_abi_client.c'), '-o', exe,
+                    '-L', libdir, '-lvk_gb300', '-Wl,-rpath,' + libdir], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.startswith('c-abi ok')
