@@ -20,8 +20,8 @@ For each workload it
 
 Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow (Ros2 attempts and
 trajectories); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
-with and without molecular diffusion, plus the reference's transport RHS and
-LHS blocks); c1rt, c1rtT (the reference's radiative transfer, T-independent
+with and without molecular diffusion) and c0vz (vertical advection), with
+the reference's transport RHS and LHS blocks; c1rt, c1rtT (the reference's radiative transfer, T-independent
 and T-dependent cross sections); lowT (rate constants with the
 low-temperature caps).
 
@@ -60,10 +60,11 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c1rtT': (0,),
         'lowT': (0,),
         'c0bc': (0, 1, 2, 10, 29),
-        'c0nomol': (0, 1, 2, 10, 29)}
+        'c0nomol': (0, 1, 2, 10, 29),
+        'c0vz': (0, 1, 2, 10, 29)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1, 'c0bc': 30,
-          'c0nomol': 30}
+          'c0nomol': 30, 'c0vz': 30}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -88,6 +89,10 @@ BC_FILES = {'atm/BC_top_golden.txt': '#species flux [cm-2 s-1]\nCO2  1.0E+12\nH2
             'atm/BC_bot_golden.txt': ('#species flux [cm-2 s-1]   v_dep [cm s-1]\n'
                                       'CH4  1.0E+14  0.\nCO  0.  1.0E-02\nH2O  2.0E+14  1.0E-03\n')}
 BC_TAGS = ('c0bc', 'c0nomol')
+# vertical advection: a vz profile that changes sign (upwind branches both
+# ways), injected like T and Kzz
+EXTRA_CFG['c0vz'] = 'use_vz = True\n'
+VZ_TAGS = ('c0vz',)
 PHOTO_TAGS = ('c1rt', 'c1rtT')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
 RATE_TAGS = ('lowT',)
@@ -121,6 +126,8 @@ atm.Tco = inp['Tco'].copy()
 atm.M = atm.pco / (kb * atm.Tco)
 atm.n_0 = atm.M.copy()
 atm.Kzz = inp['Kzz'].copy()
+if 'vz' in inp.files:
+    atm.vz = inp['vz'].copy()
 rate = op.ReadRate()
 var = rate.read_rate(var, atm)
 var = rate.rev_rate(var, atm)
@@ -176,7 +183,7 @@ class RecRos2(op.Ros2):
         return v
 
 solver = RecRos2()
-if vulcan_cfg.use_topflux or vulcan_cfg.use_botflux or not vulcan_cfg.use_moldiff:
+if vulcan_cfg.use_topflux or vulcan_cfg.use_botflux or not vulcan_cfg.use_moldiff or np.any(atm.vz):
     # the reference's own transport RHS and LHS at the initial state, with the
     # functions its Ros2.solver picks for these options (op.py:2870-2888); the
     # LHS with every rate constant zero and dt = 1e10 s, so that its blocks are
@@ -266,6 +273,8 @@ atm.Tco = inp['Tco'].copy()
 atm.M = atm.pco / (kb * atm.Tco)
 atm.n_0 = atm.M.copy()
 atm.Kzz = inp['Kzz'].copy()
+if 'vz' in inp.files:
+    atm.vz = inp['vz'].copy()
 rate = op.ReadRate()
 var = rate.read_rate(var, atm)
 var = rate.rev_rate(var, atm)
@@ -453,8 +462,13 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
         f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, tag in PHOTO_TAGS,
                                          EXTRA_CFG.get(tag, '')))
     keys = sorted(spec.photo_J) if spec.photo_J else []
+    extra_in = {}
+    if tag in VZ_TAGS:     # cm/s on the nz-1 interfaces: +100 below, -100 above
+        x = np.linspace(0., 1., nz - 1)
+        extra_in['vz'] = 100. * np.cos(np.pi * x)
     np.savez(os.path.join(dst, 'golden_inputs.npz'), Tco=spec.Tco, Kzz=spec.Kzz,
-             photo_J=np.array([spec.photo_J[k] for k in keys]) if keys else np.zeros((0, nz)))
+             photo_J=np.array([spec.photo_J[k] for k in keys]) if keys else np.zeros((0, nz)),
+             **extra_in)
     with open(os.path.join(dst, 'golden_meta.json'), 'w') as f:
         json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep)}, f)
     with open(os.path.join(dst, 'golden_driver.py'), 'w') as f:
@@ -520,7 +534,7 @@ def slim_photo(d):
 
 
 def make(tag, ref_root, workdir, full_dir=None):
-    if tag in ('c0', 'c0bc', 'c0nomol'):
+    if tag in ('c0', 'c0bc', 'c0nomol', 'c0vz'):
         spec = configs.config0()
     elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]

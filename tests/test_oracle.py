@@ -118,39 +118,55 @@ def test_reference_does_not_meet_tight_criterion():
 
 
 
-@pytest.mark.parametrize('tag', ['c0bc', 'c0nomol'])
+TRANSPORT_TAGS = ['c0bc', 'c0nomol', 'c0vz']
+
+
+@pytest.mark.parametrize('tag', TRANSPORT_TAGS)
 def test_transport_options_match_reference(tag):
-    """Constant top and bottom fluxes with deposition velocities on the c0
-    column, with molecular diffusion (c0bc: diffdf, lhs_jac_tot) and without
-    (c0nomol: diffdf_no_mol, lhs_jac_no_mol): the reference's own transport
-    RHS at the initial state, and its LHS blocks with the chemistry switched
-    off (k = 0, dt = 1e10 s) so that they hold the transport Jacobian."""
+    """Transport options on the c0 column against the reference's own
+    functions at the initial state: constant top and bottom fluxes with
+    deposition velocities, with molecular diffusion (c0bc: diffdf,
+    lhs_jac_tot) and without (c0nomol: diffdf_no_mol, lhs_jac_no_mol), and
+    vertical advection changing sign with height (c0vz).  The RHS, and the
+    LHS blocks with the chemistry switched off (k = 0, dt = 1e10 s) so that
+    they hold the transport Jacobian."""
     import dataclasses
     from helpers import base_atm, fixture_flags
     g = golden(tag)
     flags = fixture_flags(g)
-    assert flags.use_topflux and flags.use_botflux and flags.use_moldiff == (tag == 'c0bc')
+    fluxes = tag != 'c0vz'
+    assert flags.use_topflux == flags.use_botflux == fluxes
+    assert flags.use_moldiff == (tag != 'c0nomol')
     atm = base_atm(g)
     d = O.diffdf(g['y_ini'], atm, flags)
     np.testing.assert_array_equal(d, g['diffdf0'])
-    # the fluxes are not lost in the rounding of the other terms
-    plain = O.diffdf(g['y_ini'], atm, dataclasses.replace(flags, use_topflux=False,
-                                                          use_botflux=False))
+    # the option is not lost in the rounding of the other terms
+    if fluxes:
+        plain_flags, plain_atm = dataclasses.replace(flags, use_topflux=False,
+                                                     use_botflux=False), atm
+    else:
+        assert np.any(g['vz'] > 0) and np.any(g['vz'] < 0)
+        plain_flags, plain_atm = flags, dict(atm, vz=np.zeros_like(atm['vz']))
+    plain = O.diffdf(g['y_ini'], plain_atm, plain_flags)
     assert np.max(np.abs(plain - d) / np.maximum(np.abs(d), 1e-300)) > 1e-3
     on = oracle_net(tag, g)
     kz = np.zeros_like(g['k'])
     D, U, L = O.lhs_blocks(on, g['y_ini'], g['M'], kz, float(g['lhs_dt']), atm, flags)
-    D0, _, _ = O.lhs_blocks(on, g['y_ini'], g['M'], kz, float(g['lhs_dt']), atm,
-                            dataclasses.replace(flags, use_botflux=False))
     rel = lambda a, b: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
     for i, l in enumerate(g['lhs_layers']):
         assert rel(D[l], g['lhs_D'][i]) <= 1e-15
         assert rel(U[l], g['lhs_U'][i]) <= 1e-15 and rel(L[l], g['lhs_L'][i]) <= 1e-15
-    # the deposition velocity's Jacobian term is visible in the bottom block
+    # the deposition velocity's / advection's Jacobian terms are visible
+    D0, U0, L0 = O.lhs_blocks(on, g['y_ini'], g['M'], kz, float(g['lhs_dt']), plain_atm,
+                              dataclasses.replace(flags, use_botflux=False)
+                              if fluxes else plain_flags)
     assert rel(D0[0], g['lhs_D'][0]) > 1e-5
+    if not fluxes:
+        mid = list(g['lhs_layers']).index(len(g['y_ini']) // 2)
+        assert rel(U0[len(g['y_ini']) // 2], g['lhs_U'][mid]) > 1e-5
 
 
-@pytest.mark.parametrize('tag,n', _attempts('c0bc') + _attempts('c0nomol'))
+@pytest.mark.parametrize('tag,n', [a for t in TRANSPORT_TAGS for a in _attempts(t)])
 def test_transport_option_attempts_match_reference(tag, n):
     """The recorded attempts of the same runs (30 steps; top fluxes as the
     reference's update_phi_esc left them, H escaping in c0bc), banded and

@@ -1,8 +1,9 @@
 """Device attempts with the reference's transport options against the
 attempts it recorded: constant top and bottom fluxes with deposition
 velocities and H escape through the top flux, with molecular diffusion
-(fixture c0bc) and without it (c0nomol).  The oracle reproduces the same
-fixtures (tests/test_oracle.py)."""
+(fixture c0bc) and without it (c0nomol), and vertical advection changing sign
+with height (c0vz).  The oracle reproduces the same fixtures
+(tests/test_oracle.py)."""
 import numpy as np
 import pytest
 
@@ -18,16 +19,18 @@ def built():
 
 
 @pytest.mark.parametrize('precision', [0, 1])
-@pytest.mark.parametrize('tag', ['c0bc', 'c0nomol'])
+@pytest.mark.parametrize('tag', ['c0bc', 'c0nomol', 'c0vz'])
 def test_attempts_with_transport_options(tag, precision):
     from vulcan_gb300 import capi
     from vulcan_gb300.solver import ColumnBatch, GPUNetwork, Ros2Handle
     g = golden(tag)
     net = network(tag)
     gn = GPUNetwork(net, [str(a) for a in g['atom_list']])
-    flags = capi.VK_F_TOPFLUX | capi.VK_F_BOTFLUX
-    if bool(g['use_moldiff']):
-        flags |= capi.VK_F_MOLDIFF
+    flags = 0
+    for key, bit in (('use_moldiff', capi.VK_F_MOLDIFF), ('use_topflux', capi.VK_F_TOPFLUX),
+                     ('use_botflux', capi.VK_F_BOTFLUX)):
+        if bool(g[key]):
+            flags |= bit
     items = []
     for n in range(len(g['att_index'])):
         col = column_from_golden(g, n)
