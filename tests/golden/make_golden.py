@@ -22,8 +22,8 @@ Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow (Ros2 attempts and
 trajectories); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
 with and without molecular diffusion) and c0vz (vertical advection), with
 the reference's transport RHS and LHS blocks; c1rt, c1rtT (the reference's radiative transfer, T-independent
-and T-dependent cross sections); lowT (rate constants with the
-low-temperature caps).
+and T-dependent cross sections); lowT, rmlist (rate constants with the
+low-temperature caps, and with reactions removed).
 
 Usage:  python tests/golden/make_golden.py [tag ...] [--ref /root/reference]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
@@ -61,10 +61,11 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'lowT': (0,),
         'c0bc': (0, 1, 2, 10, 29),
         'c0nomol': (0, 1, 2, 10, 29),
-        'c0vz': (0, 1, 2, 10, 29)}
+        'c0vz': (0, 1, 2, 10, 29),
+        'rmlist': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1, 'c0bc': 30,
-          'c0nomol': 30, 'c0vz': 30}
+          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -95,7 +96,9 @@ EXTRA_CFG['c0vz'] = 'use_vz = True\n'
 VZ_TAGS = ('c0vz',)
 PHOTO_TAGS = ('c1rt', 'c1rtT')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
-RATE_TAGS = ('lowT',)
+RATE_TAGS = ('lowT', 'rmlist')
+# remove_list: two forward rates and one reverse rate taken out
+EXTRA_CFG['rmlist'] = 'remove_list = [5, 12, 101]\n'
 
 DRIVER = r'''
 import os, sys, time, json
@@ -542,6 +545,8 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a column of the 512-column batch that has not converged after 4000 steps
         # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
         spec = configs.config2_columns(ncols=512, seed=2)[60]
+    elif tag == 'rmlist':
+        spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]
     elif tag == 'lowT':
         # a cold column (150 -> 450 K) crossing the three low-temperature caps
         spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]

@@ -104,3 +104,16 @@ def test_low_temperature_caps_bit_exact():
                      'H + C2H5 + M -> C2H6 + M'}
     kind, t_max, params = net.rate_caps()
     assert int((kind > 0).sum()) == 3 and set(t_max[kind > 0]) == {277.5, 300., 200.}
+
+
+def test_remove_list_bit_exact():
+    """remove_list = [5, 12, 101] (two forward rates, one reverse rate): the
+    reference's rev_rate / remove_rate zero exactly those slots; a removed
+    forward rate keeps its reverse (fixture rmlist)."""
+    g = golden('rmlist')
+    net = network('c2')
+    k = net.rate_constants(g['Tco'], g['M'], remove_list=[5, 12, 101])
+    np.testing.assert_array_equal(k, g['k'])
+    for i in (5, 12, 101):
+        assert np.all(k[i - 1] == 0)
+    assert np.all(k[5] > 0) and np.all(k[101] > 0)    # reverses of 5 and 101
