@@ -21,7 +21,8 @@ For each workload it
 Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow (Ros2 attempts and
 trajectories); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
 with and without molecular diffusion) and c0vz (vertical advection), with
-the reference's transport RHS and LHS blocks; c1rt, c1rtT (the reference's radiative transfer, T-independent
+the reference's transport RHS and LHS blocks; c0n2, c0o2, c0co2, c0rocky
+(column set-up with another molecular-diffusion base gas, rocky surface); c1rt, c1rtT (the reference's radiative transfer, T-independent
 and T-dependent cross sections); lowT, rmlist (rate constants with the
 low-temperature caps, and with reactions removed).
 
@@ -62,10 +63,12 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c0bc': (0, 1, 2, 10, 29),
         'c0nomol': (0, 1, 2, 10, 29),
         'c0vz': (0, 1, 2, 10, 29),
-        'rmlist': (0,)}
+        'rmlist': (0,),
+        'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1, 'c0bc': 30,
-          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1}
+          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
+          'c0rocky': 2}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -93,6 +96,10 @@ BC_TAGS = ('c0bc', 'c0nomol')
 # vertical advection: a vz profile that changes sign (upwind branches both
 # ways), injected like T and Kzz
 EXTRA_CFG['c0vz'] = 'use_vz = True\n'
+# column set-up variants: molecular-diffusion base gas, rocky surface
+for _t, _base in (('c0n2', 'N2'), ('c0o2', 'O2'), ('c0co2', 'CO2')):
+    EXTRA_CFG[_t] = "atm_base = '%s'\n" % _base
+EXTRA_CFG['c0rocky'] = 'rocky = True\n'
 VZ_TAGS = ('c0vz',)
 PHOTO_TAGS = ('c1rt', 'c1rtT')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
@@ -157,7 +164,8 @@ setup = dict(pico=atm.pico, M=atm.M, n_0=atm.n_0, mu=atm.mu, g=atm.g.copy(),
              pref_indx=atm.pref_indx, top_flux=atm.top_flux.copy(), bot_flux=atm.bot_flux.copy(),
              bot_vdep=atm.bot_vdep.copy(), use_moldiff=bool(vulcan_cfg.use_moldiff),
              use_topflux=bool(vulcan_cfg.use_topflux), use_botflux=bool(vulcan_cfg.use_botflux),
-             diff_esc=np.array(list(vulcan_cfg.diff_esc), dtype='U8'))
+             diff_esc=np.array(list(vulcan_cfg.diff_esc), dtype='U8'),
+             atm_base=str(vulcan_cfg.atm_base), rocky=bool(vulcan_cfg.rocky))
 # chemistry pins at the initial state
 setup['chemdf0'] = chem_funs.chemdf(var.y, atm.M, var.k)
 ATT, STEPS = [], []
@@ -537,7 +545,7 @@ def slim_photo(d):
 
 
 def make(tag, ref_root, workdir, full_dir=None):
-    if tag in ('c0', 'c0bc', 'c0nomol', 'c0vz'):
+    if tag in ('c0', 'c0bc', 'c0nomol', 'c0vz', 'c0n2', 'c0o2', 'c0co2', 'c0rocky'):
         spec = configs.config0()
     elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]

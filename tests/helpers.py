@@ -13,7 +13,9 @@ NETS = {'c0': 'net_CHO_thermo.npz', 'c1': 'net_NCHO_photo.npz', 'c2': 'net_NCHO_
         'c2long': 'net_NCHO_thermo.npz', 'c2conv': 'net_NCHO_thermo.npz',
         'c2tight': 'net_NCHO_thermo.npz', 'c2slow': 'net_NCHO_thermo.npz',
         'c0bc': 'net_CHO_thermo.npz', 'c0nomol': 'net_CHO_thermo.npz',
-        'c0vz': 'net_CHO_thermo.npz'}
+        'c0vz': 'net_CHO_thermo.npz', 'c0n2': 'net_CHO_thermo.npz',
+        'c0o2': 'net_CHO_thermo.npz', 'c0co2': 'net_CHO_thermo.npz',
+        'c0rocky': 'net_CHO_thermo.npz'}
 
 
 def golden(tag):

@@ -30,12 +30,17 @@ def test_rate_constants_bit_exact(tag):
     np.testing.assert_array_equal(k, g['k'])
 
 
-@pytest.mark.parametrize('tag', ['c0', 'c2'])
+@pytest.mark.parametrize('tag', ['c0', 'c2', 'c0n2', 'c0o2', 'c0co2', 'c0rocky'])
 def test_column_setup_bit_exact(tag):
+    """pico, M, n_0, mu, g, Hp, dz, dzi, Ti, Hpi, Dzz, ms, alpha as the
+    reference's f_pico / f_mu_dz / mol_diff built them, for the H2 base gas
+    and the N2, O2 and CO2 ones (c0n2, c0o2, c0co2) and a rocky surface."""
     g = golden(tag)
     net = network(tag)
+    base = str(g.get('atm_base', 'H2'))
+    rocky = bool(g.get('rocky', False))
     col = C.build_column(net, g['pco'], g['Tco'], g['Kzz'], gs=configs.GS, Rp=configs.RP,
-                         ymix0=g['ymix_ini'])
+                         rocky=rocky, atm_base=base, ymix0=g['ymix_ini'])
     assert col.pref_indx == int(g['pref_indx'])
     for key in ('pico', 'M', 'n_0', 'mu', 'g', 'Hp', 'dz', 'dzi', 'Ti', 'Hpi', 'Dzz', 'ms', 'alpha'):
         np.testing.assert_array_equal(getattr(col, key), g[key], err_msg=key)
