@@ -180,3 +180,19 @@ def test_transport_option_attempts_match_reference(tag, n):
         r = O.ros2_attempt(*args, solve)
         assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
         assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
+
+
+@pytest.mark.parametrize('tag,n', [a for t in ('c0n2', 'c0o2', 'c0co2', 'c0rocky')
+                                   for a in _attempts(t)])
+def test_setup_variant_attempts_match_reference(tag, n):
+    """The first recorded attempt on the N2 / O2 / CO2 base-gas columns and
+    the rocky one (their molecular diffusion and gravity differ)."""
+    from helpers import fixture_flags
+    g = golden(tag)
+    on = oracle_net(tag, g)
+    args = (on, g['att_y'][n], g['att_ymix'][n], float(g['att_dt'][n]), g['k'],
+            attempt_atm(g, n), fixture_flags(g), O.Tol())
+    for solve in ('banded', 'block'):
+        r = O.ros2_attempt(*args, solve)
+        assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
+        assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
