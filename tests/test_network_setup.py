@@ -30,19 +30,24 @@ def test_rate_constants_bit_exact(tag):
     np.testing.assert_array_equal(k, g['k'])
 
 
-@pytest.mark.parametrize('tag', ['c0', 'c2', 'c0n2', 'c0o2', 'c0co2', 'c0rocky'])
+@pytest.mark.parametrize('tag', ['c0', 'c2', 'c0n2', 'c0o2', 'c0co2', 'c0rocky', 'c0nomol'])
 def test_column_setup_bit_exact(tag):
     """pico, M, n_0, mu, g, Hp, dz, dzi, Ti, Hpi, Dzz, ms, alpha as the
     reference's f_pico / f_mu_dz / mol_diff built them, for the H2 base gas
-    and the N2, O2 and CO2 ones (c0n2, c0o2, c0co2) and a rocky surface."""
+    and the N2, O2 and CO2 ones (c0n2, c0o2, c0co2), a rocky surface, and
+    without molecular diffusion (no interface T or Hp then)."""
     g = golden(tag)
     net = network(tag)
     base = str(g.get('atm_base', 'H2'))
     rocky = bool(g.get('rocky', False))
+    mol = bool(g.get('use_moldiff', True))
     col = C.build_column(net, g['pco'], g['Tco'], g['Kzz'], gs=configs.GS, Rp=configs.RP,
-                         rocky=rocky, atm_base=base, ymix0=g['ymix_ini'])
+                         rocky=rocky, atm_base=base, use_moldiff=mol, ymix0=g['ymix_ini'])
     assert col.pref_indx == int(g['pref_indx'])
     for key in ('pico', 'M', 'n_0', 'mu', 'g', 'Hp', 'dz', 'dzi', 'Ti', 'Hpi', 'Dzz', 'ms', 'alpha'):
+        if not mol and key in ('Ti', 'Hpi'):
+            assert getattr(col, key) is None and not np.any(g[key])
+            continue
         np.testing.assert_array_equal(getattr(col, key), g[key], err_msg=key)
 
 
