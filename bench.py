@@ -210,6 +210,14 @@ def _measure(args, precision, clocks=None, dist=None):
     net, items, h, b, ctrl = _setup(args, precision)
     h.run(ctrl, max_steps=args.warmup, timeout_s=1800)
     st0, c0 = h.state(), h.counters()
+    launch = None
+    if getattr(args, 'autotune', False):
+        # launch settings measured on this batch at its current step sizes
+        # (attempts do not advance the state; the clock is put back after)
+        from vulcan_gb300 import autotune
+        launch = autotune.tune(h, st0['dt'], precision=precision, repeats=2)
+        h.set_state(st0['y'], st0['ymix'])
+        h.set_clock(dt=st0['dt'], t=st0['t'], count=st0['count'])
     if clocks is not None:
         clocks.__enter__()
         time.sleep(0.3)
@@ -228,6 +236,9 @@ def _measure(args, precision, clocks=None, dist=None):
     steps_all, sec_max = replicas.reduce_run(dist, steps, ms_dev * 1e-3)
     out = dict(value=steps_all / sec_max, ms=sec_max * 1e3, steps=steps, attempts=attempts,
                launches=tm['launches'], fallbacks=int((c1[:, 4] - c0[:, 4]).sum()))
+    if launch is not None:
+        out['launch'] = {k: (list(v) if isinstance(v, tuple) else round(v, 3))
+                         for k, v in launch.items()}
     # per-kernel device times of one attempt from the current state
     h.set_state(st1['y'], st1['ymix'])
     for _ in range(2):
@@ -346,6 +357,8 @@ def run_gpu(args):
                                        'unit': 'TFLOP/s', 'frac': round(lu64 / peak64, 4),
                                        'peak_source': 'measured cuBLAS DGEMM 8192^3 in this run'}},
         'mixed_over_plain': round(mixed['value'] / plain['value'], 3),
+        'launch_tuning': ({'mixed': mixed['launch'], 'plain_fp64': plain['launch']}
+                          if 'launch' in mixed else 'built-in defaults'),
         'rates_kernel': {'bound': 'hbm', 'achieved': round(rate_bytes / (am['rates'] * 1e-3) / 1e9, 1),
                          'peak': hbm, 'unit': 'GB/s', 'peak_source': hbm_kind,
                          'frac': round(rate_bytes / (am['rates'] * 1e-3) / 1e9 / hbm, 4)},
@@ -596,6 +609,8 @@ def main():
     ap.add_argument('--photo', action='store_true',
                     help='radiative-transfer update throughput (photochemistry workload)')
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
+    ap.add_argument('--autotune', action='store_true',
+                    help='tune the per-column kernels\' launch settings on the batch first')
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
     ap.add_argument('--converge-timeout', type=float, default=1800.0)

@@ -215,6 +215,21 @@ VK_API int  vk_set_rate_params(vk_handle *h, const int *kind, const int *rev, co
 VK_API int  vk_set_rate_caps(vk_handle *h, const int *kind, const double *t_max,
                              const double *params);
 VK_API int  vk_compute_k(vk_handle *h);
+/* ---- launch tuning (for an autotuner; no counterpart in the reference) ----
+ * The per-column kernels take columns from a work queue; their grid is
+ * ctas_per_sm x SMs CTAs.  kernel: VK_TUNE_*; ctas_per_sm 0..8 (0: the
+ * kernel's built-in default, or VK_CTAS_PER_SM from the environment);
+ * variant: for VK_TUNE_LU32 the register tiling of the FP32 Gauss-Jordan,
+ * 0..3 covering blocks up to 48, 80, 112, 160 species (-1: the smallest that
+ * covers ni; a tiling smaller than ni is refused), ignored otherwise.  A
+ * change drops the captured vk_run graph, which is captured again. */
+#define VK_TUNE_LU32    0   /* k_lu32: FP32 block-Thomas factorisation        */
+#define VK_TUNE_LU64    1   /* k_lu_fwd_f64: FP64 factorisation + first sweep */
+#define VK_TUNE_SWEEP64 2   /* k_back_f64, k_solve_f64: FP64 sweeps           */
+#define VK_TUNE_REFINE  3   /* k_refine: FP64 refinement with FP32 factors    */
+#define VK_TUNE_N       4
+VK_API int  vk_set_launch(vk_handle *h, int kernel, int ctas_per_sm, int variant);
+VK_API int  vk_get_launch(vk_handle *h, int kernel, int *ctas_per_sm, int *variant);
 /* Diagnostic: the device rate constants [L][nr] back to the host. */
 VK_API int  vk_get_k(vk_handle *h, double *k);
 

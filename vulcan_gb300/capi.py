@@ -14,6 +14,8 @@ from ._build import LIB
 VK_OK, VK_EINVAL, VK_ECUDA, VK_ESINGULAR, VK_ENAN, VK_EMAXATTEMPT, VK_ETIMEOUT, VK_ENOMEM = range(8)
 VK_PREC_FP64, VK_PREC_MIXED = 0, 1
 VK_F_MOLDIFF, VK_F_TOPFLUX, VK_F_BOTFLUX = 1, 2, 4
+VK_TUNE_LU32, VK_TUNE_LU64, VK_TUNE_SWEEP64, VK_TUNE_REFINE = 0, 1, 2, 3
+LU32_TILING_CAP = (48, 80, 112, 160)      # species each k_lu32 tiling covers
 (ATM_M, ATM_N0, ATM_TCO, ATM_G, ATM_DZI, ATM_KZZ, ATM_VZ, ATM_TI, ATM_HPI, ATM_HP,
  ATM_PICO, ATM_PICOU, ATM_DZ) = range(13)
 ATM_NF = 13
@@ -35,7 +37,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
-           'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps')
+           'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps',
+           'vk_set_launch', 'vk_get_launch')
 
 
 class VkNetworkDesc(C.Structure):
@@ -104,6 +107,8 @@ def lib(path=None):
         'vk_set_rate_params': (i, [vp, pi, pi, pd, pd]),
         'vk_compute_k': (i, [vp]),
         'vk_set_rate_caps': (i, [vp, pi, pd, pd]),
+        'vk_set_launch': (i, [vp, i, i, i]),
+        'vk_get_launch': (i, [vp, i, pi, pi]),
         'vk_get_k': (i, [vp, pd]),
         'vk_photo_setup': (i, [vp, i, pd, pd, i, pi, pi, pd, i, pi, pd, i, pi, pd, pd,
                                C.c_double, C.c_double, C.c_double, C.c_double]),

@@ -60,6 +60,8 @@ struct vk_handle {
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
     int nsm = 0;                        // SMs of the device
     int cps = 0;                        // VK_CTAS_PER_SM override (0: kernel defaults)
+    int cps_k[VK_TUNE_N] = {0, 0, 0, 0}; // vk_set_launch: CTAs per SM per kernel
+    int lu32_tiling = -1;               // vk_set_launch: k_lu32 tiling (-1: by ni)
     double *d_k = nullptr, *d_atm = nullptr, *d_Dzz = nullptr, *d_spf = nullptr;
     vk::Work w{};
     // batched-run state
@@ -94,6 +96,8 @@ struct vk_handle {
         b.queue = d_queue;
         b.nsm = nsm;
         b.cps = cps;
+        for (int i = 0; i < VK_TUNE_N; ++i) b.cps_k[i] = cps_k[i];
+        b.lu32_tiling = lu32_tiling;
         return b;
     }
 };
@@ -624,6 +628,32 @@ extern "C" int vk_set_rate_params(vk_handle *h, const int *kind, const int *rev,
     VK_CUDA(h, cudaMemcpy(h->d_krev, rev, h->npair * sizeof(int), cudaMemcpyHostToDevice));
     VK_CUDA(h, cudaMemcpy(h->d_kpar, params, (size_t)h->npair * 6 * sizeof(double), cudaMemcpyHostToDevice));
     VK_CUDA(h, cudaMemcpy(h->d_nasa9, nasa9, (size_t)h->ni * 20 * sizeof(double), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+extern "C" int vk_set_launch(vk_handle *h, int kernel, int ctas_per_sm, int variant) {
+    if (!h) return fail(h, VK_EINVAL, "handle is NULL");
+    if (kernel < 0 || kernel >= VK_TUNE_N) return fail(h, VK_EINVAL, "kernel must be a VK_TUNE_* value");
+    if (ctas_per_sm < 0 || ctas_per_sm > 8) return fail(h, VK_EINVAL, "ctas_per_sm must be 0..8");
+    if (kernel == VK_TUNE_LU32 && variant != -1 &&
+        (vk::lu32_tiling_cap(variant) == 0 || vk::lu32_tiling_cap(variant) < h->ni))
+        return fail(h, VK_EINVAL, "k_lu32 tiling " + std::to_string(variant) + " does not cover " +
+                                      std::to_string(h->ni) + " species");
+    if (h->stream) VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->gexec) {                        // the captured loop has the old grids
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    h->cps_k[kernel] = ctas_per_sm;
+    if (kernel == VK_TUNE_LU32) h->lu32_tiling = variant;
+    return VK_OK;
+}
+
+extern "C" int vk_get_launch(vk_handle *h, int kernel, int *ctas_per_sm, int *variant) {
+    if (!h) return fail(h, VK_EINVAL, "handle is NULL");
+    if (kernel < 0 || kernel >= VK_TUNE_N) return fail(h, VK_EINVAL, "kernel must be a VK_TUNE_* value");
+    if (ctas_per_sm) *ctas_per_sm = h->cps_k[kernel];
+    if (variant) *variant = kernel == VK_TUNE_LU32 ? h->lu32_tiling : -1;
     return VK_OK;
 }
 

@@ -91,12 +91,14 @@ struct DevBatch {
     int nsm;                   // SMs of the device
     int cps;                   // resident CTAs per SM of the per-column kernels
                                // (0: each kernel's own default)
+    int cps_k[VK_TUNE_N];      // per-kernel setting of vk_set_launch (0: cps)
+    int lu32_tiling;           // k_lu32 register tiling (-1: by ni)
 };
 
-// Grid of a per-column kernel: cps CTAs per SM (the batch's override, else
-// the kernel's default), never more than the columns.
-inline int column_grid(const DevBatch &b, int cps_default) {
-    const int cps = b.cps > 0 ? b.cps : cps_default;
+// Grid of a per-column kernel: CTAs per SM from vk_set_launch, else the
+// batch's override, else the kernel's default; never more than the columns.
+inline int column_grid(const DevBatch &b, int kernel, int cps_default) {
+    const int cps = b.cps_k[kernel] > 0 ? b.cps_k[kernel] : b.cps > 0 ? b.cps : cps_default;
     const long long g = (long long)cps * b.nsm;
     return (g > 0 && g < b.ncols) ? (int)g : b.ncols;
 }
@@ -200,5 +202,6 @@ void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
 cudaError_t init_lureg_kernels(const DevNet &net);
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
+int lu32_tiling_cap(int tiling);     // largest block a k_lu32 tiling covers (0: none)
 
 }  // namespace vk

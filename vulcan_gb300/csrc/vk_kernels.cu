@@ -475,21 +475,21 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
     const int n = net.ni;
     size_t sm = lu_fwd_smem(n);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_lu_fwd_f64<<<column_grid(b, 2), 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
+    k_lu_fwd_f64<<<column_grid(b, VK_TUNE_LU64, 2), 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
                                                     w.status);
 }
 
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
                      const double *z, double *x, const double *y, double *yk2, cudaStream_t s) {
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_back_f64<<<column_grid(b, 2), 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, z, x, y, yk2);
+    k_back_f64<<<column_grid(b, VK_TUNE_SWEEP64, 2), 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, z, x, y, yk2);
 }
 
 void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
                       const double *dC, const double *rhs, double *zbuf, double *x,
                       cudaStream_t s) {
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_solve_f64<<<column_grid(b, 2), 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, dC, rhs, zbuf, x);
+    k_solve_f64<<<column_grid(b, VK_TUNE_SWEEP64, 2), 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, dC, rhs, zbuf, x);
 }
 
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags, double mtol,

@@ -238,6 +238,10 @@ static size_t smem_prep(const DevNet &net) {
 
 #define VK_LU_TILINGS(X) X(16, 3, 3) X(16, 5, 5) X(16, 7, 7) X(32, 5, 10)
 
+// largest block each tiling covers (rows = TY * RA, columns = 16 * RB)
+static const int kTilingCap[4] = {48, 80, 112, 160};
+int lu32_tiling_cap(int t) { return t >= 0 && t < 4 ? kTilingCap[t] : 0; }
+
 static int tiling_of(int n) {
     if (n <= 48) return 0;
     if (n <= 80) return 1;
@@ -268,11 +272,14 @@ void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaSt
     const int nb = lu32_nbuf(n);
     size_t sm = smem32(n, nb);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    switch (tiling_of(n)) {
-    case 0: k_lu32<16, 3, 3><<<column_grid(b, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    case 1: k_lu32<16, 5, 5><<<column_grid(b, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    case 2: k_lu32<16, 7, 7><<<column_grid(b, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
-    default: k_lu32<32, 5, 10><<<column_grid(b, 1), 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    // vk_set_launch may pick a larger tiling than the smallest covering ni;
+    // every tiling zero-pads the rows and columns beyond ni
+    const int t = b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n);
+    switch (t) {
+    case 0: k_lu32<16, 3, 3><<<column_grid(b, VK_TUNE_LU32, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 1: k_lu32<16, 5, 5><<<column_grid(b, VK_TUNE_LU32, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    case 2: k_lu32<16, 7, 7><<<column_grid(b, VK_TUNE_LU32, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
+    default: k_lu32<32, 5, 10><<<column_grid(b, VK_TUNE_LU32, 1), 512, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
     }
 }
 

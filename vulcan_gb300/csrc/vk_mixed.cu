@@ -248,7 +248,7 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
     const int n = net.ni;
     size_t sm = 16 + (size_t)2 * block_stride32(n) * sizeof(float) + 2 * n * sizeof(float);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_refine<<<column_grid(b, 3), 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
+    k_refine<<<column_grid(b, VK_TUNE_REFINE, 3), 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
                                       rhs, x, w.r, w.zf, yscale, yk2, w.y, max_sweeps, tol,
                                       w.fallback, w.sweeps, w.status, w.refine_err, w.thr64,
                                       w.act32);

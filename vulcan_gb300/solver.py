@@ -308,6 +308,17 @@ class Ros2Handle:
         check(lib().vk_photo_get(self.h, ptr(tau), ptr(af), ptr(J)), self.h)
         return tau, af, J
 
+    def set_launch(self, kernel, ctas_per_sm=0, variant=-1):
+        """Launch tuning of one per-column kernel (vk_set_launch): CTAs per SM
+        (0: default) and, for capi.VK_TUNE_LU32, the register tiling (-1: by ni)."""
+        check(lib().vk_set_launch(self.h, int(kernel), int(ctas_per_sm), int(variant)), self.h)
+
+    def get_launch(self, kernel):
+        """(ctas_per_sm, variant) set for a kernel (vk_get_launch)."""
+        c, v = C.c_int(), C.c_int()
+        check(lib().vk_get_launch(self.h, int(kernel), C.byref(c), C.byref(v)), self.h)
+        return c.value, v.value
+
     def conv_stats(self):
         """(longdy, longdydt) of each column's last steady-state test."""
         b = self.batch
