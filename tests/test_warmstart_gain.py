@@ -65,7 +65,7 @@ def test_network_beats_equilibrium_and_const_mix_starts():
     X, Y, col = _data()
     assert X.shape[1] == int(w['dims'][0]) and len(np.unique(col)) >= 6
     e_mlp, e_eq, e_cm = _errors(_forward(w, X), X, Y, col)
-    # measured: 0.12 dex against 0.86 (equilibrium) and 13 (const_mix)
+    # measured: 0.09 dex against 2.5 (equilibrium) and 13 (const_mix)
     assert e_mlp < 0.2
     assert e_mlp < 0.3 * e_eq < e_cm
     # and column by column
