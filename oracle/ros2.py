@@ -1,7 +1,8 @@
 """Numpy restatement of the reference Ros2 kinetics-diffusion step (TEST ORACLE).
 
 Test infrastructure: imported only by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline / reference arm, as the checker or timed CPU path.
+bench.py's CPU-baseline / reference arm, as the oracle results are compared
+with or as the timed CPU path.
 
 Follows, function by function (paths relative to the reference project):
   chemdf            make_chem_funs.py:113-430 (generated chemdf / v_j lambdas)
