@@ -196,3 +196,26 @@ def test_setup_variant_attempts_match_reference(tag, n):
         r = O.ros2_attempt(*args, solve)
         assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
         assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
+
+
+@pytest.mark.parametrize('tag', TRANSPORT_TAGS + ['c0n2', 'c0rocky'])
+def test_trajectory_lockstep_with_options(tag):
+    """Free-running oracle with the fixture's transport options / column
+    set-up reproduces the reference's accept/reject and dt sequence over the
+    recorded steps (30 for the transport options, 2 for the set-up variants)."""
+    from helpers import fixture_flags
+    from vulcan_gb300 import configs
+    g = golden(tag)
+    on = oracle_net(tag, g)
+    atm = dict(attempt_atm(g, 0), dz=g['dz'], zco=g['zco'])
+    if 'att_top_flux' in g:               # as update_phi_esc set it at count 0
+        atm['top_flux'] = g['att_top_flux'][-1]
+    st = O.ColState(y=g['y_ini'].copy(), ymix=g['ymix_ini'].copy(), dt=1e-10,
+                    atom_ini=g['atom_ini'], atom_loss=np.zeros(g['atom_ini'].size))
+    n = len(g['traj_natt'])
+    dts, natt = [], []
+    O.integrate(on, st, g['k'], atm, fixture_flags(g), O.Tol(), configs.GS, configs.RP,
+                int(g['pref_indx']), max_steps=n, solve='block',
+                on_step=lambda s, a: (dts.append(s.dt), natt.append(s.attempts)))
+    np.testing.assert_array_equal(natt, g['traj_natt'])
+    np.testing.assert_allclose(dts, g['traj_dt_next'], rtol=1e-9)
