@@ -44,3 +44,43 @@ def test_unimplemented_options_raise(kw, name):
     var = types.SimpleNamespace(y=None)
     with pytest.raises(NotImplementedError, match=name.split()[0]):
         cls().solver(var, None, None)
+
+
+def test_dropin_packs_transport_options():
+    """Ros2GPU hands the reference's atm fluxes, deposition velocities and
+    vz to the device and turns use_moldiff / use_topflux / use_botflux into
+    the attempt flags (host side of fixtures c0bc and c0vz)."""
+    import numpy as np
+    from helpers import column_from_golden, golden, network
+    from vulcan_gb300 import capi
+    from vulcan_gb300.solver import GPUNetwork, _flags_from_cfg
+    for tag in ('c0bc', 'c0vz'):
+        g = golden(tag)
+        net = network(tag)
+        cfg = _cfg(use_topflux=bool(g['use_topflux']), use_botflux=bool(g['use_botflux']),
+                   atom_list=[str(a) for a in g['atom_list']])
+        f = _flags_from_cfg(cfg)
+        assert f & capi.VK_F_MOLDIFF
+        assert bool(f & capi.VK_F_TOPFLUX) == bool(g['use_topflux'])
+        assert bool(f & capi.VK_F_BOTFLUX) == bool(g['use_botflux'])
+
+        class FakeRos2:
+            pass
+
+        cls = make_ros2gpu(types.SimpleNamespace(Ros2=FakeRos2), cfg, net.species)
+        s = cls()
+        s._vk_gnet = GPUNetwork(net, cfg.atom_list)       # host-side tables only
+        col = column_from_golden(g, 1)
+        col.top_flux = g['att_top_flux'][1].copy()
+        col.bot_flux, col.bot_vdep = g['bot_flux'].copy(), g['bot_vdep'].copy()
+        atm = types.SimpleNamespace(**{k: getattr(col, k) for k in (
+            'M', 'n_0', 'Tco', 'g', 'dzi', 'Kzz', 'vz', 'Ti', 'Hpi', 'Hp', 'pico', 'dz', 'Dzz',
+            'ms', 'alpha', 'top_flux', 'bot_flux', 'bot_vdep', 'pref_indx')})
+        var = types.SimpleNamespace(y=g['att_y'][1], ymix=g['att_ymix'][1],
+                                    k={i: g['k'][i - 1] for i in range(1, net.nr + 1)})
+        b = s._vk_pack(var, atm)
+        np.testing.assert_array_equal(b.spf[0, capi.SP_TOPFLUX], col.top_flux)
+        np.testing.assert_array_equal(b.spf[0, capi.SP_BOTFLUX], col.bot_flux)
+        np.testing.assert_array_equal(b.spf[0, capi.SP_BOTVDEP], col.bot_vdep)
+        np.testing.assert_array_equal(b.atm[:-1, capi.ATM_VZ], g['vz'])
+        np.testing.assert_array_equal(b.k, g['k'].T)
