@@ -64,3 +64,30 @@ def test_minimises_gibbs_energy():
         d[big] = null.T @ rng.normal(size=null.shape[0])
         step = 1e-3 * np.min(x[big] / (np.abs(d[big]) + 1e-300))
         assert G(x + step * d) >= g0 - 1e-12 * abs(g0)
+
+
+def test_matches_the_reference_fastchem():
+    """The equilibrium start against the reference's own FastChem (fixture
+    golden_eq: five columns of the 512-column workload, FastChem built from
+    the reference's sources and run the way its ini_fc runs it, with the
+    same NASA-9 data): every network species above 1e-10 within 1e-3 dex
+    (FastChem iterates to 1e-4 relative) -- except the two FastChem lists
+    twice (CH2_1, C4H2: two data sets under one name, both present in its
+    equilibrium, where the network has one)."""
+    import os
+    from conftest import GOLDEN
+    from helpers import network
+    from vulcan_gb300 import eqchem
+    g = np.load(os.path.join(GOLDEN, 'golden_eq.npz'))
+    net = network('c2')
+    atoms = [str(a) for a in g['atoms']]
+    assert g['have'].all()
+    worst = 0.0
+    for c in g['columns']:
+        ref = g['x_%d' % c]
+        x = eqchem.equilibrium(net, g['tco_%d' % c], g['pco_%d' % c], g['abund_%d' % c], atoms)
+        m = (ref > 1e-10) & ~g['dup'][None, :]
+        err = np.abs(np.log10(np.maximum(x[m], 1e-300)) - np.log10(ref[m]))
+        worst = max(worst, float(err.max()))
+    assert worst < 1e-3, worst
+    assert sorted(net.species[i] for i in np.nonzero(g['dup'])[0]) == ['C4H2', 'CH2_1']
