@@ -43,3 +43,51 @@ def test_write_read_round_trip():
     assert missing == ['XYZ']
     np.testing.assert_array_equal(yr[:, :-1], y[nz0:][:, ::-1])
     np.testing.assert_array_equal(yr[:, -1], 0.0)
+
+
+# what the reference saves (store.py:83-86) and what its plot_py scripts read
+REF_VAR_SAVE = ['k', 'y', 'ymix', 'y_ini', 't', 'dt', 'longdy', 'longdydt', 'atom_ini',
+                'atom_sum', 'atom_loss', 'atom_conden', 'aflux_change', 'Rf']
+REF_PHOTO_SAVE = ['nbin', 'bins', 'dbin1', 'dbin2', 'tau', 'sflux', 'aflux', 'cross',
+                  'cross_scat', 'cross_J', 'J_sp', 'n_branch']
+PLOT_ATM = ['pco', 'zco', 'zmco', 'pico', 'dz', 'Tco', 'Kzz']
+PLOT_VAR = ['species', 'ymix', 'y', 'y_ini']
+PLOT_VAR_PHOTO = ['bins', 'cross_scat', 'aflux', 'cross', 'tau']
+
+
+def test_layout_has_what_the_reference_saves_and_plots():
+    from conftest import GOLDEN
+    from vulcan_gb300 import photo
+    net = network('c2')
+    specs = configs.config2_columns(ncols=2, seed=3, nz_range=(40, 50))
+    items = batch.build_items(specs, net)
+    L = sum(it['col'].nz for it in items)
+    y = np.concatenate([it['y'] for it in items])
+    state = dict(y=y, ymix=y / y.sum(axis=1, keepdims=True), t=np.ones(2), dt=np.ones(2),
+                 count=np.ones(2, dtype=np.int32), end_case=np.ones(2, dtype=np.int32),
+                 delta=np.zeros(2))
+    tables = photo.PhotoTables.from_fixture(dict(np.load(os.path.join(GOLDEN, 'golden_c1rt.npz'))))
+    nb, nch = len(tables.bins), len(tables.ch_sp)
+    rng = np.random.default_rng(1)
+    tau, aflux, J = rng.random((L + 2, nb)), rng.random((L, nb)), rng.random((L, nch))
+    os.makedirs(BUILD, exist_ok=True)
+    paths = [os.path.join(BUILD, 'ph%d.vul' % c) for c in range(2)]
+    vulio.write_batch(paths, net, items, state, ATOMS, photo=(tables, tau, aflux, J))
+    with open(paths[1], 'rb') as f:
+        d = pickle.load(f)
+    v, atm = d['variable'], d['atm']
+    for key in REF_VAR_SAVE + REF_PHOTO_SAVE + PLOT_VAR + PLOT_VAR_PHOTO:
+        assert key in v, key
+    for key in PLOT_ATM:
+        assert key in atm, key
+    nz0, nz1 = items[0]['col'].nz, items[1]['col'].nz
+    # staggered rows of the second column start at nz0 + 1
+    np.testing.assert_array_equal(v['tau'], tau[nz0 + 1:nz0 + 1 + nz1 + 1])
+    np.testing.assert_array_equal(v['aflux'], aflux[nz0:])
+    ch = list(zip(tables.ch_sp, tables.ch_br))
+    sp, br = ch[0]
+    np.testing.assert_array_equal(v['J_sp'][(sp, br)], J[nz0:, 0])
+    tot = sum(J[nz0:, i] for i, c in enumerate(ch) if c[0] == sp)
+    np.testing.assert_allclose(v['J_sp'][(sp, 0)], tot, rtol=1e-14)
+    np.testing.assert_allclose(atm['zmco'], 0.5 * (atm['zco'][:-1] + atm['zco'][1:]))
+    assert atm['zmco'].size == nz1

@@ -7,8 +7,10 @@ The reference saves a run as a pickle (protocol 4) of
 ``k`` (dict reaction index -> [nz]), ``y``, ``ymix``, ``y_ini``, ``t``, ``dt``,
 ``longdy``, ``longdydt``, ``atom_ini``, ``atom_sum``, ``atom_loss``,
 ``atom_conden`` (dicts over atom_list), ``aflux_change`` and ``Rf`` (dict
-reaction index -> text).  Downstream scripts (the reference's plot_py/) read
-``variable['ymix']``, ``variable['species']``, ``atm['pco']`` and friends.
+reaction index -> text), with photochemistry also the radiative-transfer
+entries (store.py:85-86, ``photo_fields``).  Downstream scripts (the
+reference's plot_py/) read ``variable['ymix']``, ``variable['species']``,
+``atm['pco']``, ``atm['zco']``, ``atm['zmco']`` and friends.
 
 ``ini_mix = 'vulcan_ini'`` (build_atm.py:166-181) starts a run from the ``y``
 of such a file, species matched by name; :func:`read_vul_y` does the same.
@@ -24,9 +26,35 @@ ATM_KEYS = ('pco', 'pico', 'Tco', 'Kzz', 'vz', 'M', 'n_0', 'mu', 'g', 'Hp', 'dz'
             'pref_indx', 'gs', 'Rp')
 
 
+PHOTO_KEYS = ('nbin', 'bins', 'dbin1', 'dbin2', 'tau', 'sflux', 'aflux', 'cross', 'cross_scat',
+              'cross_J', 'J_sp', 'n_branch')
+
+
+def photo_fields(tables, tau, aflux, J):
+    """The photochemistry entries of var_save (store.py:85-86) for one column:
+    ``tables`` a photo.PhotoTables, ``tau`` [nz+1, nbins], ``aflux`` [nz,
+    nbins] and ``J`` [nz, nch] of that column (Ros2Handle.photo_get rows)."""
+    chans = list(zip(tables.ch_sp, tables.ch_br))
+    sflux = tables.sflux_top * np.exp(-1. * tau / np.cos(tables.sl_angle))
+    J_sp = {(sp, 0): np.zeros(aflux.shape[0]) for sp in tables.absp_sp}
+    n_branch = {sp: 0 for sp in tables.absp_sp}
+    for c, (sp, br) in enumerate(chans):
+        J_sp[(sp, br)] = np.array(J[:, c])
+        J_sp[(sp, 0)] = J_sp[(sp, 0)] + J[:, c]
+        n_branch[sp] = max(n_branch[sp], br)
+    return {'nbin': len(tables.bins), 'bins': np.array(tables.bins),
+            'dbin1': float(tables.dbin1), 'dbin2': float(tables.dbin2),
+            'tau': np.array(tau), 'sflux': sflux, 'aflux': np.array(aflux),
+            'cross': {sp: np.array(tables.cross[i]) for i, sp in enumerate(tables.absp_sp)},
+            'cross_scat': {sp: np.array(tables.cross_scat[i]) for i, sp in enumerate(tables.scat_sp)},
+            'cross_J': {c: np.array(tables.cross_J[i]) for i, c in enumerate(chans)},
+            'J_sp': J_sp, 'n_branch': n_branch}
+
+
 def vul_dict(net, item, y, ymix, t, dt, count, end_case, atom_list, longdy=0.0, longdydt=0.0,
-             delta=0.0):
-    """The save_out dictionary of one column (state arrays [nz, ni])."""
+             delta=0.0, photo=None):
+    """The save_out dictionary of one column (state arrays [nz, ni]); with
+    ``photo`` (photo_fields) also the photochemistry entries."""
     from .column import atom_totals
     col = item['col']
     k = item['k']
@@ -43,8 +71,13 @@ def vul_dict(net, item, y, ymix, t, dt, count, end_case, atom_list, longdy=0.0, 
            'atom_conden': {a: 0.0 for a in atom_list},
            'aflux_change': 0.0,
            'Rf': {r.index: r.text for r in net.reactions}}
+    if photo is not None:
+        var.update(photo)
     atm = {key: np.array(getattr(col, key)) if hasattr(getattr(col, key, None), '__len__')
            else getattr(col, key) for key in ATM_KEYS if hasattr(col, key)}
+    if getattr(col, 'zco', None) is not None:      # layer mid-points (f_mu_dz's zmco)
+        z = np.asarray(col.zco)
+        atm['zmco'] = 0.5 * (z[:-1] + z[1:])
     para = {'count': int(count), 'end_case': int(end_case), 'delta': float(delta),
             'solver_str': 'Ros2GPU'}
     return {'variable': var, 'atm': atm, 'parameter': para}
@@ -55,17 +88,24 @@ def write_vul(path, data):
         pickle.dump(data, f, protocol=4)
 
 
-def write_batch(paths, net, items, state, atom_list, conv=None):
+def write_batch(paths, net, items, state, atom_list, conv=None, photo=None):
     """One .vul per column of a batch state (Ros2Handle.state()); ``paths``
-    lists the file names; ``conv`` = (longdy, longdydt) per column."""
+    lists the file names; ``conv`` = (longdy, longdydt) per column; ``photo``
+    = (tables, tau, aflux, J) of the batch (Ros2Handle.photo_get) adds the
+    photochemistry entries."""
     off = np.concatenate([[0], np.cumsum([it['col'].nz for it in items])])
     for c, (path, it) in enumerate(zip(paths, items)):
         sl = slice(off[c], off[c + 1])
         ld = conv[0][c] if conv is not None else 0.0
         ldt = conv[1][c] if conv is not None else 0.0
+        ph = None
+        if photo is not None:
+            tables, tau, aflux, J = photo
+            # staggered rows of column c start at off[c] + c (nz + 1 of them)
+            ph = photo_fields(tables, tau[off[c] + c:off[c + 1] + c + 1], aflux[sl], J[sl])
         write_vul(path, vul_dict(net, it, state['y'][sl], state['ymix'][sl], state['t'][c],
                                  state['dt'][c], state['count'][c], state['end_case'][c],
-                                 atom_list, ld, ldt, state['delta'][c]))
+                                 atom_list, ld, ldt, state['delta'][c], photo=ph))
 
 
 def read_vul_y(path, species, nz=None):
