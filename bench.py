@@ -578,12 +578,17 @@ def run_profile(args):
 def run_reference(args):
     # one bounded sample: cpu_cols columns x the run's timed steps, all host cores
     res = cpu_baseline(args.cpu_cols, max(args.cpu_steps, args.steps), args.cpu_workers)
+    from vulcan_gb300 import configs
+    L = int(sum(sp.pco.size for sp in configs.config2_columns(ncols=NCOLS, seed=SEED)))
     out = {'metric': METRIC, 'value': round(res['value'], 3), 'unit': UNIT, 'n_gpus': args.gpus,
            'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True,
            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
            'data': 'synthetic (seeded columns; no dataset)', 'impl': 'reference',
-           'config': {'workload': 'batched Ros2, 512 uneven NCHO-thermo columns (ni=69, nz 60-200), '
-                                  'bounded sample on host cores'},
+           'config': {'workload': ('batched Ros2 steps, %d uneven NCHO-thermo columns (ni=69, '
+                                   'nz 60-200, sum nz=%d)' % (NCOLS, L)),
+                      'ncols': NCOLS, 'layers': L, 'network': 'NCHO_thermo (69 species, 391 pairs)',
+                      'precision': 'f64 (the reference step restated, LAPACK banded solve)',
+                      'sample': res.get('sample')},
            'cpu_baseline': res,
            'e2e': {'value': round(res['value'], 3), 'unit': UNIT, 'h2d_bytes_per_step': 0,
                    'd2h_bytes_per_step': 0}}
