@@ -4,7 +4,6 @@ velocities and H escape through the top flux, with molecular diffusion
 (fixture c0bc) and without it (c0nomol), and vertical advection changing sign
 with height (c0vz).  The oracle reproduces the same fixtures
 (tests/test_oracle.py)."""
-import numpy as np
 import pytest
 
 from helpers import column_from_golden, floor_err, golden, network
