@@ -84,3 +84,37 @@ def test_dropin_packs_transport_options():
         np.testing.assert_array_equal(b.spf[0, capi.SP_BOTVDEP], col.bot_vdep)
         np.testing.assert_array_equal(b.atm[:-1, capi.ATM_VZ], g['vz'])
         np.testing.assert_array_equal(b.k, g['k'].T)
+
+
+def test_batch_api_takes_the_transport_and_setup_options():
+    """ColumnSpec's top / bottom fluxes, deposition velocities, vz, base gas
+    and rocky flag reach the batch arrays, and run_batch's cfg turns
+    use_moldiff / use_topflux / use_botflux into the run's flags."""
+    import dataclasses
+    import numpy as np
+    from helpers import golden, network
+    from vulcan_gb300 import batch, capi, configs
+    from vulcan_gb300.solver import ColumnBatch, ctrl_from
+    net = network('c0')
+    g = golden('c0bc')
+    sp = configs.config0()
+    vz = 100.0 * np.cos(np.linspace(0, np.pi, sp.pco.size - 1))
+    sp = dataclasses.replace(sp, top_flux={'CO2': 1e12, 'H2O': 4e11},
+                             bot_flux={'CH4': (1e14, 0.0), 'CO': (0.0, 1e-2), 'H2O': (2e14, 1e-3)},
+                             vz=vz, atm_base='N2')
+    it = batch.build_items([sp], net)[0]
+    b = ColumnBatch([it], net.ni)
+    i = net.species.index
+    assert b.spf[0, capi.SP_TOPFLUX, i('CO2')] == 1e12
+    assert b.spf[0, capi.SP_BOTVDEP, i('CO')] == 1e-2 and b.spf[0, capi.SP_BOTFLUX, i('H2O')] == 2e14
+    # the same boundary arrays as the reference's BC_flux read from the same values
+    np.testing.assert_array_equal(b.spf[0, capi.SP_TOPFLUX], g['top_flux'])
+    np.testing.assert_array_equal(b.spf[0, capi.SP_BOTFLUX], g['bot_flux'])
+    np.testing.assert_array_equal(b.spf[0, capi.SP_BOTVDEP], g['bot_vdep'])
+    np.testing.assert_array_equal(b.atm[:-1, capi.ATM_VZ], vz)
+    assert it['col'].atm_base == 'N2'
+    assert ctrl_from(None).flags == capi.VK_F_MOLDIFF
+    assert ctrl_from({'use_topflux': True, 'use_botflux': True}).flags == \
+        capi.VK_F_MOLDIFF | capi.VK_F_TOPFLUX | capi.VK_F_BOTFLUX
+    assert ctrl_from(types.SimpleNamespace(use_moldiff=False)).flags == 0
+    assert ctrl_from({'rtol': 0.1}, flags=capi.VK_F_BOTFLUX).flags == capi.VK_F_BOTFLUX

@@ -22,7 +22,16 @@ def build_items(specs, net):
         pco = sp.pco
         n_0 = pco / (C.KB * sp.Tco)
         y, ymix = C.const_mix_state(net, n_0, sp.const_mix)
-        col = C.build_column(net, pco, sp.Tco, sp.Kzz, gs=configs.GS, Rp=configs.RP, ymix0=ymix)
+        col = C.build_column(net, pco, sp.Tco, sp.Kzz, gs=configs.GS, Rp=configs.RP,
+                             rocky=getattr(sp, 'rocky', False),
+                             use_moldiff=getattr(sp, 'use_moldiff', True),
+                             atm_base=getattr(sp, 'atm_base', 'H2'), vz=getattr(sp, 'vz', None),
+                             ymix0=ymix)
+        for name, v in (getattr(sp, 'top_flux', None) or {}).items():     # BC_flux, build_atm.py:742-762
+            col.top_flux[net.species.index(name)] = v
+        for name, (v, vdep) in (getattr(sp, 'bot_flux', None) or {}).items():
+            col.bot_flux[net.species.index(name)] = v
+            col.bot_vdep[net.species.index(name)] = vdep
         k = net.rate_constants(sp.Tco, col.M)
         if sp.photo_J:
             pidx = net.photo_index()
@@ -50,7 +59,9 @@ def make_batch_handle(net, items, atom_list, precision=capi.VK_PREC_FP64):
 
 def run_batch(net, specs, atom_list, max_steps=0, timeout_s=0.0, cfg=None,
               precision=capi.VK_PREC_FP64):
-    """Integrate every column to steady state (or max_steps); returns state dict."""
+    """Integrate every column to steady state (or max_steps); returns state
+    dict.  ``cfg`` (dict or vulcan_cfg-like module) gives the solver knobs and
+    use_moldiff / use_topflux / use_botflux."""
     items = build_items(specs, net)
     h, b = make_batch_handle(net, items, atom_list, precision)
     h.run(ctrl_from(cfg, gs=configs.GS, Rp=configs.RP), max_steps=max_steps, timeout_s=timeout_s)

@@ -43,6 +43,13 @@ class ColumnSpec:
     atom_list: list
     conver_ignore: list
     photo_J: dict = None    # {(sp, branch): J[nz]} frozen photolysis rates
+    # the reference's transport and set-up options (vulcan_cfg names):
+    top_flux: dict = None   # {sp: flux} constant top flux (BC_top file), cm^-2 s^-1
+    bot_flux: dict = None   # {sp: (flux, v_dep)} bottom flux and deposition (BC_bot file)
+    vz: np.ndarray = None   # [nz-1] vertical advection (cm/s, + upward)
+    use_moldiff: bool = True
+    atm_base: str = 'H2'
+    rocky: bool = False
 
 
 def log_p_grid(nz):

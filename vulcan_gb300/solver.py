@@ -131,9 +131,18 @@ class ColumnBatch:
         return [arr[self.off[c]:self.off[c + 1]] for c in range(self.ncols)]
 
 
-def ctrl_from(cfg=None, flags=capi.VK_F_MOLDIFF, gs=2140., Rp=1.138 * 7.1492E9,
-              max_attempts=400):
-    """vk_ctrl from a dict / module of vulcan_cfg-style knobs (defaults = reference)."""
+def ctrl_from(cfg=None, flags=None, gs=2140., Rp=1.138 * 7.1492E9, max_attempts=400):
+    """vk_ctrl from a dict / module of vulcan_cfg-style knobs (defaults = reference).
+    flags: VK_F_* bits; by default those of the cfg's use_moldiff / use_topflux
+    / use_botflux (molecular diffusion only without a cfg)."""
+    if flags is None:
+        if cfg is None:
+            flags = capi.VK_F_MOLDIFF
+        else:
+            get = cfg.get if isinstance(cfg, dict) else (lambda k, d: getattr(cfg, k, d))
+            flags = ((capi.VK_F_MOLDIFF if get('use_moldiff', True) else 0)
+                     | (capi.VK_F_TOPFLUX if get('use_topflux', False) else 0)
+                     | (capi.VK_F_BOTFLUX if get('use_botflux', False) else 0))
     v = dict(SOLVER_DEFAULTS)
     if cfg is not None:
         for k in v:
