@@ -399,3 +399,39 @@ def test_dropin_radiative_transfer_matches_reference(tag):
     assert abs(var.aflux_change / float(d['rec1_aflux_change']) - 1) < 1e-9
     assert var.tau.shape == (nz + 1, len(d['bins'])) and calls == []
     s._vk_h.close()
+
+
+def test_attach_cross_T_checks_shapes_and_slots():
+    """photo.attach_cross_T (host side): per-layer tables must be [L, nbins]
+    of the handle's batch; absorber and channel slots follow the tables'
+    lists (checked on a stand-in library)."""
+    import types
+    from vulcan_gb300 import capi, photo
+    d = _fixture('c1rtT')
+    t = photo.PhotoTables.from_fixture(d)
+    calls = []
+
+    class FakeLib:
+        def vk_photo_set_cross_T(self, *a):
+            calls.append(a)
+            return 0
+
+    h = types.SimpleNamespace(h=None, photo_tables=t, batch=types.SimpleNamespace(L=150))
+    orig_lib, orig_check = capi.lib, capi.check
+    capi.lib, capi.check = (lambda: FakeLib()), (lambda rc, hh=None: None)
+    try:
+        ct = {str(sp): d['cross_T'][i] for i, sp in enumerate(d['T_cross_sp'])}
+        cj = {(str(sp), int(br)): d['cross_J_T'][i]
+              for i, (sp, br) in enumerate(zip(d['chT_sp'], d['chT_br']))}
+        photo.attach_cross_T(h, ct, cj)
+        a = calls[-1]
+        assert a[1] == 3 and a[4] == 7
+        assert [t.absp_sp[a[2][i]] for i in range(a[1])] == list(ct)
+        chans = list(zip(t.ch_sp, t.ch_br))
+        assert [chans[a[5][i]] for i in range(a[4])] == list(cj)
+        with pytest.raises(ValueError):
+            photo.attach_cross_T(h, {k: v[:-1] for k, v in ct.items()}, cj)
+        photo.attach_cross_T(h, {}, {})                  # removes the tables
+        assert calls[-1][1] == 0 and calls[-1][4] == 0
+    finally:
+        capi.lib, capi.check = orig_lib, orig_check
