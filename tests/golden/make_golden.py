@@ -59,6 +59,7 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c2slow': (0,),
         'c1rt': (0,),
         'c1rtT': (0,),
+        'c1rtA': (0,),
         'lowT': (0,),
         'c0bc': (0, 1, 2, 10, 29),
         'c0nomol': (0, 1, 2, 10, 29),
@@ -66,7 +67,7 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'rmlist': (0,),
         'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
-          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'lowT': 1, 'c0bc': 30,
+          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'lowT': 1, 'c0bc': 30,
           'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
           'c0rocky': 2}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
@@ -101,7 +102,12 @@ for _t, _base in (('c0n2', 'N2'), ('c0o2', 'O2'), ('c0co2', 'CO2')):
     EXTRA_CFG[_t] = "atm_base = '%s'\n" % _base
 EXTRA_CFG['c0rocky'] = 'rocky = True\n'
 VZ_TAGS = ('c0vz',)
-PHOTO_TAGS = ('c1rt', 'c1rtT')
+# other radiative-transfer parameters: zenith angle 60 deg, Eddington
+# coefficient 0.669, f_diurnal 0.5, and dbin_12trans beyond the bins (the
+# reference then sums J with index -1, build_atm.py:647, op.py:2770-2774)
+EXTRA_CFG['c1rtA'] = ('dbin1 = 2.0\nsl_angle = 60. / 180. * 3.14159\nedd = 0.669\n'
+                      'f_diurnal = 0.5\ndbin_12trans = 900.\n')
+PHOTO_TAGS = ('c1rt', 'c1rtT', 'c1rtA')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
 RATE_TAGS = ('lowT', 'rmlist')
 # remove_list: two forward rates and one reverse rate taken out
@@ -326,6 +332,7 @@ out = dict(bins=var.bins, dbin1=var.dbin1, dbin2=var.dbin2,
            ch_kindex=np.array([var.pho_rate_index[c] for c in CH]),
            cross_J=np.array([var.cross_J[c] for c in CH]),
            sl_angle=vulcan_cfg.sl_angle, edd=vulcan_cfg.edd, f_diurnal=vulcan_cfg.f_diurnal,
+           dbin_12trans=vulcan_cfg.dbin_12trans,
            flux_atol=vulcan_cfg.flux_atol, spec_list=np.array(chem_funs.spec_list),
            pco=atm.pco, Tco=atm.Tco, M=atm.M, n_0=atm.n_0)
 TSP = list(vulcan_cfg.T_cross_sp)
@@ -502,7 +509,8 @@ def photo_setup_check(d, ref_root):
                             use_photo=True)
     t = photo.PhotoTables.from_reference_files(
         net, ref_root, 'atm/stellar_flux/sflux-HD189_Moses11.txt', 0.805, 0.03142,
-        float(d['sl_angle']), dbin1=float(d['dbin1']))
+        float(d['sl_angle']), dbin1=float(d['dbin1']), dbin2=float(d['dbin2']),
+        dbin_12trans=float(d['dbin_12trans']) if 'dbin_12trans' in d else 240.0)
     rel = lambda a, b: float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
     same = (len(t.bins) == len(d['bins']) and t.i12 == int(d['sflux_din12_indx'])
             and t.absp_sp == [str(s) for s in d['absp_sp']]
@@ -559,7 +567,7 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a cold column (150 -> 450 K) crossing the three low-temperature caps
         spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]
         spec.Tco = configs.linear_logp_T(spec.pco, 450., 150.)
-    elif tag in ('c1', 'c1rt', 'c1rtT'):
+    elif tag in ('c1', 'c1rt', 'c1rtT', 'c1rtA'):
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
                                 use_photo=True)
         spec = configs.config1(sorted(net.photo_index()))
