@@ -156,3 +156,20 @@ def test_attempt_matches_oracle_ncho_items(precision):
             r, fl = item_floor(on, it, dt)
             assert floor_err(sol[sl], r.sol, it['col'].n_0) <= max(1e-10, 10 * fl), (dt, c, fl)
     h.close()
+
+
+def test_species_missing_from_composition_file_is_named(tmp_path):
+    """A network species absent from all_compose.txt stops the set-up with
+    its name (the reference fails there too, at compo_row.index)."""
+    import shutil
+    from vulcan_gb300.network import Network
+    src = synthnet.generate(str(tmp_path / 'syn'))
+    d = os.path.dirname(src)
+    comp = os.path.join(d, 'all_compose.txt')
+    lines = open(comp).read().splitlines()
+    victim = lines[5].split()[0]
+    with open(comp, 'w') as f:
+        f.write('\n'.join(ln for ln in lines if ln.split()[:1] != [victim]) + '\n')
+    with pytest.raises(ValueError, match=victim):
+        Network.from_file(src, use_photo=True)
+    shutil.rmtree(d)

@@ -247,6 +247,10 @@ class Network:
         self.compo_atoms = atoms
         comp = np.zeros((self.ni, len(atoms)))
         mass = np.zeros(self.ni)
+        missing = [sp for sp in self.species if sp not in table]
+        if missing:      # the reference fails here too (compo_row.index, build_atm.py)
+            raise ValueError('species not in the composition file %s: %s'
+                             % (com_file, ', '.join(missing)))
         for k, sp in enumerate(self.species):
             row = table[sp]
             comp[k] = [int(v) for v in row[:len(atoms)]]
