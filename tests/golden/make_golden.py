@@ -23,8 +23,8 @@ trajectories); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
 with and without molecular diffusion) and c0vz (vertical advection), with
 the reference's transport RHS and LHS blocks; c0n2, c0o2, c0co2, c0rocky
 (column set-up with another molecular-diffusion base gas, rocky surface); c1rt, c1rtT (the reference's radiative transfer, T-independent
-and T-dependent cross sections); lowT, rmlist (rate constants with the
-low-temperature caps, and with reactions removed).
+and T-dependent cross sections); lowT, rmlist, snchok (rate constants with
+the low-temperature caps, with reactions removed, and of the sulfur network).
 
 Usage:  python tests/golden/make_golden.py [tag ...] [--ref /root/reference]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
@@ -65,10 +65,11 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c0nomol': (0, 1, 2, 10, 29),
         'c0vz': (0, 1, 2, 10, 29),
         'rmlist': (0,),
+        'snchok': (0,),
         'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'lowT': 1, 'c0bc': 30,
-          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
+          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'snchok': 1, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
           'c0rocky': 2}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
@@ -109,7 +110,9 @@ EXTRA_CFG['c1rtA'] = ('dbin1 = 2.0\nsl_angle = 60. / 180. * 3.14159\nedd = 0.669
                       'f_diurnal = 0.5\ndbin_12trans = 900.\n')
 PHOTO_TAGS = ('c1rt', 'c1rtT', 'c1rtA')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
-RATE_TAGS = ('lowT', 'rmlist')
+RATE_TAGS = ('lowT', 'rmlist', 'snchok')
+# the sulfur network with its photolysis slots (rate constants only)
+RATE_PHOTO_TAGS = ('snchok',)
 # remove_list: two forward rates and one reverse rate taken out
 EXTRA_CFG['rmlist'] = 'remove_list = [5, 12, 101]\n'
 
@@ -477,7 +480,8 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
     # run time: photochemistry (radiative transfer) off, J frozen in k -- except
     # for the radiative-transfer fixtures, which record the reference's own J
     with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
-        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1, tag in PHOTO_TAGS,
+        f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1,
+                                         tag in PHOTO_TAGS or tag in RATE_PHOTO_TAGS,
                                          EXTRA_CFG.get(tag, '')))
     keys = sorted(spec.photo_J) if spec.photo_J else []
     extra_in = {}
@@ -561,6 +565,11 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a column of the 512-column batch that has not converged after 4000 steps
         # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
         spec = configs.config2_columns(ncols=512, seed=2)[60]
+    elif tag == 'snchok':
+        import dataclasses
+        spec = dataclasses.replace(configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0],
+                                   network='SNCHO_photo_network.txt', use_photo=True,
+                                   atom_list=['H', 'O', 'C', 'He', 'N', 'S'])
     elif tag == 'rmlist':
         spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]
     elif tag == 'lowT':
@@ -580,6 +589,7 @@ def make(tag, ref_root, workdir, full_dir=None):
     if tag in RATE_TAGS:
         out = os.path.join(HERE, 'golden_%s.npz' % tag)
         np.savez_compressed(out, **d)
+        net.to_npz(os.path.join(HERE, 'net_%s.npz' % spec.network.replace('_network.txt', '')))
         print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
         return
     if tag in PHOTO_TAGS:

@@ -127,3 +127,18 @@ def test_remove_list_bit_exact():
     for i in (5, 12, 101):
         assert np.all(k[i - 1] == 0)
     assert np.all(k[5] > 0) and np.all(k[101] > 0)    # reverses of 5 and 101
+
+
+def test_sulfur_network_rate_constants_bit_exact():
+    """The SNCHO photochemical network (89 species, 1 150 rate slots): the
+    reference's read_rate / lim_lowT_rates / rev_rate on a 40-layer column
+    (fixture snchok); photolysis slots are zero placeholders in both until J
+    is computed."""
+    import os
+    from conftest import GOLDEN
+    from vulcan_gb300.network import Network
+    g = golden('snchok')
+    net = Network.from_npz(os.path.join(GOLDEN, 'net_SNCHO_photo.npz'))
+    assert net.ni == 89 and net.nr == 1150
+    k = net.rate_constants(g['Tco'], g['M'], use_lowT_limit_rates=True)
+    np.testing.assert_array_equal(k, g['k'])
