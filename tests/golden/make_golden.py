@@ -377,8 +377,11 @@ k_plain = np.array([np.array(var.k[i], dtype=float) for i in range(1, chem_funs.
 var = rate.lim_lowT_rates(var, atm)
 var = rate.rev_rate(var, atm)
 var = rate.remove_rate(var)
+K = np.array([var.k[i] for i in range(1, chem_funs.nr + 1)])
+# the generated chemistry source at a seeded positive state (term-order pin)
+Y = 10.0 ** np.random.default_rng(7).uniform(0.0, 18.0, (atm.Tco.size, chem_funs.ni))
 np.savez_compressed('golden_out.npz', Tco=atm.Tco, M=atm.M, pco=atm.pco, k_plain=k_plain,
-                    k=np.array([var.k[i] for i in range(1, chem_funs.nr + 1)]))
+                    k=K, y_rand=Y, chemdf_rand=chem_funs.chemdf(Y, atm.M, var.k))
 print('rate constants', chem_funs.nr, 'layers', atm.Tco.size)
 '''
 

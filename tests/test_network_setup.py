@@ -142,3 +142,15 @@ def test_sulfur_network_rate_constants_bit_exact():
     assert net.ni == 89 and net.nr == 1150
     k = net.rate_constants(g['Tco'], g['M'], use_lowT_limit_rates=True)
     np.testing.assert_array_equal(k, g['k'])
+
+
+def test_sulfur_network_chemical_source_bit_exact():
+    """The oracle's chemistry source on the sulfur network equals the
+    reference's generated chemdf at a seeded positive state (fixture snchok)."""
+    import os
+    from conftest import GOLDEN
+    from oracle import ros2 as O
+    g = golden('snchok')
+    on = O.OracleNet.from_npz(os.path.join(GOLDEN, 'net_SNCHO_photo.npz'),
+                              ['H', 'O', 'C', 'He', 'N', 'S'])
+    np.testing.assert_array_equal(O.chemdf(on, g['y_rand'], g['M'], g['k']), g['chemdf_rand'])
