@@ -380,8 +380,13 @@ var = rate.remove_rate(var)
 K = np.array([var.k[i] for i in range(1, chem_funs.nr + 1)])
 # the generated chemistry source at a seeded positive state (term-order pin)
 Y = 10.0 ** np.random.default_rng(7).uniform(0.0, 18.0, (atm.Tco.size, chem_funs.ni))
+ni = chem_funs.ni
+J0 = chem_funs.neg_symjac(Y, atm.M, var.k)
+lays = [0, atm.Tco.size // 2]
 np.savez_compressed('golden_out.npz', Tco=atm.Tco, M=atm.M, pco=atm.pco, k_plain=k_plain,
-                    k=K, y_rand=Y, chemdf_rand=chem_funs.chemdf(Y, atm.M, var.k))
+                    k=K, y_rand=Y, chemdf_rand=chem_funs.chemdf(Y, atm.M, var.k),
+                    negjac_layers=np.array(lays),
+                    negjac_blocks=np.array([J0[l*ni:(l+1)*ni, l*ni:(l+1)*ni] for l in lays]))
 print('rate constants', chem_funs.nr, 'layers', atm.Tco.size)
 '''
 

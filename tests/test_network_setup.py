@@ -154,3 +154,20 @@ def test_sulfur_network_chemical_source_bit_exact():
     on = O.OracleNet.from_npz(os.path.join(GOLDEN, 'net_SNCHO_photo.npz'),
                               ['H', 'O', 'C', 'He', 'N', 'S'])
     np.testing.assert_array_equal(O.chemdf(on, g['y_rand'], g['M'], g['k']), g['chemdf_rand'])
+
+
+def test_sulfur_network_jacobian_blocks():
+    """The oracle's chemistry Jacobian on the sulfur network against the
+    reference's sympy-generated neg_symjac at the same state: the same
+    sparsity, values within 1e-14 of the block scale (fixture snchok)."""
+    import os
+    from conftest import GOLDEN
+    from oracle import ros2 as O
+    g = golden('snchok')
+    on = O.OracleNet.from_npz(os.path.join(GOLDEN, 'net_SNCHO_photo.npz'),
+                              ['H', 'O', 'C', 'He', 'N', 'S'])
+    J = O.neg_jac_blocks(on, g['y_rand'], g['M'], g['k'])
+    for i, l in enumerate(g['negjac_layers']):
+        ref = g['negjac_blocks'][i]
+        assert np.max(np.abs(J[l] - ref)) <= 1e-14 * np.abs(ref).max()
+        assert np.all((J[l] != 0) == (ref != 0))
