@@ -18,8 +18,8 @@ For each workload it
   4. stores the compiled network (our parser's tables) beside the reference's
      own view of it (species order, nr) and the atmosphere arrays.
 
-Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow (Ros2 attempts and
-trajectories); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
+Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow, c3s (Ros2 attempts
+and trajectories; c3s on the sulfur network); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
 with and without molecular diffusion) and c0vz (vertical advection), with
 the reference's transport RHS and LHS blocks; c0n2, c0o2, c0co2, c0rocky
 (column set-up with another molecular-diffusion base gas, rocky surface); c1rt, c1rtT (the reference's radiative transfer, T-independent
@@ -66,10 +66,11 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c0vz': (0, 1, 2, 10, 29),
         'rmlist': (0,),
         'snchok': (0,),
+        'c3s': (0, 1, 2, 5, 9),
         'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'lowT': 1, 'c0bc': 30,
-          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'snchok': 1, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
+          'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'snchok': 1, 'c3s': 10, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
           'c0rocky': 2}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
@@ -573,6 +574,18 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a column of the 512-column batch that has not converged after 4000 steps
         # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
         spec = configs.config2_columns(ncols=512, seed=2)[60]
+    elif tag == 'c3s':
+        # the sulfur network (SNCHO, photolysis slots present with J = 0) on a
+        # 40-layer column with H2S in the start
+        import dataclasses
+        spec = dataclasses.replace(configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0],
+                                   network='SNCHO_photo_network.txt', use_photo=True,
+                                   atom_list=['H', 'O', 'C', 'He', 'N', 'S'],
+                                   const_mix={'H2': 0.85, 'He': 0.145, 'H2O': 1e-3, 'CH4': 5e-4,
+                                              'NH3': 1e-4, 'H2S': 3e-5},
+                                   conver_ignore=[])
+        snet = Network.from_file(os.path.join(ref_root, 'thermo', spec.network), use_photo=True)
+        spec.photo_J = {key: np.zeros(spec.pco.size) for key in sorted(snet.photo_index())}
     elif tag == 'snchok':
         import dataclasses
         spec = dataclasses.replace(configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0],

@@ -219,3 +219,23 @@ def test_trajectory_lockstep_with_options(tag):
                 on_step=lambda s, a: (dts.append(s.dt), natt.append(s.attempts)))
     np.testing.assert_array_equal(natt, g['traj_natt'])
     np.testing.assert_allclose(dts, g['traj_dt_next'], rtol=1e-9)
+
+
+def test_sulfur_network_chemdf_bit_exact():
+    g = golden('c3s')
+    on = oracle_net('c3s', g)
+    np.testing.assert_array_equal(O.chemdf(on, g['y_ini'], g['M'], g['k']), g['chemdf0'])
+
+
+@pytest.mark.parametrize('tag,n', _attempts('c3s'))
+def test_sulfur_network_attempts_match_reference(tag, n):
+    """Ros2 attempts on the reference's 89-species sulfur network (SNCHO, H2S
+    in the start, photolysis slots at J = 0; fixture c3s)."""
+    g = golden(tag)
+    on = oracle_net(tag, g)
+    args = (on, g['att_y'][n], g['att_ymix'][n], float(g['att_dt'][n]), g['k'],
+            attempt_atm(g, n), O.Flags(), O.Tol())
+    for solve in ('banded', 'block'):
+        r = O.ros2_attempt(*args, solve)
+        assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
+        assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
