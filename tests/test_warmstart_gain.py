@@ -8,7 +8,6 @@ reference's convergence test) is measured by ``bench.py --converge``."""
 import os
 
 import numpy as np
-import pytest
 
 from conftest import GOLDEN, REPO
 
