@@ -60,6 +60,7 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c1rt': (0,),
         'c1rtT': (0,),
         'c1rtA': (0,),
+        'c3rt': (0,),
         'lowT': (0,),
         'c0bc': (0, 1, 2, 10, 29),
         'c0nomol': (0, 1, 2, 10, 29),
@@ -69,7 +70,7 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'c3s': (0, 1, 2, 5, 9),
         'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
-          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'lowT': 1, 'c0bc': 30,
+          'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'c3rt': 2, 'lowT': 1, 'c0bc': 30,
           'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'snchok': 1, 'c3s': 10, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
           'c0rocky': 2}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
@@ -109,7 +110,9 @@ VZ_TAGS = ('c0vz',)
 # reference then sums J with index -1, build_atm.py:647, op.py:2770-2774)
 EXTRA_CFG['c1rtA'] = ('dbin1 = 2.0\nsl_angle = 60. / 180. * 3.14159\nedd = 0.669\n'
                       'f_diurnal = 0.5\ndbin_12trans = 900.\n')
-PHOTO_TAGS = ('c1rt', 'c1rtT', 'c1rtA')
+# the sulfur network's radiative transfer (37 absorbers, 60 channels)
+EXTRA_CFG['c3rt'] = 'dbin1 = 2.0\n'
+PHOTO_TAGS = ('c1rt', 'c1rtT', 'c1rtA', 'c3rt')
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
 RATE_TAGS = ('lowT', 'rmlist', 'snchok')
 # the sulfur network with its photolysis slots (rate constants only)
@@ -336,7 +339,7 @@ out = dict(bins=var.bins, dbin1=var.dbin1, dbin2=var.dbin2,
            ch_kindex=np.array([var.pho_rate_index[c] for c in CH]),
            cross_J=np.array([var.cross_J[c] for c in CH]),
            sl_angle=vulcan_cfg.sl_angle, edd=vulcan_cfg.edd, f_diurnal=vulcan_cfg.f_diurnal,
-           dbin_12trans=vulcan_cfg.dbin_12trans,
+           dbin_12trans=vulcan_cfg.dbin_12trans, network=str(vulcan_cfg.network),
            flux_atol=vulcan_cfg.flux_atol, spec_list=np.array(chem_funs.spec_list),
            pco=atm.pco, Tco=atm.Tco, M=atm.M, n_0=atm.n_0)
 TSP = list(vulcan_cfg.T_cross_sp)
@@ -518,8 +521,8 @@ def photo_setup_check(d, ref_root):
     same files -- stored in the fixture so the CPU tests pin the restatement
     without the reference's data files."""
     from vulcan_gb300 import photo
-    net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
-                            use_photo=True)
+    name = os.path.basename(str(d['network'])) if 'network' in d else 'NCHO_photo_network.txt'
+    net = Network.from_file(os.path.join(ref_root, 'thermo', name), use_photo=True)
     t = photo.PhotoTables.from_reference_files(
         net, ref_root, 'atm/stellar_flux/sflux-HD189_Moses11.txt', 0.805, 0.03142,
         float(d['sl_angle']), dbin1=float(d['dbin1']), dbin2=float(d['dbin2']),
@@ -574,7 +577,7 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a column of the 512-column batch that has not converged after 4000 steps
         # on the device (nz = 62, T 1602 -> 1303 K, Kzz 6.9e6)
         spec = configs.config2_columns(ncols=512, seed=2)[60]
-    elif tag == 'c3s':
+    elif tag in ('c3s', 'c3rt'):
         # the sulfur network (SNCHO, photolysis slots present with J = 0) on a
         # 40-layer column with H2S in the start
         import dataclasses

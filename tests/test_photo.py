@@ -49,7 +49,7 @@ def _rel(a, b, floor=1e-300):
     return float(np.max(np.abs(a - b)[m] / np.abs(b)[m]))
 
 
-@pytest.mark.parametrize('tag', ['c1rt', 'c1rtT', 'c1rtA'])
+@pytest.mark.parametrize('tag', ['c1rt', 'c1rtT', 'c1rtA', 'c3rt'])
 def test_oracle_matches_reference_records(tag):
     d = _fixture(tag)
     nz, nb = d['rec0_y'].shape[0], len(d['bins'])
@@ -95,6 +95,12 @@ def test_host_tables_match_the_reference_set_up():
     assert bool(a['setup_same_layout']) and int(a['sflux_din12_indx']) == -1
     for key in ('bins', 'cross', 'cross_J', 'cross_scat', 'sflux_top'):
         assert float(a['setup_rel_' + key]) <= 1e-15, key
+    # the sulfur network: 37 absorbers, 60 channels, a branching-ratio table
+    # whose last rows are out of order (CH3SH; interp1d sorts, so do we)
+    sn = _fixture('c3rt')
+    assert bool(sn['setup_same_layout']) and len(sn['absp_sp']) == 37 and len(sn['ch_sp']) == 60
+    for key in ('bins', 'cross', 'cross_J', 'cross_scat', 'sflux_top'):
+        assert float(sn['setup_rel_' + key]) <= 1e-15, key
 
 
 def _tcross(temps, base=2e-18):

@@ -34,6 +34,14 @@ R_SUN = 6.957E10          # cm (phy_const.py)
 AU = 1.49597871E13         # cm (phy_const.py)
 
 
+def _interp(x, xp, fp, left=0.0, right=0.0):
+    """Linear interpolation as the reference's scipy interp1d does it: the
+    table sorted by its abscissa first (stable; a few of the reference's
+    tables are not in order), ``left`` / ``right`` outside it."""
+    o = np.argsort(xp, kind='mergesort')
+    return np.interp(x, np.asarray(xp)[o], np.asarray(fp)[o], left=left, right=right)
+
+
 def j_weights(nbins, i12, dbin1, dbin2):
     """Weight of each bin in the reference's J sum (see module docstring)."""
     w = np.zeros(nbins)
@@ -118,12 +126,14 @@ class PhotoTables:
                                    np.arange(dbin_12trans, bin_max, dbin2)))
         else:
             bins = np.arange(bin_min, bin_max, dbin1)
-        interp0 = lambda x, xp, fp: np.interp(x, xp, fp, left=0.0, right=0.0)
+        interp0 = lambda x, xp, fp: _interp(x, xp, fp)
         cross = np.array([interp0(bins, raw[sp]['lambda'], raw[sp]['cross']) for sp in photo_sp])
         cross_J = []
         for sp, br in chans:
             key = 'br_ratio_%d' % br
-            r = np.interp(bins, ratio[sp]['lambda'], ratio[sp][key])      # edge values held
+            # held at the table's first and last rows as written (fill_value)
+            r = _interp(bins, ratio[sp]['lambda'], ratio[sp][key],
+                        ratio[sp][key][0], ratio[sp][key][-1])
             cross_J.append(interp0(bins, raw[sp]['lambda'], raw[sp]['disso']) * r)
         scat = []
         for sp in scat_sp:
@@ -183,14 +193,15 @@ class TCross:
             for s, b in zip(tables.ch_sp, tables.ch_br):
                 if s == sp:
                     key = 'br_ratio_%d' % b
-                    ratio[(s, b)] = np.interp(tables.bins, br['lambda'], br[key])
+                    ratio[(s, b)] = _interp(tables.bins, br['lambda'], br[key],
+                                            br[key][0], br[key][-1])
         return cls(tables, raw, ratio)
 
     def for_column(self, Tco):
         """(cross_T {sp: [nz, nbins]}, cross_J_T {(sp, branch): [nz, nbins]})."""
         t = self.tables
         bins = t.bins
-        interp0 = lambda tab, col: np.interp(bins, tab[0], tab[col], left=0.0, right=0.0)
+        interp0 = lambda tab, col: _interp(bins, tab[0], tab[col])
         cross_T, cross_J_T = {}, {}
         for sp, tabs in self.raw.items():
             base = t.cross[t.absp_sp.index(sp)]
