@@ -18,13 +18,19 @@ For each workload it
   4. stores the compiled network (our parser's tables) beside the reference's
      own view of it (species order, nr) and the atmosphere arrays.
 
-Workloads: c0, c1, c2, c2long, c2conv, c2tight, c2slow, c3s (Ros2 attempts
-and trajectories; c3s on the sulfur network); c0bc, c0nomol (top / bottom fluxes, deposition, H escape,
-with and without molecular diffusion) and c0vz (vertical advection), with
-the reference's transport RHS and LHS blocks; c0n2, c0o2, c0co2, c0rocky
-(column set-up with another molecular-diffusion base gas, rocky surface); c1rt, c1rtT (the reference's radiative transfer, T-independent
-and T-dependent cross sections); lowT, rmlist, snchok (rate constants with
-the low-temperature caps, with reactions removed, and of the sulfur network).
+Workloads:
+  c0, c1, c2, c2long, c2conv, c2tight, c2slow, c3s   Ros2 attempts and
+      trajectories (c3s on the 89-species sulfur network);
+  c0bc, c0nomol, c0vz   transport options (top / bottom fluxes, deposition,
+      H escape, no molecular diffusion, vertical advection) with the
+      reference's transport RHS and LHS blocks;
+  c0n2, c0o2, c0co2, c0rocky   column set-up with another base gas for
+      molecular diffusion, rocky surface;
+  c1rt, c1rtT, c1rtA, c3rt   the reference's radiative transfer
+      (T-independent and T-dependent cross sections, other parameters, the
+      sulfur network);
+  lowT, rmlist, snchok   rate constants (low-temperature caps, reactions
+      removed, the sulfur network).
 
 Usage:  python tests/golden/make_golden.py [tag ...] [--ref /root/reference]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
