@@ -1,6 +1,7 @@
-"""The device radiative transfer on other parameters (fixture c1rtA: zenith
+"""The device radiative transfer on other parameters and networks (c1rtA: zenith
 angle 60 deg, Eddington coefficient 0.669, f_diurnal 0.5, 2 nm bins, the bin
-switch beyond the bins so that J sums with index -1): against the oracle and,
+switch beyond the bins so that J sums with index -1; c3rt: the sulfur
+network): against the oracle and, for c1rtA,
 through the drop-in, against the reference's records.  Tolerances as for the
 drop-in on c1rt (actinic flux 1e-10: the deep layers' flux is exp(-tau/mu)
 of a large optical depth)."""
@@ -12,14 +13,17 @@ from test_photo import _attach, _dropin, _fixture, _oracle_call, _rel
 pytestmark = pytest.mark.gpu
 
 
-def test_device_matches_oracle_on_other_parameters():
+@pytest.mark.parametrize('tag,column', [('c1rtA', 'c1'), ('c3rt', 'c3s')])
+def test_device_matches_oracle_on_other_parameters(tag, column):
+    """c1rtA on the NCHO column; c3rt: the 89-species sulfur network's
+    radiative transfer (37 absorbers, 60 channels) on the c3s column."""
     from test_gpu_parity import make_handle
     from vulcan_gb300 import _build
     _build.build()
-    d = _fixture('c1rtA')
-    assert int(d['sflux_din12_indx']) == -1
-    g, net, gn, h, b = make_handle('c1')
+    d = _fixture(tag)
+    g, net, gn, h, b = make_handle(column)
     np.testing.assert_array_equal(g['Tco'], d['Tco'])
+    np.testing.assert_allclose(g['dz'], d['rec0_dz'], rtol=1e-14)
     _attach(h, d, net)
     nz, nb = d['rec0_y'].shape[0], len(d['bins'])
     du, dd = np.zeros((nz + 1, nb)), np.zeros((nz + 1, nb))
@@ -37,7 +41,8 @@ def test_device_matches_oracle_on_other_parameters():
             assert abs(change[0] / ch - 1) < 1e-9
         k = h.k()
         for c, ki in enumerate(d['ch_kindex']):
-            np.testing.assert_allclose(k[:, int(ki) - 1], 0.5 * J_d[:, c], rtol=1e-15)
+            np.testing.assert_allclose(k[:, int(ki) - 1], float(d['f_diurnal']) * J_d[:, c],
+                                       rtol=1e-15)
     h.close()
 
 
