@@ -158,6 +158,10 @@ VK_API int  vk_set_atom_ini(vk_handle *h, const double *atom_ini /*[ncols][natom
  * a per-species mask [ni] of species ignored by the steady-state test
  * (vulcan_cfg.conver_ignore); either pointer may be NULL. */
 VK_API int  vk_set_column_info(vk_handle *h, const int *pref_indx, const int *conv_ignore);
+/* Per-column masks [ncols][ni] of species the steady-state test ignores (the
+ * conver_ignore list of each column's cfg, op.py:1043-1045); replaces the one
+ * mask vk_set_column_info gives every column. */
+VK_API int  vk_set_conv_ignore(vk_handle *h, const int *conv_ignore);
 
 /* Integrate every column on the device until each one reaches steady state
  * or a limit (count_max / runtime), or until max_steps accepted steps per
@@ -297,8 +301,7 @@ VK_API int  vk_mlp_adam(long long n, float *w, void *w_bf16, const float *g, flo
 /* ---- block-tridiagonal solve without allocation ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a framework that owns all device memory through its own pool, a plugin
- * that is handed its buffers, code about to be captured into a stream): the
- * solver's scratch (block inverses and sweep vector) is a fixed 16 MiB
+ * that is handed its buffers): the solver's scratch (block inverses and sweep vector) is a fixed 16 MiB
  * __device__ array inside this library, held by every GPU that loads it until
  * the process exits.  Solves lower[j] o x[j-1] + D[j] x[j] + upper[j] o x[j+1]
  * = b[j] for one column; D is [nz][ni][ni], lower/upper/b/x are [nz][ni], all

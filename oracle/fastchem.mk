@@ -3,7 +3,9 @@
 # oracle/_ref/fastchem.  Test infrastructure only: the equilibrium fixture
 # (tests/golden/make_fastchem_golden.py) runs it; nothing else does.
 #   make -f oracle/fastchem.mk REF=<path of the VULCAN tree>
-REF ?= /root/reference
+ifndef REF
+$(error give the VULCAN source tree: make -f oracle/fastchem.mk REF=<path>)
+endif
 FC   = $(REF)/fastchem_vulcan
 SRC  = $(wildcard $(FC)/fastchem_src/*.cpp) $(FC)/model_main/model_main.cpp \
        $(FC)/model_main/read_config.cpp

@@ -11,7 +11,8 @@ stores the mixing ratios of the network's species (tests/golden/golden_eq.npz)
 and which of them FastChem lists twice (two data sets under one name, of
 which the reference reads the first).
 
-Usage:  python tests/golden/make_fastchem_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_fastchem_golden.py [--ref <VULCAN tree>]
+        (default: $VULCAN_REFERENCE)
 """
 import argparse
 import os
@@ -85,8 +86,11 @@ def run_fastchem(exe, ref, spec, net, workdir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', default=os.environ.get('VULCAN_REFERENCE'),
+                    help='the VULCAN source tree (default: $VULCAN_REFERENCE)')
     a = ap.parse_args()
+    if not a.ref or not os.path.isdir(os.path.join(a.ref, 'fastchem_vulcan')):
+        ap.error('give the VULCAN source tree with --ref or VULCAN_REFERENCE (got %r)' % a.ref)
     subprocess.run(['make', '-s', '-f', os.path.join(REPO, 'oracle', 'fastchem.mk'), 'REF=' + a.ref],
                    check=True)
     exe = os.path.join(REPO, 'oracle', '_ref', 'fastchem')

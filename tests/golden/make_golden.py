@@ -1,8 +1,8 @@
 """Generate golden fixtures by running the reference VULCAN itself.
 
-Test infrastructure only: run in a container that has the reference source
-(default ``/root/reference``); the GPU machine only reads the committed
-``tests/golden/*.npz``.
+Test infrastructure only: run where the reference source is at hand (its
+path from ``--ref`` or the VULCAN_REFERENCE environment variable); the GPU
+machine only reads the committed ``tests/golden/*.npz``.
 
 For each workload it
   1. copies the reference tree to a temporary directory (the reference's code
@@ -32,7 +32,7 @@ Workloads:
   lowT, rmlist, snchok   rate constants (low-temperature caps, reactions
       removed, the sulfur network).
 
-Usage:  python tests/golden/make_golden.py [tag ...] [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py [tag ...] [--ref <VULCAN tree>]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
 """
 from __future__ import annotations
@@ -651,13 +651,16 @@ def make(tag, ref_root, workdir, full_dir=None):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('tags', nargs='*', default=['c0', 'c1', 'c2'])
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', default=os.environ.get('VULCAN_REFERENCE'),
+                    help='the VULCAN source tree (default: $VULCAN_REFERENCE)')
     ap.add_argument('--full-dir', default=None,
                     help='also keep every recorded attempt here (not committed)')
     ap.add_argument('--setup-only', action='store_true',
                     help='radiative-transfer fixtures: recompute only the host set-up '
                          'comparisons of an existing fixture (no reference run)')
     a = ap.parse_args()
+    if not a.ref or not os.path.isfile(os.path.join(a.ref, 'op.py')):
+        ap.error('give the VULCAN source tree with --ref or VULCAN_REFERENCE (got %r)' % a.ref)
     if a.setup_only:
         for t in a.tags:
             path = os.path.join(HERE, 'golden_%s.npz' % t)

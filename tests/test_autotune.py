@@ -1,6 +1,6 @@
 """Launch autotuner: search logic and cache on a stand-in handle (CPU); the
 launch settings themselves on the device (GPU test in
-tests/test_zzz_launch_tuning.py)."""
+tests/test_launch_tuning.py)."""
 import pytest
 
 from vulcan_gb300 import autotune, capi

@@ -23,6 +23,10 @@ def test_sulfur_network_chemical_source_bit_exact():
     spec = dataclasses.replace(configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0],
                                const_mix={'H2': 0.85, 'He': 0.15}, atom_list=atoms)
     items = batch.build_items([spec], net)
+    # the fixture's own M and k: the seeded column is rebuilt with numpy's
+    # exp/log, whose last bit differs between x86 and Arm builds of numpy,
+    # and a one-ulp change of M moves every termolecular rate by an ulp
+    items[0]['col'].M = g['M'].copy()
     items[0]['k'] = g['k']
     h, b = batch.make_batch_handle(net, items, atoms)
     np.testing.assert_array_equal(h.chem_source(g['y_rand']), g['chemdf_rand'])

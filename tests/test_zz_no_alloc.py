@@ -9,7 +9,8 @@ block-tridiagonal matrix, so solving that matrix for b = A k1 must give k1
 back, within the per-step tolerance of the parity tests.  Two different
 systems are solved back to back (the shared scratch keeps the previous call's
 contents), then the first one again, which must reproduce its answer bit for
-bit.  This file is collected last on purpose.
+bit.  A singular and a non-finite block must be reported, and the next good
+call must not see their status.  This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -78,6 +79,47 @@ def test_noalloc_solve_matches_attempt_twice():
     assert floor_err(x1, s1[4], s1[5]) <= 1e-10
     x0b = _solve(lib, *s0[:4])                # scratch reused: same answer again
     np.testing.assert_array_equal(x0b, x0)
+
+
+def _status(lib, D, lower, upper, rhs):
+    """Return code of one call on caller-owned device buffers."""
+    import torch
+    dev = torch.device('cuda:0')
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (D, lower, upper, rhs)]
+    x = torch.empty_like(t[3])
+    torch.cuda.synchronize()
+    nz, ni = rhs.shape
+    p = lambda a: C.c_void_p(a.data_ptr())
+    return lib.vk_block_solve_noalloc(nz, ni, p(t[0]), p(t[1]), p(t[2]), p(t[3]), p(x), None), x
+
+
+def test_noalloc_reports_singular_and_nan_then_recovers():
+    """A zero diagonal block gives VK_ESINGULAR and a NaN in a block VK_ENAN;
+    the status word lives in the shared scratch, so a good solve right after
+    each must return VK_OK with the right answer (the kernel clears it)."""
+    pytest.importorskip('torch')
+    from vulcan_gb300 import _build, capi
+    _build.build()
+    lib = capi.lib()
+    nz, ni = 2, 3
+    rng = np.random.default_rng(3)
+    good = np.stack([np.eye(ni) * 4.0 + 0.1 * rng.standard_normal((ni, ni)) for _ in range(nz)])
+    lower = 0.1 * rng.standard_normal((nz, ni))
+    upper = 0.1 * rng.standard_normal((nz, ni))
+    xt = rng.standard_normal((nz, ni))
+    rhs = np.einsum('lij,lj->li', good, xt)
+    rhs[1:] += lower[1:] * xt[:-1]
+    rhs[:-1] += upper[:-1] * xt[1:]
+    zero = good.copy()
+    zero[0] = 0.0
+    nan = good.copy()
+    nan[1, 1, 2] = np.nan
+    for bad, code in ((zero, capi.VK_ESINGULAR), (nan, capi.VK_ENAN)):
+        rc, _ = _status(lib, bad, lower, upper, rhs)
+        assert rc == code, (rc, lib.vk_last_error(None))
+        rc, x = _status(lib, good, lower, upper, rhs)
+        assert rc == capi.VK_OK, lib.vk_last_error(None)
+        np.testing.assert_allclose(x.cpu().numpy(), xt, rtol=1e-12, atol=1e-12)
 
 
 def test_noalloc_rejects_sizes_beyond_scratch():

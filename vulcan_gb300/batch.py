@@ -49,9 +49,10 @@ def make_batch_handle(net, items, atom_list, precision=capi.VK_PREC_FP64):
     h = Ros2Handle(gnet, b.ncols, b.L, precision)
     h.set_columns(b)
     h.set_atom_ini(np.stack([it['atom_ini'] for it in items]))
-    mask = np.zeros(net.ni, dtype=np.int32)
-    for sp in items[0]['ignore']:
-        mask[net.species.index(sp)] = 1
+    mask = np.zeros((len(items), net.ni), dtype=np.int32)
+    for c, it in enumerate(items):
+        for sp in it['ignore']:
+            mask[c, net.species.index(sp)] = 1
     h.set_conv_ignore(mask)
     h.set_clock(dt=configs.SOLVER_DEFAULTS['dttry'], t=0.0, count=0)
     return h, b

@@ -283,9 +283,10 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &r.atom_ini, (size_t)max_cols * VK_MAX_NATOM));
     TRY(dalloc(h, &r.loss, (size_t)max_cols * VK_MAX_NATOM));
     TRY(dalloc(h, &r.loss_prev, (size_t)max_cols * VK_MAX_NATOM));
-    TRY(dalloc(h, &r.ignore, ni));
+    TRY(dalloc(h, &r.ignore, (size_t)max_cols * ni));
     TRY(dalloc(h, &h->d_nactive, 1));
-    TRY(cudaMemset(r.ignore, 0, ni * sizeof(int)) == cudaSuccess ? VK_OK : fail(h, VK_ECUDA, "memset"));
+    TRY(cudaMemset(r.ignore, 0, (size_t)max_cols * ni * sizeof(int)) == cudaSuccess ? VK_OK
+                                                                               : fail(h, VK_ECUDA, "memset"));
 #undef TRY
     *out = h;
     return VK_OK;
@@ -568,8 +569,21 @@ extern "C" int vk_set_column_info(vk_handle *h, const int *pref_indx, const int 
                 return fail(h, VK_EINVAL, "pref_indx outside the column");
         VK_CUDA(h, cudaMemcpy(h->rs.pref, pref_indx, h->ncols * sizeof(int), cudaMemcpyHostToDevice));
     }
-    if (conv_ignore)
-        VK_CUDA(h, cudaMemcpy(h->rs.ignore, conv_ignore, h->ni * sizeof(int), cudaMemcpyHostToDevice));
+    if (conv_ignore) {                    // one mask for every column
+        std::vector<int> m((size_t)h->ncols * h->ni);
+        for (int c = 0; c < h->ncols; ++c)
+            std::copy(conv_ignore, conv_ignore + h->ni, m.begin() + (size_t)c * h->ni);
+        VK_CUDA(h, cudaMemcpy(h->rs.ignore, m.data(), m.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return VK_OK;
+}
+
+extern "C" int vk_set_conv_ignore(vk_handle *h, const int *conv_ignore) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!conv_ignore) return fail(h, VK_EINVAL, "conv_ignore is NULL");
+    VK_CUDA(h, cudaMemcpy(h->rs.ignore, conv_ignore, (size_t)h->ncols * h->ni * sizeof(int),
+                          cudaMemcpyHostToDevice));
     return VK_OK;
 }
 

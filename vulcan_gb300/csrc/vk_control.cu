@@ -116,7 +116,7 @@ __device__ int conv_test(const DevNet &net, const DevBatch &b, const RunState &r
         const double ym = rs.ymix[g];
         const double yv = rs.y[g];
         if (!(ym > 0.0)) continue;
-        if (ym < cc.mtol_conv || yv < cc.atol || rs.ignore[i]) continue;
+        if (ym < cc.mtol_conv || yv < cc.atol || rs.ignore[(size_t)c * n + i]) continue;
         const double n0 = b.atm[(size_t)(l0 + j) * VK_ATM_NF + VK_ATM_N0];
         ld = fmax(ld, fabs((ynow[g] - yref[g]) / n0) / ym);
     }

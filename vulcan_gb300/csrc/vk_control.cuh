@@ -14,7 +14,7 @@ struct RunState {
     double *atom_ini, *loss, *loss_prev;  // [ncols][VK_MAX_NATOM]
     double *hist_y;                     // [conv_step][L][ni] ring of accepted states
     double *hist_t;                     // [ncols][conv_step]
-    int *ignore;                        // [ni]
+    int *ignore;                        // [max_cols][ni]
 };
 
 struct RunCtrl {

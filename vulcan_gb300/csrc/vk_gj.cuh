@@ -2,7 +2,8 @@
 // with partial pivoting (largest |a| in the pivot column, lowest row on
 // ties), used by the block-Thomas factorisations.  All threads of the block
 // must call it.  *s_sing becomes 1 for a zero pivot column, 2 when no finite
-// pivot candidate exists (NaN state).
+// pivot candidate exists (NaN state); the first cause seen is kept (a zero
+// pivot makes every later candidate non-finite).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -33,7 +34,7 @@ __device__ __forceinline__ void gj_invert_f64(double *A, int n, double *colk, do
             }
             if (lane == 0) {
                 // no finite candidate -> NaN state (2); all zero -> singular (1)
-                if (best < 0.0 || bi >= n) { *s_sing = 2; bi = k; }
+                if (best < 0.0 || bi >= n) { if (*s_sing == 0) *s_sing = 2; bi = k; }
                 else if (!(best > 0.0)) { if (*s_sing == 0) *s_sing = 1; bi = k; }
                 *s_piv = bi;
                 *s_pval = A[bi * n + k];

@@ -2,12 +2,13 @@
 //
 // For callers that cannot call cudaMalloc: code running where a host-side
 // allocation is not allowed or not wanted -- inside a framework that owns all
-// device memory through its own pool, a plugin handed pre-allocated buffers by
-// its host, or a stream about to be captured -- and that still need the
-// solver's scratch space.  The scratch (block inverses and the forward-sweep
-// vector) lives in one file-scope __device__ array of fixed size, so nothing
-// is allocated at call time; every GPU that loads the library holds that array
-// until the process exits.
+// device memory through its own pool, or a plugin handed pre-allocated
+// buffers by its host -- and that still need the solver's scratch space.  The
+// scratch (block inverses and the forward-sweep vector) lives in one
+// file-scope __device__ array of fixed size, so nothing is allocated at call
+// time; every GPU that loads the library holds that array until the process
+// exits.  Each call waits for its stream to finish (it reads the status word
+// back to report a singular or non-finite block).
 //
 // Solves, for one column of nz layers with ni species,
 //     lower[j] o x[j-1] + D[j] x[j] + upper[j] o x[j+1] = b[j]
@@ -155,6 +156,12 @@ extern "C" int vk_block_solve_noalloc(int nz, int ni, const double *D, const dou
     int rc = noalloc_setup(dev, &scratch);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    // an error left pending by earlier, unrelated work is reported as such
+    // (and cleared) rather than blamed on this launch
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return noalloc_fail(VK_ECUDA, std::string("CUDA error pending from earlier work (nothing launched): ") +
+                                          cudaGetErrorString(e));
     size_t sm = (size_t)(ni * ni + 4 * ni) * sizeof(double) + (size_t)ni * sizeof(int);
     k_block_solve_noalloc<<<1, 256, sm, s>>>(nz, ni, D, lower, upper, b, x, scratch);
     e = cudaGetLastError();

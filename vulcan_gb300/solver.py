@@ -243,7 +243,13 @@ class Ros2Handle:
         check(lib().vk_set_atom_ini(self.h, ptr(np.ascontiguousarray(atom_ini, dtype=float))), self.h)
 
     def set_conv_ignore(self, mask):
-        check(lib().vk_set_column_info(self.h, None, ptr(np.ascontiguousarray(mask, dtype=np.int32), C.c_int)), self.h)
+        """Species the steady-state test ignores: one mask [ni] for every
+        column, or one per column [ncols][ni]."""
+        m = np.ascontiguousarray(mask, dtype=np.int32)
+        if m.ndim == 1:
+            check(lib().vk_set_column_info(self.h, None, ptr(m, C.c_int)), self.h)
+        else:
+            check(lib().vk_set_conv_ignore(self.h, ptr(m, C.c_int)), self.h)
 
     def set_clock(self, dt=None, t=None, count=None):
         b = self.batch
