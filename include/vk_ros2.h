@@ -224,9 +224,10 @@ VK_API int  vk_compute_k(vk_handle *h);
  * ctas_per_sm x SMs CTAs.  kernel: VK_TUNE_*; ctas_per_sm 0..8 (0: the
  * kernel's built-in default, or VK_CTAS_PER_SM from the environment);
  * variant: for VK_TUNE_LU32 the register tiling of the FP32 Gauss-Jordan,
- * 0..3 covering blocks up to 48, 80, 112, 160 species (-1: the smallest that
- * covers ni; a tiling smaller than ni is refused), ignored otherwise.  A
- * change drops the captured vk_run graph, which is captured again. */
+ * 0..3 covering blocks up to 48, 80, 112, 160 species, or 4: the
+ * tensor-core factorisation (tcgen05, blocks up to 128 species) (-1: the
+ * default for ni; a variant smaller than ni is refused), ignored otherwise.
+ * A change drops the captured vk_run graph, which is captured again. */
 #define VK_TUNE_LU32    0   /* k_lu32: FP32 block-Thomas factorisation        */
 #define VK_TUNE_LU64    1   /* k_lu_fwd_f64: FP64 factorisation + first sweep */
 #define VK_TUNE_SWEEP64 2   /* k_back_f64, k_solve_f64: FP64 sweeps           */
@@ -325,6 +326,10 @@ VK_API int  vk_get_refine_stats(vk_handle *h, int *max_sweeps, int *n_fallback);
 VK_API const char *vk_network_last_error(void);
 /* Chemistry source term alone (the generated chemdf) of state y [L][ni]. */
 VK_API int  vk_chem_source(vk_handle *h, const double *y, double *dydt);
+/* FP32 inverses of the scaled diagonal blocks of the last mixed-precision
+ * attempt, [L][ni*ni] row-major (columns that attempt solved in FP64 hold
+ * stale values). */
+VK_API int  vk_get_lu32(vk_handle *h, float *G);
 /* LHS pieces of the last attempt: -J entries [L][nnz_jac] in the order of
  * vk_network_jac_pattern, and the transport coefficients dA/dB/dC [L][ni]
  * (dy_j/dt = dA y_j + dB y_{j+1} + dC y_{j-1}). */

@@ -15,7 +15,8 @@ VK_OK, VK_EINVAL, VK_ECUDA, VK_ESINGULAR, VK_ENAN, VK_EMAXATTEMPT, VK_ETIMEOUT, 
 VK_PREC_FP64, VK_PREC_MIXED = 0, 1
 VK_F_MOLDIFF, VK_F_TOPFLUX, VK_F_BOTFLUX = 1, 2, 4
 VK_TUNE_LU32, VK_TUNE_LU64, VK_TUNE_SWEEP64, VK_TUNE_REFINE = 0, 1, 2, 3
-LU32_TILING_CAP = (48, 80, 112, 160)      # species each k_lu32 tiling covers
+LU32_TILING_CAP = (48, 80, 112, 160, 128)  # species each LU32 variant covers
+LU32_TC = 4                                # the tensor-core factorisation (k_lu_tc)
 (ATM_M, ATM_N0, ATM_TCO, ATM_G, ATM_DZI, ATM_KZZ, ATM_VZ, ATM_TI, ATM_HPI, ATM_HP,
  ATM_PICO, ATM_PICOU, ATM_DZ) = range(13)
 ATM_NF = 13
@@ -38,7 +39,7 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
            'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps',
-           'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore')
+           'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore', 'vk_get_lu32')
 
 
 class VkNetworkDesc(C.Structure):
@@ -100,6 +101,7 @@ def lib(path=None):
         'vk_set_atom_ini': (i, [vp, pd]),
         'vk_set_column_info': (i, [vp, pi, pi]),
         'vk_set_conv_ignore': (i, [vp, pi]),
+        'vk_get_lu32': (i, [vp, P(C.c_float)]),
         'vk_run': (i, [vp, P(VkCtrl), i, d]),
         'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
         'vk_set_clock': (i, [vp, pd, pd, pi]),

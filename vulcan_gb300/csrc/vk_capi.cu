@@ -28,6 +28,7 @@ struct vk_handle {
     int max_refine = 6;
     double refine_tol = 1e-10;
     int geo_flags = -1;         // flags the transport geometry was built for (-1: stale)
+    CUtensorMap tmap_d32{};     // k_lu_tc's view of w.D32 (mixed mode, ni <= 128)
     int ncols = 0, L = 0;
     std::vector<int> col_off;
     // network tables
@@ -166,6 +167,25 @@ extern "C" void vk_destroy(vk_handle *h) {
     delete h;
 }
 
+// Buffers of the mixed-precision path: the FP32 inverses (packed n x n per
+// layer) and the scaled blocks, sized for k_lu32's packed layout or k_lu_tc's
+// zero-padded NP x NP tiles, with the tensor map k_lu_tc loads them through.
+static int alloc_mixed(vk_handle *h) {
+    const size_t st = (size_t)((h->ni * h->ni + 3) & ~3);
+    const bool tc = vk::lu_tc_supported(h->ni);
+    const size_t sd = tc ? std::max(st, vk::lu_tc_block_floats(h->ni)) : st;
+    int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * st);
+    if (!rc) rc = dalloc(h, &h->w.D32, (size_t)h->max_layers * sd);
+    if (rc) return rc;
+    if (tc) {
+        cudaError_t e = vk::lu_tc_make_map(&h->tmap_d32, h->w.D32, h->ni, h->max_layers);
+        if (e != cudaSuccess)
+            return fail(h, VK_ECUDA, std::string("tensor map of the scaled blocks: ") + cudaGetErrorString(e));
+        h->w.tmap_d32 = &h->tmap_d32;
+    }
+    return VK_OK;
+}
+
 extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, int precision,
                          vk_handle **out) {
     if (!out) return fail(nullptr, VK_EINVAL, "out is NULL");
@@ -252,10 +272,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &w.geo, L * 5 * ni));
     // FP64 inverses always (the mixed path falls back to them per column)
     TRY(dalloc(h, &w.G, L * ni * ni));
-    if (precision == VK_PREC_MIXED) {
-        TRY(dalloc(h, &w.G32, L * (size_t)((ni * ni + 3) & ~3)));
-        TRY(dalloc(h, &w.D32, L * (size_t)((ni * ni + 3) & ~3)));
-    }
+    if (precision == VK_PREC_MIXED) TRY(alloc_mixed(h));
     TRY(dalloc(h, &w.zf, L * ni));
     TRY(dalloc(h, &w.fallback, max_cols));
     TRY(dalloc(h, &w.act32, max_cols));
@@ -271,6 +288,8 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
                                                      : fail(h, VK_ECUDA, "cudaFuncSetAttribute (mixed) failed"));
     TRY(vk::init_lureg_kernels(h->net()) == cudaSuccess ? VK_OK
                                                      : fail(h, VK_ECUDA, "cudaFuncSetAttribute (LU) failed"));
+    TRY(vk::init_lu_tc(h->ni) == cudaSuccess ? VK_OK
+                                             : fail(h, VK_ECUDA, "cudaFuncSetAttribute (tensor-core LU) failed"));
     // per-column run state (small); the history ring is sized at the first vk_run
     vk::RunState &r = h->rs;
     r.y = w.y; r.ymix = w.ymix; r.dt = w.dt; r.delta = w.delta; r.atm = h->d_atm;
@@ -295,9 +314,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
 extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol) {
     if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
     if (precision == VK_PREC_MIXED && !h->w.G32) {
-        const size_t st = (size_t)((h->ni * h->ni + 3) & ~3);
-        int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * st);
-        if (!rc) rc = dalloc(h, &h->w.D32, (size_t)h->max_layers * st);
+        int rc = alloc_mixed(h);
         if (rc) return rc;
     }
     if (precision != VK_PREC_FP64 && precision != VK_PREC_MIXED)
@@ -535,6 +552,20 @@ extern "C" int vk_get_lhs(vk_handle *h, double *jv, double *dA, double *dB, doub
     if (dA) VK_CUDA(h, cudaMemcpy(dA, h->w.dA, nb, cudaMemcpyDeviceToHost));
     if (dB) VK_CUDA(h, cudaMemcpy(dB, h->w.dB, nb, cudaMemcpyDeviceToHost));
     if (dC) VK_CUDA(h, cudaMemcpy(dC, h->w.dC, nb, cudaMemcpyDeviceToHost));
+    return VK_OK;
+}
+
+// Test hook: the FP32 inverses of the scaled blocks of the last mixed attempt,
+// [L][ni*ni] natural order (layers of columns solved in FP64 are stale).
+extern "C" int vk_get_lu32(vk_handle *h, float *G) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!G) return fail(h, VK_EINVAL, "G is NULL");
+    if (!h->w.G32) return fail(h, VK_EINVAL, "no FP32 factors (precision is FP64)");
+    const size_t nn = (size_t)h->ni * h->ni, st = (nn + 3) & ~(size_t)3;
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    VK_CUDA(h, cudaMemcpy2D(G, nn * sizeof(float), h->w.G32, st * sizeof(float), nn * sizeof(float),
+                            h->L, cudaMemcpyDeviceToHost));
     return VK_OK;
 }
 

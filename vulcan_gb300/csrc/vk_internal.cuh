@@ -1,6 +1,7 @@
 // Internal declarations shared by the vk_* translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
@@ -172,6 +173,7 @@ struct Work {                  // per-handle device work buffers
     double *dt;                // [ncols]
     double *delta;             // [ncols]
     int *status;               // [ncols]  VK_* per column (singular pivot ...)
+    const void *tmap_d32;      // host: CUtensorMap over D32 as k_lu_tc's padded tiles
 };
 
 void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
@@ -203,5 +205,13 @@ cudaError_t init_mixed_kernels(int n);
 cudaError_t init_lureg_kernels(const DevNet &net);
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
 int lu32_tiling_cap(int tiling);     // largest block a k_lu32 tiling covers (0: none)
+// tensor-core factorisation (vk_lutc.cu): the LU32 tiling value that selects it
+constexpr int VK_LU_TC = 4;
+bool lu_tc_supported(int n);
+cudaError_t lu_tc_make_map(CUtensorMap *map, const float *D32, int n, int max_layers);
+void launch_lu_tc(const DevNet &net, const DevBatch &b, const Work &w, const CUtensorMap &map,
+                  cudaStream_t s);
+size_t lu_tc_block_floats(int n);    // floats per layer of its padded scaled blocks
+cudaError_t init_lu_tc(int n);
 
 }  // namespace vk

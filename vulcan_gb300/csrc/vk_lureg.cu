@@ -6,6 +6,7 @@
 // Columns come from the work queue (longest first); each CTA walks a column's
 // layers in order.  Block sizes up to 160 species are covered by four
 // register tilings (vk_gjreg.cuh).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -35,11 +36,13 @@ __device__ __forceinline__ void tile_coords(int &ty, int &tx) {
 // Per-layer preparation for the FP32 factorisation (fully parallel over
 // layers): power-of-two row scales (row maxima of D_j) and column scales
 // (column maxima of R_j D_j) in FP64, and the dense scaled block R_j D_j S_j
-// rounded once to FP32, written with a 16-byte-aligned stride for TMA.
+// rounded once to FP32, written with a 16-byte-aligned stride for TMA: rows of
+// ld floats, bstride floats per layer (ld = n for k_lu32's packed blocks; ld =
+// NP, the size rounded up to 16, for k_lu_tc's zero-padded NP x NP tiles).
 __global__ void __launch_bounds__(256)
 k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
          const double *__restrict__ dt, float *__restrict__ D32, double *__restrict__ rsc,
-         double *__restrict__ csc) {
+         double *__restrict__ csc, int ld, int bstride) {
     extern __shared__ double sp[];
     const int n = net.ni, nn = n * n, nnz = net.nnz;
     const int l = blockIdx.x;
@@ -98,8 +101,15 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
     for (int r = tid; r < n; r += nth)
         if (net.jmap[r * n + r] < 0) dense[r * n + r] = (float)(rs[r] * dg[r] * cs[r]);
     __syncthreads();
-    float *Dl = D32 + (size_t)l * block_stride32(n);
-    for (int e = tid; e < nn; e += nth) Dl[e] = dense[e];
+    float *Dl = D32 + (size_t)l * bstride;
+    if (ld == n) {
+        for (int e = tid; e < nn; e += nth) Dl[e] = dense[e];
+    } else {
+        for (int e = tid; e < ld * ld; e += nth) {
+            const int r = e / ld, q = e - r * ld;
+            Dl[e] = (r < n && q < n) ? dense[r * n + q] : 0.0f;
+        }
+    }
     for (int t = tid; t < n; t += nth) {
         rsc[(size_t)l * n + t] = rs[t];
         csc[(size_t)l * n + t] = cs[t];
@@ -238,9 +248,13 @@ static size_t smem_prep(const DevNet &net) {
 
 #define VK_LU_TILINGS(X) X(16, 3, 3) X(16, 5, 5) X(16, 7, 7) X(32, 5, 10)
 
-// largest block each tiling covers (rows = TY * RA, columns = 16 * RB)
+// largest block each tiling covers (rows = TY * RA, columns = 16 * RB); tiling
+// VK_LU_TC is the tensor-core factorisation (vk_lutc.cu), up to 128 species
 static const int kTilingCap[4] = {48, 80, 112, 160};
-int lu32_tiling_cap(int t) { return t >= 0 && t < 4 ? kTilingCap[t] : 0; }
+int lu32_tiling_cap(int t) {
+    if (t == VK_LU_TC) return 128;
+    return t >= 0 && t < 4 ? kTilingCap[t] : 0;
+}
 
 static int tiling_of(int n) {
     if (n <= 48) return 0;
@@ -268,13 +282,23 @@ cudaError_t init_lureg_kernels(const DevNet &net) {
 
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s) {
     const int n = net.ni;
-    k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs);
+    // vk_set_launch may pick a larger tiling than the smallest covering ni;
+    // every tiling zero-pads the rows and columns beyond ni
+    int t = b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n);
+    if (t == VK_LU_TC && !w.tmap_d32) t = tiling_of(n);   // no tile map: CUDA-core kernel
+    if (t == VK_LU_TC) {
+        const int NP = (n + 15) / 16 * 16;
+        k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs,
+                                                  NP, NP * NP);
+        cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
+        launch_lu_tc(net, b, w, *static_cast<const CUtensorMap *>(w.tmap_d32), s);
+        return;
+    }
+    k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs,
+                                              n, block_stride32(n));
     const int nb = lu32_nbuf(n);
     size_t sm = smem32(n, nb);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    // vk_set_launch may pick a larger tiling than the smallest covering ni;
-    // every tiling zero-pads the rows and columns beyond ni
-    const int t = b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n);
     switch (t) {
     case 0: k_lu32<16, 3, 3><<<column_grid(b, VK_TUNE_LU32, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;
     case 1: k_lu32<16, 5, 5><<<column_grid(b, VK_TUNE_LU32, 3), 256, sm, s>>>(net, b, w.D32, w.dB, w.dC, w.rs, w.cs, w.G32, w.status, nb); break;

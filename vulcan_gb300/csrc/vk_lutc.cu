@@ -1,0 +1,485 @@
+// FP32 block-Thomas factorisation on the tensor cores (mixed path, blocks of
+// up to 128 species): k_lu_tc replaces k_lu32's register Gauss-Jordan with a
+// blocked Gauss-Jordan whose trailing updates run as tcgen05 MMAs.
+//
+// Per column (work queue, one column at a time per CTA of 4 warps), per layer j:
+//   A  the scaled block D~_j (R_j D_j S_j, written by k_prep32 zero-padded to
+//      NP x NP, NP = ni rounded up to 16) arrives by a 2-D TMA tensor copy; the
+//      Schur complement D~'_j = D~_j - diag(alpha) G~_{j-1} diag(beta) is formed
+//      row by row (thread r <-> row r <-> TMEM lane r) and stored into TMEM,
+//      which holds the block as an FP32 accumulator for the whole inversion;
+//   B  Gauss-Jordan in panels of 16 pivot columns with implicit pivoting (rows
+//      are never exchanged; step k takes the unused row with the largest |a|,
+//      lowest row on ties):
+//        B1 the panel's 16 columns leave TMEM (tcgen05.ld) for shared memory;
+//        B2 one warp eliminates the 16 pivots on the panel alone (3-4 rows per
+//           lane in registers, warp reductions, no block barrier per pivot);
+//           the panel's eliminations form E = I + X S^T, S selecting the pivot
+//           rows, X = (final panel) - S;
+//        B3 the pivot rows of the block before the update, R = S^T A, leave
+//           TMEM into shared memory (zero in the panel's columns), the final
+//           panel goes back into TMEM;
+//        B4 A <- A + X R on the tensor cores: X and R split into TF32 high and
+//           low parts, D += Xh Rh + Xh Rl + Xl Rh (FP32 accumulate in TMEM),
+//           K = 16 as two k-steps of 8;
+//   C  the inverse (permuted labels: inverse[kinv[r]][perm[c]] = A[r][c]) is
+//      stored in natural order into shared memory, kept for layer j+1's Schur
+//      complement and written to G32 by a bulk copy.
+// Split TF32 keeps FP32's accuracy for the refinement: a numpy emulation of
+// this factorisation needs the same refinement sweeps as FP32 Gauss-Jordan.
+//
+// Every wait (TMA, MMA completion) is bounded; on a timeout the CTA records
+// VK_ETIMEOUT for its column, waits (bounded) for its own copies and MMAs in
+// flight, frees its TMEM and leaves.
+//
+// Reference: the banded LU of the Ros2 LHS, op.py:2913-2929 (solve_banded on
+// the matrix store_bandM builds, op.py:2833-2858).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "vk_internal.cuh"
+#include "vk_tc.cuh"
+#include "vk_tma.cuh"
+
+namespace vk {
+
+namespace {
+
+constexpr int kTmemCols = 128;          // D: NP <= 128 columns
+constexpr int kPW = 16;                 // panel width (pivots per MMA update)
+
+struct TcSmem {
+    // byte offsets into the dynamic shared memory (base 1024-byte aligned)
+    int dbuf, gs, ahi, alo, bhi, blo, pex, alpha, beta, prow, perm, kinv, bars, tslot, total;
+};
+
+__host__ __device__ inline int round_up(int x, int a) { return (x + a - 1) / a * a; }
+
+__host__ __device__ inline TcSmem tc_layout(int n) {
+    const int NP = round_up(n, 16);
+    TcSmem s;
+    int o = 0;
+    s.dbuf = o;  o += round_up(NP * NP * 4, 1024);
+    s.gs = o;    o += round_up(block_stride32(n) * 4, 128);
+    s.ahi = o;   o += 128 * kPW * 4;
+    s.alo = o;   o += 128 * kPW * 4;
+    s.bhi = o;   o += round_up(NP * kPW * 4, 128);
+    s.blo = o;   o += round_up(NP * kPW * 4, 128);
+    s.pex = o;   o += round_up(NP * (kPW + 1) * 4, 16);
+    s.alpha = o; o += round_up(NP * 4, 16);
+    s.beta = o;  o += round_up(NP * 4, 16);
+    s.prow = o;  o += 32 * 4;
+    s.perm = o;  o += round_up(NP * 4, 16);
+    s.kinv = o;  o += round_up(NP * 4, 16);
+    s.bars = o;  o += 4 * 8;
+    s.tslot = o; o += 16;
+    s.total = o + 1024;                  // slack for aligning the base
+    return s;
+}
+
+// operand offset (floats) of element (row i, k) in the K-major core-matrix layout
+__device__ __forceinline__ int op_off(int i, int k) {
+    return ((i >> 3) * 4 + (k >> 2)) * 32 + (i & 7) * 4 + (k & 3);
+}
+
+// pivot search result of the panel warp: lowest row among the largest |a|
+// of unused rows (used: bit a of umask for row lane + 32 a)
+template <int RA>
+__device__ __forceinline__ int panel_pivot(const float (&col)[RA], unsigned umask, int lane,
+                                           int &stat) {
+    unsigned best = 0;
+    bool have = false;
+#pragma unroll
+    for (int a = 0; a < RA; ++a) {
+        if (!((umask >> a) & 1u)) {
+            const float v = fabsf(col[a]);
+            if (v == v) {               // NaN never pivots
+                const unsigned bv = __float_as_uint(v);
+                if (!have || bv > best) best = bv;
+                have = true;
+            }
+        }
+    }
+    const unsigned any = __ballot_sync(0xffffffffu, have);
+    const unsigned m = __reduce_max_sync(0xffffffffu, have ? best : 0u);
+    unsigned cand = 0xffffffffu;
+#pragma unroll
+    for (int a = RA - 1; a >= 0; --a) {
+        if (!((umask >> a) & 1u)) {
+            const float v = fabsf(col[a]);
+            if (v == v && __float_as_uint(v) == m) cand = (unsigned)(lane + 32 * a);
+        }
+    }
+    const unsigned p = __reduce_min_sync(0xffffffffu, cand);
+    if (!any || p == 0xffffffffu || m >= 0x7f800000u) {
+        stat = 2;                       // no finite candidate: NaN / Inf state
+        return -1;
+    }
+    if (m == 0u && stat == 0) stat = 1; // zero pivot column: singular
+    return (int)p;
+}
+
+template <int RA>
+__global__ void __launch_bounds__(128, 1)
+k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
+        const double *__restrict__ dB, const double *__restrict__ dC,
+        const double *__restrict__ rsc, const double *__restrict__ csc,
+        float *__restrict__ G32, int *__restrict__ status) {
+    extern __shared__ unsigned char smraw[];
+    unsigned char *smb = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    const int n = net.ni, NP = round_up(n, 16), NNP = block_stride32(n);
+    const TcSmem L = tc_layout(n);
+    float *Dbuf = reinterpret_cast<float *>(smb + L.dbuf);   // [NP][NP] TMA tile
+    float *Gs = reinterpret_cast<float *>(smb + L.gs);       // [n][n] (+pad) natural inverse
+    float *Ahi = reinterpret_cast<float *>(smb + L.ahi);     // X, 128 x 16 operand
+    float *Alo = reinterpret_cast<float *>(smb + L.alo);
+    float *Bhi = reinterpret_cast<float *>(smb + L.bhi);     // R^T, NP x 16 operand
+    float *Blo = reinterpret_cast<float *>(smb + L.blo);
+    float *Pex = reinterpret_cast<float *>(smb + L.pex);     // [NP][17] panel exchange
+    float *alpha = reinterpret_cast<float *>(smb + L.alpha); // [NP] Schur row factors
+    float *beta = reinterpret_cast<float *>(smb + L.beta);   // [NP] Schur column factors
+    float *prow = reinterpret_cast<float *>(smb + L.prow);   // [16] pivot row of the panel
+    int *perm = reinterpret_cast<int *>(smb + L.perm);       // [NP] pivot row of step k
+    int *kinv = reinterpret_cast<int *>(smb + L.kinv);       // [NP] step of pivot row r
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smb + L.bars);   // [0] TMA, [1] MMA
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smb + L.tslot);
+    __shared__ int s_col, s_stat;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r = tid;                                       // row = TMEM lane
+    const bool row_warp = warp * 32 < NP;                    // warp-uniform
+    const uint32_t tbytes = (uint32_t)NP * NP * 4;
+    const uint32_t idesc = idesc_tf32(128, NP);
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&tmap_d) : "memory");
+    }
+    if (warp == 0) tmem_alloc(tslot, kTmemCols);
+    // operands: rows beyond the block (A) stay zero for good
+    for (int e = tid; e < 128 * kPW; e += 128) { Ahi[e] = 0.f; Alo[e] = 0.f; }
+    for (int e = tid; e < NP * kPW; e += 128) { Bhi[e] = 0.f; Blo[e] = 0.f; }
+    for (int e = n * n + tid; e < NNP; e += 128) Gs[e] = 0.f;
+    fence_async_smem();                  // the zero rows are read by the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's lanes, column 0
+
+    int u_tma = 0, u_mma = 0;          // completed phases of bars[0] / bars[1]
+    bool failed = false;
+    for (int c; !failed && (c = next_column(b, &s_col)) >= 0;) {
+        if (b.active && !b.active[c]) continue;
+        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        if (tid == 0) {
+            s_stat = 0;
+            tma_load_2d(Dbuf, &tmap_d, 0, l0 * NP, tbytes, &bars[0]);
+        }
+        for (int j = 0; j < nz && !failed; ++j) {
+            const size_t l = (size_t)l0 + j;
+            // ---- A: Schur complement into TMEM ----
+            const bool ok = mbar_wait(&bars[0], u_tma & 1);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) { status[c] = VK_ETIMEOUT; mbar_wait(&bars[0], u_tma & 1); }
+                failed = true;
+                break;
+            }
+            ++u_tma;
+            if (tid < NP) kinv[tid] = 1 << 30;          // no row is a pivot yet
+            if (row_warp) {
+                const bool live = r < n && j > 0;
+                const float ar = live ? alpha[r] : 0.f;
+#pragma unroll 1
+                for (int q = 0; q < NP; q += 16) {
+                    float v[16];
+#pragma unroll
+                    for (int t = 0; t < 16; t += 4) {
+                        float4 d4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (r < NP) d4 = *reinterpret_cast<const float4 *>(Dbuf + r * NP + q + t);
+                        v[t] = d4.x; v[t + 1] = d4.y; v[t + 2] = d4.z; v[t + 3] = d4.w;
+                    }
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) {
+                        const int cc = q + t;
+                        if (r >= n || cc >= n) v[t] = 0.f;
+                        else if (live) v[t] -= ar * Gs[r * n + cc] * beta[cc];
+                    }
+                    tmem_st16(tlane + q, v);
+                }
+                tmem_wait_st();
+            }
+            tc_fence_before();
+            __syncthreads();                 // Dbuf read by all; TMEM written
+            tc_fence_after();
+            if (tid == 0 && j + 1 < nz) tma_load_2d(Dbuf, &tmap_d, 0, (int)(l + 1) * NP, tbytes, &bars[0]);
+            // Schur factors of layer j+1 (computed now, used after C)
+            float a_nx = 0.f, b_nx = 0.f;
+            if (tid < n && j + 1 < nz) {
+                a_nx = (float)(rsc[(l + 1) * n + tid] * dC[(l + 1) * n + tid] * csc[l * n + tid]);
+                b_nx = (float)(rsc[l * n + tid] * dB[l * n + tid] * csc[(l + 1) * n + tid]);
+            }
+            // ---- B: panels ----
+            for (int k0 = 0; k0 < n && !failed; k0 += kPW) {
+                const int w = n - k0 < kPW ? n - k0 : kPW;
+                // B1: panel columns TMEM -> Pex
+                if (row_warp) {
+                    float v[16];
+                    tmem_ld16(tlane + k0, v);
+                    if (r < NP) {
+#pragma unroll
+                        for (int t = 0; t < 16; ++t) Pex[r * (kPW + 1) + t] = v[t];
+                    }
+                }
+                __syncthreads();
+                // B2: one warp eliminates the panel's pivots
+                if (warp == 0) {
+                    float P[RA][kPW];
+                    unsigned umask = 0;
+#pragma unroll
+                    for (int a = 0; a < RA; ++a) {
+                        const int rr = lane + 32 * a;
+                        const bool in = rr < n;
+                        if (!in || kinv[rr] < k0) umask |= 1u << a;   // padding or pivot of an earlier panel
+#pragma unroll
+                        for (int t = 0; t < kPW; ++t) P[a][t] = in ? Pex[rr * (kPW + 1) + t] : 0.f;
+                    }
+                    int stat = s_stat;
+#pragma unroll
+                    for (int t = 0; t < kPW; ++t) {
+                        if (t < w) {
+                            float col[RA];
+#pragma unroll
+                            for (int a = 0; a < RA; ++a) col[a] = P[a][t];
+                            int p = panel_pivot<RA>(col, umask, lane, stat);
+                            if (p < 0) {                 // no finite candidate: lowest unused row
+                                unsigned lowest = 0xffffffffu;
+#pragma unroll
+                                for (int a = RA - 1; a >= 0; --a)
+                                    if (!((umask >> a) & 1u)) lowest = (unsigned)(lane + 32 * a);
+                                p = (int)__reduce_min_sync(0xffffffffu, lowest);
+                            }
+                            const int pl = p & 31, pa = p >> 5;
+                            if (lane == pl) {
+#pragma unroll
+                                for (int a = 0; a < RA; ++a)
+                                    if (a == pa) {
+#pragma unroll
+                                        for (int q = 0; q < kPW; ++q) prow[q] = P[a][q];
+                                        umask |= 1u << a;
+                                    }
+                            }
+                            if (lane == 0) {
+                                perm[k0 + t] = p;
+                                kinv[p] = k0 + t;
+                            }
+                            __syncwarp();
+                            float rp[kPW];
+#pragma unroll
+                            for (int q = 0; q < kPW; q += 4) {
+                                const float4 x4 = *reinterpret_cast<const float4 *>(prow + q);
+                                rp[q] = x4.x; rp[q + 1] = x4.y; rp[q + 2] = x4.z; rp[q + 3] = x4.w;
+                            }
+                            __syncwarp();
+                            const float pinv = __frcp_rn(rp[t]);
+#pragma unroll
+                            for (int q = 0; q < kPW; ++q) rp[q] = (q == t) ? pinv : rp[q] * pinv;
+#pragma unroll
+                            for (int a = 0; a < RA; ++a) {
+                                const int rr = lane + 32 * a;
+                                if (rr >= n) continue;
+                                if (rr == p) {
+#pragma unroll
+                                    for (int q = 0; q < kPW; ++q) P[a][q] = rp[q];
+                                } else {
+                                    const float f = P[a][t];
+#pragma unroll
+                                    for (int q = 0; q < kPW; ++q)
+                                        P[a][q] = (q == t) ? -f * pinv : fmaf(-f, rp[q], P[a][q]);
+                                }
+                            }
+                        }
+                    }
+                    if (lane == 0) s_stat = stat;
+                    // final panel -> Pex; X = panel - S (hi / lo TF32) -> A operand
+#pragma unroll
+                    for (int a = 0; a < RA; ++a) {
+                        const int rr = lane + 32 * a;
+                        if (rr >= n) continue;
+                        const int kr = kinv[rr] - k0;           // this row's pivot slot in the panel
+#pragma unroll
+                        for (int t = 0; t < kPW; ++t) Pex[rr * (kPW + 1) + t] = P[a][t];
+#pragma unroll
+                        for (int t = 0; t < kPW; t += 4) {
+                            float xh[4], xl[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                float x = (t + e < w) ? P[a][t + e] - ((kr == t + e) ? 1.f : 0.f) : 0.f;
+                                xh[e] = to_tf32(x);
+                                xl[e] = to_tf32(x - xh[e]);
+                            }
+                            *reinterpret_cast<float4 *>(Ahi + op_off(rr, t)) = make_float4(xh[0], xh[1], xh[2], xh[3]);
+                            *reinterpret_cast<float4 *>(Alo + op_off(rr, t)) = make_float4(xl[0], xl[1], xl[2], xl[3]);
+                        }
+                    }
+                    fence_async_smem();
+                }
+                __syncthreads();
+                // B3: pivot rows (pre-update) -> B operand; final panel -> TMEM
+                if (row_warp) {
+                    const int kr = (r < n) ? kinv[r] - k0 : -1;
+                    const bool piv = kr >= 0 && kr < w;
+#pragma unroll 1
+                    for (int q = 0; q < NP; q += 16) {
+                        float v[16];
+                        tmem_ld16(tlane + q, v);
+                        if (piv) {
+#pragma unroll
+                            for (int t = 0; t < 16; ++t) {
+                                const int cc = q + t;
+                                const float x = (cc >= k0 && cc < k0 + kPW) || cc >= n ? 0.f : v[t];
+                                const float xh = to_tf32(x);
+                                Bhi[op_off(cc, kr)] = xh;
+                                Blo[op_off(cc, kr)] = to_tf32(x - xh);
+                            }
+                        }
+                    }
+                    float pv[16];
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) pv[t] = r < n ? Pex[r * (kPW + 1) + t] : 0.f;
+                    tmem_st16(tlane + k0, pv);
+                    tmem_wait_st();
+                    fence_async_smem();
+                }
+                // a narrow last panel: the unused k-rows of B must be zero
+                if (w < kPW) {
+                    for (int e = tid; e < NP * (kPW - w); e += 128) {
+                        const int cc = e / (kPW - w), t = w + e % (kPW - w);
+                        Bhi[op_off(cc, t)] = 0.f;
+                        Blo[op_off(cc, t)] = 0.f;
+                    }
+                    fence_async_smem();
+                }
+                tc_fence_before();
+                __syncthreads();
+                // B4: A += X R on the tensor cores
+                if (tid == 0) {
+                    tc_fence_after();
+                    const uint32_t ah = smem_u32(Ahi), al = smem_u32(Alo);
+                    const uint32_t bh = smem_u32(Bhi), bl = smem_u32(Blo);
+                    const int ksteps = w > 8 ? 2 : 1;
+                    for (int s = 0; s < ksteps; ++s) {
+                        const uint32_t ko = 256u * s;
+                        mma_tf32(tmem, smem_desc(ah + ko, 128, 512), smem_desc(bh + ko, 128, 512), idesc);
+                        mma_tf32(tmem, smem_desc(ah + ko, 128, 512), smem_desc(bl + ko, 128, 512), idesc);
+                        mma_tf32(tmem, smem_desc(al + ko, 128, 512), smem_desc(bh + ko, 128, 512), idesc);
+                    }
+                    mma_commit(&bars[1]);
+                }
+                const bool mok = mbar_wait(&bars[1], u_mma & 1);
+                if (__syncthreads_or(!mok)) {
+                    if (tid == 0) { status[c] = VK_ETIMEOUT; mbar_wait(&bars[1], u_mma & 1); }
+                    failed = true;
+                    break;
+                }
+                ++u_mma;
+                tc_fence_after();
+            }
+            if (failed) break;
+            // ---- C: natural-order inverse -> Gs -> G32 ----
+            if (tid == 0) bulk_wait_read();        // the previous layer's store has read Gs
+            __syncthreads();
+            if (row_warp) {
+                const int row = r < n ? kinv[r] : 0;
+#pragma unroll 1
+                for (int q = 0; q < NP; q += 16) {
+                    float v[16];
+                    tmem_ld16(tlane + q, v);
+                    if (r < n) {
+#pragma unroll
+                        for (int t = 0; t < 16; ++t)
+                            if (q + t < n) Gs[row * n + perm[q + t]] = v[t];
+                    }
+                }
+            }
+            if (tid < n && j + 1 < nz) { alpha[tid] = a_nx; beta[tid] = b_nx; }
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) bulk_store(G32 + l * NNP, Gs, (uint32_t)NNP * 4);
+        }
+        if (failed) break;
+        if (tid == 0 && s_stat) status[c] = s_stat == 2 ? VK_ENAN : VK_ESINGULAR;
+    }
+    if (tid == 0) bulk_wait_all();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static cudaError_t get_encode() {
+    if (g_encode) return cudaSuccess;
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    return cudaSuccess;
+}
+
+bool lu_tc_supported(int n) { return n >= 1 && n <= 128; }
+
+size_t lu_tc_block_floats(int n) { int NP = round_up(n, 16); return (size_t)NP * NP; }
+
+// Tensor map over the padded scaled blocks: [max_layers * NP rows][NP floats].
+cudaError_t lu_tc_make_map(CUtensorMap *map, const float *D32, int n, int max_layers) {
+    cudaError_t e = get_encode();
+    if (e != cudaSuccess) return e;
+    const int NP = round_up(n, 16);
+    cuuint64_t dims[2] = {(cuuint64_t)NP, (cuuint64_t)max_layers * NP};
+    cuuint64_t strides[1] = {(cuuint64_t)NP * 4};
+    cuuint32_t box[2] = {(cuuint32_t)NP, (cuuint32_t)NP};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)D32, dims, strides, box,
+                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+size_t lu_tc_smem(int n) { return (size_t)tc_layout(n).total; }
+
+cudaError_t init_lu_tc(int n) {
+    if (!lu_tc_supported(n)) return cudaSuccess;
+    const int sm = (int)lu_tc_smem(n);
+    cudaError_t e = cudaFuncSetAttribute(k_lu_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_lu_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return e;
+}
+
+void launch_lu_tc(const DevNet &net, const DevBatch &b, const Work &w, const CUtensorMap &map,
+                  cudaStream_t s) {
+    const int n = net.ni, NP = round_up(n, 16);
+    const size_t sm = lu_tc_smem(n);
+    const int grid = column_grid(b, VK_TUNE_LU32, 2);
+    if (NP <= 96)
+        k_lu_tc<3><<<grid, 128, sm, s>>>(net, b, map, w.dB, w.dC, w.rs, w.cs, w.G32, w.status);
+    else
+        k_lu_tc<4><<<grid, 128, sm, s>>>(net, b, map, w.dB, w.dC, w.rs, w.cs, w.G32, w.status);
+}
+
+}  // namespace vk
