@@ -1,19 +1,27 @@
-"""Benchmark: batched Ros2 steps of uneven NCHO columns on one GB300.
+"""Benchmark: batched Ros2 steps of uneven NCHO columns on one GB300, and
+columns to steady state per hour.
 
 Workload: 512 seeded columns on the NCHO thermo network (ni=69, 782 rate
 slots), nz ~ U{60..200} (sum 66 752 layers), T/Kzz/metallicity/C-O seeded
 (vulcan_gb300.configs.config2_columns, seed 2).  One bench step = one Ros2 step
 (attempts until accepted, device step control) of every column.
 
-value  = accepted column-steps per second with the state resident in HBM.
+value  = accepted column-steps per second of the mixed path (FP32 tensor-core
+         block LU + FP64 refinement) with the state resident in HBM, over the
+         timed steps after the warm-up (early steps from const_mix).
 e2e    = the same through the C-ABI with host buffers: every step copies the
          state (y, ymix) host->device, runs one step, and copies y back.
-roofline = the dominant kernel (block LU) against the measured FP64 peak
-         (cuBLAS DGEMM) -- GB300's FP64 rate, not HBM, bounds it; the rate
-         kernel is also reported against the measured HBM copy bandwidth.
+roofline = the dominant kernel of that path against its measured peak; the
+         rate kernel is also reported against the measured HBM bandwidth.
+plain_fp64 = the same for the FP64 path.
+columns_to_steady_state = learned start + mixed vs const_mix + plain FP64:
+         every column under the reference's convergence test within a wall
+         budget per path (--converge-budget); converged columns per hour,
+         column-steps per second over the whole trajectories, and the final
+         mixing ratios against the FP64 path's.
 cpu_baseline = the numpy restatement of the reference's step (banded LAPACK
          solve, as the reference does it) on a bounded sample of the same
-         workload, on the host cores.
+         workload, on the host cores, timed inside the worker processes.
 
 --impl reference  times that CPU path alone (process pool over host cores).
 """
@@ -55,9 +63,21 @@ def peaks():
     return 6800.0, 'fallback'
 
 
+def tf32_peak():
+    """Dense TF32 tensor rate: half the measured dense BF16 burst rate (the
+    same tensor cores at half the BF16 throughput), else the fallback."""
+    p = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if 'bf16_tflops' in d:
+            return d['bf16_tflops'] / 2, 'measured bf16 burst / 2 (TF32 dense)'
+    return 1900.0 / 2, 'fallback bf16 / 2 (TF32 dense)'
+
+
 # ------------------------------------------------------------ CPU baseline
 def _cpu_worker(args):
-    """Integrate one column with the numpy oracle for a fixed number of steps."""
+    """Integrate one column with the numpy oracle for a fixed number of steps;
+    returns (steps, seconds inside the integration loop, attempts)."""
     idx, nsteps = args
     sys.path.insert(0, REPO)
     from oracle import ros2 as O
@@ -79,19 +99,36 @@ def _cpu_worker(args):
     return st.count, time.perf_counter() - t0, st.attempts
 
 
+def _cpu_warm(_):
+    """Pool warm-up: the imports every job needs (not timed)."""
+    sys.path.insert(0, REPO)
+    from oracle import ros2  # noqa: F401
+    from vulcan_gb300 import batch, configs  # noqa: F401
+    return os.getpid()
+
+
 def cpu_baseline(ncols_sample, nsteps, workers):
+    """The numpy restatement of the reference step on `workers` host cores.
+    value = steps / (integration seconds summed over jobs / workers): the rate
+    of `workers` cores each integrating columns back to back, measured inside
+    the jobs (no interpreter start-up, imports or column set-up)."""
     ctx = mp.get_context('spawn')
     jobs = [(i, nsteps) for i in range(ncols_sample)]
-    t0 = time.perf_counter()
     with ctx.Pool(workers) as pool:
+        pool.map(_cpu_warm, range(workers))
+        t0 = time.perf_counter()
         res = pool.map(_cpu_worker, jobs)
-    wall = time.perf_counter() - t0
+        wall = time.perf_counter() - t0
     steps = sum(r[0] for r in res)
-    return dict(value=steps / wall, unit=UNIT, cores=workers, kind='port',
+    busy = sum(r[1] for r in res)
+    value = steps / (busy / workers)
+    return dict(value=value, unit=UNIT, cores=workers, kind='port',
                 sample='%d columns x %d Ros2 steps of the 512-column workload (numpy port of '
-                       'the reference step, LAPACK banded solve), %d worker processes; '
-                       '%.1f s wall' % (ncols_sample, nsteps, workers, wall),
-                wall_s=wall, attempts=sum(r[2] for r in res))
+                       'the reference step, LAPACK banded solve), %d worker processes; %.1f s of '
+                       'integration per core, timed inside the jobs' % (ncols_sample, nsteps, workers,
+                                                                         busy / workers),
+                wall_s=round(wall, 2), wall_rate=round(steps / wall, 3),
+                attempts=sum(r[2] for r in res))
 
 
 # ------------------------------------------------------------ clocks
@@ -190,6 +227,7 @@ def _setup(args, precision, ncols=None, warm_model=None, start='const_mix'):
     net, specs = _workload(args, ncols)
     items = batch.build_items(specs, net)
     used = None
+    items_const = items
     if warm_model is not None:
         from vulcan_gb300 import warmstart
         items, used = warmstart.warm_items(warm_model, specs, net, items, ATOMS, precision)
@@ -197,6 +235,10 @@ def _setup(args, precision, ncols=None, warm_model=None, start='const_mix'):
         from vulcan_gb300 import warmstart
         items = warmstart.eq_items(specs, net, items, ATOMS)
     h, b = batch.make_batch_handle(net, items, ATOMS, precision=precision)
+    if warm_model is not None:
+        # the proposal stands only where it does not raise the chemical residual
+        from vulcan_gb300 import warmstart
+        items, used = warmstart.judge_proposals(h, b, items, items_const)
     ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
     if warm_model is not None:
         return net, items, h, b, ctrl, used
@@ -230,6 +272,7 @@ def _measure(args, precision, clocks=None, dist=None):
     replicas.barrier(dist)
     tm = h.timing()
     st1, c1 = h.state(), h.counters()
+    final = (st1['ymix'].copy(), st1['count'].copy(), st1['t'].copy(), b.off.copy())
     steps = int((st1['count'] - st0['count']).sum())
     attempts = int((c1[:, 0] - c0[:, 0]).sum())
     ms_dev = tm['rates']                  # device time of the whole run (CUDA events)
@@ -269,6 +312,7 @@ def _measure(args, precision, clocks=None, dist=None):
     out['ni'] = net.ni
     out['nr'] = net.nr
     out['npair'] = net.npair
+    out['_final'] = final
     h.close()
     return out
 
@@ -306,11 +350,19 @@ def run_gpu(args):
     am = mixed['attempt_ms']
     dom = max(('lu', 'solve', 'rates'), key=lambda k: am[k])
     stride = (ni * ni + 3) // 4 * 4
+    peak32 = fp32_peak_tflops()
     if dom == 'lu':
-        fl = float(L) * ni ** 3 * 2.0          # FP32 Gauss-Jordan: ni^3 FMA per layer
-        peak = fp32_peak_tflops()
-        roof = {'bound': 'fp32', 'kernel': 'k_lu32 (+k_prep32)', 'achieved': fl / (am['lu'] * 1e-3) / 1e12,
-                'peak': peak, 'unit': 'TFLOP/s', 'peak_source': 'measured cuBLAS SGEMM 8192^3 (no TF32) in this run'}
+        fl = float(L) * ni ** 3 * 2.0          # Gauss-Jordan: ni^3 FMA per layer
+        ach = fl / (am['lu'] * 1e-3) / 1e12
+        if ni <= 128:                          # the tensor-core factorisation (default)
+            ptf, src = tf32_peak()
+            roof = {'bound': 'tensor', 'kernel': 'k_lu_tc (+k_prep32)', 'achieved': ach, 'peak': ptf,
+                    'unit': 'TFLOP/s', 'peak_source': src,
+                    'fp32_core': {'peak': round(peak32, 3), 'frac': round(ach / peak32, 4),
+                                  'peak_source': 'measured cuBLAS SGEMM 8192^3 (no TF32) in this run'}}
+        else:
+            roof = {'bound': 'fp32', 'kernel': 'k_lu32 (+k_prep32)', 'achieved': ach, 'peak': peak32,
+                    'unit': 'TFLOP/s', 'peak_source': 'measured cuBLAS SGEMM 8192^3 (no TF32) in this run'}
     else:
         # refinement + second RHS: every sweep streams the FP32 inverses twice
         by = float(L) * stride * 4 * 2 * 2 * 3
@@ -363,10 +415,45 @@ def run_gpu(args):
                          'peak': hbm, 'unit': 'GB/s', 'peak_source': hbm_kind,
                          'frac': round(rate_bytes / (am['rates'] * 1e-3) / 1e9 / hbm, 4)},
     }
+    # precision: mixed vs FP64 after the same timed steps, on the columns
+    # whose step sequence matched (same count and time)
+    ymm, cm, tmm, off = mixed.pop('_final')
+    ymp, cp, tp, _ = plain.pop('_final')
+    same = (cm == cp) & (np.abs(tmm / tp - 1) < 1e-9)
+    em = np.where(same, 1, 0)
+    out['mixed_vs_fp64_after_timed_steps'] = dict(err_vs_fp64(ymm, em, ymp, em, off),
+                                                  same_step_sequence=int(same.sum()))
     out['clocks'] = clocks.summary()
+    if args.converge_budget > 0 and args.workload == 'c2' and ws == 1:
+        out['columns_to_steady_state'] = converge_block(args)
     if not args.no_cpu and args.workload == 'c2' and ws == 1:
         out['cpu_baseline'] = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
     print(json.dumps(out))
+
+
+def converge_block(args):
+    """Columns to steady state per hour, learned + mixed vs plain FP64, on
+    the full 512-column workload within a wall budget per path."""
+    model = None
+    if os.path.exists(args.weights):
+        from vulcan_gb300 import warmstart
+        model = warmstart.MLP.load(args.weights)
+    paths = ([('learned_mixed', 1)] if model is not None else []) + [('plain_fp64', 0)]
+    res, fin, off = {}, {}, None
+    for name, prec in paths:
+        res[name], fin[name], nib = converge_path(args, name, prec, model, budget=args.converge_budget)
+        off = nib[2].off
+    for name in res:
+        if name != 'plain_fp64':
+            res[name]['vs_fp64_ymix_rel_gt_1e-20'] = err_vs_fp64(
+                fin[name][1], fin[name][2], fin['plain_fp64'][1], fin['plain_fp64'][2], off)
+            res[name]['columns_per_hour_over_fp64'] = round(
+                res[name]['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
+    res['setup'] = ('%d columns from const_mix (plain) or the learned proposal judged by its '
+                    'chemical residual (learned); wall budget %.0f s per path, count_max %d, '
+                    'the reference convergence test; columns per hour = converged columns / wall'
+                    % (args.ncols, args.converge_budget, args.count_max))
+    return res
 
 
 def fp32_peak_tflops():
@@ -391,9 +478,83 @@ def fp32_peak_tflops():
     return best
 
 
+def converge_path(args, name, prec, model=None, budget=None):
+    """One path to steady state: every column of the workload from its start
+    (learned proposal, equilibrium or const_mix) under the reference's
+    convergence test (op.py:1018-1085), replayed in chunks of args.chunk steps
+    until every column has ended or `budget` seconds of wall time have passed.
+    Returns (result dict, final (y, ymix, end_case, count, dt, t), items)."""
+    from vulcan_gb300 import capi
+    budget = args.converge_timeout if budget is None else budget
+    t0 = time.perf_counter()
+    extra = {}
+    if name == 'learned_mixed':
+        net, items, h, b, ctrl, used = _setup(args, prec, warm_model=model)
+        extra = {'warm_started': int(used.sum()), 'proposal_s': round(time.perf_counter() - t0, 2)}
+    elif name == 'eq_mixed':
+        net, items, h, b, ctrl = _setup(args, prec, start='eq')
+        extra = {'proposal_s': round(time.perf_counter() - t0, 2)}
+    else:
+        net, items, h, b, ctrl = _setup(args, prec)
+        t0 = time.perf_counter()
+    ctrl.count_max = args.count_max
+    if args.yconv:
+        ctrl.yconv_cri = ctrl.yconv_min = args.yconv
+    curve = []
+    dev_s = 0.0
+    while True:
+        left = budget - (time.perf_counter() - t0)
+        try:
+            h.run(ctrl, max_steps=args.chunk, timeout_s=max(left, 1.0))
+        except capi.VkError as e:
+            if e.code != capi.VK_ETIMEOUT:
+                raise
+        dev_s += h.timing()['rates'] * 1e-3
+        st = h.state()
+        wall = time.perf_counter() - t0
+        curve.append((round(wall, 1), int(st['count'].max()), int((st['end_case'] == 1).sum()),
+                      int((st['end_case'] != 0).sum())))
+        if (st['end_case'] != 0).all() or wall >= budget:
+            break
+    cnt = h.counters()
+    conv = st['end_case'] == 1
+    res = {'wall_s': round(wall, 2), 'device_s': round(dev_s, 2),
+           'converged': int(conv.sum()), 'ncols': b.ncols,
+           'steps_to_converge_mean': float(st['count'][conv].mean()) if conv.any() else None,
+           'steps_to_converge_median': float(np.median(st['count'][conv])) if conv.any() else None,
+           'steps_max': int(st['count'].max()),
+           'attempts': int(cnt[:, 0].sum()), 'fp64_fallbacks': int(cnt[:, 4].sum()),
+           'columns_per_hour': round(conv.sum() / wall * 3600, 1),
+           'column_steps_per_s': round(float(st['count'].sum()) / wall, 1),
+           'column_steps_per_device_s': round(float(st['count'].sum()) / max(dev_s, 1e-9), 1),
+           'end_cases': {str(k): int(v) for k, v in zip(*np.unique(st['end_case'], return_counts=True))},
+           'curve_wall_maxcount_converged_done': curve, **extra}
+    final = (st['y'], st['ymix'], st['end_case'], st['count'], st['dt'], st['t'])
+    h.close()
+    return res, final, (net, items, b)
+
+
+def err_vs_fp64(ym, em, yp, ep, off):
+    """Per column converged on both paths: max |ymix - ymix_fp64| / ymix_fp64
+    over species with ymix_fp64 > 1e-20; summary over those columns."""
+    both = (em == 1) & (ep == 1)
+    errs, meds = [], []
+    for c in np.nonzero(both)[0]:
+        a, r = ym[off[c]:off[c + 1]], yp[off[c]:off[c + 1]]
+        m = r > 1e-20
+        rel = np.abs(a[m] - r[m]) / r[m]
+        errs.append(float(rel.max()))
+        meds.append(float(np.median(rel)))
+    return {'both_converged_with_fp64': int(both.sum()),
+            'max_over_columns_of_max': max(errs) if errs else None,
+            'median_over_columns_of_max': float(np.median(errs)) if errs else None,
+            'median_over_columns_of_median': float(np.median(meds)) if meds else None,
+            'columns_within_1e-3': int(sum(e <= 1e-3 for e in errs))}
+
+
 def run_converge(args):
-    """Every column to steady state on both paths, in chunks of steps: steps to
-    converge, columns per hour, agreement of the final states."""
+    """Every column to steady state on the selected paths, in chunks of steps:
+    steps to converge, columns per hour, agreement of the final states."""
     from vulcan_gb300 import capi
     res = {}
     finals = {}
@@ -408,62 +569,25 @@ def run_converge(args):
     if args.precision_only:
         keep = args.precision_only.split(',')
         paths = [p for p in paths if p[0] in keep]
+    items_by = {}
     for name, prec in paths:
-        t0 = time.perf_counter()
-        if name == 'learned_mixed':
-            net, items, h, b, ctrl, used = _setup(args, prec, warm_model=model)
-            res_extra = {'warm_started': int(used.sum()),
-                         'proposal_s': round(time.perf_counter() - t0, 2)}
-        elif name == 'eq_mixed':
-            net, items, h, b, ctrl = _setup(args, prec, start='eq')
-            res_extra = {'proposal_s': round(time.perf_counter() - t0, 2)}
-        else:
-            net, items, h, b, ctrl = _setup(args, prec)
-            res_extra = {}
-            t0 = time.perf_counter()
-        ctrl.count_max = args.count_max
-        if args.yconv:
-            ctrl.yconv_cri = ctrl.yconv_min = args.yconv
-        curve = []
-        dev_s = 0.0
-        while True:
-            try:
-                h.run(ctrl, max_steps=args.chunk, timeout_s=args.converge_timeout)
-            except capi.VkError as e:
-                if e.code != capi.VK_ETIMEOUT:
-                    raise
-            dev_s += h.timing()['rates'] * 1e-3
-            st = h.state()
-            wall = time.perf_counter() - t0
-            curve.append((round(wall, 1), int(st['count'].max()), int((st['end_case'] == 1).sum()),
-                          int((st['end_case'] != 0).sum())))
-            if (st['end_case'] != 0).all() or wall > args.converge_timeout:
-                break
-        cnt = h.counters()
-        conv = st['end_case'] == 1
-        res[name] = {'wall_s': round(wall, 2), 'device_s': round(dev_s, 2),
-                     'converged': int(conv.sum()), 'ncols': b.ncols,
-                     'steps_to_converge_mean': float(st['count'][conv].mean()) if conv.any() else None,
-                     'steps_to_converge_median': float(np.median(st['count'][conv])) if conv.any() else None,
-                     'steps_max': int(st['count'].max()),
-                     'attempts': int(cnt[:, 0].sum()), 'fp64_fallbacks': int(cnt[:, 4].sum()),
-                     'columns_per_hour': round(conv.sum() / wall * 3600, 1),
-                     'column_steps_per_s': round(float(st['count'].sum()) / wall, 1),
-                     'end_cases': {str(k): int(v) for k, v in zip(*np.unique(st['end_case'], return_counts=True))},
-                     'curve_wall_maxcount_converged_done': curve, **res_extra}
-        finals[name] = (st['ymix'], st['end_case'], st['count'])
-        h.close()
+        res[name], finals[name], items_by[name] = converge_path(args, name, prec, model)
         if args.polish:
             # continue every column from its final state for args.polish more
             # steps with a criterion that never fires: the slow transport modes
             # the convergence test does not resolve keep relaxing
             from vulcan_gb300 import batch
-            pol = [dict(it, y=st['y'][b.off[c]:b.off[c + 1]], ymix=st['ymix'][b.off[c]:b.off[c + 1]])
+            from vulcan_gb300.solver import ctrl_from
+            from vulcan_gb300 import configs
+            net, items, b = items_by[name]
+            y, ymix, ec, count, dt, t = finals[name]
+            pol = [dict(it, y=y[b.off[c]:b.off[c + 1]], ymix=ymix[b.off[c]:b.off[c + 1]])
                    for c, it in enumerate(items)]
             hp, bp = batch.make_batch_handle(net, pol, ATOMS, precision=prec)
-            hp.set_clock(dt=st['dt'], t=st['t'], count=st['count'])
+            hp.set_clock(dt=dt, t=t, count=count)
+            ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
             ctrl.yconv_cri = ctrl.yconv_min = 1e-12
-            ctrl.count_max = int(st['count'].max()) + args.polish + 1
+            ctrl.count_max = int(count.max()) + args.polish + 1
             try:
                 hp.run(ctrl, max_steps=args.polish, timeout_s=args.converge_timeout)
             except capi.VkError as e:
@@ -471,45 +595,27 @@ def run_converge(args):
                     raise
             sp = hp.state()
             hp.close()
-            finals[name + '_polished'] = (sp['ymix'], st['end_case'], sp['count'])
+            finals[name + '_polished'] = (sp['y'], sp['ymix'], ec, sp['count'], sp['dt'], sp['t'])
             res[name]['polished_t_median'] = float(np.median(sp['t']))
     res['metric'] = METRIC
     res['workload'] = ('%d uneven NCHO-thermo columns to steady state (%s, count_max %d)'
                        % (args.ncols, 'reference conv criterion' if not args.yconv else
                           'yconv_cri = yconv_min = %g' % args.yconv, args.count_max))
     if 'plain_fp64' in finals:
-        bsz = [it.pco.size for it in _workload(args)[1]]
-        off = np.concatenate([[0], np.cumsum(bsz)])
-        yp, ep = finals['plain_fp64'][0], finals['plain_fp64'][1]
+        off = items_by['plain_fp64'][2].off
         pairs = [(n, 'plain_fp64') for n in finals if n != 'plain_fp64' and not n.endswith('_polished')]
         if 'plain_fp64_polished' in finals:
             pairs += [(n, 'plain_fp64_polished') for n in finals
                       if n.endswith('_polished') and n != 'plain_fp64_polished']
             pairs += [('plain_fp64_polished', 'plain_fp64')]
         for name, refname in pairs:
-            yp, ep = finals[refname][0], finals[refname][1]
-            ym, em = finals[name][0], finals[name][1]
+            e = err_vs_fp64(finals[name][1], finals[name][2], finals[refname][1], finals[refname][2], off)
             key = name if name in res else name.replace('_polished', '')
             if name.endswith('_polished') or refname.endswith('_polished'):
-                res.setdefault('polish', {})
-                tgt = res['polish'].setdefault('%s_vs_%s' % (name, refname), {})
+                res.setdefault('polish', {})['%s_vs_%s' % (name, refname)] = e
             else:
-                tgt = res[key]
-            both = (em == 1) & (ep == 1)
-            errs, meds = [], []
-            for c in np.nonzero(both)[0]:
-                a, r = ym[off[c]:off[c + 1]], yp[off[c]:off[c + 1]]
-                m = r > 1e-20
-                rel = np.abs(a[m] - r[m]) / r[m]
-                errs.append(float(rel.max()))
-                meds.append(float(np.median(rel)))
-            tgt['both_converged_with_fp64'] = int(both.sum())
-            tgt['vs_fp64_ymix_rel_gt_1e-20'] = {
-                'max_over_columns_of_max': max(errs) if errs else None,
-                'median_over_columns_of_max': float(np.median(errs)) if errs else None,
-                'median_over_columns_of_median': float(np.median(meds)) if meds else None}
-            if tgt is res.get(key):
-                tgt['speedup_columns_per_hour_vs_fp64'] = round(
+                res[key]['vs_fp64_ymix_rel_gt_1e-20'] = e
+                res[key]['speedup_columns_per_hour_vs_fp64'] = round(
                     res[key]['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
     print(json.dumps(res))
 
@@ -619,7 +725,10 @@ def main():
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
-    ap.add_argument('--count-max', type=int, default=30000)
+    ap.add_argument('--converge-budget', type=float, default=150.0,
+                    help='default run: wall seconds per path for the columns-to-steady-state '
+                         'measurement (0: skip)')
+    ap.add_argument('--count-max', type=int, default=3000)
     ap.add_argument('--chunk', type=int, default=500)
     ap.add_argument('--polish', type=int, default=0,
                     help='converge mode: continue every column this many steps past its stop '

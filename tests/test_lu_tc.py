@@ -37,6 +37,9 @@ def test_tensor_core_factors_match_cuda_core_factors(tag, ns):
     from vulcan_gb300 import capi
     g, net, gn, h, b = make_handle(tag, ns=ns, precision=1)
     dt = g['att_dt'][ns]
+    # the CUDA-core kernel: the smallest register tiling that covers ni
+    h.set_launch(capi.VK_TUNE_LU32, 0, min(t for t, cap in enumerate(capi.LU32_TILING_CAP[:4])
+                                           if cap >= net.ni))
     out_ref = h.attempt(dt)
     sw_ref, fb_ref = h.refine_stats()
     G_ref = _factors(h, net.ni, b.L)
@@ -62,7 +65,19 @@ def test_tensor_core_factors_match_cuda_core_factors(tag, ns):
         assert floor_err(sols[i], g['att_sol'][n], g['n_0']) <= 1e-10
 
 
-def test_tensor_core_default_refused_beyond_128_species():
-    """Variant 4 covers at most 128 species."""
+def test_tensor_core_is_the_default_up_to_128_species():
+    """Without a launch setting the mixed path factorises on the tensor cores
+    (variant -1 resolves to it for ni <= 128): its factors equal an explicit
+    variant-4 run bit for bit."""
+    from test_gpu_parity import make_handle
     from vulcan_gb300 import capi
+    g, net, gn, h, b = make_handle('c2', ns=[0, 1], precision=1)
+    dt = g['att_dt'][[0, 1]]
+    h.attempt(dt)
+    G0 = _factors(h, net.ni, b.L)
+    h.set_launch(capi.VK_TUNE_LU32, 0, capi.LU32_TC)
+    h.attempt(dt)
+    G1 = _factors(h, net.ni, b.L)
+    h.close()
+    np.testing.assert_array_equal(G0, G1)
     assert capi.LU32_TILING_CAP[capi.LU32_TC] == 128

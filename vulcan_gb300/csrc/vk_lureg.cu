@@ -284,7 +284,9 @@ void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaSt
     const int n = net.ni;
     // vk_set_launch may pick a larger tiling than the smallest covering ni;
     // every tiling zero-pads the rows and columns beyond ni
-    int t = b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n);
+    // default (-1): the tensor-core factorisation where it covers ni
+    int t = b.lu32_tiling == -1 ? (lu_tc_supported(n) ? VK_LU_TC : tiling_of(n))
+          : (b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n));
     if (t == VK_LU_TC && !w.tmap_d32) t = tiling_of(n);   // no tile map: CUDA-core kernel
     if (t == VK_LU_TC) {
         const int NP = (n + 15) / 16 * 16;

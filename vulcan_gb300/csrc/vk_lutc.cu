@@ -49,10 +49,11 @@ namespace {
 
 constexpr int kTmemCols = 128;          // D: NP <= 128 columns
 constexpr int kPW = 16;                 // panel width (pivots per MMA update)
+constexpr int kLdGroup = 3;             // TMEM loads of 16 columns issued per wait
 
 struct TcSmem {
-    // byte offsets into the dynamic shared memory (base 1024-byte aligned)
-    int dbuf, gs, ahi, alo, bhi, blo, pex, alpha, beta, prow, perm, kinv, bars, tslot, total;
+    // byte offsets into the dynamic shared memory (base 128-byte aligned)
+    int dbuf, gs, ahi, alo, bhi, blo, pex, alpha, beta, perm, kinv, bars, tslot, total;
 };
 
 __host__ __device__ inline int round_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -61,7 +62,7 @@ __host__ __device__ inline TcSmem tc_layout(int n) {
     const int NP = round_up(n, 16);
     TcSmem s;
     int o = 0;
-    s.dbuf = o;  o += round_up(NP * NP * 4, 1024);
+    s.dbuf = o;  o += round_up(NP * NP * 4, 128);
     s.gs = o;    o += round_up(block_stride32(n) * 4, 128);
     s.ahi = o;   o += 128 * kPW * 4;
     s.alo = o;   o += 128 * kPW * 4;
@@ -70,12 +71,11 @@ __host__ __device__ inline TcSmem tc_layout(int n) {
     s.pex = o;   o += round_up(NP * (kPW + 1) * 4, 16);
     s.alpha = o; o += round_up(NP * 4, 16);
     s.beta = o;  o += round_up(NP * 4, 16);
-    s.prow = o;  o += 32 * 4;
     s.perm = o;  o += round_up(NP * 4, 16);
     s.kinv = o;  o += round_up(NP * 4, 16);
     s.bars = o;  o += 4 * 8;
     s.tslot = o; o += 16;
-    s.total = o + 1024;                  // slack for aligning the base
+    s.total = o + 128;                   // slack for aligning the base
     return s;
 }
 
@@ -84,41 +84,103 @@ __device__ __forceinline__ int op_off(int i, int k) {
     return ((i >> 3) * 4 + (k >> 2)) * 32 + (i & 7) * 4 + (k & 3);
 }
 
-// pivot search result of the panel warp: lowest row among the largest |a|
-// of unused rows (used: bit a of umask for row lane + 32 a)
+// Pivot of the panel warp's current column (slot 0 of every row it holds):
+// the unused row with the largest |a|, lowest row on ties, found by one warp
+// reduction of a key that is |a| with its 7 low mantissa bits replaced by
+// 127 - row (so values equal to 2^-16 relative also go to the lowest row --
+// any such choice is a valid partial pivot).  NaN rows never pivot.  Returns
+// -1 (stat 2) when no finite candidate is left; stat 1 for a zero column.
 template <int RA>
 __device__ __forceinline__ int panel_pivot(const float (&col)[RA], unsigned umask, int lane,
                                            int &stat) {
-    unsigned best = 0;
-    bool have = false;
+    unsigned key = 0;
 #pragma unroll
     for (int a = 0; a < RA; ++a) {
-        if (!((umask >> a) & 1u)) {
-            const float v = fabsf(col[a]);
-            if (v == v) {               // NaN never pivots
-                const unsigned bv = __float_as_uint(v);
-                if (!have || bv > best) best = bv;
-                have = true;
-            }
-        }
+        const float v = fabsf(col[a]);
+        const unsigned k = (__float_as_uint(v) & ~127u) | (unsigned)(127 - (lane + 32 * a));
+        if (!((umask >> a) & 1u) && v == v) key = max(key, k | 0x80000000u);
     }
-    const unsigned any = __ballot_sync(0xffffffffu, have);
-    const unsigned m = __reduce_max_sync(0xffffffffu, have ? best : 0u);
-    unsigned cand = 0xffffffffu;
+    const unsigned m = __reduce_max_sync(0xffffffffu, key);
+    if (m == 0u || (m & 0x7fffffffu) >= 0x7f800000u) { stat = 2; return -1; }
+    if (((m & 0x7fffff80u) == 0u) && stat == 0) stat = 1;
+    return 127 - (int)(m & 127u);
+}
+
+// Gauss-Jordan on the panel alone, by one warp: P[a][q] holds row lane + 32a,
+// panel column q.  The panel rotates one column to the left per pivot step
+// (the consumed column moves to slot 15, where its inverse entries are
+// stored), so the pivot column is always slot 0 and the loop body is the same
+// code for every step; after kPW steps (padding steps rotate only) the slots
+// are back in panel order.  Records perm / kinv in shared memory.
+template <int RA>
+__device__ __forceinline__ void panel_eliminate(float (&P)[RA][kPW], unsigned &umask, int lane,
+                                                int k0, int w, int *perm, int *kinv, int &stat) {
+    int myp = 0;
+#pragma unroll 1
+    for (int t = 0; t < kPW; ++t) {
+        if (t >= w) {                     // past the last pivot: rotate only
 #pragma unroll
-    for (int a = RA - 1; a >= 0; --a) {
-        if (!((umask >> a) & 1u)) {
-            const float v = fabsf(col[a]);
-            if (v == v && __float_as_uint(v) == m) cand = (unsigned)(lane + 32 * a);
+            for (int a = 0; a < RA; ++a) {
+                const float c0 = P[a][0];
+#pragma unroll
+                for (int q = 0; q < kPW - 1; ++q) P[a][q] = P[a][q + 1];
+                P[a][kPW - 1] = c0;
+            }
+            continue;
         }
+        float col[RA];
+#pragma unroll
+        for (int a = 0; a < RA; ++a) col[a] = P[a][0];
+        int p = panel_pivot<RA>(col, umask, lane, stat);
+        if (p < 0) {                      // no finite candidate: lowest unused row
+            unsigned lowest = 0xffffffffu;
+#pragma unroll
+            for (int a = RA - 1; a >= 0; --a)
+                if (!((umask >> a) & 1u)) lowest = (unsigned)(lane + 32 * a);
+            p = (int)__reduce_min_sync(0xffffffffu, lowest);
+        }
+        if ((unsigned)p >= 32u * RA) p = 0;          // (cannot happen: a row is always left)
+        const int pl = p & 31, pa = p >> 5;          // warp-uniform
+        // pivot row from its lane (uniform switch on the row slot)
+        float rs[kPW];
+        switch (pa) {
+#define VK_BCAST(A)                                                           \
+        case A:                                                               \
+            if constexpr (A < RA) {                                           \
+                _Pragma("unroll") for (int q = 0; q < kPW; ++q)               \
+                    rs[q] = __shfl_sync(0xffffffffu, P[A][q], pl);            \
+            }                                                                 \
+            break;
+        VK_BCAST(0) VK_BCAST(1) VK_BCAST(2) VK_BCAST(3)
+#undef VK_BCAST
+        default: break;
+        }
+        float pinv;                                   // 1/pivot (FP32 factors: refined in FP64)
+        asm("rcp.approx.f32 %0, %1;" : "=f"(pinv) : "f"(rs[0]));
+#pragma unroll
+        for (int q = 1; q < kPW; ++q) rs[q] *= pinv;
+        // eliminate column 0 from every row, shifting left by one; the pivot
+        // row itself becomes the scaled row with 1/pivot in the consumed slot
+#pragma unroll
+        for (int a = 0; a < RA; ++a) {
+            const bool isp = lane + 32 * a == p;
+            const float f = P[a][0];
+#pragma unroll
+            for (int q = 0; q < kPW - 1; ++q) {
+                const float e = fmaf(-f, rs[q + 1], P[a][q + 1]);
+                P[a][q] = isp ? rs[q + 1] : e;
+            }
+            P[a][kPW - 1] = isp ? pinv : -f * pinv;
+            if (isp) umask |= 1u << a;
+        }
+        if (lane == t) myp = p;                      // lane t records step t
     }
-    const unsigned p = __reduce_min_sync(0xffffffffu, cand);
-    if (!any || p == 0xffffffffu || m >= 0x7f800000u) {
-        stat = 2;                       // no finite candidate: NaN / Inf state
-        return -1;
+    __syncwarp();
+    if (lane < w) {
+        perm[k0 + lane] = myp;
+        kinv[myp] = k0 + lane;
     }
-    if (m == 0u && stat == 0) stat = 1; // zero pivot column: singular
-    return (int)p;
+    __syncwarp();
 }
 
 template <int RA>
@@ -129,7 +191,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
         float *__restrict__ G32, int *__restrict__ status) {
     extern __shared__ unsigned char smraw[];
     unsigned char *smb = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+        (reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
     const int n = net.ni, NP = round_up(n, 16), NNP = block_stride32(n);
     const TcSmem L = tc_layout(n);
     float *Dbuf = reinterpret_cast<float *>(smb + L.dbuf);   // [NP][NP] TMA tile
@@ -141,7 +203,6 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
     float *Pex = reinterpret_cast<float *>(smb + L.pex);     // [NP][17] panel exchange
     float *alpha = reinterpret_cast<float *>(smb + L.alpha); // [NP] Schur row factors
     float *beta = reinterpret_cast<float *>(smb + L.beta);   // [NP] Schur column factors
-    float *prow = reinterpret_cast<float *>(smb + L.prow);   // [16] pivot row of the panel
     int *perm = reinterpret_cast<int *>(smb + L.perm);       // [NP] pivot row of step k
     int *kinv = reinterpret_cast<int *>(smb + L.kinv);       // [NP] step of pivot row r
     uint64_t *bars = reinterpret_cast<uint64_t *>(smb + L.bars);   // [0] TMA, [1] MMA
@@ -250,61 +311,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
                         for (int t = 0; t < kPW; ++t) P[a][t] = in ? Pex[rr * (kPW + 1) + t] : 0.f;
                     }
                     int stat = s_stat;
-#pragma unroll
-                    for (int t = 0; t < kPW; ++t) {
-                        if (t < w) {
-                            float col[RA];
-#pragma unroll
-                            for (int a = 0; a < RA; ++a) col[a] = P[a][t];
-                            int p = panel_pivot<RA>(col, umask, lane, stat);
-                            if (p < 0) {                 // no finite candidate: lowest unused row
-                                unsigned lowest = 0xffffffffu;
-#pragma unroll
-                                for (int a = RA - 1; a >= 0; --a)
-                                    if (!((umask >> a) & 1u)) lowest = (unsigned)(lane + 32 * a);
-                                p = (int)__reduce_min_sync(0xffffffffu, lowest);
-                            }
-                            const int pl = p & 31, pa = p >> 5;
-                            if (lane == pl) {
-#pragma unroll
-                                for (int a = 0; a < RA; ++a)
-                                    if (a == pa) {
-#pragma unroll
-                                        for (int q = 0; q < kPW; ++q) prow[q] = P[a][q];
-                                        umask |= 1u << a;
-                                    }
-                            }
-                            if (lane == 0) {
-                                perm[k0 + t] = p;
-                                kinv[p] = k0 + t;
-                            }
-                            __syncwarp();
-                            float rp[kPW];
-#pragma unroll
-                            for (int q = 0; q < kPW; q += 4) {
-                                const float4 x4 = *reinterpret_cast<const float4 *>(prow + q);
-                                rp[q] = x4.x; rp[q + 1] = x4.y; rp[q + 2] = x4.z; rp[q + 3] = x4.w;
-                            }
-                            __syncwarp();
-                            const float pinv = __frcp_rn(rp[t]);
-#pragma unroll
-                            for (int q = 0; q < kPW; ++q) rp[q] = (q == t) ? pinv : rp[q] * pinv;
-#pragma unroll
-                            for (int a = 0; a < RA; ++a) {
-                                const int rr = lane + 32 * a;
-                                if (rr >= n) continue;
-                                if (rr == p) {
-#pragma unroll
-                                    for (int q = 0; q < kPW; ++q) P[a][q] = rp[q];
-                                } else {
-                                    const float f = P[a][t];
-#pragma unroll
-                                    for (int q = 0; q < kPW; ++q)
-                                        P[a][q] = (q == t) ? -f * pinv : fmaf(-f, rp[q], P[a][q]);
-                                }
-                            }
-                        }
-                    }
+                    panel_eliminate<RA>(P, umask, lane, k0, w, perm, kinv, stat);
                     if (lane == 0) s_stat = stat;
                     // final panel -> Pex; X = panel - S (hi / lo TF32) -> A operand
 #pragma unroll
@@ -335,17 +342,24 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
                     const int kr = (r < n) ? kinv[r] - k0 : -1;
                     const bool piv = kr >= 0 && kr < w;
 #pragma unroll 1
-                    for (int q = 0; q < NP; q += 16) {
-                        float v[16];
-                        tmem_ld16(tlane + q, v);
-                        if (piv) {
+                    for (int g0 = 0; g0 < NP; g0 += 16 * kLdGroup) {
+                        float v[kLdGroup][16];           // kLdGroup chunks per wait
 #pragma unroll
-                            for (int t = 0; t < 16; ++t) {
-                                const int cc = q + t;
-                                const float x = (cc >= k0 && cc < k0 + kPW) || cc >= n ? 0.f : v[t];
-                                const float xh = to_tf32(x);
-                                Bhi[op_off(cc, kr)] = xh;
-                                Blo[op_off(cc, kr)] = to_tf32(x - xh);
+                        for (int ch = 0; ch < kLdGroup; ++ch)
+                            if (g0 + ch * 16 < NP) tmem_ld16_nowait(tlane + g0 + ch * 16, v[ch]);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int ch = 0; ch < kLdGroup; ++ch) {
+                            tmem_reg_dep(v[ch]);
+                            if (piv && g0 + ch * 16 < NP) {
+#pragma unroll
+                                for (int t = 0; t < 16; ++t) {
+                                    const int cc = g0 + ch * 16 + t;
+                                    const float x = (cc >= k0 && cc < k0 + kPW) || cc >= n ? 0.f : v[ch][t];
+                                    const float xh = to_tf32(x);
+                                    Bhi[op_off(cc, kr)] = xh;
+                                    Blo[op_off(cc, kr)] = to_tf32(x - xh);
+                                }
                             }
                         }
                     }
@@ -397,13 +411,22 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
             if (row_warp) {
                 const int row = r < n ? kinv[r] : 0;
 #pragma unroll 1
-                for (int q = 0; q < NP; q += 16) {
-                    float v[16];
-                    tmem_ld16(tlane + q, v);
-                    if (r < n) {
+                for (int g0 = 0; g0 < NP; g0 += 16 * kLdGroup) {
+                    float v[kLdGroup][16];
 #pragma unroll
-                        for (int t = 0; t < 16; ++t)
-                            if (q + t < n) Gs[row * n + perm[q + t]] = v[t];
+                    for (int ch = 0; ch < kLdGroup; ++ch)
+                        if (g0 + ch * 16 < NP) tmem_ld16_nowait(tlane + g0 + ch * 16, v[ch]);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int ch = 0; ch < kLdGroup; ++ch) {
+                        tmem_reg_dep(v[ch]);
+                        if (r < n) {
+#pragma unroll
+                            for (int t = 0; t < 16; ++t) {
+                                const int cc = g0 + ch * 16 + t;
+                                if (cc < n) Gs[row * n + perm[cc]] = v[ch][t];
+                            }
+                        }
                     }
                 }
             }

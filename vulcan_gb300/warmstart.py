@@ -404,6 +404,22 @@ def warm_items(model, specs, net, items, atoms, precision=1):
     return out, np.ones(len(items), dtype=bool)
 
 
+def judge_proposals(h, batch, items_warm, items_const):
+    """The solver's judge of the learned start: a column keeps its proposal
+    only where it does not raise the chemical residual (chem_residual) above
+    that of the const_mix start; elsewhere the const_mix state goes back into
+    the handle.  Returns (items, used mask)."""
+    n0 = np.concatenate([it['col'].n_0 for it in items_const])
+    yw = np.concatenate([it['y'] for it in items_warm])
+    yc = np.concatenate([it['y'] for it in items_const])
+    used = chem_residual(h, yw, n0, batch) <= chem_residual(h, yc, n0, batch)
+    items = [iw if u else ic for iw, ic, u in zip(items_warm, items_const, used)]
+    if not used.all():
+        h.set_state(np.concatenate([it['y'] for it in items]),
+                    np.concatenate([it['ymix'] for it in items]))
+    return items, used
+
+
 def eq_items(specs, net, items, atoms):
     """Items started from thermochemical equilibrium (the reference's
     ini_mix = 'EQ' seam), projected onto the const_mix start's element
