@@ -326,6 +326,11 @@ VK_API int  vk_get_refine_stats(vk_handle *h, int *max_sweeps, int *n_fallback);
 VK_API const char *vk_network_last_error(void);
 /* Chemistry source term alone (the generated chemdf) of state y [L][ni]. */
 VK_API int  vk_chem_source(vk_handle *h, const double *y, double *dydt);
+/* Right-hand side f(y) = chemdf + diffdf of state y [L][ni] (the handle's
+ * state when y is NULL) with the transport terms `flags` selects (VK_F_*):
+ * the f of Ros2.solver (op.py:2888); f is [L][ni].  Leaves the handle's
+ * state and its last attempt untouched. */
+VK_API int  vk_rhs(vk_handle *h, const double *y, int flags, double *f);
 /* FP32 inverses of the scaled diagonal blocks of the last mixed-precision
  * attempt, [L][ni*ni] row-major (columns that attempt solved in FP64 hold
  * stale values). */

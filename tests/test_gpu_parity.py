@@ -270,16 +270,23 @@ def test_device_run_converges_like_reference(precision):
     g, st = _run_to_steady('c2conv', precision)
     assert st['end_case'][0] == 1
     assert 0.4 * g['final_count'] <= st['count'][0] <= 2.5 * g['final_count']
-    # the final state against the reference's, for species above 1e-20: within
-    # the criterion's own tolerance (yconv_min = 0.1 relative change over the
-    # last half of the run time), in the median and the 90th percentile
-    ref = g['final_ymix']
-    m = ref > 1e-20
+    # the final state against the reference's, on the entries the
+    # convergence test itself judges (op.py:1041-1046: ymix >= mtol_conv,
+    # y >= atol, conver_ignore species left out): within the criterion's own
+    # tolerances -- yconv_cri (0.01) in the median, yconv_min (0.1 relative
+    # change over the last half of the run time) at the 90th percentile
+    tol = O.Tol()
+    ref, yref = g['final_ymix'], g['final_y']
+    m = (ref >= tol.mtol_conv) & (yref >= tol.atol)
+    net = network('c2conv')
+    for sp in g['conver_ignore']:
+        m[:, net.species.index(str(sp))] = False
     rel = np.abs(st['ymix'][m] - ref[m]) / ref[m]
     q50, q90, q99, qmax = np.percentile(rel, [50, 90, 99, 100])
-    print('c2conv final ymix vs reference (precision %d): median %.2e, 90%% %.2e, 99%% %.2e, max %.2e'
-          % (precision, q50, q90, q99, qmax))
-    assert q50 <= 0.1 and q90 <= 0.1
+    print('c2conv final ymix vs reference (precision %d, t %.3e vs %.3e s): median %.2e, '
+          '90%% %.2e, 99%% %.2e, max %.2e'
+          % (precision, st['t'][0], g['final_t'], q50, q90, q99, qmax))
+    assert q50 <= tol.yconv_cri and q90 <= tol.yconv_min
 
 
 @pytest.mark.parametrize('precision', [0, 1])

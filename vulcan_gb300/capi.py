@@ -39,7 +39,7 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
            'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps',
-           'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore', 'vk_get_lu32')
+           'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore', 'vk_get_lu32', 'vk_rhs')
 
 
 class VkNetworkDesc(C.Structure):
@@ -102,6 +102,7 @@ def lib(path=None):
         'vk_set_column_info': (i, [vp, pi, pi]),
         'vk_set_conv_ignore': (i, [vp, pi]),
         'vk_get_lu32': (i, [vp, P(C.c_float)]),
+        'vk_rhs': (i, [vp, pd, i, pd]),
         'vk_run': (i, [vp, P(VkCtrl), i, d]),
         'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
         'vk_set_clock': (i, [vp, pd, pd, pi]),

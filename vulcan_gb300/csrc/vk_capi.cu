@@ -529,6 +529,28 @@ extern "C" int vk_ros2_attempt(vk_handle *h, const double *dt, int flags, double
     return VK_OK;
 }
 
+// Right-hand side of the Ros2 system at state y (or the handle's state when y
+// is NULL): chemistry plus the transport terms the flags select, the f of
+// op.py:2888 (chemdf + diffdf).
+extern "C" int vk_rhs(vk_handle *h, const double *y, int flags, double *f) {
+    int rc = need_batch(h);
+    if (rc) return rc;
+    if (!f) return fail(h, VK_EINVAL, "f is NULL");
+    size_t bytes = (size_t)h->L * h->ni * sizeof(double);
+    const double *yd = h->w.y;
+    if (y) {
+        VK_CUDA(h, cudaMemcpyAsync(h->w.yk2, y, bytes, cudaMemcpyHostToDevice, h->stream));
+        yd = h->w.yk2;
+    }
+    ensure_geometry(h, flags);
+    vk::launch_rates(h->net(), h->batch(), yd, h->w.f2, h->w.jv, h->w.dA, h->w.dB, h->w.dC, nullptr,
+                     h->w.dt, h->w.geo, flags, false, h->stream);
+    VK_CUDA(h, cudaGetLastError());
+    VK_CUDA(h, cudaMemcpyAsync(f, h->w.f2, bytes, cudaMemcpyDeviceToHost, h->stream));
+    VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    return VK_OK;
+}
+
 // Test hook: chemistry source term only (the generated chemdf) of the state y.
 extern "C" int vk_chem_source(vk_handle *h, const double *y, double *dydt) {
     int rc = need_batch(h);

@@ -22,8 +22,10 @@
 // reach condition numbers of 1e10..1e16 (c0 -> 0 exposes the conserved and
 // slow chemical modes), beyond what FP32 factors can precondition: refinement
 // diverges.  A column whose refinement failed at step size dt therefore sends
-// every later attempt with a step >= dt straight to the FP64 path (thr64),
-// and tries the mixed path again only after its step has dropped below it.
+// every later attempt with a step >= dt/4 straight to the FP64 path (thr64),
+// and tries the mixed path again only after its step has dropped below that:
+// the margin keeps a rejected attempt (dt halved) and the step-size rule's
+// 0.5x..2x changes from retrying a factorisation that has just failed.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -31,6 +33,8 @@
 #include "vk_tma.cuh"
 
 namespace vk {
+
+constexpr double kRouteMargin = 0.25;   // FP64 from dt >= kRouteMargin x the failed step
 
 
 // Iterative refinement of A x = b with the FP32 factors (one column at a time
@@ -91,20 +95,52 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
         issue(0);
         int sweep = 0, converged = 0, timed_out = 0;
         double m_prev = INFINITY;
+        // per-layer vectors of a visit, loaded into registers one visit ahead
+        // (the sweeps are a chain of dependent visits: nothing else hides the
+        // global-memory latency)
+        struct Visit { double rsc, a, bc, cscn, csc, x, ys, n0; float zf; };
+        auto fetch = [&](int v) {
+            Visit q{0, 0, 0, 0, 0, 0, 0, 0, 0.f};
+            const int j = layer_of(v);
+            const size_t l = (size_t)l0 + j;
+            const bool fwd = v < nz;
+            if (tid < n) {
+                const size_t e = l * n + tid;
+                q.rsc = rsc[e];
+                if (fwd) {
+                    q.a = res[e];
+                    if (j > 0) { q.bc = dC[e]; q.cscn = csc[e - n]; }
+                } else {
+                    q.bc = dB[e];
+                    q.cscn = csc[e + n];
+                }
+                if (!fwd || j == nz - 1) {
+                    q.csc = csc[e];
+                    q.x = x[e];
+                    q.ys = yscale ? fabs(yscale[e]) : 0.0;
+                    q.n0 = b.atm[l * VK_ATM_NF + VK_ATM_N0];
+                }
+            }
+            if (!fwd && mrow < n && mhalf == 0) q.zf = zf[l * n + mrow];
+            return q;
+        };
         for (; sweep < max_sweeps && !converged && !timed_out; ++sweep) {
             double dmax = 0.0;
+            Visit cur = fetch(0);
             for (int v = 0; v < per_sweep; ++v) {
                 const int j = layer_of(v);
                 const size_t l = (size_t)l0 + j;
                 const bool fwd = v < nz;
+                Visit nxt = cur;
+                if (v + 1 < per_sweep) nxt = fetch(v + 1);
                 // right-hand side of this visit
                 if (tid < n) {
                     double vi;
                     if (fwd) {
-                        vi = rsc[l * n + tid] * res[l * n + tid];
-                        if (j > 0) vi += rsc[l * n + tid] * dC[l * n + tid] * csc[(l - 1) * n + tid] * (double)vout[tid];
+                        vi = cur.rsc * cur.a;
+                        if (j > 0) vi += cur.rsc * cur.bc * cur.cscn * (double)vout[tid];
                     } else {
-                        vi = rsc[l * n + tid] * dB[l * n + tid] * csc[(l + 1) * n + tid] * (double)vout[tid];
+                        vi = cur.rsc * cur.bc * cur.cscn * (double)vout[tid];
                     }
                     vin[tid] = (float)vi;
                 }
@@ -138,7 +174,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                     if (fwd) {
                         zf[l * n + mrow] = sacc;
                     } else {
-                        sacc += zf[l * n + mrow];
+                        sacc += cur.zf;
                     }
                     vout[mrow] = sacc;
                 }
@@ -147,15 +183,15 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 if ((fwd && j == nz - 1) || !fwd) {
                     if (tid < n) {
                         const size_t e = l * n + tid;
-                        const double d = csc[e] * (double)vout[tid];
-                        const double xn = x[e] + d;
+                        const double d = cur.csc * (double)vout[tid];
+                        const double xn = cur.x + d;
                         x[e] = xn;
-                        const double sc = fabs(xn) + (yscale ? fabs(yscale[e]) : 0.0)
-                                          + 1e-10 * b.atm[l * VK_ATM_NF + VK_ATM_N0];
+                        const double sc = fabs(xn) + cur.ys + 1e-10 * cur.n0;
                         dmax = isfinite(d) ? fmax(dmax, fabs(d) / sc) : INFINITY;
                     }
                 }
                 __syncthreads();
+                cur = nxt;
             }
             if (timed_out) break;
             for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
@@ -198,7 +234,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 if (!converged) {
                     fallback[c] = 1;
                     act32[c] = 0;                   // later mixed launches of this attempt skip it
-                    thr64[c] = fmin(thr64[c], dt[c]);
+                    thr64[c] = fmin(thr64[c], kRouteMargin * dt[c]);
                 }
                 if (sweeps_out) atomicMax(sweeps_out, sweep + (converged ? 1 : 0));
                 if (err_out) err_out[c] = fmax(err_out[c], m_prev);

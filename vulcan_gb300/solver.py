@@ -224,6 +224,13 @@ class Ros2Handle:
         check(lib().vk_chem_source(self.h, ptr(np.ascontiguousarray(y)), ptr(out)), self.h)
         return out
 
+    def rhs(self, y=None, flags=capi.VK_F_MOLDIFF):
+        """f(y) = chemistry + transport (vk_rhs) [L][ni]; y None: the handle's state."""
+        out = np.empty((self.batch.L, self.ni))
+        yp = ptr(np.ascontiguousarray(y)) if y is not None else None
+        check(lib().vk_rhs(self.h, yp, int(flags), ptr(out)), self.h)
+        return out
+
     def lhs(self):
         b = self.batch
         jv = np.empty((b.L, self.gnet.nnz))

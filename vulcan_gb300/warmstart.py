@@ -320,13 +320,43 @@ class MLP:
         return m
 
 
+_EQ_NET = None
+
+
+def _eq_init(net):
+    global _EQ_NET
+    _EQ_NET = net
+
+
+def _eq_job(spec):
+    return eq_mix(spec, _EQ_NET)
+
+
+def eq_mix_many(specs, net, workers=None):
+    """eq_mix of many columns on the host cores (a spawned process pool: the
+    Gibbs minimisation is CPU work, ~0.06 s a column)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+    workers = workers or min(16, os.cpu_count() or 1, len(specs))
+    if workers <= 1 or len(specs) < 8:
+        return [eq_mix(sp, net) for sp in specs]
+    with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context('spawn'),
+                                initializer=_eq_init, initargs=(net,)) as ex:
+        return list(ex.map(_eq_job, specs, chunksize=max(1, len(specs) // (4 * workers))))
+
+
 def propose(model, specs, net, items, atom_list=('H', 'O', 'C', 'He', 'N')):
     """Warm-start states for column items (from batch.build_items): returns a
     list of (y, ymix), each proposal projected onto its column's element
     totals (those of the const_mix start, which the run then conserves)."""
     comp = net.compo_for(list(atom_list)).astype(float)
     with_eq = model.dims[0] > N_BASE_FEATURES
-    feats = [features_eq(sp, net) if with_eq else column_features(sp, net) for sp in specs]
+    if with_eq:
+        xeq = eq_mix_many(specs, net)
+        feats = [features_eq(sp, net, x) for sp, x in zip(specs, xeq)]
+    else:
+        feats = [column_features(sp, net) for sp in specs]
     logx = model.predict(np.concatenate(feats))
     off = np.concatenate([[0], np.cumsum([f.shape[0] for f in feats])])
     xs = [10.0 ** np.clip(logx[off[c]:off[c + 1]], LOG_FLOOR, 0.0) for c in range(len(specs))]
@@ -335,10 +365,14 @@ def propose(model, specs, net, items, atom_list=('H', 'O', 'C', 'He', 'N')):
     return [(n0[:, None] * x, x) for n0, x in zip(n0s, xs)]
 
 
-def chem_residual(h, y, n0, batch):
-    """Mean over layers of max_i |chemical source| / n_0 (s^-1) per column."""
-    src = h.chem_source(np.ascontiguousarray(y))
-    r = np.abs(src) / n0[:, None]
+def rhs_residual(h, y, n0, batch, flags=None):
+    """Residual of a state under the Ros2 system: mean over a column's layers
+    of max_i |f_i(y)| / (|y_i| + 1e-10 n_0), f = chemistry + transport
+    (vk_rhs) -- the rate (s^-1) at which the state still moves; zero at the
+    steady state.  One value per column."""
+    from . import capi
+    f = h.rhs(y, capi.VK_F_MOLDIFF if flags is None else flags)
+    r = np.abs(f) / (np.abs(y) + 1e-10 * n0[:, None])
     per_layer = r.max(axis=1)
     return np.array([per_layer[batch.off[c]:batch.off[c + 1]].mean() for c in range(batch.ncols)])
 
@@ -404,15 +438,15 @@ def warm_items(model, specs, net, items, atoms, precision=1):
     return out, np.ones(len(items), dtype=bool)
 
 
-def judge_proposals(h, batch, items_warm, items_const):
+def judge_proposals(h, batch, items_warm, items_const, flags=None):
     """The solver's judge of the learned start: a column keeps its proposal
-    only where it does not raise the chemical residual (chem_residual) above
-    that of the const_mix start; elsewhere the const_mix state goes back into
-    the handle.  Returns (items, used mask)."""
+    only where it does not raise the residual of the Ros2 system
+    (rhs_residual) above that of the const_mix start; elsewhere the
+    const_mix state goes back into the handle.  Returns (items, used mask)."""
     n0 = np.concatenate([it['col'].n_0 for it in items_const])
     yw = np.concatenate([it['y'] for it in items_warm])
     yc = np.concatenate([it['y'] for it in items_const])
-    used = chem_residual(h, yw, n0, batch) <= chem_residual(h, yc, n0, batch)
+    used = rhs_residual(h, yw, n0, batch, flags) <= rhs_residual(h, yc, n0, batch, flags)
     items = [iw if u else ic for iw, ic, u in zip(items_warm, items_const, used)]
     if not used.all():
         h.set_state(np.concatenate([it['y'] for it in items]),
