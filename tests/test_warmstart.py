@@ -44,6 +44,29 @@ def test_project_column_restores_element_totals():
     assert np.max(np.abs(x0[sel] / g["final_ymix"][sel] - 1)) < 3e-2
 
 
+def test_projection_target_is_the_normalised_start():
+    """The seeded const_mix starts have mixing ratios summing to more than 1
+    (metallicity up to 100x solar), so the reference's atom_ini (from the
+    un-normalised y) is out of reach for layers that sum to 1; a noisy
+    proposal projected onto the totals of the normalised start (start_totals,
+    what the run conserves after its first renormalisation) meets them and
+    the layer sums to rounding."""
+    from vulcan_gb300 import batch, warmstart
+    net = network('c2')
+    atoms = ['H', 'O', 'C', 'He', 'N']
+    comp = net.compo_for(atoms).astype(float)
+    specs = configs.config2_columns(ncols=40, seed=2)[24:40]
+    items = batch.build_items(specs, net)
+    rng = np.random.default_rng(1)
+    xs = [np.clip(it['ymix'] + 1e-6, 0, 1) * 10 ** rng.normal(0, 0.3, it['ymix'].shape) for it in items]
+    tgt = [warmstart.start_totals(it, comp) for it in items]
+    assert max(abs(t / np.asarray(it['atom_ini']) - 1).max() for t, it in zip(tgt, items)) > 1e-3
+    out = warmstart.project_columns(xs, [it['col'].n_0 for it in items], comp, tgt)
+    for x, it, t in zip(out, items, tgt):
+        np.testing.assert_allclose(x.sum(axis=1), 1.0, rtol=1e-12)
+        np.testing.assert_allclose((it['col'].n_0[:, None] * x).sum(axis=0) @ comp, t, rtol=1e-10)
+
+
 def test_column_features_shape():
     net = network('c2')
     spec = configs.config2_columns(ncols=1, seed=2)[0]

@@ -59,6 +59,9 @@ struct vk_handle {
     double *d_capT = nullptr, *d_capp = nullptr;
     int caps_on = 0;
     unsigned *d_queue = nullptr;        // work-queue position of the per-column kernels
+    unsigned *d_queue2 = nullptr;       // the same for the FP64 branch of a mixed attempt
+    cudaStream_t stream2 = nullptr;     // FP64 branch of a mixed attempt (routed columns)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int nsm = 0;                        // SMs of the device
     int cps = 0;                        // VK_CTAS_PER_SM override (0: kernel defaults)
     int cps_k[VK_TUNE_N] = {0, 0, 0, 0}; // vk_set_launch: CTAs per SM per kernel
@@ -163,6 +166,9 @@ extern "C" void vk_destroy(vk_handle *h) {
     if (h->rs.hist_t) cudaFree(h->rs.hist_t);
     for (void *p : h->allocs) cudaFree(p);
     for (auto &e : h->ev) if (e) cudaEventDestroy(e);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->stream2) cudaStreamDestroy(h->stream2);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -250,6 +256,13 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &h->d_col_off, max_cols + 1));
     TRY(dalloc(h, &h->d_order, max_cols));
     TRY(dalloc(h, &h->d_queue, 1));
+    TRY(dalloc(h, &h->d_queue2, 1));
+    TRY(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking) == cudaSuccess
+            ? VK_OK : fail(h, VK_ECUDA, "cudaStreamCreate (FP64 branch)"));
+    TRY(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) == cudaSuccess
+            ? VK_OK : fail(h, VK_ECUDA, "cudaEventCreate"));
+    TRY(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) == cudaSuccess
+            ? VK_OK : fail(h, VK_ECUDA, "cudaEventCreate"));
     {
         // per-column kernels: k resident CTAs per SM take columns from the queue;
         // k = VK_CTAS_PER_SM when set, else each kernel's measured best
@@ -276,6 +289,8 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &w.zf, L * ni));
     TRY(dalloc(h, &w.fallback, max_cols));
     TRY(dalloc(h, &w.act32, max_cols));
+    TRY(dalloc(h, &w.routed, max_cols));
+    TRY(dalloc(h, &w.failed, max_cols));
     TRY(dalloc(h, &w.thr64, max_cols));
     TRY(dalloc(h, &w.sweeps, 1));
     TRY(dalloc(h, &w.refine_err, max_cols));
@@ -462,6 +477,20 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         cudaMemsetAsync(w.sweeps, 0, sizeof(int), s);
         cudaMemsetAsync(w.refine_err, 0, b.ncols * sizeof(double), s);
         vk::launch_route(b, w, s);
+        // the routed columns' FP64 solves run beside the mixed ones, on the
+        // second stream with their own work queue (disjoint columns; f(y) and
+        // the LHS of the first launch are in place for both)
+        cudaStream_t s2 = h->stream2;
+        cudaEventRecord(h->ev_fork, s);
+        cudaStreamWaitEvent(s2, h->ev_fork, 0);
+        DevBatch br = b;
+        br.active = w.routed;
+        br.queue = h->d_queue2;
+        vk::launch_lu_fwd_f64(net, br, w, w.f, w.z, flags, s2);
+        vk::launch_back_f64(net, br, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s2);
+        vk::launch_rates(net, br, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s2);
+        vk::launch_solve_f64(net, br, w.G, w.dB, w.dC, w.f, w.z, w.k2, s2);
+        cudaEventRecord(h->ev_join, s2);
         DevBatch b32 = b;
         b32.active = w.act32;
         vk::launch_lu_reg32(net, b32, w, s);
@@ -469,14 +498,16 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         vk::launch_refine(net, b32, w, w.f, w.k1, w.y, w.yk2, h->max_refine, h->refine_tol, s);
         vk::launch_rates(net, b32, w.yk2, w.f2, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
         vk::launch_refine(net, b32, w, w.f2, w.k2, w.y, nullptr, h->max_refine, h->refine_tol, s);
-        // FP64 columns: f(y) and the LHS of the first launch are still in place
+        cudaStreamWaitEvent(s, h->ev_join, 0);
+        // columns whose refinement failed: FP64 after the others (their f(y)
+        // is still in place: neither branch wrote it)
         DevBatch bf = b;
-        bf.active = w.fallback;
+        bf.active = w.failed;
         vk::launch_lu_fwd_f64(net, bf, w, w.f, w.z, flags, s);
         vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
         vk::launch_rates(net, bf, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
         vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
-        h->launches += 12;
+        h->launches += 16;
     }
     if (timed) cudaEventRecord(h->ev[3], s);
     vk::launch_stage(net, b, w, flags, mtol, atol, s);
@@ -1033,7 +1064,7 @@ extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double t
     int launches = 0;
     for (;;) {
         VK_CUDA(h, cudaGraphLaunch(h->gexec, s));
-        launches += kGraphAttempts * (h->precision == VK_PREC_MIXED ? 13 : 7) + 1;
+        launches += kGraphAttempts * (h->precision == VK_PREC_MIXED ? 17 : 7) + 1;
         int nact = 0;
         VK_CUDA(h, cudaMemcpyAsync(&nact, h->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
         VK_CUDA(h, cudaStreamSynchronize(s));

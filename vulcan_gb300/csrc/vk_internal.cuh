@@ -166,6 +166,8 @@ struct Work {                  // per-handle device work buffers
     float *D32;                // [L][stride] dense scaled FP32 blocks (mixed mode)
     int *fallback;             // [ncols] attempt solved in FP64 (routed or refinement failed)
     int *act32;                // [ncols] attempt solved by the FP32 factors + refinement
+    int *routed;               // [ncols] attempt solved in FP64 from the start (routing)
+    int *failed;               // [ncols] refinement failed: redone in FP64 after the others
     double *thr64;             // [ncols] step size at which refinement last failed: an
                                //         attempt with dt >= thr64 goes straight to FP64
     int *sweeps;               // [1] most refinement sweeps any column needed

@@ -49,7 +49,7 @@ namespace {
 
 constexpr int kTmemCols = 128;          // D: NP <= 128 columns
 constexpr int kPW = 16;                 // panel width (pivots per MMA update)
-constexpr int kLdGroup = 3;             // TMEM loads of 16 columns issued per wait
+constexpr int kLdGroup = 1;             // TMEM loads of 16 columns per wait (1: no spills at 3 CTAs/SM)
 
 struct TcSmem {
     // byte offsets into the dynamic shared memory (base 128-byte aligned)
@@ -184,7 +184,7 @@ __device__ __forceinline__ void panel_eliminate(float (&P)[RA][kPW], unsigned &u
 }
 
 template <int RA>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 3)
 k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
         const double *__restrict__ dB, const double *__restrict__ dC,
         const double *__restrict__ rsc, const double *__restrict__ csc,
@@ -498,7 +498,7 @@ void launch_lu_tc(const DevNet &net, const DevBatch &b, const Work &w, const CUt
                   cudaStream_t s) {
     const int n = net.ni, NP = round_up(n, 16);
     const size_t sm = lu_tc_smem(n);
-    const int grid = column_grid(b, VK_TUNE_LU32, 2);
+    const int grid = column_grid(b, VK_TUNE_LU32, 3);
     if (NP <= 96)
         k_lu_tc<3><<<grid, 128, sm, s>>>(net, b, map, w.dB, w.dC, w.rs, w.cs, w.G32, w.status);
     else

@@ -51,7 +51,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
          float *__restrict__ zf, const double *__restrict__ yscale, double *__restrict__ yk2,
          const double *__restrict__ y, int max_sweeps, double tol, int *__restrict__ fallback,
          int *__restrict__ sweeps_out, int *__restrict__ status, double *__restrict__ err_out,
-         double *__restrict__ thr64, int *act32) {
+         double *__restrict__ thr64, int *act32, int *__restrict__ failed) {
     extern __shared__ __align__(16) unsigned char smr[];
     const int n = net.ni, NNP = block_stride32(n);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smr);           // [2]
@@ -234,6 +234,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 if (!converged) {
                     fallback[c] = 1;
                     act32[c] = 0;                   // later mixed launches of this attempt skip it
+                    failed[c] = 1;                  // redone in FP64 after the routed columns
                     thr64[c] = fmin(thr64[c], kRouteMargin * dt[c]);
                 }
                 if (sweeps_out) atomicMax(sweeps_out, sweep + (converged ? 1 : 0));
@@ -250,14 +251,22 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
 
 // fallback[c] = 1: this attempt of column c is solved in FP64 (its step is at or
 // above the size at which its refinement last failed); act32[c] = 1: mixed.
+// Routing of one attempt: routed[c] = 1: solved in FP64 from the start (its
+// step is at or above the size at which its refinement last failed, with the
+// margin); act32[c] = 1: mixed; fallback[c] = every FP64 solve of the attempt
+// (routed, and mixed columns whose refinement fails, which k_refine adds
+// together with failed[c]).
 __global__ void k_route(DevBatch b, const double *__restrict__ dt, const double *__restrict__ thr64,
-                        int *__restrict__ fallback, int *__restrict__ act32) {
+                        int *__restrict__ fallback, int *__restrict__ act32, int *__restrict__ routed,
+                        int *__restrict__ failed) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= b.ncols) return;
     const int a = b.active ? b.active[c] : 1;
     const int f64 = a && !(dt[c] < thr64[c]);
     fallback[c] = f64;
+    routed[c] = f64;
     act32[c] = a && !f64;
+    failed[c] = 0;
 }
 
 __global__ void k_reset_route(int ncols, double *__restrict__ thr64) {
@@ -266,7 +275,8 @@ __global__ void k_reset_route(int ncols, double *__restrict__ thr64) {
 }
 
 void launch_route(const DevBatch &b, const Work &w, cudaStream_t s) {
-    k_route<<<(b.ncols + 127) / 128, 128, 0, s>>>(b, w.dt, w.thr64, w.fallback, w.act32);
+    k_route<<<(b.ncols + 127) / 128, 128, 0, s>>>(b, w.dt, w.thr64, w.fallback, w.act32, w.routed,
+                                                   w.failed);
 }
 
 void launch_reset_route(const Work &w, int ncols, cudaStream_t s) {
@@ -287,7 +297,7 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
     k_refine<<<column_grid(b, VK_TUNE_REFINE, 3), 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
                                       rhs, x, w.r, w.zf, yscale, yk2, w.y, max_sweeps, tol,
                                       w.fallback, w.sweeps, w.status, w.refine_err, w.thr64,
-                                      w.act32);
+                                      w.act32, w.failed);
 }
 
 }  // namespace vk

@@ -85,93 +85,98 @@ def log_targets(ymix):
     return np.log10(np.clip(ymix, 10.0 ** LOG_FLOOR, None))
 
 
-def project_columns(xs, n0s, comp, atom_inis, iters=100, tol=1e-12):
+def project_columns(xs, n0s, comp, atom_inis, iters=200, tol=1e-12):
     """Closest mixing ratios (in relative entropy) to each proposal x [nz, ni]
     with sum_i x[j, i] = 1 in every layer and the column element totals
-    sum_j n0[j] sum_i comp[i, a] x[j, i] = atom_ini[a] (the reference's
-    atom_ini, op.py:2474-2481, sums number densities over layers).
+    sum_j n0[j] sum_i comp[i, a] x[j, i] = atom_ini[a] (number densities
+    summed over layers, like the reference's atom_ini, op.py:2474-2481).
+    The totals must be those of a state whose layers sum to 1 (see
+    start_totals): the reference's atom_ini of a const_mix start whose
+    mixing ratios sum to more than 1 is not reachable under that constraint.
 
-    x[j, i] = q[j, i] exp(comp[i] . lam + mu[j]); Newton on the convex dual in
-    (lam, mu) with mu eliminated by its diagonal block, Armijo backtracking;
-    all columns at once (layers padded to the longest column)."""
+    The solution is x[j, i] = q[j, i] exp(comp[i] . lam) / Z_j(lam), each
+    layer normalised exactly, where lam minimises the convex dual
+        phi(lam) = sum_j w_j log Z_j(lam) - lam . A,   w_j = n0_j / sum n0,
+    A = atom_ini / sum n0: Newton on lam (one small Hessian per column, the
+    weighted covariance of the element counts) with Armijo backtracking, all
+    columns at once (layers padded to the longest column).  Elements a column
+    does not hold (A_a = 0) remove the species that contain them."""
     comp = np.asarray(comp, dtype=float)
     nc, ni = len(xs), comp.shape[0]
+    K = comp.shape[1]
     nzs = np.array([x.shape[0] for x in xs])
     Z = int(nzs.max())
     lay = np.arange(Z)[None, :] < nzs[:, None]                      # [nc, Z]
     tot = np.array([n.sum() for n in n0s])
     w = np.zeros((nc, Z))
-    logq = np.full((nc, Z, ni), -1e4)
+    logq = np.full((nc, Z, ni), -np.inf)
     for c in range(nc):
         w[c, :nzs[c]] = n0s[c] / tot[c]
-        lq = np.log(np.clip(xs[c], 1e-300, None))
-        logq[c, :nzs[c]] = lq - lq.max(axis=1, keepdims=True)
-    A = np.stack(atom_inis) / tot[:, None]                         # [nc, nel]
+        logq[c, :nzs[c]] = np.log(np.clip(xs[c], 1e-300, None))
+    A = np.stack(atom_inis) / tot[:, None]                         # [nc, K]
     act = (A > 0) & (comp.sum(axis=0) > 0)[None, :]
+    # species holding an element the column has none of cannot appear
+    kill = ((comp[None, :, :] > 0) & ~act[:, None, :]).any(axis=2)   # [nc, ni]
+    logq = np.where(kill[:, None, :], -np.inf, logq)
+    logq[~lay] = 0.0                                                # padding layers: harmless
     T = np.where(act, A, 1.0)
-    F = comp
-    K = F.shape[1]
     eye = np.eye(K)
+
+    def state(lam, ix):
+        lx = logq[ix] + np.einsum('ia,ca->ci', comp, lam * act[ix])[:, None, :]
+        m = lx.max(axis=2, keepdims=True)
+        e = np.exp(lx - m)
+        zs = e.sum(axis=2)
+        x = e / zs[:, :, None]
+        logz = np.log(zs) + m[:, :, 0]
+        ww = w[ix]
+        phi = (ww * logz).sum(1) - (lam * A[ix] * act[ix]).sum(1)
+        ef = x @ comp                                                # [n, Z, K]
+        g = np.where(act[ix], np.einsum('cj,cja->ca', ww, ef) - A[ix], 0.0)
+        return x, phi, g, ef
+
+    def error(g, ix):
+        return np.max(np.abs(g) / T[ix], axis=1)
+
     lam = np.zeros((nc, K))
-    mu = -np.log(np.maximum(np.exp(logq).sum(axis=2), 1e-300)) * lay
-
-    def evalf(lm, mm):
-        lx = logq + np.einsum('ia,ca->ci', F, lm)[:, None, :] + mm[:, :, None]
-        xx = np.exp(np.clip(lx, -745.0, 700.0)) * lay[:, :, None]
-        s = xx.sum(axis=2)
-        xf = xx @ F                                               # [nc, Z, K]
-        g_l = np.where(act, np.einsum('cj,cja->ca', w, xf) - A, 0.0)
-        g_m = w * (s - 1.0)
-        phi = (w * s).sum(1) - (lm * A * act).sum(1) - (w * mm).sum(1)
-        return xx, s, xf, g_l, g_m, phi
-
-    def error(g_l, s):
-        return np.maximum(np.max(np.abs(g_l) / T, axis=1),
-                          np.max(np.where(lay, np.abs(s - 1.0), 0.0), axis=1))
-
-    xx, s, xf, g_l, g_m, phi = evalf(lam, mu)
+    allix = np.arange(nc)
+    x, phi, g, ef = state(lam, allix)
     done = np.zeros(nc, dtype=bool)
     for _ in range(iters):
-        err = error(g_l, s)
-        done |= err < tol
+        done |= error(g, allix) < tol
         if done.all():
             break
-        v = np.einsum('cj,cji->ci', w, xx)
-        Hll = np.einsum('ci,ia,ib->cab', v, F, F, optimize=True)
-        h = w[:, :, None] * xf                                    # [nc, Z, K]
-        d = w * s + (~lay) + 1e-300
-        Sc = Hll - np.einsum('cja,cjb->cab', h, h / d[:, :, None], optimize=True)
-        # inactive elements: identity rows
-        Sc = np.where(act[:, :, None] & act[:, None, :], Sc, 0.0) + (~act)[:, :, None] * eye
-        tr = np.einsum('caa->c', Sc)
-        Sc = Sc + (1e-12 * tr / K + 1e-300)[:, None, None] * eye
-        rhs = g_l - np.einsum('cja,cj->ca', h, g_m / d)
-        dl = np.linalg.solve(Sc, rhs[:, :, None])[:, :, 0] * act
-        dm = (g_m - np.einsum('cja,ca->cj', h, dl)) / d * lay
-        dl[done], dm[done] = 0.0, 0.0
-        dec = (g_l * dl).sum(1) + (g_m * dm).sum(1)
-        t = np.ones(nc)
-        acc = done.copy()
-        new = [v.copy() for v in (xx, s, xf, g_l, g_m, phi)]
-        lam_n, mu_n = lam.copy(), mu.copy()
+        ix = np.nonzero(~done)[0]
+        xi, efi, wi = x[ix], ef[ix], w[ix]
+        # Hessian: weighted covariance of the element counts per layer
+        H = (np.einsum('cj,cji,ia,ib->cab', wi, xi, comp, comp, optimize=True)
+             - np.einsum('cj,cja,cjb->cab', wi, efi, efi, optimize=True))
+        H = np.where(act[ix][:, :, None] & act[ix][:, None, :], H, 0.0) + (~act[ix])[:, :, None] * eye
+        H = H + (1e-14 * np.einsum('caa->c', H) / K + 1e-300)[:, None, None] * eye
+        step = np.linalg.solve(H, g[ix][:, :, None])[:, :, 0] * act[ix]
+        dec = (g[ix] * step).sum(1)
+        t = np.ones(ix.size)
+        acc = np.zeros(ix.size, dtype=bool)
         for _ in range(60):
-            cl, cm = lam - t[:, None] * dl, mu - t[:, None] * dm
-            cand = evalf(cl, cm)
-            # Armijo on the dual, or (once its decrease is below rounding of
-            # phi) a halving of the constraint error
-            ok = (~acc) & ((cand[5] <= phi - 1e-4 * t * dec)
-                           | (error(cand[3], cand[1]) < 0.5 * err))
-            for v, cv in zip(new, cand):
-                v[ok] = cv[ok]
-            lam_n[ok], mu_n[ok] = cl[ok], cm[ok]
-            acc |= ok
+            jx = np.nonzero(~acc)[0]
+            cand = lam[ix[jx]] - t[jx, None] * step[jx]
+            xc, pc, gc, ec = state(cand, ix[jx])
+            ok = (pc <= phi[ix[jx]] - 1e-4 * t[jx] * dec[jx]) | (error(gc, ix[jx]) < 0.5 * error(g[ix[jx]], ix[jx]))
+            sel = ix[jx[ok]]
+            lam[sel], x[sel], phi[sel], g[sel], ef[sel] = cand[ok], xc[ok], pc[ok], gc[ok], ec[ok]
+            acc[jx[ok]] = True
             if acc.all():
                 break
             t = np.where(acc, t, 0.5 * t)
-        done |= ~acc                                  # no decrease possible: at the floor
-        lam, mu = lam_n, mu_n
-        xx, s, xf, g_l, g_m, phi = new
-    return [xx[c, :nzs[c]] for c in range(nc)]
+        done[ix[~acc]] = True                       # no decrease possible: at the floor
+    return [x[c, :nzs[c]] for c in range(nc)]
+
+
+def start_totals(item, comp):
+    """Element totals of the normalised start n0 * ymix (what a run conserves
+    after its first renormalisation y = n0 ymix, op.py:894), the projection
+    target of a proposal for that column."""
+    return (item['col'].n_0[:, None] * item['ymix'] @ comp).sum(axis=0)
 
 
 def project_column(x, n0, comp, atom_ini, iters=100, tol=1e-12):
@@ -361,7 +366,7 @@ def propose(model, specs, net, items, atom_list=('H', 'O', 'C', 'He', 'N')):
     off = np.concatenate([[0], np.cumsum([f.shape[0] for f in feats])])
     xs = [10.0 ** np.clip(logx[off[c]:off[c + 1]], LOG_FLOOR, 0.0) for c in range(len(specs))]
     n0s = [it['col'].n_0 for it in items]
-    xs = project_columns(xs, n0s, comp, [np.asarray(it['atom_ini'], dtype=float) for it in items])
+    xs = project_columns(xs, n0s, comp, [start_totals(it, comp) for it in items])
     return [(n0[:, None] * x, x) for n0, x in zip(n0s, xs)]
 
 
@@ -428,8 +433,10 @@ def generate(net, seeds, ncols, atoms, count_max=4000, timeout_s=900, precision=
 
 
 def warm_items(model, specs, net, items, atoms, precision=1):
-    """Items started from the projected MLP proposal (element totals, and so
-    atom_ini, those of the const_mix start); returns (items, used_mask).
+    """Items started from the projected MLP proposal (element totals those
+    of the normalised const_mix start; atom_ini stays the reference's, so the
+    run's conservation check reads as from const_mix); returns (items,
+    used_mask).
     The solver judges the proposal: its step control and convergence test are
     the reference's, and a column that does not converge from it can be rerun
     from const_mix (fallback_items)."""
@@ -456,12 +463,12 @@ def judge_proposals(h, batch, items_warm, items_const, flags=None):
 
 def eq_items(specs, net, items, atoms):
     """Items started from thermochemical equilibrium (the reference's
-    ini_mix = 'EQ' seam), projected onto the const_mix start's element
-    totals."""
+    ini_mix = 'EQ' seam), projected onto the normalised const_mix start's
+    element totals."""
     comp = net.compo_for(list(atoms)).astype(float)
     xs = [eq_mix(sp, net, atoms) for sp in specs]
     n0s = [it['col'].n_0 for it in items]
-    xs = project_columns(xs, n0s, comp, [np.asarray(it['atom_ini'], dtype=float) for it in items])
+    xs = project_columns(xs, n0s, comp, [start_totals(it, comp) for it in items])
     return [dict(it, y=n0[:, None] * x, ymix=x) for it, n0, x in zip(items, n0s, xs)]
 
 
