@@ -433,27 +433,66 @@ def run_gpu(args):
 
 
 def converge_block(args):
-    """Columns to steady state per hour, learned + mixed vs plain FP64, on
-    the full 512-column workload within a wall budget per path."""
+    """Columns to steady state per hour, learned + mixed vs plain FP64: a
+    stream of args.stream_cols seeded columns through 512 slots
+    (continuous batching, batch.run_stream), each path for a wall budget."""
+    from vulcan_gb300 import batch, configs, warmstart
+    from vulcan_gb300.network import Network
+    from vulcan_gb300.solver import ctrl_from
     model = None
     if os.path.exists(args.weights):
-        from vulcan_gb300 import warmstart
         model = warmstart.MLP.load(args.weights)
+    net = Network.from_npz(NET)
+    specs = configs.config2_columns(ncols=args.stream_cols, seed=SEED)
+    items_const = batch.build_items(specs, net)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    ctrl.count_max = args.count_max
     paths = ([('learned_mixed', 1)] if model is not None else []) + [('plain_fp64', 0)]
-    res, fin, off = {}, {}, None
+    res, fin = {}, {}
     for name, prec in paths:
-        res[name], fin[name], nib = converge_path(args, name, prec, model, budget=args.converge_budget)
-        off = nib[2].off
-    for name in res:
-        if name != 'plain_fp64':
-            res[name]['vs_fp64_ymix_rel_gt_1e-20'] = err_vs_fp64(
-                fin[name][1], fin[name][2], fin['plain_fp64'][1], fin['plain_fp64'][2], off)
-            res[name]['columns_per_hour_over_fp64'] = round(
-                res[name]['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
-    res['setup'] = ('%d columns from const_mix (plain) or the learned proposal judged by its '
-                    'chemical residual (learned); wall budget %.0f s per path, count_max %d, '
-                    'the reference convergence test; columns per hour = converged columns / wall'
-                    % (args.ncols, args.converge_budget, args.count_max))
+        t0 = time.perf_counter()
+        extra = {}
+        items = items_const
+        if name == 'learned_mixed':
+            items, used = warmstart.judged_items(model, specs, net, items_const, ATOMS, prec)
+            extra = {'warm_started': int(used.sum()), 'proposal_s': round(time.perf_counter() - t0, 2)}
+        left = args.converge_budget - (time.perf_counter() - t0)
+        out, wall = batch.run_stream(net, items, ATOMS, nslots=min(NCOLS, len(items)), ctrl=ctrl,
+                                     precision=prec, slot_cap=200, chunk=args.chunk_stream,
+                                     budget_s=left, keep_state=True)
+        wall = time.perf_counter() - t0
+        conv = [i for i, r in out.items() if r['end_case'] == 1]
+        steps = sorted(out[i]['count'] for i in conv)
+        res[name] = {'wall_s': round(wall, 2), 'streamed_columns': len(items),
+                     'ended': len(out), 'converged': len(conv),
+                     'columns_per_hour': round(len(conv) / wall * 3600, 1),
+                     'steps_to_converge_median': float(np.median(steps)) if steps else None,
+                     'steps_to_converge_mean': float(np.mean(steps)) if steps else None,
+                     'end_cases': {str(k): sum(1 for r in out.values() if r['end_case'] == k)
+                                   for k in sorted({r['end_case'] for r in out.values()})},
+                     **extra}
+        fin[name] = out
+    if 'learned_mixed' in res:
+        both = [i for i in fin['learned_mixed'] if i in fin['plain_fp64']
+                and fin['learned_mixed'][i]['end_case'] == 1 and fin['plain_fp64'][i]['end_case'] == 1]
+        errs = []
+        for i in both:
+            a, r = fin['learned_mixed'][i]['ymix'], fin['plain_fp64'][i]['ymix']
+            m = r > 1e-20
+            errs.append(float(np.max(np.abs(a[m] - r[m]) / r[m])))
+        res['learned_mixed']['vs_fp64_ymix_rel_gt_1e-20'] = {
+            'both_converged_with_fp64': len(both),
+            'median_over_columns_of_max': float(np.median(errs)) if errs else None,
+            'max_over_columns_of_max': max(errs) if errs else None,
+            'columns_within_1e-3': int(sum(e <= 1e-3 for e in errs))}
+        res['learned_mixed']['columns_per_hour_over_fp64'] = round(
+            res['learned_mixed']['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
+    res['setup'] = ('a stream of %d seeded columns through %d slots (continuous batching: a slot '
+                    'whose column ends takes the next one), %.0f s of wall time per path '
+                    'including the learned proposals and their judge (the residual of the Ros2 '
+                    'system, vk_rhs); count_max %d; the reference convergence test; columns per '
+                    'hour = converged columns / wall' % (args.stream_cols, NCOLS,
+                                                         args.converge_budget, args.count_max))
     return res
 
 
@@ -728,7 +767,11 @@ def main():
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
-    ap.add_argument('--converge-budget', type=float, default=150.0,
+    ap.add_argument('--stream-cols', type=int, default=1536,
+                    help='default run: columns streamed through the 512 slots per path')
+    ap.add_argument('--chunk-stream', type=int, default=20,
+                    help='steps between refills of the streamed slots')
+    ap.add_argument('--converge-budget', type=float, default=180.0,
                     help='default run: wall seconds per path for the columns-to-steady-state '
                          'measurement (0: skip)')
     ap.add_argument('--count-max', type=int, default=3000)

@@ -140,6 +140,29 @@ VK_API int  vk_set_precision(vk_handle *h, int precision, int max_refine, double
 VK_API int  vk_set_columns(vk_handle *h, int ncols, const int *nz, const double *k,
                     const double *atm, const double *Dzz, const double *spf,
                     const double *y, const double *ymix);
+/* The same set-up in the slotted layout used for continuous batching (no
+ * counterpart in the reference, which integrates one column per run): column
+ * c occupies layers c*slot_cap .. c*slot_cap + nz[c] - 1 of the device arrays
+ * ([ncols*slot_cap] layers; the rest of each slot holds no column), so a
+ * finished column can be replaced by vk_refill without moving the others.
+ * Inputs are packed as for vk_set_columns; requires nz[c] <= slot_cap and
+ * ncols*slot_cap <= max_layers.  Outputs indexed by layer (vk_get_state,
+ * vk_ros2_attempt, ...) use the slotted layout. */
+VK_API int  vk_set_columns_slotted(vk_handle *h, int ncols, int slot_cap, const int *nz,
+                                   const double *k, const double *atm, const double *Dzz,
+                                   const double *spf, const double *y, const double *ymix);
+/* Continuous batching: put n new columns into the given slots (slotted
+ * layout only), packed inputs as vk_set_columns, plus their element totals
+ * atom_ini [n][natom] (vk_set_atom_ini), 1-bar reference levels pref_indx
+ * [n] and steady-state ignore masks conv_ignore [n][ni] (NULL: keep the
+ * slot's).  Each refilled column starts a run: t = 0, count = 0, dt = 1e-10,
+ * end_case 0, its history and routing reset; the other columns are
+ * untouched.  The loop it feeds is Integration.__call__ (op.py:808-936), run
+ * per column. */
+VK_API int  vk_refill(vk_handle *h, int n, const int *slots, const int *nz, const double *k,
+                      const double *atm, const double *Dzz, const double *spf,
+                      const double *y, const double *ymix, const double *atom_ini,
+                      const int *pref_indx, const int *conv_ignore);
 /* Update only the fields that change during a run (y, ymix, atm, k). */
 VK_API int  vk_update_state(vk_handle *h, const double *y, const double *ymix);
 VK_API int  vk_update_atm(vk_handle *h, const double *atm);

@@ -43,19 +43,84 @@ def build_items(specs, net):
     return items
 
 
-def make_batch_handle(net, items, atom_list, precision=capi.VK_PREC_FP64):
-    gnet = GPUNetwork(net, atom_list)
-    b = ColumnBatch(items, net.ni)
-    h = Ros2Handle(gnet, b.ncols, b.L, precision)
-    h.set_columns(b)
-    h.set_atom_ini(np.stack([it['atom_ini'] for it in items]))
+def ignore_masks(net, items):
+    """[n][ni] steady-state ignore masks (conver_ignore) of column items."""
     mask = np.zeros((len(items), net.ni), dtype=np.int32)
     for c, it in enumerate(items):
         for sp in it['ignore']:
             mask[c, net.species.index(sp)] = 1
-    h.set_conv_ignore(mask)
+    return mask
+
+
+def make_batch_handle(net, items, atom_list, precision=capi.VK_PREC_FP64, slot_cap=0):
+    """Handle with the items' columns loaded (slot_cap > 0: the slotted layout
+    of continuous batching, each column in a slot of slot_cap layers)."""
+    gnet = GPUNetwork(net, atom_list)
+    b = ColumnBatch(items, net.ni, slot_cap)
+    h = Ros2Handle(gnet, b.ncols, b.L, precision)
+    h.set_columns(b)
+    h.set_atom_ini(np.stack([it['atom_ini'] for it in items]))
+    h.set_conv_ignore(ignore_masks(net, items))
     h.set_clock(dt=configs.SOLVER_DEFAULTS['dttry'], t=0.0, count=0)
     return h, b
+
+
+def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64, slot_cap=None,
+               chunk=20, budget_s=None, keep_state=False):
+    """Continuous batching: the column items (build_items order) stream
+    through nslots slots of one handle; every `chunk` steps the slots whose
+    column has ended (converged, count_max, runtime, error) take the next
+    items (vk_refill), so the GPU keeps a full batch while columns finish at
+    different times.  Each column runs the reference's loop (op.py:808-936)
+    from its own start, exactly as in a batch of its own.  Stops when every
+    item has ended or after budget_s seconds of wall time.
+
+    Returns (results, wall_s): results[i] = dict(end_case, count, t, wall_s
+    at which it ended[, y, ymix]) for every item that ended."""
+    import time
+    from . import capi as _capi
+    slot_cap = slot_cap or int(max(it['col'].nz for it in items))
+    first = list(items[:nslots])
+    h, b = make_batch_handle(net, first, atom_list, precision, slot_cap=slot_cap)
+    slot_item = list(range(len(first)))
+    nxt = len(first)
+    results = {}
+    t0 = time.perf_counter()
+    try:
+        while True:
+            left = None if budget_s is None else budget_s - (time.perf_counter() - t0)
+            if left is not None and left <= 0:
+                break
+            try:
+                h.run(ctrl, max_steps=chunk, timeout_s=max(left, 1.0) if left is not None else 0.0)
+            except _capi.VkError as e:
+                if e.code != _capi.VK_ETIMEOUT:
+                    raise
+            st = h.state()
+            now = time.perf_counter() - t0
+            ended = [c for c in range(b.ncols) if slot_item[c] is not None and st['end_case'][c] != 0]
+            for c in ended:
+                r = dict(end_case=int(st['end_case'][c]), count=int(st['count'][c]),
+                         t=float(st['t'][c]), wall_s=now)
+                if keep_state:
+                    r['y'] = st['y'][b.off[c]:b.end[c]].copy()
+                    r['ymix'] = st['ymix'][b.off[c]:b.end[c]].copy()
+                results[slot_item[c]] = r
+                slot_item[c] = None
+            new = list(range(nxt, min(nxt + len(ended), len(items))))
+            if new:
+                slots = ended[:len(new)]
+                nitems = [items[i] for i in new]
+                h.refill(slots, nitems, np.stack([it['atom_ini'] for it in nitems]),
+                         ignore_masks(net, nitems))
+                for c, i in zip(slots, new):
+                    slot_item[c] = i
+                nxt += len(new)
+            if all(si is None for si in slot_item):
+                break
+    finally:
+        h.close()
+    return results, time.perf_counter() - t0
 
 
 def run_batch(net, specs, atom_list, max_steps=0, timeout_s=0.0, cfg=None,

@@ -39,7 +39,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
            'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps',
-           'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore', 'vk_get_lu32', 'vk_rhs')
+           'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore', 'vk_get_lu32', 'vk_rhs',
+           'vk_set_columns_slotted', 'vk_refill')
 
 
 class VkNetworkDesc(C.Structure):
@@ -103,6 +104,8 @@ def lib(path=None):
         'vk_set_conv_ignore': (i, [vp, pi]),
         'vk_get_lu32': (i, [vp, P(C.c_float)]),
         'vk_rhs': (i, [vp, pd, i, pd]),
+        'vk_set_columns_slotted': (i, [vp, i, i, pi, pd, pd, pd, pd, pd, pd]),
+        'vk_refill': (i, [vp, i, pi, pi, pd, pd, pd, pd, pd, pd, pd, pi, pi]),
         'vk_run': (i, [vp, P(VkCtrl), i, d]),
         'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
         'vk_set_clock': (i, [vp, pd, pd, pi]),

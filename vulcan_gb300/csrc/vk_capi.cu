@@ -30,7 +30,8 @@ struct vk_handle {
     int geo_flags = -1;         // flags the transport geometry was built for (-1: stale)
     CUtensorMap tmap_d32{};     // k_lu_tc's view of w.D32 (mixed mode, ni <= 128)
     int ncols = 0, L = 0;
-    std::vector<int> col_off;
+    std::vector<int> col_off, col_end;  // first / one past last layer of each column
+    int slot_cap = 0;                   // > 0: slotted layout (vk_set_columns_slotted)
     // network tables
     PairDesc *d_pairs = nullptr;
     int *d_src_ptr = nullptr;
@@ -45,7 +46,8 @@ struct vk_handle {
     int *d_jrow = nullptr, *d_jcol = nullptr, *d_jrowptr = nullptr, *d_jmap = nullptr;
     double *d_compo = nullptr;
     // batch
-    int *d_col_off = nullptr, *d_lay_col = nullptr;
+    int *d_col_off = nullptr, *d_col_end = nullptr, *d_lay_col = nullptr;
+    int *d_cols = nullptr;              // [max_cols] column list of reset_columns
     int *d_order = nullptr;             // columns by decreasing nz
     PhotoDev ph{};                  // radiative transfer (vk_photo_setup)
     int *d_phmask = nullptr;            // [max_cols] columns of a masked photo update
@@ -93,7 +95,7 @@ struct vk_handle {
     }
     DevBatch batch() const {
         DevBatch b;
-        b.ncols = ncols; b.L = L; b.col_off = d_col_off; b.lay_col = d_lay_col;
+        b.ncols = ncols; b.L = L; b.col_off = d_col_off; b.col_end = d_col_end; b.lay_col = d_lay_col;
         b.k = d_k; b.atm = d_atm; b.Dzz = d_Dzz; b.spf = d_spf;
         b.active = nullptr;
         b.order = d_order;
@@ -254,6 +256,8 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_jmap, net->jmap));
     const size_t L = (size_t)max_layers, ni = (size_t)h->ni;
     TRY(dalloc(h, &h->d_col_off, max_cols + 1));
+    TRY(dalloc(h, &h->d_col_end, max_cols));
+    TRY(dalloc(h, &h->d_cols, max_cols));
     TRY(dalloc(h, &h->d_order, max_cols));
     TRY(dalloc(h, &h->d_queue, 1));
     TRY(dalloc(h, &h->d_queue2, 1));
@@ -342,73 +346,164 @@ extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, dou
     return VK_OK;
 }
 
-extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const double *k,
-                              const double *atm, const double *Dzz, const double *spf,
-                              const double *y, const double *ymix) {
+// Per-column start of a run (clock, counters, conservation reference,
+// routing threshold, dt = 1e-10) of the columns cs, by one kernel.
+static int reset_columns(vk_handle *h, const std::vector<int> &cs) {
+    if (cs.empty()) return VK_OK;
+    cudaStream_t s = h->stream;
+    VK_CUDA(h, cudaMemcpyAsync(h->d_cols, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    vk::launch_reset_columns(h->rs, (int)cs.size(), h->d_cols, h->w.dt, h->w.status, h->w.thr64, s);
+    VK_CUDA(h, cudaGetLastError());
+    VK_CUDA(h, cudaStreamSynchronize(s));      // cs may be a temporary
+    return VK_OK;
+}
+
+// Longest columns first: the work queue then balances the SMs.
+static int upload_order(vk_handle *h) {
+    std::vector<int> order(h->ncols);
+    for (int c = 0; c < h->ncols; ++c) order[c] = c;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b2) {
+        return h->col_end[a] - h->col_off[a] > h->col_end[b2] - h->col_off[b2];
+    });
+    VK_CUDA(h, cudaMemcpy(h->d_order, order.data(), h->ncols * sizeof(int), cudaMemcpyHostToDevice));
+    return VK_OK;
+}
+
+// Packed (slot_cap 0: column c at the layers after column c-1) or slotted
+// (column c at layers c * slot_cap .. + nz[c], the rest of the slot gap
+// layers) set-up of every column from packed host arrays.
+static int set_columns_impl(vk_handle *h, int ncols, int slot_cap, const int *nz, const double *k,
+                            const double *atm, const double *Dzz, const double *spf,
+                            const double *y, const double *ymix) {
     if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
     if (ncols <= 0 || ncols > h->max_cols)
         return fail(h, VK_EINVAL, "ncols must be in 1.." + std::to_string(h->max_cols));
     if (!nz || !k || !atm || !Dzz || !spf || !y || !ymix)
         return fail(h, VK_EINVAL, "NULL input array");
-    std::vector<int> off(ncols + 1, 0);
+    if (slot_cap < 0 || slot_cap > 1024) return fail(h, VK_EINVAL, "slot_cap must be in 0..1024");
+    std::vector<int> off(ncols + 1, 0), end(ncols, 0), pk(ncols + 1, 0);
     for (int c = 0; c < ncols; ++c) {
         if (nz[c] < 2 || nz[c] > 1024) return fail(h, VK_EINVAL, "every column needs 2 <= nz <= 1024");
-        off[c + 1] = off[c] + nz[c];
+        if (slot_cap && nz[c] > slot_cap)
+            return fail(h, VK_EINVAL, "column " + std::to_string(c) + " has more layers than slot_cap");
+        pk[c + 1] = pk[c] + nz[c];
+        off[c + 1] = slot_cap ? (c + 1) * slot_cap : pk[c + 1];
+        end[c] = off[c] + nz[c];
         if (off[c + 1] > h->max_layers)
             return fail(h, VK_EINVAL, "total layers exceed max_layers=" + std::to_string(h->max_layers));
     }
     const int L = off[ncols];
-    std::vector<int> lay_col(L);
+    std::vector<int> lay_col(L, -1);
     for (int c = 0; c < ncols; ++c)
-        for (int l = off[c]; l < off[c + 1]; ++l) lay_col[l] = c;
+        for (int l = off[c]; l < end[c]; ++l) lay_col[l] = c;
     const size_t ni = h->ni;
     cudaStream_t s = h->stream;
     VK_CUDA(h, cudaMemcpyAsync(h->d_col_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    {
-        // longest columns first: the work queue then balances the SMs
-        std::vector<int> order(ncols);
-        for (int c = 0; c < ncols; ++c) order[c] = c;
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b2) { return nz[a] > nz[b2]; });
-        VK_CUDA(h, cudaMemcpyAsync(h->d_order, order.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, s));
-        VK_CUDA(h, cudaStreamSynchronize(s));
-    }
+    VK_CUDA(h, cudaMemcpyAsync(h->d_col_end, end.data(), end.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaMemcpyAsync(h->d_lay_col, lay_col.data(), L * sizeof(int), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemcpyAsync(h->d_k, k, (size_t)L * h->nr * sizeof(double), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemcpyAsync(h->d_atm, atm, (size_t)L * VK_ATM_NF * sizeof(double), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemcpyAsync(h->d_Dzz, Dzz, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemcpyAsync(h->d_spf, spf, (size_t)ncols * VK_SP_NF * ni * sizeof(double), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemcpyAsync(h->w.y, y, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemcpyAsync(h->w.ymix, ymix, (size_t)L * ni * sizeof(double), cudaMemcpyHostToDevice, s));
-    VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, ncols * sizeof(int), s));
-    vk::launch_reset_route(h->w, ncols, s);          // every column starts on the mixed path
-    {
-        vk::RunState &r = h->rs;
-        VK_CUDA(h, cudaMemsetAsync(r.t, 0, ncols * sizeof(double), s));
-        VK_CUDA(h, cudaMemsetAsync(r.aflux_change, 0, ncols * sizeof(double), s));
-        {
-            // the reference starts longdy = longdydt = 1 (store.Variables)
-            std::vector<double> one(ncols, 1.0);
-            VK_CUDA(h, cudaMemcpy(r.longdy, one.data(), ncols * sizeof(double), cudaMemcpyHostToDevice));
-            VK_CUDA(h, cudaMemcpy(r.longdydt, one.data(), ncols * sizeof(double), cudaMemcpyHostToDevice));
-        }
-        VK_CUDA(h, cudaMemsetAsync(r.count, 0, ncols * sizeof(int), s));
-        VK_CUDA(h, cudaMemsetAsync(r.end_case, 0, ncols * sizeof(int), s));
-        VK_CUDA(h, cudaMemsetAsync(r.counters, 0, ncols * VK_NCOUNTERS * sizeof(int), s));
-        VK_CUDA(h, cudaMemsetAsync(r.pref, 0, ncols * sizeof(int), s));
-        VK_CUDA(h, cudaMemsetAsync(r.loss, 0, ncols * VK_MAX_NATOM * sizeof(double), s));
-        std::vector<double> dt0(ncols, 1e-10);
-        VK_CUDA(h, cudaMemcpyAsync(h->w.dt, dt0.data(), ncols * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (slot_cap) {
+        // gap layers hold zeros (finite) in every per-layer input
+        VK_CUDA(h, cudaMemsetAsync(h->d_k, 0, (size_t)L * h->nr * sizeof(double), s));
+        VK_CUDA(h, cudaMemsetAsync(h->d_atm, 0, (size_t)L * VK_ATM_NF * sizeof(double), s));
+        VK_CUDA(h, cudaMemsetAsync(h->d_Dzz, 0, (size_t)L * ni * sizeof(double), s));
+        VK_CUDA(h, cudaMemsetAsync(h->w.y, 0, (size_t)L * ni * sizeof(double), s));
+        VK_CUDA(h, cudaMemsetAsync(h->w.ymix, 0, (size_t)L * ni * sizeof(double), s));
     }
+    // per column (one copy per array when packed: the ranges are contiguous)
+    const int nblk = slot_cap ? ncols : 1;
+    for (int c = 0; c < nblk; ++c) {
+        const int src = slot_cap ? pk[c] : 0, dst = off[c], n = slot_cap ? nz[c] : L;
+        VK_CUDA(h, cudaMemcpyAsync(h->d_k + (size_t)dst * h->nr, k + (size_t)src * h->nr,
+                                   (size_t)n * h->nr * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->d_atm + (size_t)dst * VK_ATM_NF, atm + (size_t)src * VK_ATM_NF,
+                                   (size_t)n * VK_ATM_NF * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->d_Dzz + (size_t)dst * ni, Dzz + (size_t)src * ni,
+                                   (size_t)n * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->w.y + (size_t)dst * ni, y + (size_t)src * ni,
+                                   (size_t)n * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->w.ymix + (size_t)dst * ni, ymix + (size_t)src * ni,
+                                   (size_t)n * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    VK_CUDA(h, cudaMemcpyAsync(h->d_spf, spf, (size_t)ncols * VK_SP_NF * ni * sizeof(double), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaStreamSynchronize(s));
-    if (h->gexec && (h->ncols != ncols || h->L != off[ncols])) {
+    if (h->gexec && (h->ncols != ncols || h->L != L)) {
         cudaGraphExecDestroy(h->gexec);
         h->gexec = nullptr;
     }
     h->ncols = ncols;
     h->L = L;
     h->col_off = off;
+    h->col_end = end;
+    h->slot_cap = slot_cap;
     h->geo_flags = -1;
-    return VK_OK;
+    int rc = upload_order(h);
+    if (rc) return rc;
+    VK_CUDA(h, cudaMemset(h->rs.pref, 0, ncols * sizeof(int)));
+    std::vector<int> all(ncols);
+    for (int c = 0; c < ncols; ++c) all[c] = c;
+    return reset_columns(h, all);
+}
+
+extern "C" int vk_set_columns(vk_handle *h, int ncols, const int *nz, const double *k,
+                              const double *atm, const double *Dzz, const double *spf,
+                              const double *y, const double *ymix) {
+    return set_columns_impl(h, ncols, 0, nz, k, atm, Dzz, spf, y, ymix);
+}
+
+extern "C" int vk_set_columns_slotted(vk_handle *h, int ncols, int slot_cap, const int *nz,
+                                      const double *k, const double *atm, const double *Dzz,
+                                      const double *spf, const double *y, const double *ymix) {
+    if (slot_cap < 2) return fail(h, VK_EINVAL, "slot_cap must be at least 2");
+    return set_columns_impl(h, ncols, slot_cap, nz, k, atm, Dzz, spf, y, ymix);
+}
+
+extern "C" int vk_refill(vk_handle *h, int n, const int *slots, const int *nz, const double *k,
+                         const double *atm, const double *Dzz, const double *spf, const double *y,
+                         const double *ymix, const double *atom_ini, const int *pref_indx,
+                         const int *conv_ignore) {
+    if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
+    if (!h->slot_cap) return fail(h, VK_EINVAL, "refill needs the slotted layout (vk_set_columns_slotted)");
+    if (n <= 0) return VK_OK;
+    if (!slots || !nz || !k || !atm || !Dzz || !spf || !y || !ymix || !atom_ini || !pref_indx)
+        return fail(h, VK_EINVAL, "NULL input array");
+    const size_t ni = h->ni;
+    std::vector<int> seen(h->ncols, 0);
+    for (int i = 0; i < n; ++i) {
+        const int c = slots[i];
+        if (c < 0 || c >= h->ncols || seen[c]++) return fail(h, VK_EINVAL, "bad or repeated slot");
+        if (nz[i] < 2 || nz[i] > h->slot_cap) return fail(h, VK_EINVAL, "refill column exceeds slot_cap");
+        if (pref_indx[i] < 0 || pref_indx[i] >= nz[i]) return fail(h, VK_EINVAL, "pref_indx outside the column");
+    }
+    cudaStream_t s = h->stream;
+    VK_CUDA(h, cudaStreamSynchronize(s));
+    size_t src = 0;
+    std::vector<int> lay(h->slot_cap);
+    for (int i = 0; i < n; ++i) {
+        const int c = slots[i], dst = h->col_off[c];
+        const size_t m = nz[i];
+        VK_CUDA(h, cudaMemcpyAsync(h->d_k + (size_t)dst * h->nr, k + src * h->nr, m * h->nr * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->d_atm + (size_t)dst * VK_ATM_NF, atm + src * VK_ATM_NF, m * VK_ATM_NF * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->d_Dzz + (size_t)dst * ni, Dzz + src * ni, m * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->w.y + (size_t)dst * ni, y + src * ni, m * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->w.ymix + (size_t)dst * ni, ymix + src * ni, m * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->d_spf + (size_t)c * VK_SP_NF * ni, spf + (size_t)i * VK_SP_NF * ni, VK_SP_NF * ni * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->rs.atom_ini + (size_t)c * VK_MAX_NATOM, atom_ini + (size_t)i * h->natom, h->natom * sizeof(double), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaMemcpyAsync(h->rs.pref + c, pref_indx + i, sizeof(int), cudaMemcpyHostToDevice, s));
+        if (conv_ignore)
+            VK_CUDA(h, cudaMemcpyAsync(h->rs.ignore + (size_t)c * ni, conv_ignore + (size_t)i * ni, ni * sizeof(int), cudaMemcpyHostToDevice, s));
+        for (int l = 0; l < h->slot_cap; ++l) lay[l] = l < (int)m ? c : -1;
+        VK_CUDA(h, cudaMemcpyAsync(h->d_lay_col + dst, lay.data(), h->slot_cap * sizeof(int), cudaMemcpyHostToDevice, s));
+        VK_CUDA(h, cudaStreamSynchronize(s));   // lay is reused
+        h->col_end[c] = dst + (int)m;
+        src += m;
+    }
+    VK_CUDA(h, cudaMemcpyAsync(h->d_col_end, h->col_end.data(), h->ncols * sizeof(int), cudaMemcpyHostToDevice, s));
+    VK_CUDA(h, cudaStreamSynchronize(s));
+    h->geo_flags = -1;                            // transport geometry of the new columns
+    int rc = upload_order(h);
+    if (rc) return rc;
+    std::vector<int> cs(slots, slots + n);
+    return reset_columns(h, cs);
 }
 
 static int need_batch(vk_handle *h) {
@@ -649,7 +744,7 @@ extern "C" int vk_set_column_info(vk_handle *h, const int *pref_indx, const int 
     if (rc) return rc;
     if (pref_indx) {
         for (int c = 0; c < h->ncols; ++c)
-            if (pref_indx[c] < 0 || pref_indx[c] >= h->col_off[c + 1] - h->col_off[c])
+            if (pref_indx[c] < 0 || pref_indx[c] >= h->col_end[c] - h->col_off[c])
                 return fail(h, VK_EINVAL, "pref_indx outside the column");
         VK_CUDA(h, cudaMemcpy(h->rs.pref, pref_indx, h->ncols * sizeof(int), cudaMemcpyHostToDevice));
     }

@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_start(DevNet net, DevBatch b, RunState 
     __shared__ double red[8];
     const int c = blockIdx.x;
     if (rs.end_case[c] != 0) { if (threadIdx.x == 0) rs.active[c] = 0; return; }
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     if (threadIdx.x == 0) rs.steps_call[c] = 0;
     __syncthreads();
     start_step(net, b, rs, cc, c, l0, nz, red);
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
     const int c = blockIdx.x;
     if (!rs.active[c]) return;
     const int n = net.ni;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const size_t base = (size_t)l0 * n;
     const int NE = nz * n;
     // clip: zero values in [nega_cut, pos_cut); zero negatives where ymix < mtol
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(256) k_control(DevNet net, DevBatch b, RunStat
     if (count % cc.update_frq == 0) {
         update_mu_dz(net, b, rs, cc, c, l0, nz, mu);
         // the transport geometry depends on g, dzi, Hpi: rebuild this column's
-        const GeoCol gc = make_geocol(rs.atm, b.Dzz, b.spf, b.col_off, c, n);
+        const GeoCol gc = make_geocol(rs.atm, b.Dzz, b.spf, b.col_off, b.col_end, c, n);
         for (int e = threadIdx.x; e < NE; e += blockDim.x) {
             const int j = e / n, i = e - j * n;
             double out[GEO_NF];
@@ -375,6 +375,34 @@ void launch_control(const DevNet &net, const DevBatch &b, const RunState &rs, co
                     const double *sol, const double *ymix_sol, const double *delta,
                     const int *status, const int *fallback, double *geo, cudaStream_t s) {
     k_control<<<b.ncols, 256, 0, s>>>(net, b, rs, cc, sol, ymix_sol, delta, status, fallback, geo);
+}
+
+// A column's start of a run (vk_set_columns, vk_refill): clock, steady-state
+// statistics (the reference starts longdy = longdydt = 1, store.Variables),
+// counters, conservation losses, status, routing threshold, dt = 1e-10
+// (vulcan_cfg.dttry).
+__global__ void k_reset_columns(RunState rs, int n, const int *__restrict__ cols,
+                                double *__restrict__ dt, int *__restrict__ status,
+                                double *__restrict__ thr64) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cols[i];
+    rs.t[c] = 0.0;
+    rs.aflux_change[c] = 0.0;
+    rs.longdy[c] = 1.0;
+    rs.longdydt[c] = 1.0;
+    rs.count[c] = 0;
+    rs.end_case[c] = 0;
+    for (int k = 0; k < VK_NCOUNTERS; ++k) rs.counters[(size_t)c * VK_NCOUNTERS + k] = 0;
+    for (int a = 0; a < VK_MAX_NATOM; ++a) rs.loss[(size_t)c * VK_MAX_NATOM + a] = 0.0;
+    dt[c] = 1e-10;
+    status[c] = 0;
+    if (thr64) thr64[c] = INFINITY;
+}
+
+void launch_reset_columns(const RunState &rs, int n, const int *cols, double *dt, int *status,
+                          double *thr64, cudaStream_t s) {
+    k_reset_columns<<<(n + 127) / 128, 128, 0, s>>>(rs, n, cols, dt, status, thr64);
 }
 
 void launch_count_active(const int *active, int ncols, int *nactive, cudaStream_t s) {

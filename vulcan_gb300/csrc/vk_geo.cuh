@@ -40,14 +40,15 @@ struct GeoCol {
 };
 
 __device__ __forceinline__ GeoCol make_geocol(const double *atm, const double *Dzz,
-                                              const double *spf, const int *col_off, int c, int ni) {
+                                              const double *spf, const int *col_off,
+                                              const int *col_end, int c, int ni) {
     GeoCol g;
     g.atm = atm;
     g.Dzz = Dzz;
     g.ms = spf + (size_t)c * VK_SP_NF * ni + VK_SP_MS * ni;
     g.alpha = spf + (size_t)c * VK_SP_NF * ni + VK_SP_ALPHA * ni;
     g.l0 = col_off[c];
-    g.nz = col_off[c + 1] - g.l0;
+    g.nz = col_end[c] - g.l0;
     g.ni = ni;
     return g;
 }

@@ -81,7 +81,9 @@ struct DevBatch {
     int ncols;
     int L;                     // total layers
     const int *col_off;        // [ncols+1] first layer of each column
-    const int *lay_col;        // [L] column of each layer
+    const int *col_end;        // [ncols] one past its last layer (col_off[c+1] when packed;
+                               //  slots of a fixed capacity leave gap layers between)
+    const int *lay_col;        // [L] column of each layer, -1 for a gap layer
     const double *k;           // [L][nr]
     const double *atm;         // [L][VK_ATM_NF]
     const double *Dzz;         // [L][ni]

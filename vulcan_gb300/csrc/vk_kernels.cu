@@ -93,8 +93,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     const int ni = net.ni;
     const int l = blockIdx.x;
     const int c = b.lay_col[l];
-    if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    if (c < 0 || (b.active && !b.active[c])) return;     // gap layer of a slot, or inactive
+    const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const int j = l - l0;
     double *ys = sm;                       // [3][ni] layers j-1, j, j+1
     double *sums = ys + 3 * ni;            // [8] column sums, ysum ratios, 2/(r dt)
@@ -232,7 +232,7 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
     const int nwarp = nth >> 5;
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
-        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         if (tid == 0) s_sing = 0;
         const double c0 = 1.0 / (R_ROS * dt[c]);
         for (int j = 0; j < nz; ++j) {
@@ -286,7 +286,7 @@ k_back_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *_
     const int nwarp = nth >> 5;
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
-        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         for (int j = nz - 1; j >= 0; --j) {
             const size_t l = (size_t)l0 + j;
             if (j == nz - 1) {
@@ -326,7 +326,7 @@ k_solve_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *
     const int nwarp = nth >> 5;
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
-        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         for (int j = 0; j < nz; ++j) {
             const size_t l = (size_t)l0 + j;
             for (int t = tid; t < n; t += nth)
@@ -374,7 +374,7 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
     const int n = net.ni;
     const int c = blockIdx.x;
     if (b.active && !b.active[c]) return;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;
     const double c1 = 3. / (2. * R_ROS), c2 = 1 / (2. * R_ROS);
     double dmax = 0.0;
@@ -416,8 +416,8 @@ k_geometry(DevNet net, DevBatch b, double *__restrict__ geo, int flags) {
     if (e >= (long long)b.L * ni) return;
     const int l = (int)(e / ni), i = (int)(e - (long long)l * ni);
     const int c = b.lay_col[l];
-    if (b.active && !b.active[c]) return;
-    const GeoCol cv = make_geocol(b.atm, b.Dzz, b.spf, b.col_off, c, ni);
+    if (c < 0 || (b.active && !b.active[c])) return;
+    const GeoCol cv = make_geocol(b.atm, b.Dzz, b.spf, b.col_off, b.col_end, c, ni);
     double out[GEO_NF];
     geo_coef(cv, l - cv.l0, i, flags, out);
     double *gl = geo + (size_t)l * GEO_NF * ni;

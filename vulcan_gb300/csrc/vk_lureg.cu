@@ -47,7 +47,7 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
     const int n = net.ni, nn = n * n, nnz = net.nnz;
     const int l = blockIdx.x;
     const int c = b.lay_col[l];
-    if (b.active && !b.active[c]) return;
+    if (c < 0 || (b.active && !b.active[c])) return;
     double *jls = sp;                       // [nnz]
     double *rs = jls + nnz;                 // [n]
     double *cs = rs + n;                    // [n]
@@ -158,7 +158,7 @@ k_lu32(DevNet net, DevBatch b, const float *__restrict__ D32, const double *__re
     auto buf_of = [&](int uu) { return nbuf == 2 ? (uu & 1) : 0; };
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
-        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         if (tid == 0) {
             s_sing = 0;
             tma_load_1d(Dbuf + buf_of(u) * NNP, D32 + (size_t)l0 * NNP, bytes, &bar[buf_of(u)]);

@@ -237,7 +237,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
     bool failed = false;
     for (int c; !failed && (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
-        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         if (tid == 0) {
             s_stat = 0;
             tma_load_2d(Dbuf, &tmap_d, 0, l0 * NP, tbytes, &bars[0]);

@@ -75,7 +75,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
     int issued = 0, consumed = 0;
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
-        const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+        const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         const double c0 = 1.0 / (R_ROS * dt[c]);
         const size_t base = (size_t)l0 * n;
         const int per_sweep = 2 * nz - 1;            // blocks visited per sweep

@@ -37,7 +37,7 @@ k_photo_flux(DevNet net, DevBatch b, PhotoDev ph, const double *__restrict__ y,
     if (c >= b.ncols || n >= ph.nbins) return;
     if (b.active && !b.active[c]) return;
     const int ni = net.ni;
-    const int l0 = b.col_off[c], nz = b.col_off[c + 1] - l0;
+    const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const size_t s0 = (size_t)(l0 + c);                      // staggered rows of this column
     const int NB = ph.nbins;
     const double cosz = cos(ph.sl_angle);
@@ -122,7 +122,7 @@ k_photo_J(DevNet net, DevBatch b, PhotoDev ph, double *k, unsigned long long *ch
     __shared__ double red[8];
     const int l = blockIdx.x;
     const int c = b.lay_col[l];
-    if (b.active && !b.active[c]) return;
+    if (c < 0 || (b.active && !b.active[c])) return;
     const int NB = ph.nbins;
     const double *af = ph.aflux + (size_t)l * NB;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;

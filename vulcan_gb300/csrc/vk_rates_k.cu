@@ -53,6 +53,7 @@ k_rate_consts(DevNet net, DevBatch b, const int *__restrict__ kind, const int *_
               const double *__restrict__ nasa9, double *k) {
     extern __shared__ double gs[];                       // [ni] g/RT of this layer
     const int l = blockIdx.x;
+    if (b.lay_col[l] < 0) return;                        // gap layer of a slot
     const double *al = b.atm + (size_t)l * VK_ATM_NF;
     const double T = al[VK_ATM_TCO], M = al[VK_ATM_M];
     for (int s = threadIdx.x; s < net.ni; s += blockDim.x)

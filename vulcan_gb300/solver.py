@@ -108,11 +108,17 @@ class ColumnBatch:
     Each item is a dict with ``col`` (column.Column), ``k`` ([nr, nz] rate
     constants, row i-1 = k[i]), ``y`` and ``ymix`` ([nz, ni])."""
 
-    def __init__(self, items, ni):
+    def __init__(self, items, ni, slot_cap=0):
         self.nz = np.array([it['col'].nz for it in items], dtype=np.int32)
-        self.off = np.concatenate([[0], np.cumsum(self.nz)]).astype(np.int64)
         self.ncols = len(items)
-        self.L = int(self.off[-1])
+        self.slot_cap = int(slot_cap)
+        if self.slot_cap:
+            # slotted device layout (vk_set_columns_slotted): column c at c*slot_cap
+            self.off = (np.arange(self.ncols + 1) * self.slot_cap).astype(np.int64)
+        else:
+            self.off = np.concatenate([[0], np.cumsum(self.nz)]).astype(np.int64)
+        self.end = self.off[:-1] + self.nz
+        self.L = int(self.off[-1])               # device layers
         self.ni = ni
         self.k = np.ascontiguousarray(np.concatenate([it['k'].T for it in items]))
         self.atm = np.ascontiguousarray(np.concatenate([pack_atm(it['col']) for it in items]))
@@ -128,7 +134,18 @@ class ColumnBatch:
         self.pref = np.array([it['col'].pref_indx for it in items], dtype=np.int32)
 
     def split(self, arr):
-        return [arr[self.off[c]:self.off[c + 1]] for c in range(self.ncols)]
+        """Per-column views of a device-layout array [L][...]."""
+        return [arr[self.off[c]:self.end[c]] for c in range(self.ncols)]
+
+    def expand(self, packed):
+        """A packed per-layer array [sum nz][...] in the device layout [L][...]."""
+        if not self.slot_cap:
+            return packed
+        out = np.zeros((self.L,) + packed.shape[1:], dtype=packed.dtype)
+        p = np.concatenate([[0], np.cumsum(self.nz)])
+        for c in range(self.ncols):
+            out[self.off[c]:self.end[c]] = packed[p[c]:p[c + 1]]
+        return out
 
 
 def ctrl_from(cfg=None, flags=None, gs=2140., Rp=1.138 * 7.1492E9, max_attempts=400):
@@ -188,10 +205,33 @@ class Ros2Handle:
     def set_columns(self, batch: ColumnBatch):
         self.batch = batch
         L = lib()
-        check(L.vk_set_columns(self.h, batch.ncols, ptr(batch.nz, C.c_int), ptr(batch.k),
-                               ptr(batch.atm), ptr(batch.Dzz), ptr(batch.spf), ptr(batch.y),
-                               ptr(batch.ymix)), self.h)
+        if batch.slot_cap:
+            check(L.vk_set_columns_slotted(self.h, batch.ncols, batch.slot_cap,
+                                           ptr(batch.nz, C.c_int), ptr(batch.k), ptr(batch.atm),
+                                           ptr(batch.Dzz), ptr(batch.spf), ptr(batch.y),
+                                           ptr(batch.ymix)), self.h)
+        else:
+            check(L.vk_set_columns(self.h, batch.ncols, ptr(batch.nz, C.c_int), ptr(batch.k),
+                                   ptr(batch.atm), ptr(batch.Dzz), ptr(batch.spf), ptr(batch.y),
+                                   ptr(batch.ymix)), self.h)
         check(L.vk_set_column_info(self.h, ptr(batch.pref, C.c_int), None), self.h)
+
+    def refill(self, slots, items, atom_ini, ignore=None):
+        """Continuous batching (vk_refill): the columns of ``items`` (as for
+        ColumnBatch) start in ``slots`` of this slotted handle; atom_ini
+        [n][natom], ignore [n][ni] masks or None.  The handle's batch keeps
+        the slot layout; its nz follows the new columns."""
+        b = self.batch
+        nb = ColumnBatch(items, self.ni)
+        slots = np.ascontiguousarray(slots, dtype=np.int32)
+        ai = np.ascontiguousarray(atom_ini, dtype=float)
+        ig = None if ignore is None else np.ascontiguousarray(ignore, dtype=np.int32)
+        check(lib().vk_refill(self.h, len(slots), ptr(slots, C.c_int), ptr(nb.nz, C.c_int),
+                              ptr(nb.k), ptr(nb.atm), ptr(nb.Dzz), ptr(nb.spf), ptr(nb.y),
+                              ptr(nb.ymix), ptr(ai), ptr(nb.pref, C.c_int),
+                              ptr(ig, C.c_int) if ig is not None else None), self.h)
+        b.nz[slots] = nb.nz
+        b.end = b.off[:-1] + b.nz
 
     def set_state(self, y, ymix):
         check(lib().vk_update_state(self.h, ptr(np.ascontiguousarray(y)),

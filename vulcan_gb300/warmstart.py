@@ -461,6 +461,22 @@ def judge_proposals(h, batch, items_warm, items_const, flags=None):
     return items, used
 
 
+def judged_items(model, specs, net, items_const, atoms, precision=1, chunk=512):
+    """Learned starts for a list of columns, each kept only where it does not
+    raise the residual of the Ros2 system (judge_proposals), judged in
+    handles of `chunk` columns; returns (items, used mask)."""
+    from . import batch as bmod
+    warm, _ = warm_items(model, specs, net, items_const, atoms, precision)
+    out, used = [], []
+    for a in range(0, len(items_const), chunk):
+        h, b = bmod.make_batch_handle(net, warm[a:a + chunk], atoms, precision)
+        it, u = judge_proposals(h, b, warm[a:a + chunk], items_const[a:a + chunk])
+        h.close()
+        out += it
+        used.append(u)
+    return out, np.concatenate(used)
+
+
 def eq_items(specs, net, items, atoms):
     """Items started from thermochemical equilibrium (the reference's
     ini_mix = 'EQ' seam), projected onto the normalised const_mix start's
