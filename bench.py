@@ -319,9 +319,10 @@ def _measure(args, precision, clocks=None, dist=None):
 
 
 def profile_traffic(kernel):
-    """DRAM bytes per layer of `kernel` from the committed ncu summaries
-    (a line 'roofline-traffic <kernel> bytes_per_layer=<B>' in profiles/*.md),
-    or None."""
+    """(DRAM bytes per layer, summary file) of `kernel` from the committed ncu
+    summaries (a line 'roofline-traffic <kernel> bytes_per_layer=<B>' in
+    profiles/*.md), or (None, None).  The bench does not run ncu itself: the
+    traffic it reports is this capture's figure scaled to the launch."""
     import glob
     import re
     for path in sorted(glob.glob(os.path.join(REPO, 'profiles', '*.md'))):
@@ -329,8 +330,8 @@ def profile_traffic(kernel):
             for line in f:
                 m = re.match(r'\s*roofline-traffic\s+(\S+)\s+bytes_per_layer=([0-9.eE+]+)', line)
                 if m and m.group(1) == kernel:
-                    return float(m.group(2))
-    return None
+                    return float(m.group(2)), os.path.relpath(path, REPO)
+    return None, None
 
 
 def run_gpu(args):
@@ -372,8 +373,11 @@ def run_gpu(args):
     roof['frac'] = roof['achieved'] / roof['peak']
     # DRAM bytes per launch: the ncu capture's bytes per layer (captured on the
     # 69-species workload) x this launch's layers; none for other networks
-    tpl = profile_traffic(roof['kernel'].split()[0]) if args.workload == 'c2' else None
+    tpl, tsrc = profile_traffic(roof['kernel'].split()[0]) if args.workload == 'c2' else (None, None)
     roof['traffic'] = round(tpl * L) if tpl else None
+    if tpl:
+        roof['traffic_source'] = ('ncu capture summarised in %s: DRAM bytes per layer x the '
+                                  'launch\'s %d layers (not measured in this run)' % (tsrc, L))
     for k in ('achieved', 'peak', 'frac'):
         roof[k] = round(roof[k], 4)
     peak64 = fp64_peak_tflops()
@@ -762,8 +766,9 @@ def main():
     ap.add_argument('--photo', action='store_true',
                     help='radiative-transfer update throughput (photochemistry workload)')
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
-    ap.add_argument('--autotune', action='store_true',
-                    help='tune the per-column kernels\' launch settings on the batch first')
+    ap.add_argument('--no-autotune', dest='autotune', action='store_false',
+                    help='skip tuning the per-column kernels\' launch settings on the batch '
+                         '(after the warm-up, outside the timed region) and keep the defaults')
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
     ap.add_argument('--converge-timeout', type=float, default=1800.0)

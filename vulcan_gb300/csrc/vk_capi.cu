@@ -45,6 +45,11 @@ struct vk_handle {
     int *d_jpos = nullptr;
     int *d_jrow = nullptr, *d_jcol = nullptr, *d_jrowptr = nullptr, *d_jmap = nullptr;
     double *d_compo = nullptr;
+    int nxm = 0, nh = 0;                // extra source products, derivative half terms
+    int *d_porder = nullptr, *d_src_slot = nullptr, *d_xmul_pair = nullptr;
+    double *d_src_c = nullptr, *d_xmul_fac = nullptr, *d_hjcoef = nullptr;
+    int *d_hk = nullptr, *d_hptr = nullptr, *d_hjterm = nullptr, *d_hjptr = nullptr;
+    int16_t *d_hfac = nullptr;
     // batch
     int *d_col_off = nullptr, *d_col_end = nullptr, *d_lay_col = nullptr;
     int *d_cols = nullptr;              // [max_cols] column list of reset_columns
@@ -91,6 +96,9 @@ struct vk_handle {
         n.src_nu = d_src_nu; n.jterm_nu = d_jterm_nu;
         n.jptr = d_jptr; n.jterm = d_jterm; n.jpos = d_jpos; n.compo = d_compo;
         n.jrow = d_jrow; n.jcol = d_jcol; n.jrowptr = d_jrowptr; n.jmap = d_jmap;
+        n.nxm = nxm; n.nh = nh; n.porder = d_porder; n.src_slot = d_src_slot; n.src_c = d_src_c;
+        n.xmul_pair = d_xmul_pair; n.xmul_fac = d_xmul_fac; n.hk = d_hk; n.hptr = d_hptr;
+        n.hfac = d_hfac; n.hjterm = d_hjterm; n.hjptr = d_hjptr; n.hjcoef = d_hjcoef;
         return n;
     }
     DevBatch batch() const {
@@ -182,8 +190,13 @@ static int alloc_mixed(vk_handle *h) {
     const size_t st = (size_t)((h->ni * h->ni + 3) & ~3);
     const bool tc = vk::lu_tc_supported(h->ni);
     const size_t sd = tc ? std::max(st, vk::lu_tc_block_floats(h->ni)) : st;
+    const size_t lv = (size_t)h->max_layers * h->ni;
     int rc = dalloc(h, &h->w.G32, (size_t)h->max_layers * st);
     if (!rc) rc = dalloc(h, &h->w.D32, (size_t)h->max_layers * sd);
+    if (!rc) rc = dalloc(h, &h->w.wcf, lv);
+    if (!rc) rc = dalloc(h, &h->w.wcb, lv);
+    if (!rc) rc = dalloc(h, &h->w.raf, lv);
+    if (!rc) rc = dalloc(h, &h->w.xf, lv);
     if (rc) return rc;
     if (tc) {
         cudaError_t e = vk::lu_tc_make_map(&h->tmap_d32, h->w.D32, h->ni, h->max_layers);
@@ -243,7 +256,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
         std::vector<int> order(nnz > 0 ? nnz : 1, 0);
         for (int i = 0; i < nnz; ++i) order[i] = i;
         std::stable_sort(order.begin(), order.begin() + (nnz > 0 ? nnz : 0), [&](int a, int b2) {
-            return net->jptr[a + 1] - net->jptr[a] > net->jptr[b2 + 1] - net->jptr[b2];
+            return net->hjptr[a + 1] - net->hjptr[a] > net->hjptr[b2 + 1] - net->hjptr[b2];
         });
         TRY(upload(h, &h->d_jorder, order));
     }
@@ -254,6 +267,19 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(upload(h, &h->d_jcol, net->jcol));
     TRY(upload(h, &h->d_jrowptr, net->jrowptr));
     TRY(upload(h, &h->d_jmap, net->jmap));
+    h->nxm = (int)net->xmul_pair.size();
+    h->nh = (int)net->hk.size();
+    TRY(upload(h, &h->d_porder, net->porder));
+    TRY(upload(h, &h->d_src_slot, net->src_slot));
+    TRY(upload(h, &h->d_src_c, net->src_c));
+    TRY(upload(h, &h->d_xmul_pair, net->xmul_pair));
+    TRY(upload(h, &h->d_xmul_fac, net->xmul_fac));
+    TRY(upload(h, &h->d_hk, net->hk));
+    TRY(upload(h, &h->d_hptr, net->hptr));
+    TRY(upload(h, &h->d_hfac, net->hfac));
+    TRY(upload(h, &h->d_hjterm, net->hjterm));
+    TRY(upload(h, &h->d_hjcoef, net->hjcoef));
+    TRY(upload(h, &h->d_hjptr, net->hjptr));
     const size_t L = (size_t)max_layers, ni = (size_t)h->ni;
     TRY(dalloc(h, &h->d_col_off, max_cols + 1));
     TRY(dalloc(h, &h->d_col_end, max_cols));
@@ -288,7 +314,7 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
     TRY(dalloc(h, &w.jv, L * (size_t)std::max(h->nnz, 1)));
     TRY(dalloc(h, &w.geo, L * 5 * ni));
     // FP64 inverses always (the mixed path falls back to them per column)
-    TRY(dalloc(h, &w.G, L * ni * ni));
+    TRY(dalloc(h, &w.G, L * (size_t)block_stride64(ni)));
     if (precision == VK_PREC_MIXED) TRY(alloc_mixed(h));
     TRY(dalloc(h, &w.zf, L * ni));
     TRY(dalloc(h, &w.fallback, max_cols));
@@ -563,9 +589,9 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
     if (h->precision == VK_PREC_FP64) {
         vk::launch_lu_fwd_f64(net, b, w, w.f, w.z, flags, s);
         if (timed) cudaEventRecord(h->ev[2], s);
-        vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
+        vk::launch_back_f64(net, b, w.G, w.dB, w.z, w.k1, w.y, w.yk2, w.status, s);
         vk::launch_rates(net, b, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
-        vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+        vk::launch_solve_f64(net, b, w.G, w.dB, w.dC, w.f, w.z, w.k2, w.status, s);
         h->launches += 6;
     } else {
         // route: fallback[c] = column goes to FP64 this attempt, act32[c] = mixed
@@ -582,9 +608,9 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         br.active = w.routed;
         br.queue = h->d_queue2;
         vk::launch_lu_fwd_f64(net, br, w, w.f, w.z, flags, s2);
-        vk::launch_back_f64(net, br, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s2);
+        vk::launch_back_f64(net, br, w.G, w.dB, w.z, w.k1, w.y, w.yk2, w.status, s2);
         vk::launch_rates(net, br, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s2);
-        vk::launch_solve_f64(net, br, w.G, w.dB, w.dC, w.f, w.z, w.k2, s2);
+        vk::launch_solve_f64(net, br, w.G, w.dB, w.dC, w.f, w.z, w.k2, w.status, s2);
         cudaEventRecord(h->ev_join, s2);
         DevBatch b32 = b;
         b32.active = w.act32;
@@ -599,9 +625,9 @@ static void enqueue_attempt_kernels(vk_handle *h, const DevNet &net, const DevBa
         DevBatch bf = b;
         bf.active = w.failed;
         vk::launch_lu_fwd_f64(net, bf, w, w.f, w.z, flags, s);
-        vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, s);
+        vk::launch_back_f64(net, bf, w.G, w.dB, w.z, w.k1, w.y, w.yk2, w.status, s);
         vk::launch_rates(net, bf, w.yk2, w.f, nullptr, nullptr, nullptr, nullptr, w.k1, w.dt, w.geo, flags, false, s);
-        vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, s);
+        vk::launch_solve_f64(net, bf, w.G, w.dB, w.dC, w.f, w.z, w.k2, w.status, s);
         h->launches += 16;
     }
     if (timed) cudaEventRecord(h->ev[3], s);

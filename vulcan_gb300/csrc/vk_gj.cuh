@@ -1,73 +1,80 @@
-// In-place Gauss-Jordan inversion of an n x n FP64 block in shared memory
-// with partial pivoting (largest |a| in the pivot column, lowest row on
-// ties), used by the block-Thomas factorisations.  All threads of the block
-// must call it.  *s_sing becomes 1 for a zero pivot column, 2 when no finite
-// pivot candidate exists (NaN state); the first cause seen is kept (a zero
-// pivot makes every later candidate non-finite).
+// FP64 block helpers of the block-Thomas factorisations: in-place
+// Gauss-Jordan inversion with partial pivoting, and the matrix-vector product
+// with a block held in shared memory.
+//
+// FP64 arithmetic is the scarce resource on this chip: a warp-wide FP64
+// instruction holds a sub-partition's FP64 unit for tens of cycles, whatever
+// its kind.  So the only FP64 instructions here are the useful ones -- the
+// rank-1 updates' FMAs, the pivot row's scaling, one division per pivot and
+// the products' FMAs.  The pivot search compares the IEEE bit patterns of |a|
+// as integers (for non-negative doubles the integer order is the value order),
+// the reciprocal is computed once per pivot by one thread and shared, and the
+// update runs over the block's elements as one flat range so every lane of
+// every warp has an element.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
 
 namespace vk {
 
+// In-place inversion of the n x n block A (shared memory, row-major) with
+// partial pivoting: the largest |a| in the pivot column, the lowest row on
+// ties; NaN entries are never chosen.  All threads of the block must call it.
+// *s_sing becomes 1 for a zero pivot column, 2 when no finite pivot candidate
+// exists (NaN state); the first cause seen is kept (a zero pivot makes every
+// later candidate non-finite).  colk, rowk: n doubles each; perm: n ints.
 __device__ __forceinline__ void gj_invert_f64(double *A, int n, double *colk, double *rowk, int *perm,
-                              int *s_piv, double *s_pval, int *s_sing) {
+                                              int *s_sing) {
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nn = n * n;
-    // rank-1 update mapping: thread t owns column t % n of rows t / n + R q
-    // (R = nth / n row groups); needs nth >= n, else a flat loop
-    const int R = nth / n;
-    const int my_col = R ? tid % n : 0, my_row0 = R ? tid / n : 0;
-    const bool mapped = R > 0 && tid < R * n;
+    // flat element e = tid + nth*s as (row, column), advanced incrementally
+    const int di = nth / n, dq = nth - di * n;
+    const int i0 = tid / n, q0 = tid - i0 * n;
     for (int k = 0; k < n; ++k) {
         if (warp == 0) {
-            double best = -1.0;
+            long long best = -1;
             int bi = n;
             for (int i = k + lane; i < n; i += 32) {
-                double a = fabs(A[i * n + k]);
-                if (a > best) { best = a; bi = i; }
+                const long long a = __double_as_longlong(A[i * n + k]) & 0x7fffffffffffffffll;
+                if (a <= 0x7ff0000000000000ll && a > best) { best = a; bi = i; }
             }
             for (int o = 16; o; o >>= 1) {
-                double ob = __shfl_xor_sync(0xffffffffu, best, o);
-                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
+            int flag = 0;                 // the same in every lane after the butterfly
+            if (best < 0 || bi >= n) { flag = 2; bi = k; }
+            else if (best == 0) { flag = 1; bi = k; }
+            const int p = bi;
+            double pval = 0.0, pinv = 0.0;
             if (lane == 0) {
-                // no finite candidate -> NaN state (2); all zero -> singular (1)
-                if (best < 0.0 || bi >= n) { if (*s_sing == 0) *s_sing = 2; bi = k; }
-                else if (!(best > 0.0)) { if (*s_sing == 0) *s_sing = 1; bi = k; }
-                *s_piv = bi;
-                *s_pval = A[bi * n + k];
-                perm[k] = bi;
+                if (flag && *s_sing == 0) *s_sing = flag;
+                pval = A[p * n + k];
+                pinv = 1.0 / pval;
+                perm[k] = p;
+            }
+            pval = __shfl_sync(0xffffffffu, pval, 0);
+            pinv = __shfl_sync(0xffffffffu, pinv, 0);
+            // pivot row (scaled) and pivot column of the current block; rows
+            // k and p swap (row k's new values come from rowk in the update)
+            for (int t = lane; t < n; t += 32) {
+                const double ak = A[k * n + t], ap = A[p * n + t];
+                rowk[t] = (t == k) ? pinv : ap * pinv;
+                colk[t] = (t == k) ? pval : ((t == p) ? A[k * n + k] : A[t * n + k]);
+                if (p != k) A[p * n + t] = ak;
             }
         }
         __syncthreads();
-        const int p = *s_piv;
-        const double pval = *s_pval;
-        const double pinv = 1.0 / pval;
-        for (int t = tid; t < n; t += nth) {
-            double ak = A[k * n + t], ap = A[p * n + t];
-            rowk[t] = (t == k) ? pinv : ap * pinv;
-            if (p != k) A[p * n + t] = ak;
-            colk[t] = (t == k) ? pval : ((t == p) ? A[k * n + k] : A[t * n + k]);
-        }
-        __syncthreads();
-        if (R > 0) {
-            if (mapped) {
-                const double rj = rowk[my_col];
-                const bool is_k = my_col == k;
-                for (int i = my_row0; i < n; i += R) {
-                    double *a = A + i * n + my_col;
-                    if (i == k) *a = rj;
-                    else *a = (is_k ? 0.0 : *a) - colk[i] * rj;
-                }
-            }
-        } else {
-            for (int e = tid; e < nn; e += nth) {
-                int i = e / n, jj = e - i * n;
-                if (i == k) A[e] = rowk[jj];
-                else A[e] = (jj == k ? 0.0 : A[e]) - colk[i] * rowk[jj];
-            }
+        int i = i0, q = q0;
+        for (int e = tid; e < nn; e += nth) {
+            const double r = rowk[q];
+            const double a = (q == k) ? 0.0 : A[e];
+            const double u = __fma_rn(-colk[i], r, a);
+            A[e] = (i == k) ? r : u;
+            q += dq;
+            i += di;
+            if (q >= n) { q -= n; ++i; }
         }
         __syncthreads();
     }
@@ -82,6 +89,34 @@ __device__ __forceinline__ void gj_invert_f64(double *A, int n, double *colk, do
             __syncthreads();
         }
     }
+}
+
+// out[r] = sum_q M[r*n + q] x[q] (+ add[r] when add is not NULL) for the n x n
+// block M in shared memory.  Thread (r, g) sums the g-th of P = blockDim / n
+// contiguous chunks of row r (lanes of a warp take consecutive rows: stride
+// n doubles, conflict-free for odd n); the chunks are then added in order.
+// part: P*n doubles of shared scratch.  All threads call it; it ends with a
+// block barrier (out is readable by every thread afterwards).
+__device__ __forceinline__ void matvec_f64(const double *M, int n, const double *x, double *part,
+                                           double *out, const double *add) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int P = nth >= n ? (nth / n < 8 ? nth / n : 8) : 1;
+    const int chunk = (n + P - 1) / P;
+    for (int t = tid; t < P * n; t += nth) {
+        const int g = t / n, r = t - g * n;
+        const int q0 = g * chunk, q1 = q0 + chunk < n ? q0 + chunk : n;
+        const double *row = M + r * n;
+        double s = 0.0;
+        for (int q = q0; q < q1; ++q) s = __fma_rn(row[q], x[q], s);
+        part[g * n + r] = s;
+    }
+    __syncthreads();
+    for (int r = tid; r < n; r += nth) {
+        double s = part[r];
+        for (int g = 1; g < P; ++g) s += part[g * n + r];
+        out[r] = add ? add[r] + s : s;
+    }
+    __syncthreads();
 }
 
 }  // namespace vk

@@ -56,6 +56,18 @@ struct vk_network {
     std::vector<int> jrowptr;          // [ni+1] entries are sorted by row
     std::vector<int> jmap;             // [ni*ni] entry at (s, q) or -1
     std::vector<double> compo;         // [ni*natom]
+    // Device form of the tables (one FP64 operation per gathered term):
+    std::vector<int> porder;           // [npair] pairs by decreasing written-term count
+    std::vector<int> src_slot;         // [nsrc] slot of the rate array each source term reads
+    std::vector<double> src_c;         // [nsrc] signed power-of-two coefficient (exact product)
+    std::vector<int> xmul_pair;        // [nxm] extra slots npair+m = xmul_fac[m] * v[xmul_pair[m]]
+    std::vector<double> xmul_fac;      //       (coefficients that are not powers of two)
+    std::vector<int> hk;               // [nh] rate-constant slot (2*pair + side) of half term h
+    std::vector<int> hptr;             // [nh+1] factor list of h: indices into (y of the layer, M)
+    std::vector<int16_t> hfac;         //        index ni stands for M
+    std::vector<int> hjterm;           // [njt] half term of each Jacobian gather term
+    std::vector<double> hjcoef;        // [njt] its coefficient (stoichiometry x exponent, signed)
+    std::vector<int> hjptr;            // [nnz+1]
 };
 
 // Device view of the network tables (passed by value to kernels).
@@ -74,6 +86,18 @@ struct DevNet {
     const int *jpos;
     const int *jrow, *jcol, *jrowptr, *jmap;
     const double *compo;
+    // the gather form (vk_network): pair order, source slots and coefficients,
+    // extra products, derivative half terms, Jacobian gather terms
+    int nxm, nh;
+    const int *porder;
+    const int *src_slot;
+    const double *src_c;
+    const int *xmul_pair;
+    const double *xmul_fac;
+    const int *hk, *hptr;
+    const int16_t *hfac;
+    const int *hjterm, *hjptr;
+    const double *hjcoef;
 };
 
 // Device view of a loaded batch of columns.
@@ -97,6 +121,10 @@ struct DevBatch {
     int cps_k[VK_TUNE_N];      // per-kernel setting of vk_set_launch (0: cps)
     int lu32_tiling;           // k_lu32 register tiling (-1: by ni)
 };
+
+// Doubles per FP64 block of the n x n inverses in global memory: n*n rounded
+// up to even, so every block starts on 16 bytes (bulk-copy alignment).
+__host__ __device__ inline int block_stride64(int n) { return (n * n + 1) & ~1; }
 
 // Grid of a per-column kernel: CTAs per SM from vk_set_launch, else the
 // batch's override, else the kernel's default; never more than the columns.
@@ -159,12 +187,15 @@ struct Work {                  // per-handle device work buffers
     double *jv;                // [L][nnz]  -J_chem entries
     double *dA, *dB, *dC;      // [L][ni]   diffusion coefficients (A+Ai, B+Bi, C+Ci)
     double *geo;               // [L][5][ni] state-free transport geometry (vk_geo.cuh)
-    double *G;                 // [L][ni*ni] FP64 block inverses
+    double *G;                 // [L][block_stride64(ni)] FP64 block inverses
     float *G32;                // [L][ni*ni] FP32 inverses of the scaled blocks (mixed mode)
     double *rs, *cs;           // [L][ni] power-of-two row / column scales (mixed mode)
     double *r;                 // refinement residual
     double *f2;                // [L][ni] second-stage right-hand side (mixed mode)
     float *zf;                 // [L][ni] FP32 forward-sweep vector (mixed mode)
+    float *wcf, *wcb;          // [L][ni] scaled couplings of the refinement sweeps (mixed mode)
+    float *raf;                // [L][ni] scaled residual of the current sweep (mixed mode)
+    float *xf;                 // [L][ni] back-sweep result of the current sweep (mixed mode)
     float *D32;                // [L][stride] dense scaled FP32 blocks (mixed mode)
     int *fallback;             // [ncols] attempt solved in FP64 (routed or refinement failed)
     int *act32;                // [ncols] attempt solved by the FP32 factors + refinement
@@ -188,10 +219,10 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
                        const double *rhs, double *z, int flags, cudaStream_t s);
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G,
                      const double *dB, const double *z, double *x,
-                     const double *y, double *yk2, cudaStream_t s);
+                     const double *y, double *yk2, int *status, cudaStream_t s);
 void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G,
                       const double *dB, const double *dC, const double *rhs,
-                      double *zbuf, double *x, cudaStream_t s);
+                      double *zbuf, double *x, int *status, cudaStream_t s);
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags,
                   double mtol, double atol, cudaStream_t s);
 void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,

@@ -23,6 +23,7 @@
 #include "vk_internal.cuh"
 #include "vk_geo.cuh"
 #include "vk_gj.cuh"
+#include "vk_tma.cuh"
 
 namespace vk {
 
@@ -35,15 +36,6 @@ __device__ __forceinline__ double ipow(double x, int e) {
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
-}
-
-// acc + c*v for a coefficient code (+1, -1: signed add without a multiply;
-// 0: multiply by the tabulated coefficient).  Bit-identical to the
-// reference's "acc -1*v" / "acc +2*v" terms.
-__device__ __forceinline__ double add_coef(double acc, int code, double nu, double v) {
-    if (code == 1) return __dadd_rn(acc, v);
-    if (code == -1) return __dadd_rn(acc, __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull));
-    return __dadd_rn(acc, __dmul_rn(nu, v));
 }
 
 // Value of one side of pair p in the generated lambda order k*t1*t2*...
@@ -60,29 +52,11 @@ __device__ __forceinline__ double side_rate(double kk, const PairDesc *pd, int s
     return v;
 }
 
-// d/dy_q of kM * prod y_s^e over merged factors (kM = k M^m); pos = index of q.
-__device__ __forceinline__ double side_deriv(double kM, const int16_t *sp, const uint8_t *nu,
-                                             int n, int pos, const double *yl) {
-    double v = kM;
-    for (int t = 0; t < n; ++t) {
-        const double yv = yl[__ldg(sp + t)];
-        const int e = __ldg(nu + t);
-        if (t == pos) {
-            if (e == 2) v *= yv + yv;
-            else if (e > 2) v *= (double)e * ipow(yv, e - 1);
-        } else {
-            v *= ipow(yv, e);
-        }
-    }
-    return v;
-}
-
-__device__ __forceinline__ double mpow(double M, int m) {
-    return m == 0 ? 1.0 : (m == 1 ? M : (m == 2 ? M * M : M * M * M));
-}
-
 // ---------------------------------------------------------------------------
-// (a)+(b) rate / source / Jacobian kernel: one CTA per layer.
+// (a)+(b) rate / source / Jacobian kernel: one CTA per layer.  The FP64 pipe
+// bounds it, so every gathered term is one FP64 instruction (the gather form
+// of vk_network.cpp) and the loops a warp runs have similar lengths (pairs,
+// species, half terms and Jacobian entries in decreasing order of length).
 template <bool JAC>
 __global__ void __launch_bounds__(128)
 k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict__ f,
@@ -96,15 +70,20 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     if (c < 0 || (b.active && !b.active[c])) return;     // gap layer of a slot, or inactive
     const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const int j = l - l0;
-    double *ys = sm;                       // [3][ni] layers j-1, j, j+1
-    double *sums = ys + 3 * ni;            // [8] column sums, ysum ratios, 2/(r dt)
-    double *v = sums + 8;                  // [max(npair, nw)]
-    double *kM = v + (net.npair > net.nw ? net.npair : net.nw);   // [2*npair] (JAC only)
+    double *yl = sm;                       // [ni + 1] layer j, then M (factor index ni)
+    double *ym = yl + ni + 1;              // [ni] layer j-1
+    double *yp = ym + ni;                  // [ni] layer j+1
+    double *sums = yp + ni;                // [8] column sums, ysum ratios, 2/(r dt)
+    double *v = sums + 8;                  // [max(npair + nxm, nh)]
     const int tid = threadIdx.x, nth = blockDim.x;
+    const double *al = b.atm + (size_t)l * VK_ATM_NF;
+    const double M = al[VK_ATM_M];
     for (int t = tid; t < 3 * ni; t += nth) {
-        int jj = j - 1 + t / ni;
-        ys[t] = (jj >= 0 && jj < nz) ? y[(size_t)(l0 + jj) * ni + (t % ni)] : 0.0;
+        const int w = t / ni, s = t - w * ni, jj = j - 1 + w;
+        const double val = (jj >= 0 && jj < nz) ? y[(size_t)(l0 + jj) * ni + s] : 0.0;
+        (w == 0 ? ym : (w == 1 ? yl : yp))[s] = val;
     }
+    if (tid == 0) yl[ni] = M;
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
     const bool has_up = j + 1 < nz, has_dn = j > 0;
@@ -112,10 +91,11 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
         // layer sums and the state-dependent ysum ratios of the transport
         // operator, once per layer (FP64 divisions are costly on this chip)
         double s3[3];
+        const double *yw[3] = {ym, yl, yp};
 #pragma unroll
         for (int w = 0; w < 3; ++w) {
             double s = 0;
-            for (int i = lane; i < ni; i += 32) s += ys[w * ni + i];
+            for (int i = lane; i < ni; i += 32) s += yw[w][i];
             s3[w] = warp_sum(s);
         }
         if (lane == 0) {
@@ -127,35 +107,32 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
             sums[4] = k1 ? 2. / (R_ROS * dt[c]) : 0.0;
         }
     }
-    const double *yl = ys + ni;
-    const double *al = b.atm + (size_t)l * VK_ATM_NF;
-    const double M = al[VK_ATM_M];
     const double *kl = b.k + (size_t)l * net.nr;
-    // net rate of each pair
-    for (int p = tid; p < net.npair; p += nth) {
+    // net rate of each pair (written-order products: bit-identical to chemdf)
+    for (int i = tid; i < net.npair; i += nth) {
+        const int p = net.porder[i];
         const PairDesc *pd = net.pairs + p;
         const double2 kk = reinterpret_cast<const double2 *>(kl)[p];
         v[p] = side_rate(kk.x, pd, 0, yl, M) - side_rate(kk.y, pd, 1, yl, M);
-        if (JAC) {
-            kM[2 * p] = kk.x * mpow(M, __ldg(&pd->fm));
-            kM[2 * p + 1] = kk.y * mpow(M, __ldg(&pd->rm));
-        }
     }
     __syncthreads();
+    if (net.nxm > 0) {                     // products by coefficients that are not powers of two
+        for (int m = tid; m < net.nxm; m += nth)
+            v[net.npair + m] = __dmul_rn(net.xmul_fac[m], v[net.xmul_pair[m]]);
+        __syncthreads();
+    }
     // ysum ratios of the transport operator (state dependent part)
     const double qU0 = sums[0], qD0 = sums[1], qUp = sums[2], qDm = sums[3];
     const double hinv = sums[4];
     const double *gl = geo + (size_t)l * GEO_NF * ni;
     const double *spf = b.spf + (size_t)c * VK_SP_NF * ni;
-    // production - loss gather (generated chemdf order) + transport; species
-    // in decreasing order of term count so a warp's lanes end together
+    // production - loss gather (generated chemdf order, one fma per term) +
+    // transport; species in decreasing order of term count
     for (int si = tid; si < ni; si += nth) {
         const int s = net.src_order[si];
         double acc = 0.0;
-        for (int e = net.src_ptr[s]; e < net.src_ptr[s + 1]; ++e) {
-            const int2 t = net.src[e];
-            acc = add_coef(acc, t.y, t.y ? 0.0 : net.src_nu[e], v[t.x]);
-        }
+        for (int e = net.src_ptr[s]; e < net.src_ptr[s + 1]; ++e)
+            acc = __fma_rn(net.src_c[e], v[net.src_slot[e]], acc);
         const double gU = gl[s], gD = gl[ni + s];
         double cA = -gU * qU0 - gD * qD0 + gl[2 * ni + s];
         double cB = has_up ? gU * qUp + gl[3 * ni + s] : 0.0;
@@ -163,8 +140,8 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
         double out = acc;
         if (!chem_only) {
             double dif = cA * yl[s];
-            if (has_up) dif += cB * ys[2 * ni + s];
-            if (has_dn) dif += cC * ys[s];
+            if (has_up) dif += cB * yp[s];
+            if (has_dn) dif += cC * ym[s];
             if ((flags & VK_F_TOPFLUX) && j == nz - 1)
                 dif += spf[VK_SP_TOPFLUX * ni + s] / b.atm[(size_t)(l - 1) * VK_ATM_NF + VK_ATM_DZI];
             if ((flags & VK_F_BOTFLUX) && j == 0)
@@ -182,25 +159,19 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
     }
     if (!JAC) return;
     __syncthreads();
-    // derivative terms d v_p / d y_q
-    for (int t = tid; t < net.nw; t += nth) {
-        const WDesc wd = net.w[t];
-        const PairDesc *pd = net.pairs + wd.pair;
-        double d = 0.0;
-        if (wd.fpos >= 0) d = side_deriv(kM[2 * wd.pair], pd->fsp, pd->fnu, __ldg(&pd->nf), wd.fpos, yl);
-        if (wd.rpos >= 0) d -= side_deriv(kM[2 * wd.pair + 1], pd->rsp, pd->rnu, __ldg(&pd->nr), wd.rpos, yl);
-        v[t] = d;
+    // derivative half terms: k_side x product of the side's remaining factors
+    for (int h = tid; h < net.nh; h += nth) {
+        double d = kl[net.hk[h]];
+        for (int t = net.hptr[h]; t < net.hptr[h + 1]; ++t) d = __dmul_rn(d, yl[net.hfac[t]]);
+        v[h] = d;
     }
     __syncthreads();
     double *jl = jv + (size_t)l * net.nnz;
     for (int ei = tid; ei < net.nnz; ei += nth) {
         const int e = net.jorder[ei];
         double acc = 0.0;
-        for (int t = net.jptr[e]; t < net.jptr[e + 1]; ++t) {
-            const int2 jt = net.jterm[t];
-            acc = jt.y == 1 ? acc + v[jt.x]
-                : (jt.y == -1 ? acc - v[jt.x] : fma(net.jterm_nu[t], v[jt.x], acc));
-        }
+        for (int t = net.hjptr[e]; t < net.hjptr[e + 1]; ++t)
+            acc = __fma_rn(net.hjcoef[t], v[net.hjterm[t]], acc);
         jl[e] = -acc;                      // entries of -J (neg_symjac)
     }
 }
@@ -210,26 +181,26 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
 // per CTA (work queue).  The diagonal block
 //   D'_j = c0 I - J_j - diag(dA_j) - diag(dC_j) G_{j-1} diag(dB_{j-1})
 // is built and inverted in place in shared memory by Gauss-Jordan elimination
-// with partial pivoting (largest |a|, lowest row on ties).  (A variant with the
-// block in registers, as the FP32 path has, measured 92.9 ms against 76.4 ms
-// per attempt at 512 columns: FP64 throughput, not barriers, bounds this one.)
+// with partial pivoting (largest |a|, lowest row on ties).  FP64 throughput
+// bounds it (about 1/60 of the FP32 rate on this chip), so the inversion
+// issues no FP64 instruction beyond the useful ones (vk_gj.cuh).  The
+// inverses are stored with the padded stride block_stride64(n).
 __global__ void __launch_bounds__(256)
 k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
              const double *__restrict__ dB, const double *__restrict__ dC,
              const double *__restrict__ dt, const double *__restrict__ rhs,
              double *__restrict__ G, double *__restrict__ z, int *__restrict__ status) {
     extern __shared__ double sm[];
-    const int n = net.ni, nn = n * n;
+    const int n = net.ni, nn = n * n, gst = block_stride64(n);
+    const int tid = threadIdx.x, nth = blockDim.x;
     double *A = sm;
     double *colk = A + nn;
     double *rowk = colk + n;
     double *zp = rowk + n;
     double *bb = zp + n;
-    int *perm = reinterpret_cast<int *>(bb + n);
-    __shared__ int s_piv, s_sing, s_col;
-    __shared__ double s_pval;
-    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const int nwarp = nth >> 5;
+    double *part = bb + n;                           // [max(nth, n)]
+    int *perm = reinterpret_cast<int *>(part + (nth > n ? nth : n));
+    __shared__ int s_sing, s_col;
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
         const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
@@ -252,115 +223,173 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
             const double *jl = jv + l * net.nnz;
             for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
             __syncthreads();
-            gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
-            double *Gl = G + l * nn;
+            gj_invert_f64(A, n, colk, rowk, perm, &s_sing);
+            double *Gl = G + l * gst;
             for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
-            for (int r = warp; r < n; r += nwarp) {
-                double s = 0.0;
-                for (int q = lane; q < n; q += 32) s += A[r * n + q] * bb[q];
-                s = warp_sum(s);
-                if (lane == 0) rowk[r] = s;
-            }
-            __syncthreads();
-            for (int t = tid; t < n; t += nth) {
-                zp[t] = rowk[t];
-                z[l * n + t] = rowk[t];
-            }
-            __syncthreads();
+            matvec_f64(A, n, bb, part, zp, nullptr);     // z_j = G_j bb (ends with a barrier)
+            for (int t = tid; t < n; t += nth) z[l * n + t] = zp[t];
         }
         if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
     }
 }
 
-// x_j = z_j + G_j (dB_j o x_{j+1}); optional yk2 = y + x / r.
+// Shared memory of the FP64 sweeps: two mbarriers, nbuf blocks of the padded
+// stride, two vectors and the product's partial sums.  Two buffers (the next
+// block's copy overlaps this block's product) when they fit in a CTA's 227 KB,
+// else one (ni >~ 115).
+static __host__ __device__ inline size_t sweep64_smem(int n, int nth, int nbuf) {
+    return 16 + (size_t)(nbuf * block_stride64(n) + 2 * n + (nth > n ? nth : n)) * sizeof(double);
+}
+static inline int sweep64_nbuf(int n) { return sweep64_smem(n, 256, 2) <= 232448 ? 2 : 1; }
+
+// Copy k of a CTA's block stream lands in buffer k % nbuf and completes
+// phase (k / nbuf) & 1 of that buffer's mbarrier.
+__device__ __forceinline__ bool wait_copy(uint64_t *bar, unsigned k, int nbuf) {
+    return nbuf == 2 ? mbar_wait(&bar[k & 1], (k >> 1) & 1) : mbar_wait(&bar[0], k & 1);
+}
+
+// After a bulk copy that never landed: wait (bounded) for the copies still in
+// flight, visits [v, last), so none lands in a CTA that has left; the caller
+// then records VK_ETIMEOUT and leaves.
+__device__ __forceinline__ void drain_copies(uint64_t *bar, unsigned cnt, int v, int last, int nbuf) {
+    for (int u = v; u < last; ++u) wait_copy(bar, cnt + (unsigned)u, nbuf);
+}
+
+// x_j = z_j + G_j (dB_j o x_{j+1}); optional yk2 = y + x / r.  The inverses
+// G_{nz-2} .. G_0 stream into shared memory by bulk copies in sweep order,
+// double-buffered (nbuf = 2): the next block's copy runs during this block's
+// product.
 __global__ void __launch_bounds__(256)
 k_back_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *__restrict__ dB,
            const double *__restrict__ z, double *__restrict__ x, const double *__restrict__ y,
-           double *__restrict__ yk2) {
-    extern __shared__ double sm[];
-    const int n = net.ni, nn = n * n;
-    double *xs = sm;          // x_{j+1} * dB_j
-    double *xn = sm + n;
+           double *__restrict__ yk2, int *__restrict__ status, int nbuf) {
+    extern __shared__ __align__(16) unsigned char smb[];
+    const int n = net.ni, gst = block_stride64(n);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smb);      // [2]
+    double *Gbuf = reinterpret_cast<double *>(smb + 16);    // [nbuf][gst]
+    double *xs = Gbuf + nbuf * gst;                         // [n] dB_j o x_{j+1}
+    double *xn = xs + n;                                    // [n]
+    double *part = xn + n;                                  // [max(nth, n)]
     __shared__ int s_col;
-    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const int nwarp = nth >> 5;
+    const uint32_t bytes = (uint32_t)gst * sizeof(double);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    unsigned cnt = 0;              // copies this CTA consumed before the current column
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
         const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
-        for (int j = nz - 1; j >= 0; --j) {
-            const size_t l = (size_t)l0 + j;
-            if (j == nz - 1) {
-                for (int t = tid; t < n; t += nth) xn[t] = z[l * n + t];
-            } else {
-                const double *Gl = G + l * nn;
-                for (int r = warp; r < n; r += nwarp) {
-                    double s = 0.0;
-                    for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * xs[q];
-                    s = warp_sum(s);
-                    if (lane == 0) xn[r] = z[l * n + r] + s;
-                }
-            }
-            __syncthreads();
+        const int nvis = nz - 1;                            // G_{nz-2} .. G_0
+        auto issue = [&](int v) {                           // thread 0
+            const unsigned k = cnt + (unsigned)v, bi = k % (unsigned)nbuf;
+            tma_load_1d(Gbuf + bi * gst, G + ((size_t)l0 + nz - 2 - v) * gst, bytes, &bar[bi]);
+        };
+        if (tid == 0)
+            for (int v = 0; v < nbuf && v < nvis; ++v) issue(v);
+        {
+            const size_t l = (size_t)l0 + nz - 1;           // top layer: x = z
             for (int t = tid; t < n; t += nth) {
-                double xv = xn[t];
+                const double xv = z[l * n + t];
+                x[l * n + t] = xv;
+                if (yk2) yk2[l * n + t] = y[l * n + t] + xv / R_ROS;
+                if (nz > 1) xs[t] = dB[(l - 1) * n + t] * xv;
+            }
+        }
+        __syncthreads();
+        int v = 0, timed_out = 0;
+        for (; v < nvis; ++v) {
+            const int j = nz - 2 - v;
+            const size_t l = (size_t)l0 + j;
+            const unsigned k = cnt + (unsigned)v;
+            const bool ok = wait_copy(bar, k, nbuf);
+            if (__syncthreads_or(!ok)) { timed_out = 1; break; }
+            matvec_f64(Gbuf + (k % (unsigned)nbuf) * gst, n, xs, part, xn, z + l * n);
+            if (tid == 0 && v + nbuf < nvis) issue(v + nbuf);   // the buffer just read is free
+            for (int t = tid; t < n; t += nth) {
+                const double xv = xn[t];
                 x[l * n + t] = xv;
                 if (yk2) yk2[l * n + t] = y[l * n + t] + xv / R_ROS;
                 if (j > 0) xs[t] = dB[(l - 1) * n + t] * xv;
             }
             __syncthreads();
         }
+        if (timed_out) {
+            drain_copies(bar, cnt, v, nvis < v + nbuf ? nvis : v + nbuf, nbuf);
+            if (tid == 0) status[c] = VK_ETIMEOUT;
+            return;
+        }
+        cnt += (unsigned)nvis;
     }
 }
 
-// Forward + back sweep with stored inverses for a new right-hand side.
+// Forward + back sweep with the stored inverses for a new right-hand side.
+// The blocks stream in visit order: G_0 .. G_{nz-1} (forward), G_{nz-2} .. G_0
+// (back), bulk copies as in k_back_f64.
 __global__ void __launch_bounds__(256)
 k_solve_f64(DevNet net, DevBatch b, const double *__restrict__ G, const double *__restrict__ dB,
             const double *__restrict__ dC, const double *__restrict__ rhs,
-            double *__restrict__ zbuf, double *__restrict__ x) {
-    extern __shared__ double sm[];
-    const int n = net.ni, nn = n * n;
-    double *vin = sm;
-    double *vout = sm + n;
+            double *__restrict__ zbuf, double *__restrict__ x, int *__restrict__ status, int nbuf) {
+    extern __shared__ __align__(16) unsigned char smb[];
+    const int n = net.ni, gst = block_stride64(n);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smb);      // [2]
+    double *Gbuf = reinterpret_cast<double *>(smb + 16);    // [nbuf][gst]
+    double *vin = Gbuf + nbuf * gst;                        // [n]
+    double *vout = vin + n;                                 // [n]
+    double *part = vout + n;                                // [max(nth, n)]
     __shared__ int s_col;
-    const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
-    const int nwarp = nth >> 5;
+    const uint32_t bytes = (uint32_t)gst * sizeof(double);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    unsigned cnt = 0;
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
         const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
-        for (int j = 0; j < nz; ++j) {
+        const int nvis = 2 * nz - 1;
+        auto layer_of = [&](int v) { return v < nz ? v : 2 * nz - 2 - v; };
+        auto issue = [&](int v) {                           // thread 0
+            const unsigned k = cnt + (unsigned)v, bi = k % (unsigned)nbuf;
+            tma_load_1d(Gbuf + bi * gst, G + ((size_t)l0 + layer_of(v)) * gst, bytes, &bar[bi]);
+        };
+        if (tid == 0)
+            for (int v = 0; v < nbuf && v < nvis; ++v) issue(v);
+        int v = 0, timed_out = 0;
+        for (; v < nvis; ++v) {
+            const bool fwd = v < nz;
+            const int j = layer_of(v);
             const size_t l = (size_t)l0 + j;
-            for (int t = tid; t < n; t += nth)
-                vin[t] = rhs[l * n + t] + (j > 0 ? dC[l * n + t] * vout[t] : 0.0);
-            __syncthreads();
-            const double *Gl = G + l * nn;
-            for (int r = warp; r < n; r += nwarp) {
-                double s = 0.0;
-                for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
-                s = warp_sum(s);
-                if (lane == 0) { vout[r] = s; zbuf[l * n + r] = s; }
+            if (fwd) {
+                for (int t = tid; t < n; t += nth)
+                    vin[t] = rhs[l * n + t] + (j > 0 ? dC[l * n + t] * vout[t] : 0.0);
             }
-            __syncthreads();
-        }
-        for (int j = nz - 1; j >= 0; --j) {
-            const size_t l = (size_t)l0 + j;
-            if (j < nz - 1) {
-                const double *Gl = G + l * nn;
-                for (int r = warp; r < n; r += nwarp) {
-                    double s = 0.0;
-                    for (int q = lane; q < n; q += 32) s += Gl[r * n + q] * vin[q];
-                    s = warp_sum(s);
-                    if (lane == 0) vout[r] = zbuf[l * n + r] + s;
-                }
-            } else {
-                for (int t = tid; t < n; t += nth) vout[t] = zbuf[l * n + t];
-            }
-            __syncthreads();
+            const unsigned k = cnt + (unsigned)v;
+            const bool ok = wait_copy(bar, k, nbuf);
+            if (__syncthreads_or(!ok)) { timed_out = 1; break; }
+            const double *Gs = Gbuf + (k % (unsigned)nbuf) * gst;
+            matvec_f64(Gs, n, vin, part, vout, fwd ? nullptr : zbuf + l * n);
+            if (tid == 0 && v + nbuf < nvis) issue(v + nbuf);
             for (int t = tid; t < n; t += nth) {
-                x[l * n + t] = vout[t];
-                if (j > 0) vin[t] = dB[(l - 1) * n + t] * vout[t];
+                const double xv = vout[t];
+                if (fwd) zbuf[l * n + t] = xv;
+                if (!fwd || j == nz - 1) {                  // back sweep (starts at the top: x = z)
+                    x[l * n + t] = xv;
+                    if (j > 0) vin[t] = dB[(l - 1) * n + t] * xv;
+                }
             }
             __syncthreads();
         }
+        if (timed_out) {
+            drain_copies(bar, cnt, v, nvis < v + nbuf ? nvis : v + nbuf, nbuf);
+            if (tid == 0) status[c] = VK_ETIMEOUT;
+            return;
+        }
+        cnt += (unsigned)nvis;
     }
 }
 
@@ -431,8 +460,10 @@ void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flag
 
 // ---------------------------------------------------------------------------
 static size_t rates_smem(const DevNet &net);
-// block, colk, rowk, zp, bb (doubles) + perm (ints)
-static size_t lu_fwd_smem(int n) { return (size_t)(n * n + 4 * n) * sizeof(double) + (size_t)n * sizeof(int); }
+// block, colk, rowk, zp, bb, the product's partial sums (doubles) + perm (ints)
+static size_t lu_fwd_smem(int n) {
+    return (size_t)(n * n + 4 * n + (256 > n ? 256 : n)) * sizeof(double) + (size_t)n * sizeof(int);
+}
 
 // Opt the kernels into the dynamic shared memory this network needs; called
 // once per handle, outside any stream capture.
@@ -444,12 +475,15 @@ cudaError_t init_kernels(const DevNet &net) {
     if ((e = cudaFuncSetAttribute(k_rates<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
     if ((e = cudaFuncSetAttribute(k_rates<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
     if ((e = cudaFuncSetAttribute(k_lu_fwd_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
+    const int ssw = (int)sweep64_smem(n, 256, sweep64_nbuf(n));
+    if ((e = cudaFuncSetAttribute(k_back_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, ssw))) return e;
+    if ((e = cudaFuncSetAttribute(k_solve_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, ssw))) return e;
     return cudaSuccess;
 }
 
 static size_t rates_smem(const DevNet &net) {
-    int m = net.npair > net.nw ? net.npair : net.nw;
-    return (size_t)(3 * net.ni + 8 + m + 2 * net.npair) * sizeof(double);
+    const int m = net.npair + net.nxm > net.nh ? net.npair + net.nxm : net.nh;
+    return (size_t)(3 * net.ni + 1 + 8 + m) * sizeof(double);
 }
 
 void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double *f,
@@ -480,16 +514,21 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
 }
 
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
-                     const double *z, double *x, const double *y, double *yk2, cudaStream_t s) {
+                     const double *z, double *x, const double *y, double *yk2, int *status,
+                     cudaStream_t s) {
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_back_f64<<<column_grid(b, VK_TUNE_SWEEP64, 2), 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, z, x, y, yk2);
+    const int nbuf = sweep64_nbuf(net.ni);
+    k_back_f64<<<column_grid(b, VK_TUNE_SWEEP64, 2), 256, sweep64_smem(net.ni, 256, nbuf), s>>>(
+        net, b, G, dB, z, x, y, yk2, status, nbuf);
 }
 
 void launch_solve_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,
-                      const double *dC, const double *rhs, double *zbuf, double *x,
+                      const double *dC, const double *rhs, double *zbuf, double *x, int *status,
                       cudaStream_t s) {
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_solve_f64<<<column_grid(b, VK_TUNE_SWEEP64, 2), 256, 2 * net.ni * sizeof(double), s>>>(net, b, G, dB, dC, rhs, zbuf, x);
+    const int nbuf = sweep64_nbuf(net.ni);
+    k_solve_f64<<<column_grid(b, VK_TUNE_SWEEP64, 2), 256, sweep64_smem(net.ni, 256, nbuf), s>>>(
+        net, b, G, dB, dC, rhs, zbuf, x, status, nbuf);
 }
 
 void launch_stage(const DevNet &net, const DevBatch &b, const Work &w, int flags, double mtol,

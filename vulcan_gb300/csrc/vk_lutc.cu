@@ -207,9 +207,20 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
     int *kinv = reinterpret_cast<int *>(smb + L.kinv);       // [NP] step of pivot row r
     uint64_t *bars = reinterpret_cast<uint64_t *>(smb + L.bars);   // [0] TMA, [1] MMA
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smb + L.tslot);
-    __shared__ int s_col, s_stat;
+    __shared__ int s_col, s_stat, s_pw;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // The panel warp (B2) runs alone while the others wait, and three CTAs
+    // share an SM: give each CTA's panel warp its own sub-partition (warp
+    // slot modulo 4) rather than warp 0 everywhere, which would put the three
+    // panel chains on one issue port.  The CTA's index on the SM is read from
+    // the hardware warp slot of its first warp (consecutive slots per CTA);
+    // any value is correct, only the placement changes.
+    if (tid == 0) {
+        unsigned ws;
+        asm volatile("mov.u32 %0, %%warpid;" : "=r"(ws));
+        s_pw = (int)((ws >> 2) & 3u);
+    }
     const int r = tid;                                       // row = TMEM lane
     const bool row_warp = warp * 32 < NP;                    // warp-uniform
     const uint32_t tbytes = (uint32_t)NP * NP * 4;
@@ -231,6 +242,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
+    const int pw = s_pw;                 // panel warp of this CTA
     const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's lanes, column 0
 
     int u_tma = 0, u_mma = 0;          // completed phases of bars[0] / bars[1]
@@ -299,7 +311,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
                 }
                 __syncthreads();
                 // B2: one warp eliminates the panel's pivots
-                if (warp == 0) {
+                if (warp == pw) {
                     float P[RA][kPW];
                     unsigned umask = 0;
 #pragma unroll

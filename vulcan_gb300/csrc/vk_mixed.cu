@@ -125,7 +125,10 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
             return q;
         };
         for (; sweep < max_sweeps && !converged && !timed_out; ++sweep) {
-            double dmax = 0.0;
+            // largest |d| / sc of the sweep as a fraction (num, den): compared by
+            // cross-multiplication, divided once per thread after the sweep
+            // (FP64 divisions are long FP64-pipe sequences on this chip)
+            double dnum = 0.0, dden = 1.0;
             Visit cur = fetch(0);
             for (int v = 0; v < per_sweep; ++v) {
                 const int j = layer_of(v);
@@ -187,13 +190,16 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                         const double xn = cur.x + d;
                         x[e] = xn;
                         const double sc = fabs(xn) + cur.ys + 1e-10 * cur.n0;
-                        dmax = isfinite(d) ? fmax(dmax, fabs(d) / sc) : INFINITY;
+                        const double ad = fabs(d);
+                        if (!isfinite(d)) { dnum = INFINITY; dden = 1.0; }
+                        else if (ad * dden > dnum * sc) { dnum = ad; dden = sc; }
                     }
                 }
                 __syncthreads();
                 cur = nxt;
             }
             if (timed_out) break;
+            double dmax = dnum / dden;
             for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
             if (lane == 0) red[warp] = dmax;
             __syncthreads();

@@ -23,6 +23,105 @@
 
 static thread_local std::string g_net_err;
 
+// The tables in the form the rate kernel gathers them, so that every gathered
+// term costs one FP64 instruction and the lanes of a warp run loops of equal
+// length (FP64 issue is the rate kernel's bound on this chip):
+//  * source term (pair p, coefficient e): acc = fma(c, v[slot], acc).  For a
+//    power-of-two |e| the product e*v is exact, so the fma equals the generated
+//    chemdf's "acc + e*v" bit for bit (slot p, c = e); any other |e| reads an
+//    extra slot holding round(|e| v_p) with c = +-1, which is the same again.
+//  * derivative half term: d v_p / d y_q from one side of the pair,
+//    k_side x (product of the side's factors with q's exponent lowered by one),
+//    M a factor like the species; the exponent of q moves into the Jacobian
+//    gather coefficient (an exact integer product).
+//  * Jacobian entry (s, q): sum over half terms of coefficient x half term,
+//    coefficient = +-(net stoichiometry of s) x (exponent of q), minus for
+//    the reverse side.
+static bool pow2(int e) { return e > 0 && (e & (e - 1)) == 0; }
+
+static void build_gather_form(vk_network *n) {
+    const int ni = n->ni, np = n->npair;
+    n->porder.resize(np);
+    for (int p = 0; p < np; ++p) n->porder[p] = p;
+    std::stable_sort(n->porder.begin(), n->porder.end(), [&](int a, int b) {
+        return n->pairs[a].nt[0] + n->pairs[a].nt[1] > n->pairs[b].nt[0] + n->pairs[b].nt[1];
+    });
+    std::map<std::pair<int, int>, int> xslot;          // (pair, |e|) -> extra slot
+    for (size_t e = 0; e < n->src_nu.size(); ++e) {
+        const int p = n->src[e].x, c = (int)n->src_nu[e], a = c < 0 ? -c : c;
+        if (pow2(a)) {
+            n->src_slot.push_back(p);
+            n->src_c.push_back((double)c);
+        } else {
+            auto it = xslot.find({p, a});
+            int m;
+            if (it == xslot.end()) {
+                m = (int)n->xmul_pair.size();
+                xslot[{p, a}] = m;
+                n->xmul_pair.push_back(p);
+                n->xmul_fac.push_back((double)a);
+            } else {
+                m = it->second;
+            }
+            n->src_slot.push_back(np + m);
+            n->src_c.push_back(c < 0 ? -1.0 : 1.0);
+        }
+    }
+    // half terms of every derivative term w
+    struct Half { int k; int mult; std::vector<int16_t> fac; int w; int sign; };
+    std::vector<Half> halves;
+    for (int wi = 0; wi < (int)n->w.size(); ++wi) {
+        const WDesc &wd = n->w[wi];
+        const PairDesc &pd = n->pairs[wd.pair];
+        for (int side = 0; side < 2; ++side) {
+            const int pos = side ? wd.rpos : wd.fpos;
+            if (pos < 0) continue;
+            const int nf = side ? pd.nr : pd.nf;
+            const int16_t *sp = side ? pd.rsp : pd.fsp;
+            const uint8_t *nu = side ? pd.rnu : pd.fnu;
+            Half h;
+            h.k = 2 * wd.pair + side;
+            h.w = wi;
+            h.sign = side ? -1 : 1;
+            h.mult = nu[pos];
+            for (int i = 0; i < nf; ++i) {
+                const int cnt = (i == pos) ? nu[i] - 1 : nu[i];
+                for (int r = 0; r < cnt; ++r) h.fac.push_back(sp[i]);
+            }
+            const int mp = side ? pd.rm : pd.fm;
+            for (int r = 0; r < mp; ++r) h.fac.push_back((int16_t)ni);
+            halves.push_back(h);
+        }
+    }
+    std::vector<int> hidx(halves.size());
+    for (size_t i = 0; i < halves.size(); ++i) hidx[i] = (int)i;
+    std::stable_sort(hidx.begin(), hidx.end(), [&](int a, int b) {
+        return halves[a].fac.size() > halves[b].fac.size();
+    });
+    std::vector<std::vector<int>> of_w(n->w.size());   // w -> its half terms (new indices)
+    n->hptr.push_back(0);
+    for (size_t r = 0; r < hidx.size(); ++r) {
+        const Half &h = halves[hidx[r]];
+        n->hk.push_back(h.k);
+        n->hfac.insert(n->hfac.end(), h.fac.begin(), h.fac.end());
+        n->hptr.push_back((int)n->hfac.size());
+        of_w[h.w].push_back((int)r);
+    }
+    n->hjptr.push_back(0);
+    for (size_t e = 0; e + 1 < n->jptr.size(); ++e) {
+        for (int t = n->jptr[e]; t < n->jptr[e + 1]; ++t) {
+            const int wi = n->jterm[t].x;
+            const double nu_s = n->jterm_nu[t];
+            for (int r : of_w[wi]) {
+                const Half &h = halves[hidx[r]];
+                n->hjterm.push_back(r);
+                n->hjcoef.push_back(nu_s * h.sign * h.mult);
+            }
+        }
+        n->hjptr.push_back((int)n->hjterm.size());
+    }
+}
+
 extern "C" const char *vk_network_last_error(void) { return g_net_err.c_str(); }
 
 extern "C" int vk_network_compile(const vk_network_desc *d, vk_network **out) {
@@ -138,6 +237,7 @@ extern "C" int vk_network_compile(const vk_network_desc *d, vk_network **out) {
         n->jterm_nu.push_back((double)t.y);
         t.y = (t.y == 1 || t.y == -1) ? t.y : 0;
     }
+    build_gather_form(n);
     n->compo.assign(d->compo, d->compo + (size_t)ni * d->natom);
     *out = n;
     return VK_OK;

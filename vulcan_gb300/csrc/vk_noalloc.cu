@@ -47,8 +47,7 @@ k_block_solve_noalloc(int nz, int n, const double *__restrict__ D, const double 
     double *zp = rowk + n;
     double *bb = zp + n;
     int *perm = reinterpret_cast<int *>(bb + n);
-    __shared__ int s_piv, s_sing;
-    __shared__ double s_pval;
+    __shared__ int s_sing;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
     const int nwarp = nth >> 5;
     if (tid == 0) s_sing = 0;
@@ -65,7 +64,7 @@ k_block_solve_noalloc(int nz, int n, const double *__restrict__ D, const double 
         }
         for (int t = tid; t < n; t += nth) bb[t] = b[l * n + t] - (j > 0 ? lj[t] * zp[t] : 0.0);
         __syncthreads();
-        vk::gj_invert_f64(A, n, colk, rowk, perm, &s_piv, &s_pval, &s_sing);
+        vk::gj_invert_f64(A, n, colk, rowk, perm, &s_sing);
         double *Gl = G + l * nn;
         for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
         for (int r = warp; r < n; r += nwarp) {
