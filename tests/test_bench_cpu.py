@@ -10,7 +10,7 @@ sys.path.insert(0, ROOT)
 def test_profile_traffic_lines():
     import bench
     assert bench.profile_traffic('k_lu32') == (35300.0, os.path.join('profiles', 'k_lu32_64cols.md'))
-    assert bench.profile_traffic('k_rates')[0] == 16900.0
+    assert bench.profile_traffic('k_rates')[0] == 17600.0
     assert bench.profile_traffic('no_such_kernel') == (None, None)
 
 
