@@ -461,9 +461,10 @@ def converge_block(args):
             items, used = warmstart.judged_items(model, specs, net, items_const, ATOMS, prec)
             extra = {'warm_started': int(used.sum()), 'proposal_s': round(time.perf_counter() - t0, 2)}
         left = args.converge_budget - (time.perf_counter() - t0)
+        sst = {}
         out, wall = batch.run_stream(net, items, ATOMS, nslots=min(NCOLS, len(items)), ctrl=ctrl,
                                      precision=prec, slot_cap=200, chunk=args.chunk_stream,
-                                     budget_s=left, keep_state=True)
+                                     budget_s=left, keep_state=True, stats=sst)
         wall = time.perf_counter() - t0
         conv = [i for i, r in out.items() if r['end_case'] == 1]
         steps = sorted(out[i]['count'] for i in conv)
@@ -474,6 +475,12 @@ def converge_block(args):
                      'steps_to_converge_mean': float(np.mean(steps)) if steps else None,
                      'end_cases': {str(k): sum(1 for r in out.values() if r['end_case'] == k)
                                    for k in sorted({r['end_case'] for r in out.values()})},
+                     # whole trajectories: every accepted step of every column
+                     # that ran (ended or still in a slot at the end)
+                     'column_steps': sst['steps'], 'attempts': sst['attempts'],
+                     'column_steps_per_s': round(sst['steps'] / wall, 1),
+                     'device_s': round(sst['device_s'], 2),
+                     'column_steps_per_device_s': round(sst['steps'] / max(sst['device_s'], 1e-9), 1),
                      **extra}
         fin[name] = out
     if 'learned_mixed' in res:
@@ -666,6 +673,54 @@ def run_converge(args):
     print(json.dumps(res))
 
 
+def run_c1_converge(args):
+    """Config 1 to steady state: one NCHO-photochemistry column (nz = 150,
+    frozen seeded J, T with a seeded perturbation, Kzz log-linear 1e7-1e10)
+    from const_mix under the reference's convergence test, plain FP64 and
+    mixed (FP32 factors + FP64 refinement); steps, attempts, FP64 solves of
+    the mixed run, device and wall time, and the final mixing ratios of the
+    mixed run against the FP64 run's (where the FP64 value exceeds 1e-20)."""
+    from vulcan_gb300 import _build, batch, capi, configs
+    from vulcan_gb300.network import Network
+    from vulcan_gb300.solver import ctrl_from
+    _build.build()
+    net = Network.from_npz(os.path.join(REPO, 'tests', 'golden', 'net_NCHO_photo.npz'))
+    spec = configs.config1(sorted(net.photo_index()))
+    items = batch.build_items([spec], net)
+    res, fin = {}, {}
+    for name, prec in (('plain_fp64', 0), ('mixed', 1)):
+        h, b = batch.make_batch_handle(net, items, ATOMS, precision=prec)
+        ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+        ctrl.count_max = args.count_max
+        t0 = time.perf_counter()
+        dev = 0.0
+        while True:
+            try:
+                h.run(ctrl, max_steps=500, timeout_s=args.converge_timeout)
+            except capi.VkError as e:
+                if e.code != capi.VK_ETIMEOUT:
+                    raise
+            dev += h.timing()['rates'] * 1e-3
+            st = h.state()
+            if st['end_case'][0] != 0 or time.perf_counter() - t0 > args.converge_timeout:
+                break
+        wall = time.perf_counter() - t0
+        cnt = h.counters()
+        h.close()
+        res[name] = {'end_case': int(st['end_case'][0]), 'steps': int(st['count'][0]),
+                     't_s': float(st['t'][0]), 'attempts': int(cnt[0, 0]),
+                     'fp64_solves': int(cnt[0, 4]), 'device_s': round(dev, 3), 'wall_s': round(wall, 3),
+                     'steps_per_device_s': round(float(st['count'][0]) / max(dev, 1e-9), 1)}
+        fin[name] = st['ymix']
+    m = fin['plain_fp64'] > 1e-20
+    rel = np.abs(fin['mixed'][m] - fin['plain_fp64'][m]) / fin['plain_fp64'][m]
+    res['mixed_vs_fp64_ymix_rel_gt_1e-20'] = {'max': float(rel.max()), 'median': float(np.median(rel)),
+                                              'within_1e-3': float((rel <= 1e-3).mean())}
+    res['workload'] = ('config 1: one NCHO_photo column (69 species, nz = 150, frozen seeded J), '
+                       'const_mix start, the reference convergence test, count_max %d' % args.count_max)
+    print(json.dumps(res))
+
+
 def run_photo(args):
     """Radiative transfer throughput: vk_photo_update over --ncols columns of
     the NCHO photochemistry workload (nz = 150) on the reference's binned
@@ -718,6 +773,9 @@ def run_profile(args):
     items = batch.build_items(specs, net)
     prec = 1 if args.precision == 'mixed' else 0
     h, b = batch.make_batch_handle(net, items, ATOMS, precision=prec)
+    if args.lu_variant >= 0:
+        from vulcan_gb300 import capi
+        h.set_launch(capi.VK_TUNE_LU32, 0, args.lu_variant)
     dt = np.full(b.ncols, 1e-10)
     for _ in range(args.attempts):
         h.attempt(dt)
@@ -763,6 +821,8 @@ def main():
     ap.add_argument('--profile', action='store_true',
                     help='only run --attempts instrumented attempts (for ncu captures)')
     ap.add_argument('--attempts', type=int, default=2)
+    ap.add_argument('--lu-variant', type=int, default=-1,
+                    help='profile mode: FP32 factorisation variant (vk_set_launch; -1: default)')
     ap.add_argument('--photo', action='store_true',
                     help='radiative-transfer update throughput (photochemistry workload)')
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
@@ -771,6 +831,9 @@ def main():
                          '(after the warm-up, outside the timed region) and keep the defaults')
     ap.add_argument('--converge', action='store_true',
                     help='run --ncols columns to steady state on both paths')
+    ap.add_argument('--converge-c1', action='store_true',
+                    help='config 1 (one NCHO-photochemistry column, nz = 150) to steady state, '
+                         'plain FP64 and mixed')
     ap.add_argument('--converge-timeout', type=float, default=1800.0)
     ap.add_argument('--stream-cols', type=int, default=1536,
                     help='default run: columns streamed through the 512 slots per path')
@@ -808,6 +871,9 @@ def main():
         return
     if args.converge:
         run_converge(args)
+        return
+    if args.converge_c1:
+        run_c1_converge(args)
         return
     run_gpu(args)
 

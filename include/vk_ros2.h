@@ -132,6 +132,16 @@ VK_API const char *vk_last_error(const vk_handle *h);   /* h may be NULL */
  * (default 6) and refine_tol is the convergence test on the correction
  * relative to |x| + |y| + 1e-10 n_0 (default 1e-10). */
 VK_API int  vk_set_precision(vk_handle *h, int precision, int max_refine, double refine_tol);
+/* Mixed precision: the step size from which a column's attempts go straight
+ * to the FP64 solve (default INFINITY: every column tries the FP32 factors
+ * until its refinement first fails, then uses FP64 from a quarter of that
+ * step on).  A finite dt0 spares a column its first failure when the
+ * caller knows where FP32 factors stop preconditioning these systems (a
+ * failed refinement is redone in FP64 after the attempt's other solves, a
+ * serial FP64 chain).  Applies to every column now and at its next start;
+ * a failure still lowers a column's limit.  No counterpart in the reference,
+ * which solves every step in FP64 (op.py:2913-2929). */
+VK_API int  vk_set_route(vk_handle *h, double dt0);
 
 /* Load a batch of columns.  L = sum(nz).  k is [L][2*npair] (layer-major,
  * row l holds k[1..nr] of that layer), atm is [L][VK_ATM_NF], Dzz is [L][ni]
@@ -247,9 +257,11 @@ VK_API int  vk_compute_k(vk_handle *h);
  * ctas_per_sm x SMs CTAs.  kernel: VK_TUNE_*; ctas_per_sm 0..8 (0: the
  * kernel's built-in default, or VK_CTAS_PER_SM from the environment);
  * variant: for VK_TUNE_LU32 the register tiling of the FP32 Gauss-Jordan,
- * 0..3 covering blocks up to 48, 80, 112, 160 species, or 4: the
- * tensor-core factorisation (tcgen05, blocks up to 128 species) (-1: the
- * default for ni; a variant smaller than ni is refused), ignored otherwise.
+ * 0..3 covering blocks up to 48, 80, 112, 160 species, 4: the tensor-core
+ * factorisation (tcgen05, blocks up to 128 species) with one warp eliminating
+ * each 16-pivot panel, or 5: the same with the four warps of its CTA
+ * eliminating the panel together (identical factors) (-1: the default for
+ * ni; a variant smaller than ni is refused), ignored otherwise.
  * A change drops the captured vk_run graph, which is captured again. */
 #define VK_TUNE_LU32    0   /* k_lu32: FP32 block-Thomas factorisation        */
 #define VK_TUNE_LU64    1   /* k_lu_fwd_f64: FP64 factorisation + first sweep */

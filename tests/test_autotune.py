@@ -39,7 +39,7 @@ def _cost(kernel, ctas, variant):
 
 
 def test_candidates_cover_ni():
-    assert autotune.candidates('lu32', 69) == [(c, t) for t in (1, 2, 3, 4) for c in (1, 2, 3, 4)]
+    assert autotune.candidates('lu32', 69) == [(c, t) for t in (1, 2, 3, 4, 5) for c in (1, 2, 3, 4)]
     assert [t for _, t in autotune.candidates('lu32', 150)] == [3] * 4
     assert autotune.candidates('lu64', 69) == [(1, -1), (2, -1), (3, -1), (4, -1)]
 

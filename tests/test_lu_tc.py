@@ -81,3 +81,24 @@ def test_tensor_core_is_the_default_up_to_128_species():
     h.close()
     np.testing.assert_array_equal(G0, G1)
     assert capi.LU32_TILING_CAP[capi.LU32_TC] == 128
+
+
+@pytest.mark.parametrize('tag,ns', [('c2', [0, 1, 2, 3, 4]), ('c3s', [0, 1, 2])])
+def test_cooperative_panel_gives_the_same_factors(tag, ns):
+    """Variant 5 eliminates each panel with the CTA's four warps instead of
+    one; the pivots and every FP32 operation are the same, so the factors and
+    the attempt equal variant 4's bit for bit."""
+    from test_gpu_parity import make_handle
+    from vulcan_gb300 import capi
+    g, net, gn, h, b = make_handle(tag, ns=ns, precision=1)
+    dt = g['att_dt'][ns]
+    h.set_launch(capi.VK_TUNE_LU32, 0, capi.LU32_TC)
+    out4 = h.attempt(dt)
+    G4 = _factors(h, net.ni, b.L)
+    h.set_launch(capi.VK_TUNE_LU32, 0, capi.LU32_TC_COOP)
+    out5 = h.attempt(dt)
+    G5 = _factors(h, net.ni, b.L)
+    h.close()
+    np.testing.assert_array_equal(G5, G4)
+    np.testing.assert_array_equal(out5['sol'], out4['sol'])
+    assert capi.LU32_TILING_CAP[capi.LU32_TC_COOP] == 128

@@ -66,25 +66,34 @@ def make_batch_handle(net, items, atom_list, precision=capi.VK_PREC_FP64, slot_c
 
 
 def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64, slot_cap=None,
-               chunk=20, budget_s=None, keep_state=False):
+               chunk=20, budget_s=None, keep_state=False, stats=None, route_dt0=None):
     """Continuous batching: the column items (build_items order) stream
     through nslots slots of one handle; every `chunk` steps the slots whose
     column has ended (converged, count_max, runtime, error) take the next
     items (vk_refill), so the GPU keeps a full batch while columns finish at
     different times.  Each column runs the reference's loop (op.py:808-936)
     from its own start, exactly as in a batch of its own.  Stops when every
-    item has ended or after budget_s seconds of wall time.
+    item has ended or after budget_s seconds of wall time.  route_dt0 (mixed
+    precision): the step size from which attempts go straight to FP64
+    (vk_set_route).
 
     Returns (results, wall_s): results[i] = dict(end_case, count, t, wall_s
-    at which it ended[, y, ymix]) for every item that ended."""
+    at which it ended[, y, ymix]) for every item that ended.  A dict passed as
+    ``stats`` receives the accepted steps of every column that ran (ended or
+    still in a slot when the budget ran out), the attempts, and the device
+    time of the runs (CUDA events, s)."""
     import time
     from . import capi as _capi
     slot_cap = slot_cap or int(max(it['col'].nz for it in items))
     first = list(items[:nslots])
     h, b = make_batch_handle(net, first, atom_list, precision, slot_cap=slot_cap)
+    if route_dt0 is not None and precision == _capi.VK_PREC_MIXED:
+        h.set_route(route_dt0)
     slot_item = list(range(len(first)))
     nxt = len(first)
     results = {}
+    steps_done = attempts_done = 0
+    dev_s = 0.0
     t0 = time.perf_counter()
     try:
         while True:
@@ -96,9 +105,14 @@ def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64,
             except _capi.VkError as e:
                 if e.code != _capi.VK_ETIMEOUT:
                     raise
+            dev_s += h.timing()['rates'] * 1e-3
             st = h.state()
             now = time.perf_counter() - t0
             ended = [c for c in range(b.ncols) if slot_item[c] is not None and st['end_case'][c] != 0]
+            if ended:
+                cnt = h.counters()
+                steps_done += int(st['count'][ended].sum())
+                attempts_done += int(cnt[ended, 0].sum())
             for c in ended:
                 r = dict(end_case=int(st['end_case'][c]), count=int(st['count'][c]),
                          t=float(st['t'][c]), wall_s=now)
@@ -118,6 +132,13 @@ def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64,
                 nxt += len(new)
             if all(si is None for si in slot_item):
                 break
+        if stats is not None:
+            live = [c for c in range(b.ncols) if slot_item[c] is not None]
+            st = h.state()
+            cnt = h.counters()
+            stats['steps'] = steps_done + int(st['count'][live].sum())
+            stats['attempts'] = attempts_done + int(cnt[live, 0].sum())
+            stats['device_s'] = dev_s
     finally:
         h.close()
     return results, time.perf_counter() - t0

@@ -15,8 +15,9 @@ VK_OK, VK_EINVAL, VK_ECUDA, VK_ESINGULAR, VK_ENAN, VK_EMAXATTEMPT, VK_ETIMEOUT, 
 VK_PREC_FP64, VK_PREC_MIXED = 0, 1
 VK_F_MOLDIFF, VK_F_TOPFLUX, VK_F_BOTFLUX = 1, 2, 4
 VK_TUNE_LU32, VK_TUNE_LU64, VK_TUNE_SWEEP64, VK_TUNE_REFINE = 0, 1, 2, 3
-LU32_TILING_CAP = (48, 80, 112, 160, 128)  # species each LU32 variant covers
+LU32_TILING_CAP = (48, 80, 112, 160, 128, 128)  # species each LU32 variant covers
 LU32_TC = 4                                # the tensor-core factorisation (k_lu_tc)
+LU32_TC_COOP = 5                           # the same, four warps per panel
 (ATM_M, ATM_N0, ATM_TCO, ATM_G, ATM_DZI, ATM_KZZ, ATM_VZ, ATM_TI, ATM_HPI, ATM_HP,
  ATM_PICO, ATM_PICOU, ATM_DZ) = range(13)
 ATM_NF = 13
@@ -31,7 +32,7 @@ _ERRNAMES = {1: 'VK_EINVAL', 2: 'VK_ECUDA', 3: 'VK_ESINGULAR', 4: 'VK_ENAN',
 # Every entry point include/vk_ros2.h declares.
 EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
            'vk_network_free', 'vk_create', 'vk_destroy', 'vk_last_error',
-           'vk_set_precision', 'vk_set_columns', 'vk_update_state', 'vk_update_atm',
+           'vk_set_precision', 'vk_set_route', 'vk_set_columns', 'vk_update_state', 'vk_update_atm',
            'vk_update_k', 'vk_ros2_attempt', 'vk_set_atom_ini', 'vk_set_column_info',
            'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
@@ -94,6 +95,7 @@ def lib(path=None):
         'vk_destroy': (None, [vp]),
         'vk_last_error': (C.c_char_p, [vp]),
         'vk_set_precision': (i, [vp, i, i, d]),
+        'vk_set_route': (i, [vp, d]),
         'vk_set_columns': (i, [vp, i, pi, pd, pd, pd, pd, pd, pd]),
         'vk_update_state': (i, [vp, pd, pd]),
         'vk_update_atm': (i, [vp, pd]),

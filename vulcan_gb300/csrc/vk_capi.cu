@@ -27,6 +27,7 @@ struct vk_handle {
     int max_cols = 0, max_layers = 0, precision = VK_PREC_FP64;
     int max_refine = 6;
     double refine_tol = 1e-10;
+    double route_dt0 = INFINITY;  // vk_set_route: FP64 from this step size until a failure lowers it
     int geo_flags = -1;         // flags the transport geometry was built for (-1: stale)
     CUtensorMap tmap_d32{};     // k_lu_tc's view of w.D32 (mixed mode, ni <= 128)
     int ncols = 0, L = 0;
@@ -372,13 +373,26 @@ extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, dou
     return VK_OK;
 }
 
+extern "C" int vk_set_route(vk_handle *h, double dt0) {
+    if (!h) return fail(nullptr, VK_EINVAL, "handle is NULL");
+    if (!(dt0 > 0.0)) return fail(h, VK_EINVAL, "dt0 must be positive (INFINITY: no initial limit)");
+    h->route_dt0 = dt0;
+    if (h->w.thr64 && h->max_cols > 0) {
+        vk::launch_reset_route(h->w, h->max_cols, dt0, h->stream);
+        VK_CUDA(h, cudaGetLastError());
+        VK_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    return VK_OK;
+}
+
 // Per-column start of a run (clock, counters, conservation reference,
 // routing threshold, dt = 1e-10) of the columns cs, by one kernel.
 static int reset_columns(vk_handle *h, const std::vector<int> &cs) {
     if (cs.empty()) return VK_OK;
     cudaStream_t s = h->stream;
     VK_CUDA(h, cudaMemcpyAsync(h->d_cols, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    vk::launch_reset_columns(h->rs, (int)cs.size(), h->d_cols, h->w.dt, h->w.status, h->w.thr64, s);
+    vk::launch_reset_columns(h->rs, (int)cs.size(), h->d_cols, h->w.dt, h->w.status, h->w.thr64,
+                             h->route_dt0, s);
     VK_CUDA(h, cudaGetLastError());
     VK_CUDA(h, cudaStreamSynchronize(s));      // cs may be a temporary
     return VK_OK;

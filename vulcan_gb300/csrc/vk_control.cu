@@ -383,7 +383,7 @@ void launch_control(const DevNet &net, const DevBatch &b, const RunState &rs, co
 // (vulcan_cfg.dttry).
 __global__ void k_reset_columns(RunState rs, int n, const int *__restrict__ cols,
                                 double *__restrict__ dt, int *__restrict__ status,
-                                double *__restrict__ thr64) {
+                                double *__restrict__ thr64, double route_dt0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int c = cols[i];
@@ -397,12 +397,12 @@ __global__ void k_reset_columns(RunState rs, int n, const int *__restrict__ cols
     for (int a = 0; a < VK_MAX_NATOM; ++a) rs.loss[(size_t)c * VK_MAX_NATOM + a] = 0.0;
     dt[c] = 1e-10;
     status[c] = 0;
-    if (thr64) thr64[c] = INFINITY;
+    if (thr64) thr64[c] = route_dt0;
 }
 
 void launch_reset_columns(const RunState &rs, int n, const int *cols, double *dt, int *status,
-                          double *thr64, cudaStream_t s) {
-    k_reset_columns<<<(n + 127) / 128, 128, 0, s>>>(rs, n, cols, dt, status, thr64);
+                          double *thr64, double route_dt0, cudaStream_t s) {
+    k_reset_columns<<<(n + 127) / 128, 128, 0, s>>>(rs, n, cols, dt, status, thr64, route_dt0);
 }
 
 void launch_count_active(const int *active, int ncols, int *nactive, cudaStream_t s) {

@@ -32,6 +32,6 @@ void launch_control(const DevNet &net, const DevBatch &b, const RunState &rs, co
                     const int *status, const int *fallback, double *geo, cudaStream_t s);
 void launch_count_active(const int *active, int ncols, int *nactive, cudaStream_t s);
 void launch_reset_columns(const RunState &rs, int n, const int *cols, double *dt, int *status,
-                          double *thr64, cudaStream_t s);
+                          double *thr64, double route_dt0, cudaStream_t s);
 
 }  // namespace vk

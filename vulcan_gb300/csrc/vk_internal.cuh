@@ -235,17 +235,19 @@ void launch_photo(const DevNet &net, const DevBatch &b, const PhotoDev &ph, cons
                   const double *ymix, double *k, unsigned long long *change, cudaStream_t s);
 void launch_photo_clear(const DevBatch &b, unsigned long long *change, cudaStream_t s);
 void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
-void launch_reset_route(const Work &w, int ncols, cudaStream_t s);
+void launch_reset_route(const Work &w, int ncols, double route_dt0, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
 cudaError_t init_lureg_kernels(const DevNet &net);
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
 int lu32_tiling_cap(int tiling);     // largest block a k_lu32 tiling covers (0: none)
-// tensor-core factorisation (vk_lutc.cu): the LU32 tiling value that selects it
+// tensor-core factorisation (vk_lutc.cu): the LU32 tiling values that select
+// it with the one-warp panel and with the four-warp cooperative panel
 constexpr int VK_LU_TC = 4;
+constexpr int VK_LU_TC_COOP = 5;
 bool lu_tc_supported(int n);
 cudaError_t lu_tc_make_map(CUtensorMap *map, const float *D32, int n, int max_layers);
 void launch_lu_tc(const DevNet &net, const DevBatch &b, const Work &w, const CUtensorMap &map,
-                  cudaStream_t s);
+                  bool coop, cudaStream_t s);
 size_t lu_tc_block_floats(int n);    // floats per layer of its padded scaled blocks
 cudaError_t init_lu_tc(int n);
 

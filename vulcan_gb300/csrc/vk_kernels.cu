@@ -180,11 +180,14 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
 // (c) block-Thomas factorisation + forward sweep, FP64, one column at a time
 // per CTA (work queue).  The diagonal block
 //   D'_j = c0 I - J_j - diag(dA_j) - diag(dC_j) G_{j-1} diag(dB_{j-1})
-// is built and inverted in place in shared memory by Gauss-Jordan elimination
-// with partial pivoting (largest |a|, lowest row on ties).  FP64 throughput
-// bounds it (about 1/60 of the FP32 rate on this chip), so the inversion
-// issues no FP64 instruction beyond the useful ones (vk_gj.cuh).  The
-// inverses are stored with the padded stride block_stride64(n).
+// is built and inverted in shared memory by Gauss-Jordan elimination with
+// partial pivoting (largest |a|, lowest row on ties).  FP64 throughput bounds
+// it (about 1/60 of the FP32 rate on this chip), so the inversion issues no
+// FP64 instruction beyond the useful ones (vk_gj.cuh); with LA the block has
+// two buffers and each pivot's search and scaling overlap the previous
+// pivot's update (blocks up to 117 species; the in-place inversion above).
+// The inverses are stored with the padded stride block_stride64(n).
+template <bool LA>
 __global__ void __launch_bounds__(256)
 k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
              const double *__restrict__ dB, const double *__restrict__ dC,
@@ -193,19 +196,21 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
     extern __shared__ double sm[];
     const int n = net.ni, nn = n * n, gst = block_stride64(n);
     const int tid = threadIdx.x, nth = blockDim.x;
-    double *A = sm;
-    double *colk = A + nn;
-    double *rowk = colk + n;
-    double *zp = rowk + n;
+    double *A = sm;                                  // [nn]
+    double *B = A + nn;                              // [nn] (LA: second buffer)
+    double *colk = LA ? B + nn : A + nn;             // [2n] (LA) / [n]
+    double *rowk = colk + (LA ? 2 * n : n);
+    double *zp = rowk + (LA ? 2 * n : n);
     double *bb = zp + n;
     double *part = bb + n;                           // [max(nth, n)]
     int *perm = reinterpret_cast<int *>(part + (nth > n ? nth : n));
-    __shared__ int s_sing, s_col;
+    __shared__ int s_sing, s_col, s_piv[2];
     for (int c; (c = next_column(b, &s_col)) >= 0;) {
         if (b.active && !b.active[c]) continue;
         const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
         if (tid == 0) s_sing = 0;
         const double c0 = 1.0 / (R_ROS * dt[c]);
+        double *Ac = A;                              // holds G_{j-1}, then D'_j
         for (int j = 0; j < nz; ++j) {
             const size_t l = (size_t)l0 + j;
             const double *cj = dC + l * n;
@@ -213,20 +218,21 @@ k_lu_fwd_f64(DevNet net, DevBatch b, const double *__restrict__ jv, const double
             const double *aj = dA + l * n;
             for (int e = tid; e < nn; e += nth) {
                 int r = e / n, q = e - r * n;
-                double v = j > 0 ? -cj[r] * A[e] * bm[q] : 0.0;
+                double v = j > 0 ? -cj[r] * Ac[e] * bm[q] : 0.0;
                 if (r == q) v += c0 - aj[r];
-                A[e] = v;
+                Ac[e] = v;
             }
             for (int t = tid; t < n; t += nth)
                 bb[t] = rhs[l * n + t] + (j > 0 ? cj[t] * zp[t] : 0.0);
             __syncthreads();
             const double *jl = jv + l * net.nnz;
-            for (int e = tid; e < net.nnz; e += nth) A[net.jpos[e]] += jl[e];
+            for (int e = tid; e < net.nnz; e += nth) Ac[net.jpos[e]] += jl[e];
             __syncthreads();
-            gj_invert_f64(A, n, colk, rowk, perm, &s_sing);
+            if (LA) Ac = gj_invert_f64_la(Ac, Ac == A ? B : A, n, colk, rowk, perm, s_piv, &s_sing);
+            else gj_invert_f64(Ac, n, colk, rowk, perm, &s_sing);
             double *Gl = G + l * gst;
-            for (int e = tid; e < nn; e += nth) Gl[e] = A[e];
-            matvec_f64(A, n, bb, part, zp, nullptr);     // z_j = G_j bb (ends with a barrier)
+            for (int e = tid; e < nn; e += nth) Gl[e] = Ac[e];
+            matvec_f64(Ac, n, bb, part, zp, nullptr);     // z_j = G_j bb (ends with a barrier)
             for (int t = tid; t < n; t += nth) z[l * n + t] = zp[t];
         }
         if (tid == 0 && s_sing) status[c] = s_sing == 2 ? VK_ENAN : VK_ESINGULAR;
@@ -406,7 +412,10 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
     const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarp = blockDim.x >> 5;
     const double c1 = 3. / (2. * R_ROS), c2 = 1 / (2. * R_ROS);
-    double dmax = 0.0;
+    // the column's largest d / sol, kept as a fraction (num, den) compared by
+    // cross-multiplication and divided once per thread (an FP64 division is a
+    // long FP64-pipe sequence on this chip)
+    double dnum = 0.0, dden = 1.0;
     int bad = 0;
     for (int j = warp; j < nz; j += nwarp) {
         const size_t l = (size_t)l0 + j;
@@ -421,11 +430,12 @@ k_stage(DevNet net, DevBatch b, const double *__restrict__ y, const double *__re
             if (ymix[e] < mtol) d = 0.0;
             if (sv < atol) d = 0.0;
             if ((flags & VK_F_BOTFLUX) && j == 0) d = 0.0;
-            if (sv > 0.0) dmax = fmax(dmax, d / sv);
+            if (sv > 0.0 && d * dden > dnum * sv) { dnum = d; dden = sv; }
         }
         s = warp_sum(s);
         for (int i = lane; i < n; i += 32) ymix_out[l * n + i] = sol[l * n + i] / s;
     }
+    double dmax = dnum / dden;
     for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     if (lane == 0) wmax[warp] = dmax;
     bad = __syncthreads_or(bad);
@@ -460,21 +470,27 @@ void launch_geometry(const DevNet &net, const DevBatch &b, double *geo, int flag
 
 // ---------------------------------------------------------------------------
 static size_t rates_smem(const DevNet &net);
-// block, colk, rowk, zp, bb, the product's partial sums (doubles) + perm (ints)
-static size_t lu_fwd_smem(int n) {
-    return (size_t)(n * n + 4 * n + (256 > n ? 256 : n)) * sizeof(double) + (size_t)n * sizeof(int);
+// block(s), colk, rowk, zp, bb, the product's partial sums (doubles) + perm
+// (ints); the look-ahead variant keeps two blocks and two colk/rowk
+static size_t lu_fwd_smem(int n, bool la) {
+    const int nb = la ? 2 : 1;
+    return (size_t)(nb * n * n + (2 * nb + 2) * n + (256 > n ? 256 : n)) * sizeof(double) +
+           (size_t)n * sizeof(int);
 }
+static inline bool lu_fwd_la(int n) { return lu_fwd_smem(n, true) <= 232448; }
 
 // Opt the kernels into the dynamic shared memory this network needs; called
 // once per handle, outside any stream capture.
 cudaError_t init_kernels(const DevNet &net) {
     size_t sr = rates_smem(net);
     const int n = net.ni;
-    size_t sl = lu_fwd_smem(n);
+    size_t sl = lu_fwd_smem(n, lu_fwd_la(n));
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_rates<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
     if ((e = cudaFuncSetAttribute(k_rates<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
-    if ((e = cudaFuncSetAttribute(k_lu_fwd_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl))) return e;
+    if ((e = lu_fwd_la(n) ? cudaFuncSetAttribute(k_lu_fwd_f64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl)
+                          : cudaFuncSetAttribute(k_lu_fwd_f64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl)))
+        return e;
     const int ssw = (int)sweep64_smem(n, 256, sweep64_nbuf(n));
     if ((e = cudaFuncSetAttribute(k_back_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, ssw))) return e;
     if ((e = cudaFuncSetAttribute(k_solve_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, ssw))) return e;
@@ -507,10 +523,15 @@ void launch_lu_fwd_f64(const DevNet &net, const DevBatch &b, const Work &w,
                        const double *rhs, double *z, int flags, cudaStream_t s) {
     (void)flags;
     const int n = net.ni;
-    size_t sm = lu_fwd_smem(n);
+    const bool la = lu_fwd_la(n);
+    size_t sm = lu_fwd_smem(n, la);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-    k_lu_fwd_f64<<<column_grid(b, VK_TUNE_LU64, 2), 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt, rhs, w.G, z,
-                                                    w.status);
+    if (la)
+        k_lu_fwd_f64<true><<<column_grid(b, VK_TUNE_LU64, 2), 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt,
+                                                                          rhs, w.G, z, w.status);
+    else
+        k_lu_fwd_f64<false><<<column_grid(b, VK_TUNE_LU64, 2), 256, sm, s>>>(net, b, w.jv, w.dA, w.dB, w.dC, w.dt,
+                                                                           rhs, w.G, z, w.status);
 }
 
 void launch_back_f64(const DevNet &net, const DevBatch &b, const double *G, const double *dB,

@@ -33,12 +33,37 @@ __device__ __forceinline__ void tile_coords(int &ty, int &tx) {
 
 }  // namespace
 
+// Biased IEEE exponent field of a double.
+__device__ __forceinline__ int bexp64(double v) {
+    return (int)((__double_as_longlong(v) >> 52) & 0x7ff);
+}
+// |v| as integer bits with NaN mapped to 0 (fmax ignores NaN operands).
+__device__ __forceinline__ long long absbits_nonan(double v) {
+    const long long a = __double_as_longlong(v) & 0x7fffffffffffffffll;
+    return a > 0x7ff0000000000000ll ? 0ll : a;
+}
+// v x 2^k by the exponent field when the result stays normal (exact, as the
+// FP64 product with a power of two is); returns false otherwise.
+__device__ __forceinline__ bool scale_pow2(double v, int k, double &out) {
+    const int E = bexp64(v);
+    if (E < 1 || E > 2046 || E + k < 1 || E + k > 2046) return false;
+    const long long bits = __double_as_longlong(v);
+    out = __longlong_as_double((bits & ~(0x7ffll << 52)) | ((long long)(E + k) << 52));
+    return true;
+}
+constexpr int kNoExp = -100000;        // "this row's scale has no exponent form"
+
 // Per-layer preparation for the FP32 factorisation (fully parallel over
 // layers): power-of-two row scales (row maxima of D_j) and column scales
-// (column maxima of R_j D_j) in FP64, and the dense scaled block R_j D_j S_j
-// rounded once to FP32, written with a 16-byte-aligned stride for TMA: rows of
-// ld floats, bstride floats per layer (ld = n for k_lu32's packed blocks; ld =
+// (column maxima of R_j D_j), and the dense scaled block R_j D_j S_j rounded
+// once to FP32, written with a 16-byte-aligned stride for TMA: rows of ld
+// floats, bstride floats per layer (ld = n for k_lu32's packed blocks; ld =
 // NP, the size rounded up to 16, for k_lu_tc's zero-padded NP x NP tiles).
+// The scales are exact powers of two, so maxima, exponents and the scaled
+// values are taken from the IEEE exponent fields with integer operations --
+// the FP64 pipe (about 1/60 of the FP32 rate on this chip) only adds the
+// diagonal and converts to FP32; values outside the normal range take the
+// FP64 expressions, which give the same results.
 __global__ void __launch_bounds__(256)
 k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
          const double *__restrict__ dt, float *__restrict__ D32, double *__restrict__ rsc,
@@ -52,54 +77,96 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
     double *rs = jls + nnz;                 // [n]
     double *cs = rs + n;                    // [n]
     double *dg = cs + n;                    // [n] c0 - dA
-    float *dense = reinterpret_cast<float *>(dg + n);   // [nn]
+    double *dd = dg + n;                    // [n] diagonal of D: -J_rr + c0 - dA_r
+    float *dense = reinterpret_cast<float *>(dd + n);   // [nn]
     int *cexp = reinterpret_cast<int *>(dense + nn);    // [n]
+    int *rexp = cexp + n;                   // [n] log2 rs (kNoExp: use rs)
+    int *cxp = rexp + n;                    // [n] log2 cs
     const int tid = threadIdx.x, nth = blockDim.x;
-    const double c0 = 1.0 / (R_ROS * dt[c]);
+    __shared__ double s_c0;
+    if (tid == 0) s_c0 = 1.0 / (R_ROS * dt[c]);     // one FP64 division per layer
     const double *jl = jv + (size_t)l * nnz;
     for (int e = tid; e < nnz; e += nth) jls[e] = jl[e];
     for (int e = tid; e < nn; e += nth) dense[e] = 0.0f;
-    for (int t = tid; t < n; t += nth) {
-        dg[t] = c0 - dA[(size_t)l * n + t];
-        cexp[t] = -100000;
-    }
+    for (int t = tid; t < n; t += nth) cexp[t] = kNoExp;
     __syncthreads();
     for (int r = tid; r < n; r += nth) {
-        double m = fabs(dg[r]);
-        for (int e = net.jrowptr[r]; e < net.jrowptr[r + 1]; ++e) {
-            double v = jls[e] + (net.jcol[e] == r ? dg[r] : 0.0);
-            m = fmax(m, fabs(v));
-        }
-        rs[r] = pow2_scale_r(m);
+        dg[r] = s_c0 - dA[(size_t)l * n + r];
+        const int e = net.jmap[r * n + r];
+        dd[r] = e >= 0 ? jls[e] + dg[r] : dg[r];
     }
     __syncthreads();
+    // row scales: 2^-e with |max| in [2^(e-1), 2^e)  (frexp / ldexp)
+    for (int r = tid; r < n; r += nth) {
+        long long m = absbits_nonan(dg[r]);
+        for (int e = net.jrowptr[r]; e < net.jrowptr[r + 1]; ++e)
+            m = max(m, absbits_nonan(net.jcol[e] == r ? dd[r] : jls[e]));
+        const int E = (int)(m >> 52);
+        if (m == 0 || E == 2047) {              // no positive finite maximum
+            rs[r] = 1.0;
+            rexp[r] = 0;
+        } else if (E >= 1 && E <= 2044) {
+            rexp[r] = 1022 - E;
+            rs[r] = __longlong_as_double((long long)(1023 + 1022 - E) << 52);
+        } else {                                // subnormal or huge maximum
+            const double md = __longlong_as_double(m);
+            int ex;
+            frexp(md, &ex);
+            rs[r] = ldexp(1.0, -ex);
+            rexp[r] = kNoExp;
+        }
+    }
+    __syncthreads();
+    // column exponents of R_j D_j
     for (int e = tid; e < nnz + n; e += nth) {
         int r, q;
         double v;
         if (e < nnz) {
             r = net.jrow[e]; q = net.jcol[e];
-            v = jls[e] + (r == q ? dg[r] : 0.0);
+            v = r == q ? dd[r] : jls[e];
         } else {
             r = q = e - nnz;
             v = dg[r];
         }
-        v = fabs(v * rs[r]);
-        if (v > 0.0 && isfinite(v)) {
-            int ex;
-            frexp(v, &ex);
-            atomicMax(&cexp[q], ex);
+        if ((__double_as_longlong(v) & 0x7fffffffffffffffll) == 0) continue;    // v * rs = 0
+        const int E = bexp64(v), k = rexp[r];
+        if (k != kNoExp && E >= 1 && E <= 2046 && E + k >= 1 && E + k <= 2046) {
+            atomicMax(&cexp[q], E + k - 1022);
+        } else {
+            const double a = fabs(v * rs[r]);
+            if (a > 0.0 && isfinite(a)) {
+                int ex;
+                frexp(a, &ex);
+                atomicMax(&cexp[q], ex);
+            }
         }
     }
     __syncthreads();
-    for (int t = tid; t < n; t += nth) cs[t] = cexp[t] > -100000 ? ldexp(1.0, -cexp[t]) : 1.0;
-    __syncthreads();
-    for (int e = tid; e < nnz; e += nth) {
-        const int r = net.jrow[e], q = net.jcol[e];
-        const double v = jls[e] + (r == q ? dg[r] : 0.0);
-        dense[r * n + q] = (float)(rs[r] * v * cs[q]);
+    for (int t = tid; t < n; t += nth) {
+        cs[t] = cexp[t] > kNoExp ? ldexp(1.0, -cexp[t]) : 1.0;
+        cxp[t] = cexp[t] > kNoExp ? -cexp[t] : 0;
     }
-    for (int r = tid; r < n; r += nth)
-        if (net.jmap[r * n + r] < 0) dense[r * n + r] = (float)(rs[r] * dg[r] * cs[r]);
+    __syncthreads();
+    // dense scaled block: (rs v) cs rounded once to FP32
+    for (int e = tid; e < nnz + n; e += nth) {
+        int r, q;
+        double v;
+        if (e < nnz) {
+            r = net.jrow[e]; q = net.jcol[e];
+            v = r == q ? dd[r] : jls[e];
+        } else {
+            r = q = e - nnz;
+            if (net.jmap[r * n + r] >= 0) continue;     // the diagonal came with the Jacobian
+            v = dg[r];
+        }
+        const int k = rexp[r];
+        double t1, t2;
+        if (k != kNoExp && (__double_as_longlong(v) & 0x7fffffffffffffffll) != 0 &&
+            scale_pow2(v, k, t1) && scale_pow2(t1, cxp[q], t2))
+            dense[r * n + q] = __double2float_rn(t2);
+        else
+            dense[r * n + q] = (float)(rs[r] * v * cs[q]);
+    }
     __syncthreads();
     float *Dl = D32 + (size_t)l * bstride;
     if (ld == n) {
@@ -243,7 +310,7 @@ static int g_smem_optin = 0;         // opt-in shared memory per block of this d
 static int lu32_nbuf(int n) { return smem32(n, 2) <= (size_t)g_smem_optin ? 2 : 1; }
 static size_t smem_prep(const DevNet &net) {
     const int n = net.ni;
-    return (size_t)(net.nnz + 3 * n) * sizeof(double) + (size_t)n * n * sizeof(float) + n * sizeof(int) + 16;
+    return (size_t)(net.nnz + 4 * n) * sizeof(double) + (size_t)n * n * sizeof(float) + 3 * n * sizeof(int) + 16;
 }
 
 #define VK_LU_TILINGS(X) X(16, 3, 3) X(16, 5, 5) X(16, 7, 7) X(32, 5, 10)
@@ -252,7 +319,7 @@ static size_t smem_prep(const DevNet &net) {
 // VK_LU_TC is the tensor-core factorisation (vk_lutc.cu), up to 128 species
 static const int kTilingCap[4] = {48, 80, 112, 160};
 int lu32_tiling_cap(int t) {
-    if (t == VK_LU_TC) return 128;
+    if (t == VK_LU_TC || t == VK_LU_TC_COOP) return 128;
     return t >= 0 && t < 4 ? kTilingCap[t] : 0;
 }
 
@@ -287,13 +354,14 @@ void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaSt
     // default (-1): the tensor-core factorisation where it covers ni
     int t = b.lu32_tiling == -1 ? (lu_tc_supported(n) ? VK_LU_TC : tiling_of(n))
           : (b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n));
-    if (t == VK_LU_TC && !w.tmap_d32) t = tiling_of(n);   // no tile map: CUDA-core kernel
-    if (t == VK_LU_TC) {
+    const bool tc = t == VK_LU_TC || t == VK_LU_TC_COOP;
+    if (tc && !w.tmap_d32) t = tiling_of(n);              // no tile map: CUDA-core kernel
+    if (tc && w.tmap_d32) {
         const int NP = (n + 15) / 16 * 16;
         k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs,
                                                   NP, NP * NP);
         cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
-        launch_lu_tc(net, b, w, *static_cast<const CUtensorMap *>(w.tmap_d32), s);
+        launch_lu_tc(net, b, w, *static_cast<const CUtensorMap *>(w.tmap_d32), t == VK_LU_TC_COOP, s);
         return;
     }
     k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs,

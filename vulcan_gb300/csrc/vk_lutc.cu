@@ -53,7 +53,7 @@ constexpr int kLdGroup = 1;             // TMEM loads of 16 columns per wait (1:
 
 struct TcSmem {
     // byte offsets into the dynamic shared memory (base 128-byte aligned)
-    int dbuf, gs, ahi, alo, bhi, blo, pex, alpha, beta, perm, kinv, bars, tslot, total;
+    int dbuf, gs, ahi, alo, bhi, blo, pex, alpha, beta, perm, kinv, xch, bars, tslot, total;
 };
 
 __host__ __device__ inline int round_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -73,6 +73,7 @@ __host__ __device__ inline TcSmem tc_layout(int n) {
     s.beta = o;  o += round_up(NP * 4, 16);
     s.perm = o;  o += round_up(NP * 4, 16);
     s.kinv = o;  o += round_up(NP * 4, 16);
+    s.xch = o;   o += round_up((2 * 4 * 20 + 4) * 4, 16);   // cooperative panel: [2][4 warps][20] + 4
     s.bars = o;  o += 4 * 8;
     s.tslot = o; o += 16;
     s.total = o + 128;                   // slack for aligning the base
@@ -183,7 +184,93 @@ __device__ __forceinline__ void panel_eliminate(float (&P)[RA][kPW], unsigned &u
     __syncwarp();
 }
 
-template <int RA>
+// Gauss-Jordan on the panel by all four warps together: thread r holds row r
+// of the panel (P, 16 columns) in registers.  Step t pivots on slot t (no
+// rotation; the same values as panel_eliminate): every warp finds its
+// best candidate with one reduction of the packed |a|-and-row key, its
+// winning lane publishes its row and key in a per-step-parity slot, one block
+// barrier, and every thread takes the largest of the four keys and the
+// winner's row from shared memory.  The slots alternate by step parity, so a
+// step needs no second barrier (a warp writes slot t+2 only after every warp
+// has passed barrier t+1, that is after it has read slot t).  The rare steps
+// without a finite candidate (NaN / inf state) take two more barriers to find
+// the lowest unused row and fetch it.  All threads call it with the same w.
+__device__ __forceinline__ void panel_eliminate_coop(float (&P)[kPW], bool &used, int r, int lane,
+                                                     int warp, int k0, int w, int *perm, int *kinv,
+                                                     float *xch, int &stat) {
+#pragma unroll
+    for (int t = 0; t < kPW; ++t) {
+        if (t >= w) break;                        // uniform
+        const float v = fabsf(P[t]);
+        const unsigned key = (!used && v == v)
+            ? ((__float_as_uint(v) & ~127u) | (unsigned)(127 - (r & 127)) | 0x80000000u) : 0u;
+        const unsigned m = __reduce_max_sync(0xffffffffu, key);
+        float *slot = xch + ((t & 1) * 4 + warp) * 20;
+        if (m != 0u && key == m) {
+#pragma unroll
+            for (int q = 0; q < kPW; ++q) slot[q] = P[q];
+        }
+        if (lane == 0) reinterpret_cast<unsigned *>(slot)[16] = m;
+        __syncthreads();
+        const float *sl = xch + (t & 1) * 4 * 20;
+        unsigned M = 0;
+        int ws = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const unsigned ku = reinterpret_cast<const unsigned *>(sl + u * 20)[16];
+            if (ku > M) { M = ku; ws = u; }
+        }
+        int p;
+        const float *prow;
+        if (M == 0u || (M & 0x7fffffffu) >= 0x7f800000u) {
+            // no finite candidate: the lowest unused row, fetched from its owner
+            stat = 2;
+            const unsigned lw = __reduce_min_sync(0xffffffffu, used ? 0xffffffffu : (unsigned)r);
+            unsigned *mn = reinterpret_cast<unsigned *>(xch + 8 * 20);    // the spare words
+            if (lane == 0) mn[warp] = lw;
+            __syncthreads();
+            unsigned lo = 0xffffffffu;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) lo = min(lo, mn[u]);
+            p = lo == 0xffffffffu ? 0 : (int)lo;
+            float *fs = xch + (t & 1) * 4 * 20;      // the step's slot 0 is free again
+            __syncthreads();
+            if (r == p) {
+#pragma unroll
+                for (int q = 0; q < kPW; ++q) fs[q] = P[q];
+            }
+            __syncthreads();
+            prow = fs;
+        } else {
+            if (((M & 0x7fffff80u) == 0u) && stat == 0) stat = 1;
+            p = 127 - (int)(M & 127u);
+            prow = sl + ws * 20;
+        }
+        float rs[kPW];
+#pragma unroll
+        for (int q = 0; q < kPW; ++q) rs[q] = prow[q];
+        float pinv;
+        asm("rcp.approx.f32 %0, %1;" : "=f"(pinv) : "f"(rs[t]));
+#pragma unroll
+        for (int q = 0; q < kPW; ++q) if (q != t) rs[q] *= pinv;
+        const bool isp = r == p;
+        const float f = P[t];
+#pragma unroll
+        for (int q = 0; q < kPW; ++q) {
+            if (q == t) continue;
+            const float e = fmaf(-f, rs[q], P[q]);
+            P[q] = isp ? rs[q] : e;
+        }
+        P[t] = isp ? pinv : -f * pinv;
+        if (isp) {
+            used = true;
+            perm[k0 + t] = p;
+            kinv[p] = k0 + t;
+        }
+    }
+}
+
+template <int RA, bool COOP>
 __global__ void __launch_bounds__(128, 3)
 k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
         const double *__restrict__ dB, const double *__restrict__ dC,
@@ -205,6 +292,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
     float *beta = reinterpret_cast<float *>(smb + L.beta);   // [NP] Schur column factors
     int *perm = reinterpret_cast<int *>(smb + L.perm);       // [NP] pivot row of step k
     int *kinv = reinterpret_cast<int *>(smb + L.kinv);       // [NP] step of pivot row r
+    float *xch = reinterpret_cast<float *>(smb + L.xch);     // cooperative panel exchange
     uint64_t *bars = reinterpret_cast<uint64_t *>(smb + L.bars);   // [0] TMA, [1] MMA
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smb + L.tslot);
     __shared__ int s_col, s_stat, s_pw;
@@ -300,6 +388,39 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
             // ---- B: panels ----
             for (int k0 = 0; k0 < n && !failed; k0 += kPW) {
                 const int w = n - k0 < kPW ? n - k0 : kPW;
+                float Pc[kPW];                     // cooperative panel: this thread's row
+                if constexpr (COOP) {
+                    // B1+B2: every thread loads its row of the panel and the four
+                    // warps eliminate the panel's pivots together
+                    if (row_warp) tmem_ld16(tlane + k0, Pc);
+                    else {
+#pragma unroll
+                        for (int t = 0; t < kPW; ++t) Pc[t] = 0.f;
+                    }
+                    bool used = r >= n || kinv[r] < k0;   // padding or pivot of an earlier panel
+                    int stat = s_stat;
+                    __syncthreads();                      // s_stat read by all before it changes
+                    panel_eliminate_coop(Pc, used, r, lane, warp, k0, w, perm, kinv, xch, stat);
+                    if (tid == 0) s_stat = stat;
+                    __syncthreads();                      // perm / kinv of the panel visible
+                    // X = panel - S (hi / lo TF32) -> A operand, this thread's row
+                    if (r < n) {
+                        const int kr = kinv[r] - k0;
+#pragma unroll
+                        for (int t = 0; t < kPW; t += 4) {
+                            float xh[4], xl[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                float x = (t + e < w) ? Pc[t + e] - ((kr == t + e) ? 1.f : 0.f) : 0.f;
+                                xh[e] = to_tf32(x);
+                                xl[e] = to_tf32(x - xh[e]);
+                            }
+                            *reinterpret_cast<float4 *>(Ahi + op_off(r, t)) = make_float4(xh[0], xh[1], xh[2], xh[3]);
+                            *reinterpret_cast<float4 *>(Alo + op_off(r, t)) = make_float4(xl[0], xl[1], xl[2], xl[3]);
+                        }
+                    }
+                    fence_async_smem();
+                } else {
                 // B1: panel columns TMEM -> Pex
                 if (row_warp) {
                     float v[16];
@@ -348,6 +469,7 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
                     }
                     fence_async_smem();
                 }
+                }                                          // !COOP
                 __syncthreads();
                 // B3: pivot rows (pre-update) -> B operand; final panel -> TMEM
                 if (row_warp) {
@@ -377,7 +499,8 @@ k_lu_tc(DevNet net, DevBatch b, const __grid_constant__ CUtensorMap tmap_d,
                     }
                     float pv[16];
 #pragma unroll
-                    for (int t = 0; t < 16; ++t) pv[t] = r < n ? Pex[r * (kPW + 1) + t] : 0.f;
+                    for (int t = 0; t < 16; ++t)
+                        pv[t] = r < n ? (COOP ? Pc[t] : Pex[r * (kPW + 1) + t]) : 0.f;
                     tmem_st16(tlane + k0, pv);
                     tmem_wait_st();
                     fence_async_smem();
@@ -500,21 +623,25 @@ size_t lu_tc_smem(int n) { return (size_t)tc_layout(n).total; }
 cudaError_t init_lu_tc(int n) {
     if (!lu_tc_supported(n)) return cudaSuccess;
     const int sm = (int)lu_tc_smem(n);
-    cudaError_t e = cudaFuncSetAttribute(k_lu_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaError_t e = cudaFuncSetAttribute(k_lu_tc<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_lu_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        e = cudaFuncSetAttribute(k_lu_tc<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_lu_tc<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_lu_tc<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     return e;
 }
 
 void launch_lu_tc(const DevNet &net, const DevBatch &b, const Work &w, const CUtensorMap &map,
-                  cudaStream_t s) {
+                  bool coop, cudaStream_t s) {
     const int n = net.ni, NP = round_up(n, 16);
     const size_t sm = lu_tc_smem(n);
     const int grid = column_grid(b, VK_TUNE_LU32, 3);
-    if (NP <= 96)
-        k_lu_tc<3><<<grid, 128, sm, s>>>(net, b, map, w.dB, w.dC, w.rs, w.cs, w.G32, w.status);
-    else
-        k_lu_tc<4><<<grid, 128, sm, s>>>(net, b, map, w.dB, w.dC, w.rs, w.cs, w.G32, w.status);
+#define LAUNCH_TC(RA, CO) k_lu_tc<RA, CO><<<grid, 128, sm, s>>>(net, b, map, w.dB, w.dC, w.rs, w.cs, w.G32, w.status)
+    if (NP <= 96) { if (coop) LAUNCH_TC(3, true); else LAUNCH_TC(3, false); }
+    else          { if (coop) LAUNCH_TC(4, true); else LAUNCH_TC(4, false); }
+#undef LAUNCH_TC
 }
 
 }  // namespace vk

@@ -40,7 +40,13 @@ constexpr double kRouteMargin = 0.25;   // FP64 from dt >= kRouteMargin x the fa
 // Iterative refinement of A x = b with the FP32 factors (one column at a time
 // per CTA, columns from the work queue).
 // The inverse blocks G~_j stream into shared memory by TMA (double-buffered)
-// in the order the sweeps visit them: forward 0..nz-1, back nz-2..0.
+// in the order the sweeps visit them: forward 0..nz-1, back nz-2..0.  A
+// visit is FP32 only -- the product with G~_j, whose row r also yields row r
+// of the next visit's input (one fma with the precomputed scaled coupling),
+// so a visit costs one block barrier; everything in FP64 (the couplings, the
+// scaled residual, x += S x~ and the correction size of the convergence
+// test, the residual b - A x) runs in parallel passes over the whole column
+// between the sweeps, off the chain of dependent visits.
 // yscale (may be NULL) widens the convergence floor: k1/k2 enter sol next to y.
 __global__ void __launch_bounds__(256)
 k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__restrict__ rsc,
@@ -48,7 +54,9 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
          const double *__restrict__ dA, const double *__restrict__ dB,
          const double *__restrict__ dC, const double *__restrict__ dt,
          const double *__restrict__ rhs, double *__restrict__ x, double *__restrict__ res,
-         float *__restrict__ zf, const double *__restrict__ yscale, double *__restrict__ yk2,
+         float *__restrict__ zf, float *__restrict__ wcf, float *__restrict__ wcb,
+         float *__restrict__ raf, float *__restrict__ xf,
+         const double *__restrict__ yscale, double *__restrict__ yk2,
          const double *__restrict__ y, int max_sweeps, double tol, int *__restrict__ fallback,
          int *__restrict__ sweeps_out, int *__restrict__ status, double *__restrict__ err_out,
          double *__restrict__ thr64, int *act32, int *__restrict__ failed) {
@@ -56,8 +64,7 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
     const int n = net.ni, NNP = block_stride32(n);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smr);           // [2]
     float *Gbuf = reinterpret_cast<float *>(smr + 16);           // [2][NNP]
-    float *vin = Gbuf + 2 * NNP;                                 // [n]
-    float *vout = vin + n;                                       // [n]
+    float *vin = Gbuf + 2 * NNP;                                 // [2][n] visit inputs
     __shared__ double red[8];
     __shared__ int s_col;
     const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
@@ -87,69 +94,52 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 tma_load_1d(Gbuf + buf * NNP, G32 + ((size_t)l0 + layer_of(v)) * NNP, bytes, &bar[buf]);
             ++issued;
         };
+        // x = 0, r = b; the scaled couplings of the sweeps (FP32: they feed
+        // the FP32 preconditioner) and the scaled first residual.  The
+        // column-wide passes are unrolled so several elements' global loads
+        // are in flight per thread.
+#pragma unroll 4
         for (int e = tid; e < nz * n; e += nth) {
-            x[base + e] = 0.0;
-            res[base + e] = rhs[base + e];
+            const size_t g = base + e;
+            const int j = e / n;
+            x[g] = 0.0;
+            res[g] = rhs[g];
+            raf[g] = (float)(rsc[g] * rhs[g]);
+            wcf[g] = j > 0 ? (float)(rsc[g] * dC[g] * csc[g - n]) : 0.f;
+            wcb[g] = j < nz - 1 ? (float)(rsc[g] * dB[g] * csc[g + n]) : 0.f;
         }
         __syncthreads();
         issue(0);
         int sweep = 0, converged = 0, timed_out = 0;
         double m_prev = INFINITY;
-        // per-layer vectors of a visit, loaded into registers one visit ahead
-        // (the sweeps are a chain of dependent visits: nothing else hides the
-        // global-memory latency)
-        struct Visit { double rsc, a, bc, cscn, csc, x, ys, n0; float zf; };
+        // per-row vectors of a visit (the row's coupling, scaled residual and
+        // forward result), loaded into registers one visit ahead
+        struct Visit { float w, ra, zf; };
+        const bool rowt = mrow < n;          // this thread works on row mrow
         auto fetch = [&](int v) {
-            Visit q{0, 0, 0, 0, 0, 0, 0, 0, 0.f};
-            const int j = layer_of(v);
-            const size_t l = (size_t)l0 + j;
-            const bool fwd = v < nz;
-            if (tid < n) {
-                const size_t e = l * n + tid;
-                q.rsc = rsc[e];
-                if (fwd) {
-                    q.a = res[e];
-                    if (j > 0) { q.bc = dC[e]; q.cscn = csc[e - n]; }
-                } else {
-                    q.bc = dB[e];
-                    q.cscn = csc[e + n];
-                }
-                if (!fwd || j == nz - 1) {
-                    q.csc = csc[e];
-                    q.x = x[e];
-                    q.ys = yscale ? fabs(yscale[e]) : 0.0;
-                    q.n0 = b.atm[l * VK_ATM_NF + VK_ATM_N0];
-                }
+            Visit q{0.f, 0.f, 0.f};
+            const size_t e = ((size_t)l0 + layer_of(v)) * n + mrow;
+            if (rowt) {
+                if (v < nz) { q.w = wcf[e]; q.ra = raf[e]; }
+                else { q.w = wcb[e]; q.zf = zf[e]; }
             }
-            if (!fwd && mrow < n && mhalf == 0) q.zf = zf[l * n + mrow];
             return q;
         };
+        int p = 0;                           // vin buffer of the current visit
         for (; sweep < max_sweeps && !converged && !timed_out; ++sweep) {
-            // largest |d| / sc of the sweep as a fraction (num, den): compared by
-            // cross-multiplication, divided once per thread after the sweep
-            // (FP64 divisions are long FP64-pipe sequences on this chip)
-            double dnum = 0.0, dden = 1.0;
             Visit cur = fetch(0);
+            if (rowt && mhalf == 0) vin[p * n + mrow] = cur.ra;     // layer 0: z~_0 = G~_0 R_0 r_0
             for (int v = 0; v < per_sweep; ++v) {
                 const int j = layer_of(v);
                 const size_t l = (size_t)l0 + j;
                 const bool fwd = v < nz;
                 Visit nxt = cur;
                 if (v + 1 < per_sweep) nxt = fetch(v + 1);
-                // right-hand side of this visit
-                if (tid < n) {
-                    double vi;
-                    if (fwd) {
-                        vi = cur.rsc * cur.a;
-                        if (j > 0) vi += cur.rsc * cur.bc * cur.cscn * (double)vout[tid];
-                    } else {
-                        vi = cur.rsc * cur.bc * cur.cscn * (double)vout[tid];
-                    }
-                    vin[tid] = (float)vi;
-                }
                 const int buf = consumed & 1;
                 const bool ok = mbar_wait(&bar[buf], (consumed >> 1) & 1);
                 ++consumed;
+                // one block barrier per visit: the block has landed and every
+                // row's input (written by its row thread last visit) is visible
                 if (__syncthreads_or(!ok)) {
                     --consumed;                  // still in flight: drained below
                     timed_out = 1;
@@ -159,46 +149,54 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 if (v + 1 < per_sweep) issue(v + 1);
                 else if (sweep + 1 < max_sweeps) issue(0);
                 const float *G = Gbuf + buf * NNP;
+                const float *xin = vin + p * n;
                 // matvec: tpr adjacent lanes per row, interleaved columns
                 float sacc = 0.0f;
-                if (mrow < n) {
+                if (rowt) {
                     float s0 = 0.0f, s1 = 0.0f;
                     const float *row = G + mrow * n;
                     int q = mhalf;
                     for (; q + tpr < n; q += 2 * tpr) {
-                        s0 = fmaf(row[q], vin[q], s0);
-                        s1 = fmaf(row[q + tpr], vin[q + tpr], s1);
+                        s0 = fmaf(row[q], xin[q], s0);
+                        s1 = fmaf(row[q + tpr], xin[q + tpr], s1);
                     }
-                    if (q < n) s0 = fmaf(row[q], vin[q], s0);
+                    if (q < n) s0 = fmaf(row[q], xin[q], s0);
                     sacc = s0 + s1;
                 }
                 if (tpr == 2) sacc += __shfl_xor_sync(0xffffffffu, sacc, 1);
-                if (mrow < n && mhalf == 0) {
-                    if (fwd) {
-                        zf[l * n + mrow] = sacc;
-                    } else {
-                        sacc += cur.zf;
-                    }
-                    vout[mrow] = sacc;
+                if (rowt && mhalf == 0) {
+                    if (fwd) zf[l * n + mrow] = sacc;
+                    else sacc += cur.zf;
+                    // the back sweep's result (it starts at the top layer:
+                    // x~_{nz-1} = z~_{nz-1}), applied to x after the sweep
+                    if (!fwd || j == nz - 1) xf[l * n + mrow] = sacc;
+                    // the next visit's input row: a coupling times this row's
+                    // result (+ the scaled residual going forward)
+                    if (v + 1 < per_sweep)
+                        vin[(p ^ 1) * n + mrow] = (v + 1 < nz) ? fmaf(nxt.w, sacc, nxt.ra) : nxt.w * sacc;
                 }
-                __syncthreads();
-                // the back sweep starts at the top layer: x~_{nz-1} = z~_{nz-1} (vout)
-                if ((fwd && j == nz - 1) || !fwd) {
-                    if (tid < n) {
-                        const size_t e = l * n + tid;
-                        const double d = cur.csc * (double)vout[tid];
-                        const double xn = cur.x + d;
-                        x[e] = xn;
-                        const double sc = fabs(xn) + cur.ys + 1e-10 * cur.n0;
-                        const double ad = fabs(d);
-                        if (!isfinite(d)) { dnum = INFINITY; dden = 1.0; }
-                        else if (ad * dden > dnum * sc) { dnum = ad; dden = sc; }
-                    }
-                }
-                __syncthreads();
+                p ^= 1;
                 cur = nxt;
             }
             if (timed_out) break;
+            __syncthreads();                     // the last visit's results are visible
+            // x += S x~ and the largest |d| / (|x| + |yscale| + 1e-10 n_0) of
+            // the sweep, kept as a fraction (num, den) compared by
+            // cross-multiplication and divided once per thread (FP64 divisions
+            // are long FP64-pipe sequences on this chip)
+            double dnum = 0.0, dden = 1.0;
+#pragma unroll 4
+            for (int e = tid; e < nz * n; e += nth) {
+                const size_t g = base + e;
+                const double d = csc[g] * (double)xf[g];
+                const double xn = x[g] + d;
+                x[g] = xn;
+                const double n0 = b.atm[(size_t)(l0 + e / n) * VK_ATM_NF + VK_ATM_N0];
+                const double sc = fabs(xn) + (yscale ? fabs(yscale[g]) : 0.0) + 1e-10 * n0;
+                const double ad = fabs(d);
+                if (!isfinite(d)) { dnum = INFINITY; dden = 1.0; }
+                else if (ad * dden > dnum * sc) { dnum = ad; dden = sc; }
+            }
             double dmax = dnum / dden;
             for (int o = 16; o; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
             if (lane == 0) red[warp] = dmax;
@@ -212,7 +210,9 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
             if (!(m <= m_prev) && sweep >= 2) break;        // diverging: leave to the FP64 path
             m_prev = m;
             if (converged) break;
-            // residual r = b - A x  (FP64, matrix-free; every (layer, species) at once)
+            // residual r = b - A x  (FP64, matrix-free; every (layer, species)
+            // at once) and its scaled FP32 copy for the next sweep
+#pragma unroll 2
             for (int q = tid; q < nz * n; q += nth) {
                 const int j = q / n, sp = q - j * n;
                 const size_t l = (size_t)l0 + j;
@@ -222,7 +222,9 @@ k_refine(DevNet net, DevBatch b, const float *__restrict__ G32, const double *__
                 for (int k = net.jrowptr[sp]; k < net.jrowptr[sp + 1]; ++k) ax += jl[k] * x[l * n + net.jcol[k]];
                 if (j > 0) ax -= dC[e] * x[e - n];
                 if (j < nz - 1) ax -= dB[e] * x[e + n];
-                res[e] = rhs[e] - ax;
+                const double r = rhs[e] - ax;
+                res[e] = r;
+                raf[e] = (float)(rsc[e] * r);
             }
             __syncthreads();
         }
@@ -275,9 +277,9 @@ __global__ void k_route(DevBatch b, const double *__restrict__ dt, const double 
     failed[c] = 0;
 }
 
-__global__ void k_reset_route(int ncols, double *__restrict__ thr64) {
+__global__ void k_reset_route(int ncols, double *__restrict__ thr64, double route_dt0) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < ncols) thr64[c] = INFINITY;
+    if (c < ncols) thr64[c] = route_dt0;
 }
 
 void launch_route(const DevBatch &b, const Work &w, cudaStream_t s) {
@@ -285,8 +287,8 @@ void launch_route(const DevBatch &b, const Work &w, cudaStream_t s) {
                                                    w.failed);
 }
 
-void launch_reset_route(const Work &w, int ncols, cudaStream_t s) {
-    if (w.thr64) k_reset_route<<<(ncols + 127) / 128, 128, 0, s>>>(ncols, w.thr64);
+void launch_reset_route(const Work &w, int ncols, double route_dt0, cudaStream_t s) {
+    if (w.thr64) k_reset_route<<<(ncols + 127) / 128, 128, 0, s>>>(ncols, w.thr64, route_dt0);
 }
 
 cudaError_t init_mixed_kernels(int n) {
@@ -301,7 +303,8 @@ void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const do
     size_t sm = 16 + (size_t)2 * block_stride32(n) * sizeof(float) + 2 * n * sizeof(float);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
     k_refine<<<column_grid(b, VK_TUNE_REFINE, 3), 256, sm, s>>>(net, b, w.G32, w.rs, w.cs, w.jv, w.dA, w.dB, w.dC, w.dt,
-                                      rhs, x, w.r, w.zf, yscale, yk2, w.y, max_sweeps, tol,
+                                      rhs, x, w.r, w.zf, w.wcf, w.wcb, w.raf, w.xf, yscale, yk2, w.y,
+                                      max_sweeps, tol,
                                       w.fallback, w.sweeps, w.status, w.refine_err, w.thr64,
                                       w.act32, w.failed);
 }

@@ -394,6 +394,11 @@ class Ros2Handle:
         check(lib().vk_get_refine_stats(self.h, C.byref(a), C.byref(b)), self.h)
         return a.value, b.value
 
+    def set_route(self, dt0):
+        """Mixed precision: FP64 from step size dt0 on (until a failed
+        refinement lowers a column's limit); inf restores the default."""
+        check(lib().vk_set_route(self.h, float(dt0)), self.h)
+
     def set_precision(self, precision, max_refine=6, refine_tol=1e-10):
         check(lib().vk_set_precision(self.h, int(precision), int(max_refine), float(refine_tol)), self.h)
 
