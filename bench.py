@@ -464,7 +464,9 @@ def converge_block(args):
         sst = {}
         out, wall = batch.run_stream(net, items, ATOMS, nslots=min(NCOLS, len(items)), ctrl=ctrl,
                                      precision=prec, slot_cap=200, chunk=args.chunk_stream,
-                                     budget_s=left, keep_state=True, stats=sst)
+                                     budget_s=left, keep_state=True, stats=sst,
+                                     chunk_attempts=args.chunk_attempts or None,
+                                     route_dt0=args.route_dt if prec == 1 else None)
         wall = time.perf_counter() - t0
         conv = [i for i, r in out.items() if r['end_case'] == 1]
         steps = sorted(out[i]['count'] for i in conv)
@@ -499,11 +501,15 @@ def converge_block(args):
         res['learned_mixed']['columns_per_hour_over_fp64'] = round(
             res['learned_mixed']['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
     res['setup'] = ('a stream of %d seeded columns through %d slots (continuous batching: a slot '
-                    'whose column ends takes the next one), %.0f s of wall time per path '
-                    'including the learned proposals and their judge (the residual of the Ros2 '
-                    'system, vk_rhs); count_max %d; the reference convergence test; columns per '
-                    'hour = converged columns / wall' % (args.stream_cols, NCOLS,
-                                                         args.converge_budget, args.count_max))
+                    'whose column ends takes the next one, checked every %s), %.0f s of wall time '
+                    'per path including the learned proposals and their judge (the residual of the '
+                    'Ros2 system, vk_rhs); learned+mixed: FP32 factors below dt = %g s, FP64 above '
+                    '(vk_set_route); count_max %d; the reference convergence test; columns per '
+                    'hour = converged columns / wall' % (
+                        args.stream_cols, NCOLS,
+                        ('%d attempts of the batch' % args.chunk_attempts) if args.chunk_attempts
+                        else ('%d steps of every column' % args.chunk_stream),
+                        args.converge_budget, args.route_dt, args.count_max))
     return res
 
 
@@ -838,7 +844,15 @@ def main():
     ap.add_argument('--stream-cols', type=int, default=1536,
                     help='default run: columns streamed through the 512 slots per path')
     ap.add_argument('--chunk-stream', type=int, default=20,
-                    help='steps between refills of the streamed slots')
+                    help='steps between refills of the streamed slots (with --chunk-attempts 0)')
+    ap.add_argument('--chunk-attempts', type=int, default=24,
+                    help='attempts of the batch between refills of the streamed slots '
+                         '(vk_run_budget; 0: refill every --chunk-stream steps of every column)')
+    ap.add_argument('--route-dt', type=float, default=1e-6,
+                    help='learned+mixed stream: step size from which attempts go straight to FP64 '
+                         '(vk_set_route; inf: only after a failed refinement).  Columns started '
+                         'near steady state fail FP32-preconditioned refinement from dt ~1e-6 s on, '
+                         'and a failed refinement costs the mixed work plus a serial FP64 redo')
     ap.add_argument('--converge-budget', type=float, default=180.0,
                     help='default run: wall seconds per path for the columns-to-steady-state '
                          'measurement (0: skip)')

@@ -121,6 +121,15 @@ VK_API int  vk_network_compile(const vk_network_desc *desc, vk_network **out);
 VK_API int  vk_network_info(const vk_network *net, int *nnz_jac, int *n_dterm, int *n_src);
 /* Jacobian sparsity: row and column of each stored entry (arrays of nnz_jac) */
 VK_API int  vk_network_jac_pattern(const vk_network *net, int *rows, int *cols);
+/* Diagnostic: one layer's chemical source (the generated chemdf) and its -J
+ * entries (neg_symjac, in vk_network_jac_pattern order) evaluated on the host
+ * from the compiled gather tables with the rate kernel's own operations and
+ * order -- for checking the tables without a GPU.  y [ni], k [2*npair]
+ * (forward/reverse per pair), M the layer's total number density; either
+ * output may be NULL.  The reference's counterparts: chem_funs.chemdf and
+ * neg_symjac generated by make_chem_funs.py:113-430, 686-717. */
+VK_API int  vk_network_eval_host(const vk_network *net, const double *y, const double *k, double M,
+                                 double *dydt, double *neg_jac);
 VK_API void vk_network_free(vk_network *net);
 
 /* ---- handle ---- */
@@ -201,6 +210,14 @@ VK_API int  vk_set_conv_ignore(vk_handle *h, const int *conv_ignore);
  * column have been taken in this call (0 = no cap).  dt/t/count live on the
  * device; the loop is captured once into a CUDA graph and replayed. */
 VK_API int  vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s);
+/* vk_run with an attempt budget as well: the call also returns once the
+ * batch has made max_attempts attempts (rounded up to the graph's 8; 0 = no
+ * budget), the columns keeping their state for the next call.  For
+ * continuous batching: a column whose steps need many rejected attempts
+ * then holds the batch for at most the budget, while the others' slots are
+ * refilled between calls.  Same loop as op.py:808-936 per column. */
+VK_API int  vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, int max_attempts,
+                          double timeout_s);
 
 /* Per-column state read-back: y/ymix [L][ni]; the scalar arrays are [ncols]
  * (NULL to skip).  end_case: 0 running, 1 converged, 2 runtime, 3 count_max,
@@ -261,7 +278,8 @@ VK_API int  vk_compute_k(vk_handle *h);
  * factorisation (tcgen05, blocks up to 128 species) with one warp eliminating
  * each 16-pivot panel, or 5: the same with the four warps of its CTA
  * eliminating the panel together (identical factors) (-1: the default for
- * ni; a variant smaller than ni is refused), ignored otherwise.
+ * ni, variant 5 up to 128 species; a variant smaller than ni is refused),
+ * ignored otherwise.
  * A change drops the captured vk_run graph, which is captured again. */
 #define VK_TUNE_LU32    0   /* k_lu32: FP32 block-Thomas factorisation        */
 #define VK_TUNE_LU64    1   /* k_lu_fwd_f64: FP64 factorisation + first sweep */

@@ -67,8 +67,8 @@ def test_tensor_core_factors_match_cuda_core_factors(tag, ns):
 
 def test_tensor_core_is_the_default_up_to_128_species():
     """Without a launch setting the mixed path factorises on the tensor cores
-    (variant -1 resolves to it for ni <= 128): its factors equal an explicit
-    variant-4 run bit for bit."""
+    (variant -1 resolves to the cooperative-panel variant 5 for ni <= 128):
+    its factors equal an explicit variant-4 run bit for bit."""
     from test_gpu_parity import make_handle
     from vulcan_gb300 import capi
     g, net, gn, h, b = make_handle('c2', ns=[0, 1], precision=1)

@@ -55,18 +55,21 @@ def test_slotted_layout_matches_packed(precision):
     np.testing.assert_array_equal(t0, t1)
 
 
-@pytest.mark.parametrize('precision', [0, 1])
-def test_refilled_column_runs_as_in_its_own_batch(precision):
+@pytest.mark.parametrize('precision,chunk_attempts', [(0, None), (1, None), (0, 16), (1, 16)])
+def test_refilled_column_runs_as_in_its_own_batch(precision, chunk_attempts):
     """Three columns through two slots (count_max 60, so the first two end
     together and the third is refilled into a slot they left): every column's
-    final state, step count and time equal those of the column alone."""
+    final state, step count and time equal those of the column alone -- with
+    refills every 20 steps, and every 16 attempts of the batch
+    (vk_run_budget: a run that stops mid-step resumes exactly)."""
     from vulcan_gb300 import batch, configs
     from vulcan_gb300.solver import ctrl_from
     net, items = _items(3, seed=5)
     ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
     ctrl.count_max = 60
     res, wall = batch.run_stream(net, items, ATOMS, nslots=2, ctrl=ctrl, precision=precision,
-                                 slot_cap=100, chunk=20, keep_state=True)
+                                 slot_cap=100, chunk=20, keep_state=True,
+                                 chunk_attempts=chunk_attempts)
     assert sorted(res) == [0, 1, 2]
     for i, it in enumerate(items):
         h, b = batch.make_batch_handle(net, [it], ATOMS, precision)

@@ -66,7 +66,8 @@ def make_batch_handle(net, items, atom_list, precision=capi.VK_PREC_FP64, slot_c
 
 
 def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64, slot_cap=None,
-               chunk=20, budget_s=None, keep_state=False, stats=None, route_dt0=None):
+               chunk=20, budget_s=None, keep_state=False, stats=None, route_dt0=None,
+               chunk_attempts=None):
     """Continuous batching: the column items (build_items order) stream
     through nslots slots of one handle; every `chunk` steps the slots whose
     column has ended (converged, count_max, runtime, error) take the next
@@ -75,7 +76,10 @@ def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64,
     from its own start, exactly as in a batch of its own.  Stops when every
     item has ended or after budget_s seconds of wall time.  route_dt0 (mixed
     precision): the step size from which attempts go straight to FP64
-    (vk_set_route).
+    (vk_set_route).  chunk_attempts: refill after that many attempts of the
+    batch (vk_run_budget) instead of after `chunk` steps of every column, so
+    a column whose steps need many rejected attempts does not hold the
+    others' slots idle.
 
     Returns (results, wall_s): results[i] = dict(end_case, count, t, wall_s
     at which it ended[, y, ymix]) for every item that ended.  A dict passed as
@@ -101,7 +105,11 @@ def run_stream(net, items, atom_list, nslots, ctrl, precision=capi.VK_PREC_FP64,
             if left is not None and left <= 0:
                 break
             try:
-                h.run(ctrl, max_steps=chunk, timeout_s=max(left, 1.0) if left is not None else 0.0)
+                tmo = max(left, 1.0) if left is not None else 0.0
+                if chunk_attempts:
+                    h.run(ctrl, max_steps=0, timeout_s=tmo, max_attempts=chunk_attempts)
+                else:
+                    h.run(ctrl, max_steps=chunk, timeout_s=tmo)
             except _capi.VkError as e:
                 if e.code != _capi.VK_ETIMEOUT:
                     raise

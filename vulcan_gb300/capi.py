@@ -30,11 +30,11 @@ _ERRNAMES = {1: 'VK_EINVAL', 2: 'VK_ECUDA', 3: 'VK_ESINGULAR', 4: 'VK_ENAN',
              5: 'VK_EMAXATTEMPT', 6: 'VK_ETIMEOUT', 7: 'VK_ENOMEM'}
 
 # Every entry point include/vk_ros2.h declares.
-EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern',
+EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern', 'vk_network_eval_host',
            'vk_network_free', 'vk_create', 'vk_destroy', 'vk_last_error',
            'vk_set_precision', 'vk_set_route', 'vk_set_columns', 'vk_update_state', 'vk_update_atm',
            'vk_update_k', 'vk_ros2_attempt', 'vk_set_atom_ini', 'vk_set_column_info',
-           'vk_run', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
+           'vk_run', 'vk_run_budget', 'vk_get_state', 'vk_set_clock', 'vk_get_counters', 'vk_get_timing',
            'vk_network_last_error', 'vk_chem_source', 'vk_get_lhs',
            'vk_block_solve_noalloc', 'vk_get_refine_stats', 'vk_mlp_forward',
            'vk_mlp_backward', 'vk_mlp_adam', 'vk_get_conv', 'vk_set_rate_params',
@@ -89,6 +89,7 @@ def lib(path=None):
         'vk_network_compile': (i, [P(VkNetworkDesc), P(vp)]),
         'vk_network_info': (i, [vp, pi, pi, pi]),
         'vk_network_jac_pattern': (i, [vp, pi, pi]),
+        'vk_network_eval_host': (i, [vp, P(C.c_double), P(C.c_double), d, P(C.c_double), P(C.c_double)]),
         'vk_network_free': (None, [vp]),
         'vk_network_last_error': (C.c_char_p, []),
         'vk_create': (i, [vp, i, i, i, P(vp)]),
@@ -109,6 +110,7 @@ def lib(path=None):
         'vk_set_columns_slotted': (i, [vp, i, i, pi, pd, pd, pd, pd, pd, pd]),
         'vk_refill': (i, [vp, i, pi, pi, pd, pd, pd, pd, pd, pd, pd, pi, pi]),
         'vk_run': (i, [vp, P(VkCtrl), i, d]),
+        'vk_run_budget': (i, [vp, P(VkCtrl), i, i, d]),
         'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
         'vk_set_clock': (i, [vp, pd, pd, pi]),
         'vk_get_counters': (i, [vp, pi]),

@@ -1140,6 +1140,12 @@ static vk::RunCtrl to_run_ctrl(const vk_ctrl *c, int max_steps) {
 static const int kGraphAttempts = 8;
 
 extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s) {
+    return vk_run_budget(h, ctrl, max_steps, 0, timeout_s);
+}
+
+extern "C" int vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, int max_attempts,
+                             double timeout_s) {
+    if (max_attempts < 0) return fail(h, VK_EINVAL, "max_attempts must be >= 0");
     int rc = need_batch(h);
     if (rc) return rc;
     if (!ctrl) return fail(h, VK_EINVAL, "ctrl is NULL");
@@ -1197,13 +1203,16 @@ extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double t
     auto t0 = std::chrono::steady_clock::now();
     cudaEventRecord(h->ev[0], s);
     int launches = 0;
-    for (;;) {
+    // an attempt budget ends the call after that many attempts of the batch
+    // (whole graph replays), whatever each column's step count
+    const int max_replays = max_attempts > 0 ? (max_attempts + kGraphAttempts - 1) / kGraphAttempts : 0;
+    for (int replay = 1;; ++replay) {
         VK_CUDA(h, cudaGraphLaunch(h->gexec, s));
         launches += kGraphAttempts * (h->precision == VK_PREC_MIXED ? 17 : 7) + 1;
         int nact = 0;
         VK_CUDA(h, cudaMemcpyAsync(&nact, h->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
         VK_CUDA(h, cudaStreamSynchronize(s));
-        if (nact == 0) break;
+        if (nact == 0 || (max_replays > 0 && replay >= max_replays)) break;
         double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (timeout_s > 0 && el > timeout_s) {
             h->launches = launches;

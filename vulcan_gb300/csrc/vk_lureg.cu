@@ -53,6 +53,20 @@ __device__ __forceinline__ bool scale_pow2(double v, int k, double &out) {
 }
 constexpr int kNoExp = -100000;        // "this row's scale has no exponent form"
 
+// The FP64 expressions for values outside the normal range, as calls so the
+// compiler branches around them instead of evaluating them for every element
+// and selecting (they are FP64-pipe work).
+__device__ __noinline__ int frexp_of_scaled(double v, double rs) {
+    const double a = fabs(v * rs);
+    if (!(a > 0.0) || !isfinite(a)) return kNoExp;
+    int ex;
+    frexp(a, &ex);
+    return ex;
+}
+__device__ __noinline__ float scaled_f32(double rs, double v, double cs) {
+    return (float)(rs * v * cs);
+}
+
 // Per-layer preparation for the FP32 factorisation (fully parallel over
 // layers): power-of-two row scales (row maxima of D_j) and column scales
 // (column maxima of R_j D_j), and the dense scaled block R_j D_j S_j rounded
@@ -133,12 +147,8 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
         if (k != kNoExp && E >= 1 && E <= 2046 && E + k >= 1 && E + k <= 2046) {
             atomicMax(&cexp[q], E + k - 1022);
         } else {
-            const double a = fabs(v * rs[r]);
-            if (a > 0.0 && isfinite(a)) {
-                int ex;
-                frexp(a, &ex);
-                atomicMax(&cexp[q], ex);
-            }
+            const int ex = frexp_of_scaled(v, rs[r]);
+            if (ex != kNoExp) atomicMax(&cexp[q], ex);
         }
     }
     __syncthreads();
@@ -160,12 +170,14 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
             v = dg[r];
         }
         const int k = rexp[r];
+        const long long vb = __double_as_longlong(v);
         double t1, t2;
-        if (k != kNoExp && (__double_as_longlong(v) & 0x7fffffffffffffffll) != 0 &&
-            scale_pow2(v, k, t1) && scale_pow2(t1, cxp[q], t2))
+        if ((vb & 0x7fffffffffffffffll) == 0)             // +-0 stays +-0
+            dense[r * n + q] = __int_as_float((int)((unsigned long long)vb >> 32) & (int)0x80000000);
+        else if (k != kNoExp && scale_pow2(v, k, t1) && scale_pow2(t1, cxp[q], t2))
             dense[r * n + q] = __double2float_rn(t2);
         else
-            dense[r * n + q] = (float)(rs[r] * v * cs[q]);
+            dense[r * n + q] = scaled_f32(rs[r], v, cs[q]);
     }
     __syncthreads();
     float *Dl = D32 + (size_t)l * bstride;
@@ -351,8 +363,9 @@ void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaSt
     const int n = net.ni;
     // vk_set_launch may pick a larger tiling than the smallest covering ni;
     // every tiling zero-pads the rows and columns beyond ni
-    // default (-1): the tensor-core factorisation where it covers ni
-    int t = b.lu32_tiling == -1 ? (lu_tc_supported(n) ? VK_LU_TC : tiling_of(n))
+    // default (-1): the tensor-core factorisation where it covers ni, with the
+    // four warps sharing each panel
+    int t = b.lu32_tiling == -1 ? (lu_tc_supported(n) ? VK_LU_TC_COOP : tiling_of(n))
           : (b.lu32_tiling >= tiling_of(n) ? b.lu32_tiling : tiling_of(n));
     const bool tc = t == VK_LU_TC || t == VK_LU_TC_COOP;
     if (tc && !w.tmap_d32) t = tiling_of(n);              // no tile map: CUDA-core kernel

@@ -13,6 +13,7 @@
 //             chemistry Jacobian the list of (w, stoichiometry) to gather.
 // All tables are gathers, so the device kernels are deterministic (no atomics).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <new>
@@ -255,6 +256,58 @@ extern "C" int vk_network_jac_pattern(const vk_network *n, int *rows, int *cols)
     if (!n || !rows || !cols) return VK_EINVAL;
     std::copy(n->jrow.begin(), n->jrow.end(), rows);
     std::copy(n->jcol.begin(), n->jcol.end(), cols);
+    return VK_OK;
+}
+
+// Host evaluation of the gather form, term for term in the order and with the
+// FP64 operations the rate kernel uses (k_rates, vk_kernels.cu): the pair
+// rates in written order, the source gather as fma with the power-of-two
+// coefficients and the extra product slots, the derivative half terms and the
+// Jacobian gather.  A diagnostic, so the tables can be checked without a GPU.
+static double side_value(double kk, const PairDesc &pd, int side, const double *y, double M) {
+    double v = kk;
+    for (int t = 0; t < pd.nt[side]; ++t) {
+        const int s = pd.tsp[side][t];
+        const double f = s < 0 ? M : y[s];
+        double p = f;
+        for (int i = 1; i < pd.tnu[side][t]; ++i) p = p * f;
+        v = v * p;
+    }
+    return v;
+}
+
+extern "C" int vk_network_eval_host(const vk_network *n, const double *y, const double *k, double M,
+                                    double *dydt, double *neg_jac) {
+    if (!n || !y || !k) return VK_EINVAL;
+    const int ni = n->ni, np = n->npair;
+    std::vector<double> yl(y, y + ni);
+    yl.push_back(M);                                   // factor index ni stands for M
+    std::vector<double> v(np + n->xmul_pair.size());
+    for (int p = 0; p < np; ++p)
+        v[p] = side_value(k[2 * p], n->pairs[p], 0, yl.data(), M) -
+               side_value(k[2 * p + 1], n->pairs[p], 1, yl.data(), M);
+    for (size_t m = 0; m < n->xmul_pair.size(); ++m) v[np + m] = n->xmul_fac[m] * v[n->xmul_pair[m]];
+    if (dydt) {
+        for (int s = 0; s < ni; ++s) {
+            double acc = 0.0;
+            for (int e = n->src_ptr[s]; e < n->src_ptr[s + 1]; ++e)
+                acc = std::fma(n->src_c[e], v[n->src_slot[e]], acc);
+            dydt[s] = acc;
+        }
+    }
+    if (neg_jac) {
+        std::vector<double> h(n->hk.size());
+        for (size_t i = 0; i < n->hk.size(); ++i) {
+            double d = k[n->hk[i]];
+            for (int t = n->hptr[i]; t < n->hptr[i + 1]; ++t) d = d * yl[n->hfac[t]];
+            h[i] = d;
+        }
+        for (size_t e = 0; e + 1 < n->hjptr.size(); ++e) {
+            double acc = 0.0;
+            for (int t = n->hjptr[e]; t < n->hjptr[e + 1]; ++t) acc = std::fma(n->hjcoef[t], h[n->hjterm[t]], acc);
+            neg_jac[e] = -acc;
+        }
+    }
     return VK_OK;
 }
 

@@ -304,8 +304,14 @@ class Ros2Handle:
         dt, t, count = f(dt, float), f(t, float), f(count, np.int32)
         check(lib().vk_set_clock(self.h, ptr(dt), ptr(t), ptr(count, C.c_int)), self.h)
 
-    def run(self, ctrl, max_steps=0, timeout_s=0.0):
-        check(lib().vk_run(self.h, C.byref(ctrl), int(max_steps), float(timeout_s)), self.h)
+    def run(self, ctrl, max_steps=0, timeout_s=0.0, max_attempts=0):
+        """vk_run (max_attempts > 0: vk_run_budget, the call also ends after
+        that many attempts of the batch)."""
+        if max_attempts > 0:
+            check(lib().vk_run_budget(self.h, C.byref(ctrl), int(max_steps), int(max_attempts),
+                                      float(timeout_s)), self.h)
+        else:
+            check(lib().vk_run(self.h, C.byref(ctrl), int(max_steps), float(timeout_s)), self.h)
 
     def state(self, out=None):
         """Device state copied to host arrays: new ones, or the (e.g. pinned)
