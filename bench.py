@@ -99,6 +99,45 @@ def _cpu_worker(args):
     return st.count, time.perf_counter() - t0, st.attempts
 
 
+def _syn_npz():
+    """The 150-species synthetic network written by synthnet (deterministic)
+    and its compiled npz, in the build folder."""
+    from vulcan_gb300 import synthnet
+    from vulcan_gb300.network import Network
+    d = os.path.join(REPO, '_build', 'syn150')
+    npz = os.path.join(d, 'net.npz')
+    path = synthnet.generate(d)
+    if not os.path.exists(npz):
+        Network.from_file(path, use_photo=True).to_npz(npz)
+    return path, npz
+
+
+def _cpu_worker_c4(args):
+    """One column of the 150-species stress workload (nz = 200, frozen J) with
+    the numpy oracle for a fixed number of steps; (steps, seconds, attempts)."""
+    idx, nsteps = args
+    sys.path.insert(0, REPO)
+    from oracle import ros2 as O
+    from vulcan_gb300 import batch, configs, synthnet
+    from vulcan_gb300.network import Network
+    path, npz = _syn_npz()
+    net = Network.from_file(path, use_photo=True)
+    spec = configs.config4_columns(sorted(net.photo_index()), ncols=C4_NCOLS)[idx]
+    it = batch.build_items([spec], net)[0]
+    atoms = list(synthnet.ATOMS)
+    on = O.OracleNet.from_npz(npz, atoms)
+    col = it['col']
+    atm = dict(M=col.M, n_0=col.n_0, Tco=col.Tco, Kzz=col.Kzz, vz=col.vz, Dzz=col.Dzz, Ti=col.Ti,
+               ms=col.ms, alpha=col.alpha, pico=col.pico, dzi=col.dzi, Hpi=col.Hpi, g=col.g,
+               Hp=col.Hp, dz=col.dz, zco=col.zco)
+    st = O.ColState(y=it['y'].copy(), ymix=it['ymix'].copy(), dt=1e-10, atom_ini=it['atom_ini'],
+                    atom_loss=np.zeros(len(atoms)))
+    t0 = time.perf_counter()
+    O.integrate(on, st, it['k'], atm, O.Flags(), O.Tol(), configs.GS, configs.RP,
+                col.pref_indx, max_steps=nsteps, solve='banded')
+    return st.count, time.perf_counter() - t0, st.attempts
+
+
 def _cpu_warm(_):
     """Pool warm-up: the imports every job needs (not timed)."""
     sys.path.insert(0, REPO)
@@ -107,26 +146,30 @@ def _cpu_warm(_):
     return os.getpid()
 
 
-def cpu_baseline(ncols_sample, nsteps, workers):
+def cpu_baseline(ncols_sample, nsteps, workers, workload='c2'):
     """The numpy restatement of the reference step on `workers` host cores.
     value = steps / (integration seconds summed over jobs / workers): the rate
     of `workers` cores each integrating columns back to back, measured inside
     the jobs (no interpreter start-up, imports or column set-up)."""
     ctx = mp.get_context('spawn')
     jobs = [(i, nsteps) for i in range(ncols_sample)]
+    if workload == 'c4':
+        _syn_npz()                       # written once before the workers read it
     with ctx.Pool(workers) as pool:
         pool.map(_cpu_warm, range(workers))
         t0 = time.perf_counter()
-        res = pool.map(_cpu_worker, jobs)
+        res = pool.map(_cpu_worker_c4 if workload == 'c4' else _cpu_worker, jobs)
         wall = time.perf_counter() - t0
     steps = sum(r[0] for r in res)
     busy = sum(r[1] for r in res)
     value = steps / (busy / workers)
+    what = ('the 128-column 150-species stress workload (nz = 200)' if workload == 'c4'
+            else 'the 512-column workload')
     return dict(value=value, unit=UNIT, cores=workers, kind='port',
-                sample='%d columns x %d Ros2 steps of the 512-column workload (numpy port of '
-                       'the reference step, LAPACK banded solve), %d worker processes; %.1f s of '
-                       'integration per core, timed inside the jobs' % (ncols_sample, nsteps, workers,
-                                                                         busy / workers),
+                sample='%d columns x %d Ros2 steps of %s (numpy port of the reference step, '
+                       'LAPACK banded solve), %d worker processes; %.1f s of integration per '
+                       'core, timed inside the jobs' % (ncols_sample, nsteps, what, workers,
+                                                        busy / workers),
                 wall_s=round(wall, 2), wall_rate=round(steps / wall, 3),
                 attempts=sum(r[2] for r in res))
 
@@ -431,8 +474,11 @@ def run_gpu(args):
     out['clocks'] = clocks.summary()
     if args.converge_budget > 0 and args.workload == 'c2' and ws == 1:
         out['columns_to_steady_state'] = converge_block(args)
-    if not args.no_cpu and args.workload == 'c2' and ws == 1:
-        out['cpu_baseline'] = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
+    if not args.no_cpu and ws == 1:
+        if args.workload == 'c4':       # a step of a 150 x 200 column costs seconds on one core
+            out['cpu_baseline'] = cpu_baseline(args.cpu_cols, 3, args.cpu_workers, 'c4')
+        else:
+            out['cpu_baseline'] = cpu_baseline(args.cpu_cols, args.cpu_steps, args.cpu_workers)
     print(json.dumps(out))
 
 
