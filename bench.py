@@ -99,16 +99,18 @@ def _cpu_worker(args):
     return st.count, time.perf_counter() - t0, st.attempts
 
 
-def _syn_npz():
+def _syn_npz(write=True):
     """The 150-species synthetic network written by synthnet (deterministic)
-    and its compiled npz, in the build folder."""
+    and its compiled npz, in the build folder (write=False: only the paths of
+    files an earlier call wrote -- the CPU workers read them concurrently)."""
     from vulcan_gb300 import synthnet
     from vulcan_gb300.network import Network
     d = os.path.join(REPO, '_build', 'syn150')
     npz = os.path.join(d, 'net.npz')
+    if not write:
+        return os.path.join(d, 'SYN150_network.txt'), npz
     path = synthnet.generate(d)
-    if not os.path.exists(npz):
-        Network.from_file(path, use_photo=True).to_npz(npz)
+    Network.from_file(path, use_photo=True).to_npz(npz)
     return path, npz
 
 
@@ -120,7 +122,7 @@ def _cpu_worker_c4(args):
     from oracle import ros2 as O
     from vulcan_gb300 import batch, configs, synthnet
     from vulcan_gb300.network import Network
-    path, npz = _syn_npz()
+    path, npz = _syn_npz(write=False)
     net = Network.from_file(path, use_photo=True)
     spec = configs.config4_columns(sorted(net.photo_index()), ncols=C4_NCOLS)[idx]
     it = batch.build_items([spec], net)[0]

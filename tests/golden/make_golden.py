@@ -74,11 +74,12 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'rmlist': (0,),
         'snchok': (0,),
         'c3s': (0, 1, 2, 5, 9),
-        'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,)}
+        'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,),
+        'c0vul': (0,)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'c3rt': 2, 'lowT': 1, 'c0bc': 30,
           'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'snchok': 1, 'c3s': 10, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
-          'c0rocky': 2}
+          'c0rocky': 2, 'c0vul': 20}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -277,6 +278,8 @@ out['end_case'] = para.end_case
 out['wall_s'] = wall
 out['n_attempts'] = len(ATT)
 np.savez_compressed('golden_out.npz', **out)
+if meta.get('save_vul'):                 # the reference's own .vul (op.Output.save_out)
+    output.save_out(var, atm, para, os.getcwd())
 # full record for local deep checks (not committed)
 np.savez_compressed('golden_full.npz',
     **{('a%d_' % i) + k: np.asarray(ATT[i][k]) for i in range(len(ATT)) for k in att_keys})
@@ -510,7 +513,8 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
              photo_J=np.array([spec.photo_J[k] for k in keys]) if keys else np.zeros((0, nz)),
              **extra_in)
     with open(os.path.join(dst, 'golden_meta.json'), 'w') as f:
-        json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep)}, f)
+        json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep),
+                   'save_vul': tag == 'c0vul'}, f)
     with open(os.path.join(dst, 'golden_driver.py'), 'w') as f:
         f.write(PHOTO_DRIVER if tag in PHOTO_TAGS else RATE_DRIVER if tag in RATE_TAGS else DRIVER)
     r = subprocess.run([sys.executable, 'golden_driver.py'], cwd=dst, env=env,
@@ -575,7 +579,7 @@ def slim_photo(d):
 
 
 def make(tag, ref_root, workdir, full_dir=None):
-    if tag in ('c0', 'c0bc', 'c0nomol', 'c0vz', 'c0n2', 'c0o2', 'c0co2', 'c0rocky'):
+    if tag in ('c0', 'c0bc', 'c0nomol', 'c0vz', 'c0n2', 'c0o2', 'c0co2', 'c0rocky', 'c0vul'):
         spec = configs.config0()
     elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
         spec = configs.config2_columns(ncols=1, seed=2)[0]
@@ -628,6 +632,18 @@ def make(tag, ref_root, workdir, full_dir=None):
         out = os.path.join(HERE, 'golden_%s.npz' % tag)
         np.savez_compressed(out, **d)
         print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
+        return
+    if tag == 'c0vul':
+        # the file the reference wrote (protocol-4 pickle of var_save, vars(atm),
+        # vars(para)) next to the state it was written from
+        src = os.path.join(dst, 'output', 'golden.vul')
+        shutil.copy(src, os.path.join(HERE, 'golden_c0vul.vul'))
+        np.savez_compressed(os.path.join(HERE, 'golden_c0vul.npz'), final_y=d['final_y'],
+                            final_ymix=d['final_ymix'], final_t=d['final_t'],
+                            final_count=d['final_count'], end_case=d['end_case'], k=d['k'],
+                            y_ini=d['y_ini'], atom_list=np.array(spec.atom_list))
+        print('wrote', os.path.join(HERE, 'golden_c0vul.vul'),
+              os.path.getsize(os.path.join(HERE, 'golden_c0vul.vul')) // 1024, 'KiB')
         return
     d['atom_list'] = np.array(spec.atom_list)
     d['conver_ignore'] = np.array(spec.conver_ignore, dtype='U16')

@@ -4,7 +4,7 @@ import pickle
 
 import numpy as np
 
-from helpers import network
+from helpers import GOLDEN, network
 from vulcan_gb300 import batch, configs, vulio
 
 ATOMS = ['H', 'O', 'C', 'He', 'N']
@@ -91,3 +91,60 @@ def test_layout_has_what_the_reference_saves_and_plots():
     np.testing.assert_allclose(v['J_sp'][(sp, 0)], tot, rtol=1e-14)
     np.testing.assert_allclose(atm['zmco'], 0.5 * (atm['zco'][:-1] + atm['zco'][1:]))
     assert atm['zmco'].size == nz1
+
+
+def test_matches_a_file_the_reference_wrote():
+    """golden_c0vul.vul is the reference's own save_out (op.py:3216-3256) after
+    20 steps of config 0 (tests/golden/make_golden.py c0vul).  Written from
+    the same state, this package's file has every variable and atm entry of
+    the reference's, with the same set-up arrays, rate constants, reaction
+    texts and initial state; its parameter entries are a subset of the
+    reference's (the run-internal ones it does not track -- nega_y, small_y,
+    pic_count, where_varies_most, start_time, the plot palette -- are left
+    out); and the reference's file restarts a run (vulcan_ini) through
+    read_vul_y.  The column geometry that diffusion updates (mu, g, Hp, dz,
+    zco, zmco, dzi: update_mu_dz every update_frq steps, the first time after
+    step 1) is the reference's at its last update and the column item's here
+    (the set-up): they agree to the drift of one step, 1e-5."""
+    g = dict(np.load(os.path.join(GOLDEN, 'golden_c0vul.npz'), allow_pickle=False))
+    with open(os.path.join(GOLDEN, 'golden_c0vul.vul'), 'rb') as f:
+        ref = pickle.load(f)
+    net = network('c0')
+    atoms = [str(a) for a in g['atom_list']]
+    item = batch.build_items([configs.config0()], net)[0]
+    ours = vulio.vul_dict(net, item, g['final_y'], g['final_ymix'], float(g['final_t']), 1e-9,
+                          int(g['final_count']), int(g['end_case']), atoms,
+                          counters=np.array([26, 6, 0, 0, 0, 20]))
+    rv, ov = ref['variable'], ours['variable']
+    assert set(rv) <= set(ov)
+    assert set(ref['atm']) <= set(ours['atm'])
+    assert set(ours['parameter']) <= set(ref['parameter'])
+    assert ov['species'] == list(rv['species']) and ov['nr'] == rv['nr']
+    assert ov['Rf'] == rv['Rf']
+    assert set(ov['k']) == set(rv['k'])
+    for i in rv['k']:
+        np.testing.assert_array_equal(ov['k'][i], rv['k'][i])
+    np.testing.assert_array_equal(ov['y_ini'], rv['y_ini'])
+    for a in atoms:
+        assert abs(ov['atom_ini'][a] / rv['atom_ini'][a] - 1) < 1e-12
+        assert ov['atom_conden'][a] == rv['atom_conden'][a] == 0.0
+    for key in ('pco', 'pico', 'Tco', 'Kzz', 'M', 'n_0', 'Dzz', 'Dzz_cen', 'ms', 'alpha', 'Ti',
+                'top_flux', 'bot_flux', 'bot_vdep', 'vz', 'vm', 'vs', 'bot_fix_sp'):
+        np.testing.assert_allclose(np.asarray(ours['atm'][key], float),
+                                   np.asarray(ref['atm'][key], float), rtol=1e-13, atol=0, err_msg=key)
+    for key in ('mu', 'g', 'Hp', 'dz', 'zco', 'zmco', 'dzi', 'Hpi'):
+        o, r = np.asarray(ours['atm'][key], float), np.asarray(ref['atm'][key], float)
+        assert o.shape == r.shape, key
+        assert np.abs(o - r).max() <= 1e-5 * np.abs(r).max(), key
+    assert ours['atm']['pref_indx'] == ref['atm']['pref_indx']
+    assert ours['atm']['gs'] == ref['atm']['gs']
+    assert list(ours['atm']['gas_indx']) == list(ref['atm']['gas_indx'])
+    for key in vulio.CONDENSE_DICT_KEYS:
+        assert ours['atm'][key] == ref['atm'][key] == {}
+    p = ref['parameter']
+    assert ours['parameter']['count'] == p['count'] and ours['parameter']['end_case'] == p['end_case']
+    assert ours['parameter']['delta_count'] == p['delta_count']
+    # the reference's file as a restart: its y by species name
+    y, missing = vulio.read_vul_y(os.path.join(GOLDEN, 'golden_c0vul.vul'), net.species)
+    assert not missing
+    np.testing.assert_array_equal(y, rv['y'])

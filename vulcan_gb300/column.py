@@ -44,6 +44,7 @@ class Column:
     Ti: np.ndarray = None
     Hpi: np.ndarray = None
     Dzz: np.ndarray = None          # [nz-1, ni]
+    Dzz_cen: np.ndarray = None      # [nz, ni] the same at layer centres (written to .vul)
     ms: np.ndarray = None           # [ni]
     alpha: np.ndarray = None        # [ni]
     pref_indx: int = 0
@@ -121,9 +122,10 @@ def mol_diff(col: Column, species, mass):
     n0_i = np.delete((n_0 + np.roll(n_0, 1)) * 0.5, 0)
     alpha = np.zeros(ni)
     Dzz = np.zeros((col.nz - 1, ni))
+    Dzz_cen = np.zeros((col.nz, ni))
     col.ms = np.array(mass, dtype=np.float64)
     if not col.use_moldiff:
-        col.Dzz, col.alpha = Dzz, alpha
+        col.Dzz, col.Dzz_cen, col.alpha = Dzz, Dzz_cen, alpha
         return col
     base = col.atm_base
     if base == 'H2':
@@ -148,7 +150,8 @@ def mol_diff(col: Column, species, mass):
                 alpha[species.index(sp)] = v
     for k in range(ni):
         Dzz[:, k] = gen(Tco_i, n0_i, mass[k])
-    col.Dzz, col.alpha = Dzz, alpha
+        Dzz_cen[:, k] = gen(Tco, n_0, mass[k])
+    col.Dzz, col.Dzz_cen, col.alpha = Dzz, Dzz_cen, alpha
     return col
 
 

@@ -22,8 +22,12 @@ import pickle
 import numpy as np
 
 ATM_KEYS = ('pco', 'pico', 'Tco', 'Kzz', 'vz', 'M', 'n_0', 'mu', 'g', 'Hp', 'dz', 'zco',
-            'dzi', 'Dzz', 'ms', 'alpha', 'Ti', 'Hpi', 'top_flux', 'bot_flux', 'bot_vdep',
-            'pref_indx', 'gs', 'Rp')
+            'dzi', 'Dzz', 'Dzz_cen', 'ms', 'alpha', 'Ti', 'Hpi', 'top_flux', 'bot_flux',
+            'bot_vdep', 'pref_indx', 'gs', 'Rp')
+# atm entries of the reference's file for options this step does not run
+# (condensation, fixed species, molecular-diffusion advection and settling
+# velocities): written as the reference writes them when those are off
+CONDENSE_DICT_KEYS = ('conden_min_lev', 'fix_sp_indx', 'r_p', 'rho_p', 'sat_mix', 'sat_p')
 
 
 PHOTO_KEYS = ('nbin', 'bins', 'dbin1', 'dbin2', 'tau', 'sflux', 'aflux', 'cross', 'cross_scat',
@@ -52,9 +56,11 @@ def photo_fields(tables, tau, aflux, J):
 
 
 def vul_dict(net, item, y, ymix, t, dt, count, end_case, atom_list, longdy=0.0, longdydt=0.0,
-             delta=0.0, photo=None):
+             delta=0.0, photo=None, counters=None):
     """The save_out dictionary of one column (state arrays [nz, ni]); with
-    ``photo`` (photo_fields) also the photochemistry entries."""
+    ``photo`` (photo_fields) also the photochemistry entries; ``counters``
+    (the column's row of Ros2Handle.counters()) adds the rejection counts the
+    reference keeps in para (delta_count, nega_count, loss_count)."""
     from .column import atom_totals
     col = item['col']
     k = item['k']
@@ -78,8 +84,18 @@ def vul_dict(net, item, y, ymix, t, dt, count, end_case, atom_list, longdy=0.0, 
     if getattr(col, 'zco', None) is not None:      # layer mid-points (f_mu_dz's zmco)
         z = np.asarray(col.zco)
         atm['zmco'] = 0.5 * (z[:-1] + z[1:])
+    nz, ni = np.asarray(y).shape
+    atm['vm'] = np.zeros((nz, ni))
+    atm['vs'] = np.zeros((nz - 1, ni))
+    atm['bot_fix_sp'] = np.zeros(ni)
+    atm['gas_indx'] = list(range(ni))
+    for key in CONDENSE_DICT_KEYS:
+        atm[key] = {}
     para = {'count': int(count), 'end_case': int(end_case), 'delta': float(delta),
             'solver_str': 'Ros2GPU'}
+    if counters is not None:       # attempts, delta / negativity / loss rejections, ...
+        para.update(delta_count=int(counters[1]), nega_count=int(counters[2]),
+                    loss_count=int(counters[3]))
     return {'variable': var, 'atm': atm, 'parameter': para}
 
 
@@ -88,11 +104,12 @@ def write_vul(path, data):
         pickle.dump(data, f, protocol=4)
 
 
-def write_batch(paths, net, items, state, atom_list, conv=None, photo=None):
+def write_batch(paths, net, items, state, atom_list, conv=None, photo=None, counters=None):
     """One .vul per column of a batch state (Ros2Handle.state()); ``paths``
     lists the file names; ``conv`` = (longdy, longdydt) per column; ``photo``
     = (tables, tau, aflux, J) of the batch (Ros2Handle.photo_get) adds the
-    photochemistry entries."""
+    photochemistry entries; ``counters`` = Ros2Handle.counters() the
+    rejection counts."""
     off = np.concatenate([[0], np.cumsum([it['col'].nz for it in items])])
     for c, (path, it) in enumerate(zip(paths, items)):
         sl = slice(off[c], off[c + 1])
@@ -105,7 +122,8 @@ def write_batch(paths, net, items, state, atom_list, conv=None, photo=None):
             ph = photo_fields(tables, tau[off[c] + c:off[c + 1] + c + 1], aflux[sl], J[sl])
         write_vul(path, vul_dict(net, it, state['y'][sl], state['ymix'][sl], state['t'][c],
                                  state['dt'][c], state['count'][c], state['end_case'][c],
-                                 atom_list, ld, ldt, state['delta'][c], photo=ph))
+                                 atom_list, ld, ldt, state['delta'][c], photo=ph,
+                                 counters=None if counters is None else counters[c]))
 
 
 def read_vul_y(path, species, nz=None):
