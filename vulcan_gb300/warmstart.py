@@ -432,6 +432,44 @@ def generate(net, seeds, ncols, atoms, count_max=4000, timeout_s=900, precision=
     return np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Cs)
 
 
+def generate_stream(net, specs, atoms, model=None, budget_s=600.0, count_max=3000,
+                    route_dt0=1e-6, nslots=512, log=print):
+    """Steady states for training from a stream of columns (continuous
+    batching, batch.run_stream): every column starts from the model's judged
+    proposal (const_mix where there is no model or the judge rejects it) and
+    runs the reference's convergence test; returns (features, targets, column
+    index) of the columns that converged within budget_s seconds.  The
+    solver, not the model, decides each target."""
+    import time
+    from . import batch as bmod, configs
+    from .solver import ctrl_from
+    t0 = time.perf_counter()
+    items_const = bmod.build_items(specs, net)
+    xeq = eq_mix_many(specs, net)
+    if model is not None:
+        items, used = judged_items(model, specs, net, items_const, atoms, 1)
+    else:
+        items, used = items_const, np.zeros(len(specs), dtype=bool)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    ctrl.count_max = count_max
+    left = budget_s - (time.perf_counter() - t0)
+    res, wall = bmod.run_stream(net, items, atoms, nslots=min(nslots, len(items)), ctrl=ctrl,
+                                precision=1, slot_cap=int(max(sp.pco.size for sp in specs)),
+                                budget_s=max(left, 1.0), keep_state=True, chunk_attempts=24,
+                                route_dt0=route_dt0 if model is not None else None)
+    Xs, Ys, Cs = [], [], []
+    for i in sorted(res):
+        if res[i]['end_case'] != 1:
+            continue
+        Xs.append(features_eq(specs[i], net, xeq[i]))
+        Ys.append(log_targets(res[i]['ymix']))
+        Cs.append(np.full(res[i]['ymix'].shape[0], i))
+    log('stream: %d columns, %d ended, %d converged (%d from proposals) in %.0f s'
+        % (len(specs), len(res), len(Xs), int(sum(used[i] for i in res if res[i]['end_case'] == 1)),
+           time.perf_counter() - t0))
+    return np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Cs)
+
+
 def warm_items(model, specs, net, items, atoms, precision=1):
     """Items started from the projected MLP proposal (element totals those
     of the normalised const_mix start; atom_ini stays the reference's, so the
@@ -499,7 +537,7 @@ def main(argv=None):
     import os
     from .network import Network
     ap = argparse.ArgumentParser(description='learned warm start: generate / train / evaluate')
-    ap.add_argument('cmd', choices=['generate', 'train'])
+    ap.add_argument('cmd', choices=['generate', 'generate-stream', 'train'])
     ap.add_argument('--net', required=True, help='compiled network .npz or network text file')
     ap.add_argument('--seeds', default='10,11')
     ap.add_argument('--ncols', type=int, default=512)
@@ -512,10 +550,26 @@ def main(argv=None):
     ap.add_argument('--depth', type=int, default=4)
     ap.add_argument('--count-max', type=int, default=4000)
     ap.add_argument('--timeout', type=float, default=900)
+    ap.add_argument('--budget', type=float, default=600,
+                    help='generate-stream: wall seconds for the whole stream')
+    ap.add_argument('--proposals', default=None,
+                    help='generate-stream: start the columns from this model\'s judged proposals')
     a = ap.parse_args(argv)
     net = Network.from_npz(a.net) if a.net.endswith('.npz') else Network.from_file(a.net)
     atoms = ['H', 'O', 'C', 'He', 'N']
-    if a.cmd == 'generate':
+    if a.cmd == 'generate-stream':
+        from . import configs
+        seeds = [int(s) for s in a.seeds.split(',')]
+        specs = [sp for sd in seeds for sp in configs.config2_columns(ncols=a.ncols, seed=sd)]
+        model = MLP.load(a.proposals) if a.proposals else None
+        X, Y, cid = generate_stream(net, specs, atoms, model, budget_s=a.budget,
+                                    count_max=min(a.count_max, 3000))
+        # column ids unique across seeds: seed * 100000 + index within its seed
+        cid = np.array([seeds[c // a.ncols] * 100000 + c % a.ncols for c in cid])
+        np.savez_compressed(a.data, X=X.astype(np.float32), Y=Y.astype(np.float32), col=cid)
+        print(json.dumps({'samples': int(X.shape[0]), 'columns': int(np.unique(cid).size),
+                          'data': os.path.abspath(a.data)}))
+    elif a.cmd == 'generate':
         X, Y, cid = generate(net, [int(s) for s in a.seeds.split(',')], a.ncols, atoms,
                              count_max=a.count_max, timeout_s=a.timeout)
         np.savez_compressed(a.data, X=X.astype(np.float32), Y=Y.astype(np.float32), col=cid)
