@@ -208,16 +208,39 @@ VK_API int  vk_set_conv_ignore(vk_handle *h, const int *conv_ignore);
 /* Integrate every column on the device until each one reaches steady state
  * or a limit (count_max / runtime), or until max_steps accepted steps per
  * column have been taken in this call (0 = no cap).  dt/t/count live on the
- * device; the loop is captured once into a CUDA graph and replayed. */
+ * device; the loop is captured once into a CUDA graph of 8 attempts (of
+ * max_steps attempts when max_steps < 8) and replayed. */
 VK_API int  vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s);
 /* vk_run with an attempt budget as well: the call also returns once the
- * batch has made max_attempts attempts (rounded up to the graph's 8; 0 = no
+ * batch has made max_attempts attempts (rounded up to the graph's length; 0 = no
  * budget), the columns keeping their state for the next call.  For
  * continuous batching: a column whose steps need many rejected attempts
  * then holds the batch for at most the budget, while the others' slots are
  * refilled between calls.  Same loop as op.py:808-936 per column. */
 VK_API int  vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, int max_attempts,
                           double timeout_s);
+
+/* Several networks in one launch.  A group holds handles of any networks
+ * (any ni, each with its own columns, precision and launch settings); one
+ * vk_group_run runs all of them to steady state like vk_run_budget does each,
+ * with every handle's loop body (attempts + control) on its own stream inside
+ * one CUDA graph, forked from the group's stream and joined back, so the
+ * networks' kernels share the GPU in one graph launch per replay.  Each
+ * handle's results are bit for bit those of vk_run_budget on that handle
+ * alone: the kernels and their inputs are the same; only their placement in
+ * time differs.  Destroy the group before its handles.  Errors of these
+ * calls are read with vk_last_error(NULL); an error of one handle's run is
+ * reported as "handle i: <its message>".  The per-column loop they replace
+ * is op.py:808-936, run once per column. */
+typedef struct vk_group vk_group;
+VK_API int  vk_group_create(vk_handle *const *handles, int n, vk_group **out);
+/* ctrls: n control structs, one per handle in group order; max_steps,
+ * max_attempts and timeout_s as in vk_run_budget, for the whole group. */
+VK_API int  vk_group_run(vk_group *g, const vk_ctrl *ctrls, int max_steps, int max_attempts,
+                         double timeout_s);
+/* Device time of the last vk_group_run (ms) and the kernels it launched. */
+VK_API int  vk_group_timing(const vk_group *g, double *ms, int *launches);
+VK_API void vk_group_destroy(vk_group *g);
 
 /* Per-column state read-back: y/ymix [L][ni]; the scalar arrays are [ncols]
  * (NULL to skip).  end_case: 0 running, 1 converged, 2 runtime, 3 count_max,

@@ -82,7 +82,7 @@ def test_null_handle_errors(lib):
 
 
 NO_HANDLE = ('vk_network_compile', 'vk_network_free', 'vk_network_last_error', 'vk_destroy',
-             'vk_last_error')
+             'vk_last_error', 'vk_group_destroy')
 
 
 def test_every_entry_point_rejects_null_arguments(lib):
@@ -105,6 +105,24 @@ def test_every_entry_point_rejects_null_arguments(lib):
         assert f(*args) == capi.VK_EINVAL, name
         checked += 1
     assert checked == len(capi.EXPORTS) - len(NO_HANDLE)
+
+
+def test_group_arguments_checked_on_host(lib):
+    """vk_group_create rejects an empty list, NULL and repeated handles
+    before it creates any device object (the pointers are only compared)."""
+    from vulcan_gb300 import capi
+    out = C.c_void_p(1)
+    fake = C.c_void_p(0x1000)
+    arr = (C.c_void_p * 2)(fake, fake)
+    assert lib.vk_group_create(arr, 0, C.byref(out)) == capi.VK_EINVAL
+    assert out.value is None
+    assert lib.vk_group_create(arr, 2, C.byref(out)) == capi.VK_EINVAL
+    assert b'twice' in lib.vk_last_error(None)
+    arr0 = (C.c_void_p * 2)(fake, None)
+    assert lib.vk_group_create(arr0, 2, C.byref(out)) == capi.VK_EINVAL
+    assert b'NULL' in lib.vk_last_error(None)
+    assert lib.vk_group_create(arr, 1, None) == capi.VK_EINVAL
+    lib.vk_group_destroy(None)
 
 
 def test_c_client_builds_and_runs(lib, tmp_path):

@@ -41,7 +41,8 @@ EXPORTS = ('vk_network_compile', 'vk_network_info', 'vk_network_jac_pattern', 'v
            'vk_compute_k', 'vk_get_k', 'vk_photo_setup', 'vk_photo_reset',
            'vk_photo_update', 'vk_photo_get', 'vk_photo_set_cross_T', 'vk_set_rate_caps',
            'vk_set_launch', 'vk_get_launch', 'vk_set_conv_ignore', 'vk_get_lu32', 'vk_rhs',
-           'vk_set_columns_slotted', 'vk_refill')
+           'vk_set_columns_slotted', 'vk_refill', 'vk_group_create', 'vk_group_run',
+           'vk_group_timing', 'vk_group_destroy')
 
 
 class VkNetworkDesc(C.Structure):
@@ -111,6 +112,10 @@ def lib(path=None):
         'vk_refill': (i, [vp, i, pi, pi, pd, pd, pd, pd, pd, pd, pd, pi, pi]),
         'vk_run': (i, [vp, P(VkCtrl), i, d]),
         'vk_run_budget': (i, [vp, P(VkCtrl), i, i, d]),
+        'vk_group_create': (i, [P(vp), i, P(vp)]),
+        'vk_group_run': (i, [vp, P(VkCtrl), i, i, d]),
+        'vk_group_timing': (i, [vp, pd, pi]),
+        'vk_group_destroy': (None, [vp]),
         'vk_get_state': (i, [vp, pd, pd, pd, pd, pi, pi, pd]),
         'vk_set_clock': (i, [vp, pd, pd, pi]),
         'vk_get_counters': (i, [vp, pi]),

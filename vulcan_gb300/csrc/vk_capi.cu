@@ -83,6 +83,7 @@ struct vk_handle {
     int *d_nactive = nullptr;
     cudaGraphExec_t gexec = nullptr;
     unsigned char gkey[sizeof(vk::RunCtrl) + 2 * sizeof(int)] = {};
+    unsigned gen = 0;           // bumped whenever a captured loop of this handle goes stale
     std::vector<void *> allocs;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
@@ -163,6 +164,13 @@ static int upload(vk_handle *h, T **p, const std::vector<T> &v) {
     if (rc) return rc;
     if (!v.empty()) VK_CUDA(h, cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     return VK_OK;
+}
+
+// A captured run loop of h (its own, or a group's that holds h) no longer
+// matches the handle's buffers, grids or precision settings.
+static void drop_graph(vk_handle *h) {
+    if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+    ++h->gen;
 }
 
 extern "C" const char *vk_last_error(const vk_handle *h) {
@@ -369,7 +377,7 @@ extern "C" int vk_set_precision(vk_handle *h, int precision, int max_refine, dou
     h->precision = precision;
     h->max_refine = max_refine;
     h->refine_tol = refine_tol;
-    if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+    drop_graph(h);
     return VK_OK;
 }
 
@@ -466,10 +474,7 @@ static int set_columns_impl(vk_handle *h, int ncols, int slot_cap, const int *nz
     }
     VK_CUDA(h, cudaMemcpyAsync(h->d_spf, spf, (size_t)ncols * VK_SP_NF * ni * sizeof(double), cudaMemcpyHostToDevice, s));
     VK_CUDA(h, cudaStreamSynchronize(s));
-    if (h->gexec && (h->ncols != ncols || h->L != L)) {
-        cudaGraphExecDestroy(h->gexec);
-        h->gexec = nullptr;
-    }
+    if (h->ncols != ncols || h->L != L) drop_graph(h);
     h->ncols = ncols;
     h->L = L;
     h->col_off = off;
@@ -873,10 +878,7 @@ extern "C" int vk_set_launch(vk_handle *h, int kernel, int ctas_per_sm, int vari
         return fail(h, VK_EINVAL, "k_lu32 tiling " + std::to_string(variant) + " does not cover " +
                                       std::to_string(h->ni) + " species");
     if (h->stream) VK_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (h->gexec) {                        // the captured loop has the old grids
-        cudaGraphExecDestroy(h->gexec);
-        h->gexec = nullptr;
-    }
+    drop_graph(h);                         // the captured loop has the old grids
     h->cps_k[kernel] = ctas_per_sm;
     if (kernel == VK_TUNE_LU32) h->lu32_tiling = variant;
     return VK_OK;
@@ -1139,24 +1141,29 @@ static vk::RunCtrl to_run_ctrl(const vk_ctrl *c, int max_steps) {
 
 static const int kGraphAttempts = 8;
 
-extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s) {
-    return vk_run_budget(h, ctrl, max_steps, 0, timeout_s);
+// Attempts per replay of the run loop: a call of fewer steps than
+// kGraphAttempts (one step per call is the reference's own pattern) replays
+// that many, so the attempts after every column has taken its steps are not
+// launched; a rejection costs one more replay.
+static int graph_attempts(const vk::RunCtrl &cc) {
+    return cc.max_steps < kGraphAttempts ? cc.max_steps : kGraphAttempts;
 }
 
-extern "C" int vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, int max_attempts,
-                             double timeout_s) {
-    if (max_attempts < 0) return fail(h, VK_EINVAL, "max_attempts must be >= 0");
+// Everything of a run before its replays, on h->stream: the control values'
+// check, the history ring (conv_step accepted states of the whole batch),
+// the transport geometry and the per-call start of every column.
+static int run_prepare(vk_handle *h, const vk_ctrl *ctrl, int max_steps, vk::RunCtrl &cc) {
     int rc = need_batch(h);
     if (rc) return rc;
     if (!ctrl) return fail(h, VK_EINVAL, "ctrl is NULL");
     if (ctrl->conv_step < 2 || ctrl->update_frq < 1 || ctrl->max_attempts < 1 || ctrl->rtol <= 0)
         return fail(h, VK_EINVAL, "bad control values");
-    vk::RunCtrl cc = to_run_ctrl(ctrl, max_steps);
+    cc = to_run_ctrl(ctrl, max_steps);
     cudaStream_t s = h->stream;
-    // history ring: conv_step accepted states of the whole batch
     if (h->hist_R != cc.conv_step || !h->rs.hist_y) {
         if (h->rs.hist_y) { cudaFree(h->rs.hist_y); cudaFree(h->rs.hist_t); }
         h->rs.hist_y = nullptr; h->rs.hist_t = nullptr;
+        drop_graph(h);
         cudaError_t e1 = cudaMalloc(&h->rs.hist_y, (size_t)cc.conv_step * h->max_layers * h->ni * sizeof(double));
         cudaError_t e2 = cudaMalloc(&h->rs.hist_t, (size_t)cc.conv_step * h->max_cols * sizeof(double));
         if (e1 != cudaSuccess || e2 != cudaSuccess) {
@@ -1166,33 +1173,76 @@ extern "C" int vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, i
             return fail(h, VK_ENOMEM, "history ring allocation failed");
         }
         h->hist_R = cc.conv_step;
-        if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
     }
     if (h->precision == VK_PREC_MIXED && !h->w.G32)
         return fail(h, VK_EINVAL, "mixed precision not allocated on this handle");
     ensure_geometry(h, cc.flags);
-    DevNet net = h->net();
     DevBatch b = h->batch();
     b.active = h->rs.active;
     VK_CUDA(h, cudaMemsetAsync(h->w.status, 0, h->ncols * sizeof(int), s));
-    vk::launch_start(net, b, h->rs, cc, s);
+    vk::launch_start(h->net(), b, h->rs, cc, s);
     VK_CUDA(h, cudaGetLastError());
-    // (re)capture the attempt + control sequence when the configuration changed
-    unsigned char key[sizeof(h->gkey)];
+    return VK_OK;
+}
+
+// What a captured loop of h depends on besides its buffers (those are
+// covered by h->gen): the control values and the batch shape.
+static void run_key(const vk_handle *h, const vk::RunCtrl &cc, unsigned char *key) {
     std::memcpy(key, &cc, sizeof(cc));
     std::memcpy(key + sizeof(cc), &h->ncols, sizeof(int));
     std::memcpy(key + sizeof(cc) + sizeof(int), &h->L, sizeof(int));
+}
+
+// The replayed body on h->stream: ga attempts, each followed by the control
+// step of every active column (accept/reject, dt, steady-state test), then
+// the count of the columns still running into h->d_nactive.
+static void run_body(vk_handle *h, const vk::RunCtrl &cc, int ga) {
+    DevNet net = h->net();
+    DevBatch b = h->batch();
+    b.active = h->rs.active;
+    vk::Work &w = h->w;
+    for (int it = 0; it < ga; ++it) {
+        enqueue_attempt_kernels(h, net, b, cc.flags, cc.mtol, cc.atol, false);
+        vk::launch_control(net, b, h->rs, cc, w.sol, w.ymix_out, w.delta, w.status,
+                           h->precision == VK_PREC_MIXED ? w.fallback : nullptr, w.geo, h->stream);
+    }
+    vk::launch_count_active(h->rs.active, h->ncols, h->d_nactive, h->stream);
+}
+
+// Launches of one replay of h's body (the gpu_launches count).
+static int body_launches(const vk_handle *h, int ga) {
+    return ga * (h->precision == VK_PREC_MIXED ? 17 : 7) + 1;
+}
+
+// A column that stopped with an error status fails the call.
+static int run_check_end(vk_handle *h) {
+    std::vector<int> ec(h->ncols);
+    VK_CUDA(h, cudaMemcpy(ec.data(), h->rs.end_case, h->ncols * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < h->ncols; ++c)
+        if (ec[c] < 0) return fail(h, -ec[c], "column " + std::to_string(c) + " stopped with error " + std::to_string(-ec[c]));
+    return VK_OK;
+}
+
+extern "C" int vk_run(vk_handle *h, const vk_ctrl *ctrl, int max_steps, double timeout_s) {
+    return vk_run_budget(h, ctrl, max_steps, 0, timeout_s);
+}
+
+extern "C" int vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, int max_attempts,
+                             double timeout_s) {
+    if (max_attempts < 0) return fail(h, VK_EINVAL, "max_attempts must be >= 0");
+    vk::RunCtrl cc;
+    int rc = run_prepare(h, ctrl, max_steps, cc);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    const int ga = graph_attempts(cc);
+    // (re)capture the attempt + control sequence when the configuration changed
+    unsigned char key[sizeof(h->gkey)];
+    run_key(h, cc, key);
     if (!h->gexec || std::memcmp(key, h->gkey, sizeof(key)) != 0) {
         if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
         cudaGraph_t g;
         VK_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        vk::Work &w = h->w;
-        for (int it = 0; it < kGraphAttempts; ++it) {
-            enqueue_attempt_kernels(h, net, b, cc.flags, cc.mtol, cc.atol, false);
-            vk::launch_control(net, b, h->rs, cc, w.sol, w.ymix_out, w.delta, w.status,
-                               h->precision == VK_PREC_MIXED ? w.fallback : nullptr, w.geo, s);
-        }
-        vk::launch_count_active(h->rs.active, h->ncols, h->d_nactive, s);
+        run_body(h, cc, ga);
         cudaError_t ec = cudaStreamEndCapture(s, &g);
         if (ec != cudaSuccess) return fail(h, VK_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
         ec = cudaGraphInstantiate(&h->gexec, g, 0);
@@ -1205,10 +1255,10 @@ extern "C" int vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, i
     int launches = 0;
     // an attempt budget ends the call after that many attempts of the batch
     // (whole graph replays), whatever each column's step count
-    const int max_replays = max_attempts > 0 ? (max_attempts + kGraphAttempts - 1) / kGraphAttempts : 0;
+    const int max_replays = max_attempts > 0 ? (max_attempts + ga - 1) / ga : 0;
     for (int replay = 1;; ++replay) {
         VK_CUDA(h, cudaGraphLaunch(h->gexec, s));
-        launches += kGraphAttempts * (h->precision == VK_PREC_MIXED ? 17 : 7) + 1;
+        launches += body_launches(h, ga);
         int nact = 0;
         VK_CUDA(h, cudaMemcpyAsync(&nact, h->d_nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
         VK_CUDA(h, cudaStreamSynchronize(s));
@@ -1224,10 +1274,159 @@ extern "C" int vk_run_budget(vk_handle *h, const vk_ctrl *ctrl, int max_steps, i
     cudaEventElapsedTime(&h->ms[0], h->ev[0], h->ev[1]);
     h->ms[1] = h->ms[2] = h->ms[3] = 0.f;
     h->launches = launches;
-    std::vector<int> ec(h->ncols);
-    VK_CUDA(h, cudaMemcpy(ec.data(), h->rs.end_case, h->ncols * sizeof(int), cudaMemcpyDeviceToHost));
-    for (int c = 0; c < h->ncols; ++c)
-        if (ec[c] < 0) return fail(h, -ec[c], "column " + std::to_string(c) + " stopped with error " + std::to_string(-ec[c]));
+    return run_check_end(h);
+}
+
+// ---------------------------------------------------------------------------
+// Several handles -- one network each, any ni -- run by one graph: each
+// handle's loop body on its own stream, forked from the group's stream and
+// joined back, so the networks' kernels share the GPU in one launch.
+struct vk_group {
+    std::vector<vk_handle *> hs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    std::vector<cudaEvent_t> ev_join;   // one per handle
+    cudaEvent_t ev[2] = {};
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> key;
+    int *h_nactive = nullptr;           // pinned [n]
+    float ms = 0.f;
+    int launches = 0;
+};
+
+extern "C" void vk_group_destroy(vk_group *g) {
+    if (!g) return;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->gexec) cudaGraphExecDestroy(g->gexec);
+    if (g->ev_fork) cudaEventDestroy(g->ev_fork);
+    for (cudaEvent_t e : g->ev_join) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : g->ev) if (e) cudaEventDestroy(e);
+    if (g->h_nactive) cudaFreeHost(g->h_nactive);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+extern "C" int vk_group_create(vk_handle *const *handles, int n, vk_group **out) {
+    if (!out) return fail(nullptr, VK_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (!handles || n < 1) return fail(nullptr, VK_EINVAL, "a group needs at least one handle");
+    for (int i = 0; i < n; ++i) {
+        if (!handles[i]) return fail(nullptr, VK_EINVAL, "handle " + std::to_string(i) + " is NULL");
+        for (int j = 0; j < i; ++j)
+            if (handles[j] == handles[i])
+                return fail(nullptr, VK_EINVAL, "handle " + std::to_string(i) + " appears twice");
+    }
+    vk_group *g = new (std::nothrow) vk_group();
+    if (!g) return fail(nullptr, VK_ENOMEM, "out of host memory");
+    g->hs.assign(handles, handles + n);
+    g->ev_join.assign(n, nullptr);
+    auto bad = [&](const char *what, cudaError_t e) {
+        vk_group_destroy(g);
+        return fail(nullptr, VK_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bad("cudaStreamCreate", e);
+    if ((e = cudaEventCreateWithFlags(&g->ev_fork, cudaEventDisableTiming)) != cudaSuccess)
+        return bad("cudaEventCreate", e);
+    for (auto &ev : g->ev_join)
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+            return bad("cudaEventCreate", e);
+    for (auto &ev : g->ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bad("cudaEventCreate", e);
+    if ((e = cudaMallocHost(&g->h_nactive, n * sizeof(int))) != cudaSuccess)
+        return bad("cudaMallocHost", e);
+    *out = g;
+    return VK_OK;
+}
+
+extern "C" int vk_group_run(vk_group *g, const vk_ctrl *ctrls, int max_steps, int max_attempts,
+                            double timeout_s) {
+    if (!g) return fail(nullptr, VK_EINVAL, "group is NULL");
+    if (!ctrls) return fail(nullptr, VK_EINVAL, "ctrls is NULL");
+    if (max_attempts < 0) return fail(nullptr, VK_EINVAL, "max_attempts must be >= 0");
+    const int n = (int)g->hs.size();
+    std::vector<vk::RunCtrl> cc(n);
+    for (int i = 0; i < n; ++i) {
+        vk_handle *h = g->hs[i];
+        int rc = run_prepare(h, &ctrls[i], max_steps, cc[i]);
+        if (rc) return fail(nullptr, rc, "handle " + std::to_string(i) + ": " + h->err);
+        // the group's stream starts after every handle's per-call start
+        cudaEventRecord(g->ev_join[i], h->stream);
+        VK_CUDA(nullptr, cudaStreamWaitEvent(g->stream, g->ev_join[i], 0));
+    }
+    int ga = kGraphAttempts;
+    for (int i = 0; i < n; ++i) ga = std::min(ga, graph_attempts(cc[i]));
+    const size_t kh = sizeof(vk_handle::gkey);
+    std::vector<unsigned char> key(sizeof(int) + n * (sizeof(void *) + sizeof(unsigned) + kh));
+    unsigned char *kp = key.data();
+    std::memcpy(kp, &ga, sizeof(int)); kp += sizeof(int);
+    for (int i = 0; i < n; ++i) {
+        const vk_handle *h = g->hs[i];
+        std::memcpy(kp, &h, sizeof(void *)); kp += sizeof(void *);
+        std::memcpy(kp, &h->gen, sizeof(unsigned)); kp += sizeof(unsigned);
+        run_key(h, cc[i], kp); kp += kh;
+    }
+    cudaStream_t s = g->stream;
+    if (!g->gexec || key != g->key) {
+        if (g->gexec) { cudaGraphExecDestroy(g->gexec); g->gexec = nullptr; }
+        g->key.clear();
+        cudaGraph_t graph;
+        VK_CUDA(nullptr, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        cudaEventRecord(g->ev_fork, s);
+        for (int i = 0; i < n; ++i) {
+            vk_handle *h = g->hs[i];
+            cudaStreamWaitEvent(h->stream, g->ev_fork, 0);
+            run_body(h, cc[i], ga);
+            cudaEventRecord(g->ev_join[i], h->stream);
+            cudaStreamWaitEvent(s, g->ev_join[i], 0);
+        }
+        cudaError_t ec = cudaStreamEndCapture(s, &graph);
+        if (ec != cudaSuccess) return fail(nullptr, VK_ECUDA, std::string("group graph capture: ") + cudaGetErrorString(ec));
+        ec = cudaGraphInstantiate(&g->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ec != cudaSuccess) { g->gexec = nullptr; return fail(nullptr, VK_ECUDA, std::string("group graph instantiate: ") + cudaGetErrorString(ec)); }
+        g->key = key;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    cudaEventRecord(g->ev[0], s);
+    int launches = 0, per_replay = 0;
+    for (int i = 0; i < n; ++i) per_replay += body_launches(g->hs[i], ga);
+    const int max_replays = max_attempts > 0 ? (max_attempts + ga - 1) / ga : 0;
+    for (int replay = 1;; ++replay) {
+        VK_CUDA(nullptr, cudaGraphLaunch(g->gexec, s));
+        launches += per_replay;
+        for (int i = 0; i < n; ++i)
+            VK_CUDA(nullptr, cudaMemcpyAsync(g->h_nactive + i, g->hs[i]->d_nactive, sizeof(int),
+                                             cudaMemcpyDeviceToHost, s));
+        VK_CUDA(nullptr, cudaStreamSynchronize(s));
+        int nact = 0;
+        for (int i = 0; i < n; ++i) nact += g->h_nactive[i];
+        if (nact == 0 || (max_replays > 0 && replay >= max_replays)) break;
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_s > 0 && el > timeout_s) {
+            g->launches = launches;
+            return fail(nullptr, VK_ETIMEOUT, "vk_group_run watchdog: columns still active after " + std::to_string(el) + " s");
+        }
+    }
+    cudaEventRecord(g->ev[1], s);
+    cudaEventSynchronize(g->ev[1]);
+    cudaEventElapsedTime(&g->ms, g->ev[0], g->ev[1]);
+    g->launches = launches;
+    for (int i = 0; i < n; ++i) {
+        vk_handle *h = g->hs[i];
+        h->ms[0] = g->ms;
+        h->ms[1] = h->ms[2] = h->ms[3] = 0.f;
+        h->launches = launches;
+        int rc = run_check_end(h);
+        if (rc) return fail(nullptr, rc, "handle " + std::to_string(i) + ": " + h->err);
+    }
+    return VK_OK;
+}
+
+extern "C" int vk_group_timing(const vk_group *g, double *ms, int *launches) {
+    if (!g) return fail(nullptr, VK_EINVAL, "group is NULL");
+    if (ms) *ms = g->ms;
+    if (launches) *launches = g->launches;
     return VK_OK;
 }
 

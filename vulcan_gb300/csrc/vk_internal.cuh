@@ -126,6 +126,19 @@ struct DevBatch {
 // up to even, so every block starts on 16 bytes (bulk-copy alignment).
 __host__ __device__ inline int block_stride64(int n) { return (n * n + 1) & ~1; }
 
+// Raise a kernel's dynamic shared-memory limit to at least `bytes`, never
+// lowering it: handles of different networks share the kernels, and a loop
+// captured for the larger network must stay launchable after a smaller
+// network's handle is created.
+template <typename K>
+inline cudaError_t raise_smem_limit(K *kernel, size_t bytes) {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+    if (e != cudaSuccess) return e;
+    if ((size_t)a.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // Grid of a per-column kernel: CTAs per SM from vk_set_launch, else the
 // batch's override, else the kernel's default; never more than the columns.
 inline int column_grid(const DevBatch &b, int kernel, int cps_default) {

@@ -486,14 +486,14 @@ cudaError_t init_kernels(const DevNet &net) {
     const int n = net.ni;
     size_t sl = lu_fwd_smem(n, lu_fwd_la(n));
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_rates<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
-    if ((e = cudaFuncSetAttribute(k_rates<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sr))) return e;
-    if ((e = lu_fwd_la(n) ? cudaFuncSetAttribute(k_lu_fwd_f64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl)
-                          : cudaFuncSetAttribute(k_lu_fwd_f64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sl)))
+    if ((e = raise_smem_limit(k_rates<true>, (int)sr))) return e;
+    if ((e = raise_smem_limit(k_rates<false>, (int)sr))) return e;
+    if ((e = lu_fwd_la(n) ? raise_smem_limit(k_lu_fwd_f64<true>, (int)sl)
+                          : raise_smem_limit(k_lu_fwd_f64<false>, (int)sl)))
         return e;
     const int ssw = (int)sweep64_smem(n, 256, sweep64_nbuf(n));
-    if ((e = cudaFuncSetAttribute(k_back_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, ssw))) return e;
-    if ((e = cudaFuncSetAttribute(k_solve_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, ssw))) return e;
+    if ((e = raise_smem_limit(k_back_f64, ssw))) return e;
+    if ((e = raise_smem_limit(k_solve_f64, ssw))) return e;
     return cudaSuccess;
 }
 

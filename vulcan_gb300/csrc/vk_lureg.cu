@@ -344,16 +344,14 @@ static int tiling_of(int n) {
 
 cudaError_t init_lureg_kernels(const DevNet &net) {
     const int n = net.ni;
-    cudaError_t e = cudaFuncSetAttribute(k_prep32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem_prep(net));
+    cudaError_t e = raise_smem_limit(k_prep32, (int)smem_prep(net));
     int dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
     size_t s32 = smem32(n, lu32_nbuf(n));
 #define SETATTR(TY, RA, RB)                                                                      \
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu32<TY, RA, RB>,                           \
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s32);
+    if (e == cudaSuccess) e = raise_smem_limit(k_lu32<TY, RA, RB>, (int)s32);
     VK_LU_TILINGS(SETATTR)
 #undef SETATTR
     return e;

@@ -623,13 +623,13 @@ size_t lu_tc_smem(int n) { return (size_t)tc_layout(n).total; }
 cudaError_t init_lu_tc(int n) {
     if (!lu_tc_supported(n)) return cudaSuccess;
     const int sm = (int)lu_tc_smem(n);
-    cudaError_t e = cudaFuncSetAttribute(k_lu_tc<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaError_t e = raise_smem_limit(k_lu_tc<3, false>, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_lu_tc<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        e = raise_smem_limit(k_lu_tc<4, false>, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_lu_tc<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        e = raise_smem_limit(k_lu_tc<3, true>, sm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_lu_tc<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        e = raise_smem_limit(k_lu_tc<4, true>, sm);
     return e;
 }
 

@@ -293,7 +293,7 @@ void launch_reset_route(const Work &w, int ncols, double route_dt0, cudaStream_t
 
 cudaError_t init_mixed_kernels(int n) {
     size_t sm = 16 + (size_t)2 * block_stride32(n) * sizeof(float) + 2 * n * sizeof(float);
-    return cudaFuncSetAttribute(k_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    return raise_smem_limit(k_refine, (int)sm);
 }
 
 void launch_refine(const DevNet &net, const DevBatch &b, const Work &w, const double *rhs,

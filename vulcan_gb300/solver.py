@@ -7,6 +7,7 @@
 * ``Ros2Handle``    owns a ``vk_handle``: one attempt for every column
                     (``attempt``, = op.Ros2.solver) or a device-side run to
                     steady state (``run``, = op.Integration for every column).
+* ``Ros2Group``     several handles (networks of any size) run by one graph.
 * ``make_ros2gpu``  builds the drop-in solver class for the reference's
                     ``op`` module (see ``Ros2GPU`` below).
 """
@@ -414,6 +415,46 @@ class Ros2Handle:
         c = np.empty((self.batch.ncols, capi.NCOUNTERS), dtype=np.int32)
         check(lib().vk_get_counters(self.h, ptr(c, C.c_int)), self.h)
         return c
+
+
+class Ros2Group:
+    """Handles of several networks (any ni) run to steady state by one graph
+    per replay (C-ABI ``vk_group_*``): each handle's attempts and control on
+    its own stream, so the networks share the GPU.  Results per handle are
+    those of ``Ros2Handle.run`` on that handle alone, bit for bit.  The group
+    keeps its handles alive and is closed before them."""
+
+    def __init__(self, handles):
+        self.handles = list(handles)
+        n = len(self.handles)
+        arr = (C.c_void_p * n)(*[h.h for h in self.handles])
+        g = C.c_void_p()
+        check(lib().vk_group_create(arr, n, C.byref(g)))
+        self.g = g
+
+    def close(self):
+        if getattr(self, 'g', None):
+            lib().vk_group_destroy(self.g)
+            self.g = None
+
+    __del__ = close
+
+    def run(self, ctrls, max_steps=0, timeout_s=0.0, max_attempts=0):
+        """vk_group_run: ctrls is one VkCtrl for every handle, or a list of
+        them in handle order."""
+        n = len(self.handles)
+        if isinstance(ctrls, capi.VkCtrl):
+            ctrls = [ctrls] * n
+        if len(ctrls) != n:
+            raise ValueError('one control struct per handle: %d for %d handles' % (len(ctrls), n))
+        arr = (capi.VkCtrl * n)(*ctrls)
+        check(lib().vk_group_run(self.g, arr, int(max_steps), int(max_attempts), float(timeout_s)))
+
+    def timing(self):
+        """(device ms, kernels launched) of the last run."""
+        ms, n = C.c_double(), C.c_int()
+        check(lib().vk_group_timing(self.g, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
 
 # --------------------------------------------------------------------------
