@@ -74,6 +74,7 @@ struct vk_handle {
     int cps = 0;                        // VK_CTAS_PER_SM override (0: kernel defaults)
     int cps_k[VK_TUNE_N] = {0, 0, 0, 0}; // vk_set_launch: CTAs per SM per kernel
     int lu32_tiling = -1;               // vk_set_launch: k_lu32 tiling (-1: by ni)
+    int occ_rates = 0, occ_prep = 0;    // resident CTAs per SM of k_rates / k_prep32
     double *d_k = nullptr, *d_atm = nullptr, *d_Dzz = nullptr, *d_spf = nullptr;
     vk::Work w{};
     // batched-run state
@@ -114,6 +115,8 @@ struct vk_handle {
         b.cps = cps;
         for (int i = 0; i < VK_TUNE_N; ++i) b.cps_k[i] = cps_k[i];
         b.lu32_tiling = lu32_tiling;
+        b.grid_rates = nsm * occ_rates;
+        b.grid_prep = nsm * occ_prep;
         return b;
     }
 };
@@ -344,6 +347,9 @@ extern "C" int vk_create(const vk_network *net, int max_cols, int max_layers, in
                                                      : fail(h, VK_ECUDA, "cudaFuncSetAttribute (LU) failed"));
     TRY(vk::init_lu_tc(h->ni) == cudaSuccess ? VK_OK
                                              : fail(h, VK_ECUDA, "cudaFuncSetAttribute (tensor-core LU) failed"));
+    h->occ_rates = vk::rates_blocks_per_sm(h->net());
+    h->occ_prep = vk::prep_blocks_per_sm(h->net());
+    cudaGetLastError();                 // an occupancy query that failed leaves one CTA per layer
     // per-column run state (small); the history ring is sized at the first vk_run
     vk::RunState &r = h->rs;
     r.y = w.y; r.ymix = w.ymix; r.dt = w.dt; r.delta = w.delta; r.atm = h->d_atm;

@@ -120,7 +120,16 @@ struct DevBatch {
                                // (0: each kernel's own default)
     int cps_k[VK_TUNE_N];      // per-kernel setting of vk_set_launch (0: cps)
     int lu32_tiling;           // k_lu32 register tiling (-1: by ni)
+    int grid_rates, grid_prep; // CTAs of the per-layer kernels k_rates / k_prep32:
+                               // all of them resident at once, each striding over
+                               // the layers (0: one CTA per layer)
 };
+
+// Grid of a per-layer kernel whose CTAs stride over the layers: as many CTAs
+// as fit on the device at once (per_sm of them per SM), at most one per layer.
+inline int layer_grid(const DevBatch &b, int want) {
+    return want > 0 && want < b.L ? want : (b.L > 0 ? b.L : 1);
+}
 
 // Doubles per FP64 block of the n x n inverses in global memory: n*n rounded
 // up to even, so every block starts on 16 bytes (bulk-copy alignment).
@@ -251,6 +260,10 @@ void launch_route(const DevBatch &b, const Work &w, cudaStream_t s);
 void launch_reset_route(const Work &w, int ncols, double route_dt0, cudaStream_t s);
 cudaError_t init_mixed_kernels(int n);
 cudaError_t init_lureg_kernels(const DevNet &net);
+// Resident CTAs per SM of the per-layer kernels for a network (0: unknown);
+// call after the init_* functions have raised their shared-memory limits.
+int rates_blocks_per_sm(const DevNet &net);
+int prep_blocks_per_sm(const DevNet &net);
 void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaStream_t s);
 int lu32_tiling_cap(int tiling);     // largest block a k_lu32 tiling covers (0: none)
 // tensor-core factorisation (vk_lutc.cu): the LU32 tiling values that select

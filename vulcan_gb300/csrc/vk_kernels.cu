@@ -58,16 +58,20 @@ __device__ __forceinline__ double side_rate(double kk, const PairDesc *pd, int s
 // of vk_network.cpp) and the loops a warp runs have similar lengths (pairs,
 // species, half terms and Jacobian entries in decreasing order of length).
 template <bool JAC>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
 k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict__ f,
         double *__restrict__ jv, double *__restrict__ dA, double *__restrict__ dB,
         double *__restrict__ dC, const double *__restrict__ k1, const double *__restrict__ dt,
         const double *__restrict__ geo, int flags, int chem_only) {
     extern __shared__ double sm[];
     const int ni = net.ni;
-    const int l = blockIdx.x;
+    // the CTAs stride over the layers, so layers of inactive columns cost a
+    // test each rather than a CTA launch (an attempt in which few columns
+    // still run launches few CTAs' worth of work); every layer ends with a
+    // block barrier before the next one's shared-memory writes
+    for (int l = blockIdx.x; l < b.L; l += gridDim.x) {
     const int c = b.lay_col[l];
-    if (c < 0 || (b.active && !b.active[c])) return;     // gap layer of a slot, or inactive
+    if (c < 0 || (b.active && !b.active[c])) continue;   // gap layer of a slot, or inactive
     const int l0 = b.col_off[c], nz = b.col_end[c] - l0;
     const int j = l - l0;
     double *yl = sm;                       // [ni + 1] layer j, then M (factor index ni)
@@ -157,22 +161,25 @@ k_rates(DevNet net, DevBatch b, const double *__restrict__ y, double *__restrict
             dC[(size_t)l * ni + s] = cC;
         }
     }
-    if (!JAC) return;
-    __syncthreads();
-    // derivative half terms: k_side x product of the side's remaining factors
-    for (int h = tid; h < net.nh; h += nth) {
-        double d = kl[net.hk[h]];
-        for (int t = net.hptr[h]; t < net.hptr[h + 1]; ++t) d = __dmul_rn(d, yl[net.hfac[t]]);
-        v[h] = d;
+    if (JAC) {
+        __syncthreads();
+        // derivative half terms: k_side x product of the side's remaining factors
+        for (int h = tid; h < net.nh; h += nth) {
+            double d = kl[net.hk[h]];
+            for (int t = net.hptr[h]; t < net.hptr[h + 1]; ++t) d = __dmul_rn(d, yl[net.hfac[t]]);
+            v[h] = d;
+        }
+        __syncthreads();
+        double *jl = jv + (size_t)l * net.nnz;
+        for (int ei = tid; ei < net.nnz; ei += nth) {
+            const int e = net.jorder[ei];
+            double acc = 0.0;
+            for (int t = net.hjptr[e]; t < net.hjptr[e + 1]; ++t)
+                acc = __fma_rn(net.hjcoef[t], v[net.hjterm[t]], acc);
+            jl[e] = -acc;                      // entries of -J (neg_symjac)
+        }
     }
     __syncthreads();
-    double *jl = jv + (size_t)l * net.nnz;
-    for (int ei = tid; ei < net.nnz; ei += nth) {
-        const int e = net.jorder[ei];
-        double acc = 0.0;
-        for (int t = net.hjptr[e]; t < net.hjptr[e + 1]; ++t)
-            acc = __fma_rn(net.hjcoef[t], v[net.hjterm[t]], acc);
-        jl[e] = -acc;                      // entries of -J (neg_symjac)
     }
 }
 
@@ -506,16 +513,27 @@ void launch_rates(const DevNet &net, const DevBatch &b, const double *y, double 
                   double *jv, double *dA, double *dB, double *dC, const double *k1,
                   const double *dt, const double *geo, int flags, bool with_jac, cudaStream_t s) {
     size_t sm = rates_smem(net);
+    const int grid = layer_grid(b, b.grid_rates);
     if (with_jac)
-        k_rates<true><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, geo, flags, 0);
+        k_rates<true><<<grid, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, geo, flags, 0);
     else
-        k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, geo, flags, 0);
+        k_rates<false><<<grid, 128, sm, s>>>(net, b, y, f, jv, dA, dB, dC, k1, dt, geo, flags, 0);
+}
+
+// Resident CTAs per SM of k_rates (the larger of its two forms' register
+// footprints sets it) for this network's shared memory.
+int rates_blocks_per_sm(const DevNet &net) {
+    const size_t sm = rates_smem(net);
+    int a = 0, c = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_rates<true>, 128, sm) != cudaSuccess) a = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_rates<false>, 128, sm) != cudaSuccess) c = 0;
+    return a < c ? a : c;
 }
 
 void launch_chem_only(const DevNet &net, const DevBatch &b, const double *y, double *f,
                       const double *geo, cudaStream_t s) {
     size_t sm = rates_smem(net);
-    k_rates<false><<<b.L, 128, sm, s>>>(net, b, y, f, nullptr, nullptr, nullptr, nullptr,
+    k_rates<false><<<layer_grid(b, b.grid_rates), 128, sm, s>>>(net, b, y, f, nullptr, nullptr, nullptr, nullptr,
                                         nullptr, nullptr, geo, 0, 1);
 }
 

@@ -78,15 +78,18 @@ __device__ __noinline__ float scaled_f32(double rs, double v, double cs) {
 // the FP64 pipe (about 1/60 of the FP32 rate on this chip) only adds the
 // diagonal and converts to FP32; values outside the normal range take the
 // FP64 expressions, which give the same results.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 6)
 k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__restrict__ dA,
          const double *__restrict__ dt, float *__restrict__ D32, double *__restrict__ rsc,
          double *__restrict__ csc, int ld, int bstride) {
     extern __shared__ double sp[];
     const int n = net.ni, nn = n * n, nnz = net.nnz;
-    const int l = blockIdx.x;
+    __shared__ double s_c0;
+    // the CTAs stride over the layers (inactive columns' layers cost a test
+    // each); every layer ends with a block barrier
+    for (int l = blockIdx.x; l < b.L; l += gridDim.x) {
     const int c = b.lay_col[l];
-    if (c < 0 || (b.active && !b.active[c])) return;
+    if (c < 0 || (b.active && !b.active[c])) continue;
     double *jls = sp;                       // [nnz]
     double *rs = jls + nnz;                 // [n]
     double *cs = rs + n;                    // [n]
@@ -97,7 +100,6 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
     int *rexp = cexp + n;                   // [n] log2 rs (kNoExp: use rs)
     int *cxp = rexp + n;                    // [n] log2 cs
     const int tid = threadIdx.x, nth = blockDim.x;
-    __shared__ double s_c0;
     if (tid == 0) s_c0 = 1.0 / (R_ROS * dt[c]);     // one FP64 division per layer
     const double *jl = jv + (size_t)l * nnz;
     for (int e = tid; e < nnz; e += nth) jls[e] = jl[e];
@@ -193,7 +195,10 @@ k_prep32(DevNet net, DevBatch b, const double *__restrict__ jv, const double *__
         rsc[(size_t)l * n + t] = rs[t];
         csc[(size_t)l * n + t] = cs[t];
     }
+    __syncthreads();
+    }
 }
+
 
 // FP32 block-Thomas factorisation of the scaled system, one column at a time
 // per CTA (columns from the work queue).
@@ -342,6 +347,13 @@ static int tiling_of(int n) {
     return 3;
 }
 
+// Resident CTAs per SM of k_prep32 for this network's shared memory.
+int prep_blocks_per_sm(const DevNet &net) {
+    int a = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_prep32, 256, smem_prep(net)) != cudaSuccess) a = 0;
+    return a;
+}
+
 cudaError_t init_lureg_kernels(const DevNet &net) {
     const int n = net.ni;
     cudaError_t e = raise_smem_limit(k_prep32, (int)smem_prep(net));
@@ -369,14 +381,14 @@ void launch_lu_reg32(const DevNet &net, const DevBatch &b, const Work &w, cudaSt
     if (tc && !w.tmap_d32) t = tiling_of(n);              // no tile map: CUDA-core kernel
     if (tc && w.tmap_d32) {
         const int NP = (n + 15) / 16 * 16;
-        k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs,
-                                                  NP, NP * NP);
+        k_prep32<<<layer_grid(b, b.grid_prep), 256, smem_prep(net), s>>>(
+            net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs, NP, NP * NP);
         cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
         launch_lu_tc(net, b, w, *static_cast<const CUtensorMap *>(w.tmap_d32), t == VK_LU_TC_COOP, s);
         return;
     }
-    k_prep32<<<b.L, 256, smem_prep(net), s>>>(net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs,
-                                              n, block_stride32(n));
+    k_prep32<<<layer_grid(b, b.grid_prep), 256, smem_prep(net), s>>>(
+        net, b, w.jv, w.dA, w.dt, w.D32, w.rs, w.cs, n, block_stride32(n));
     const int nb = lu32_nbuf(n);
     size_t sm = smem32(n, nb);
     cudaMemsetAsync(b.queue, 0, sizeof(unsigned), s);
