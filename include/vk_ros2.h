@@ -385,9 +385,10 @@ VK_API int  vk_mlp_adam(long long n, float *w, void *w_bf16, const float *g, flo
  * device pointers supplied by the caller; lower[0] and upper[nz-1] are not
  * read.  Requires nz*ni*ni + nz*ni + 1 <= 2^21 (e.g. nz = 200 at ni = 100);
  * larger sizes return VK_EINVAL.  Runs on `stream` (a cudaStream_t, NULL for
- * the default stream) and synchronizes it to return VK_ESINGULAR / VK_ENAN.
- * The first call on a device resolves the array's address on that device, so
- * make it before any stream capture.  All calls share the one array: calls
+ * the default stream) and synchronizes it to return VK_ESINGULAR / VK_ENAN,
+ * so it cannot be called while any stream is being captured into a graph.
+ * The first call on a device resolves the array's address on that device.
+ * All calls share the one array: calls
  * that overlap on the GPU (other threads or streams) race; serialize them.
  * Errors: vk_last_error(NULL). */
 VK_API int  vk_block_solve_noalloc(int nz, int ni, const double *D, const double *lower,
