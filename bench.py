@@ -546,8 +546,10 @@ def converge_block(args):
             'median_over_columns_of_max': float(np.median(errs)) if errs else None,
             'max_over_columns_of_max': max(errs) if errs else None,
             'columns_within_1e-3': int(sum(e <= 1e-3 for e in errs))}
-        res['learned_mixed']['columns_per_hour_over_fp64'] = round(
-            res['learned_mixed']['columns_per_hour'] / max(res['plain_fp64']['columns_per_hour'], 1e-9), 3)
+        # no ratio when the FP64 stream converged no column within its budget
+        fp64_cph = res['plain_fp64']['columns_per_hour']
+        res['learned_mixed']['columns_per_hour_over_fp64'] = (
+            round(res['learned_mixed']['columns_per_hour'] / fp64_cph, 3) if fp64_cph > 0 else None)
     res['setup'] = ('a stream of %d seeded columns through %d slots (continuous batching: a slot '
                     'whose column ends takes the next one, checked every %s), %.0f s of wall time '
                     'per path including the learned proposals and their judge (the residual of the '
