@@ -53,7 +53,7 @@ __device__ __forceinline__ double side_rate(double kk, const PairDesc *pd, int s
 }
 
 // ---------------------------------------------------------------------------
-// (a)+(b) rate / source / Jacobian kernel: one CTA per layer.  The FP64 pipe
+// (a)+(b) rate / source / Jacobian kernel: a CTA per layer at a time.  The FP64 pipe
 // bounds it, so every gathered term is one FP64 instruction (the gather form
 // of vk_network.cpp) and the loops a warp runs have similar lengths (pairs,
 // species, half terms and Jacobian entries in decreasing order of length).
