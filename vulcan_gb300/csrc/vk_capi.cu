@@ -1395,12 +1395,13 @@ extern "C" int vk_group_run(vk_group *g, const vk_ctrl *ctrls, int max_steps, in
     }
     auto t0 = std::chrono::steady_clock::now();
     cudaEventRecord(g->ev[0], s);
-    int launches = 0, per_replay = 0;
+    int launches = 0, per_replay = 0, replays = 0;
     for (int i = 0; i < n; ++i) per_replay += body_launches(g->hs[i], ga);
     const int max_replays = max_attempts > 0 ? (max_attempts + ga - 1) / ga : 0;
     for (int replay = 1;; ++replay) {
         VK_CUDA(nullptr, cudaGraphLaunch(g->gexec, s));
         launches += per_replay;
+        replays = replay;
         for (int i = 0; i < n; ++i)
             VK_CUDA(nullptr, cudaMemcpyAsync(g->h_nactive + i, g->hs[i]->d_nactive, sizeof(int),
                                              cudaMemcpyDeviceToHost, s));
@@ -1420,9 +1421,9 @@ extern "C" int vk_group_run(vk_group *g, const vk_ctrl *ctrls, int max_steps, in
     g->launches = launches;
     for (int i = 0; i < n; ++i) {
         vk_handle *h = g->hs[i];
-        h->ms[0] = g->ms;
+        h->ms[0] = g->ms;                 // device time of the whole group call
         h->ms[1] = h->ms[2] = h->ms[3] = 0.f;
-        h->launches = launches;
+        h->launches = replays * body_launches(h, ga);
         int rc = run_check_end(h);
         if (rc) return fail(nullptr, rc, "handle " + std::to_string(i) + ": " + h->err);
     }
