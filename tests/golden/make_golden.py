@@ -30,7 +30,9 @@ Workloads:
       (T-independent and T-dependent cross sections, other parameters, the
       sulfur network);
   lowT, rmlist, snchok   rate constants (low-temperature caps, reactions
-      removed, the sulfur network).
+      removed, the sulfur network);
+  c4s   Ros2 attempts on the seeded 150-species synthetic network
+      (vulcan_gb300.synthnet, installed into the copy), 20 layers.
 
 Usage:  python tests/golden/make_golden.py [tag ...] [--ref <VULCAN tree>]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
@@ -75,11 +77,12 @@ KEEP = {'c0': (0, 1, 2, 3, 5, 8, 13, 40, 99, 100, 101, 150, 250, 499),
         'snchok': (0,),
         'c3s': (0, 1, 2, 5, 9),
         'c0n2': (0,), 'c0o2': (0,), 'c0co2': (0,), 'c0rocky': (0,),
-        'c0vul': (0,)}
+        'c0vul': (0,),
+        'c4s': (0, 1, 2, 5, 9)}
 NSTEPS = {'c0': 500, 'c1': 30, 'c2': 30, 'c2long': 2000, 'c2conv': 4000, 'c2tight': 12000,
           'c2slow': 4000, 'c1rt': 110, 'c1rtT': 110, 'c1rtA': 2, 'c3rt': 2, 'lowT': 1, 'c0bc': 30,
           'c0nomol': 30, 'c0vz': 30, 'rmlist': 1, 'snchok': 1, 'c3s': 10, 'c0n2': 2, 'c0o2': 2, 'c0co2': 2,
-          'c0rocky': 2, 'c0vul': 20}
+          'c0rocky': 2, 'c0vul': 20, 'c4s': 10}
 # convergence criterion tightened from the reference defaults (yconv_cri 0.01,
 # yconv_min 0.1): a steady state determined to ~1e-3 that another integrator
 # must reproduce, whatever path it takes there
@@ -120,6 +123,11 @@ EXTRA_CFG['c1rtA'] = ('dbin1 = 2.0\nsl_angle = 60. / 180. * 3.14159\nedd = 0.669
 # the sulfur network's radiative transfer (37 absorbers, 60 channels)
 EXTRA_CFG['c3rt'] = 'dbin1 = 2.0\n'
 PHOTO_TAGS = ('c1rt', 'c1rtT', 'c1rtA', 'c3rt')
+# the seeded 150-species synthetic network (vulcan_gb300.synthnet: network
+# file, NASA-9 files and composition table in the reference's formats,
+# installed into the temporary copy) on a 20-layer column with frozen J on
+# its 60 photolysis channels
+SYN_TAGS = ('c4s',)
 # rate constants only (no integration): read_rate, lim_lowT_rates, rev_rate
 RATE_TAGS = ('lowT', 'rmlist', 'snchok')
 # the sulfur network with its photolysis slots (rate constants only)
@@ -468,7 +476,21 @@ def cfg_overrides(spec, nz, count_max, use_photo, extra=''):
         ''') + extra
 
 
-def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
+def install_synthetic(dst, syn_dir):
+    """The synthetic network's files in the reference copy: the network into
+    thermo/, its NASA-9 files into thermo/NASA9/ (replacing the real ones of
+    the species it shares names with), its composition table as
+    thermo/all_compose.txt."""
+    thermo = os.path.join(dst, 'thermo')
+    for f in os.listdir(syn_dir):
+        if f.endswith('_network.txt'):
+            shutil.copy(os.path.join(syn_dir, f), os.path.join(thermo, f))
+    shutil.copy(os.path.join(syn_dir, 'all_compose.txt'), os.path.join(thermo, 'all_compose.txt'))
+    for f in os.listdir(os.path.join(syn_dir, 'NASA9')):
+        shutil.copy(os.path.join(syn_dir, 'NASA9', f), os.path.join(thermo, 'NASA9', f))
+
+
+def run_reference(ref_root, tag, spec, nsteps, keep, workdir, syn_dir=None):
     nz = spec.pco.size
     dst = os.path.join(workdir, 'vref_' + tag)
     shutil.copytree(ref_root, dst, ignore=shutil.ignore_patterns('output', 'plot', '.DS_Store'))
@@ -478,6 +500,8 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir):
             os.chmod(os.path.join(root, d), 0o755)
         for f in files:
             os.chmod(os.path.join(root, f), 0o644)
+    if syn_dir:
+        install_synthetic(dst, syn_dir)
     if tag in BC_TAGS:
         for name, text in BC_FILES.items():
             with open(os.path.join(dst, name), 'w') as f:
@@ -579,6 +603,7 @@ def slim_photo(d):
 
 
 def make(tag, ref_root, workdir, full_dir=None):
+    syn_dir = None                        # synthetic network files (SYN_TAGS)
     if tag in ('c0', 'c0bc', 'c0nomol', 'c0vz', 'c0n2', 'c0o2', 'c0co2', 'c0rocky', 'c0vul'):
         spec = configs.config0()
     elif tag in ('c2', 'c2long', 'c2conv', 'c2tight'):
@@ -610,15 +635,20 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a cold column (150 -> 450 K) crossing the three low-temperature caps
         spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]
         spec.Tco = configs.linear_logp_T(spec.pco, 450., 150.)
+    elif tag in SYN_TAGS:
+        from vulcan_gb300 import synthnet
+        syn_dir = os.path.join(workdir, 'syn150')
+        snet = Network.from_file(synthnet.generate(syn_dir), use_photo=True)
+        spec = configs.config4_columns(sorted(snet.photo_index()), ncols=1, nz=20)[0]
     elif tag in ('c1', 'c1rt', 'c1rtT', 'c1rtA'):
         net = Network.from_file(os.path.join(ref_root, 'thermo', 'NCHO_photo_network.txt'),
                                 use_photo=True)
         spec = configs.config1(sorted(net.photo_index()))
     else:
         raise ValueError(tag)
-    net = Network.from_file(os.path.join(ref_root, 'thermo', spec.network),
+    net = Network.from_file(os.path.join(syn_dir or os.path.join(ref_root, 'thermo'), spec.network),
                             use_photo=spec.use_photo)
-    dst = run_reference(ref_root, tag, spec, NSTEPS[tag], KEEP[tag], workdir)
+    dst = run_reference(ref_root, tag, spec, NSTEPS[tag], KEEP[tag], workdir, syn_dir)
     d = dict(np.load(os.path.join(dst, 'golden_out.npz'), allow_pickle=False))
     if tag in RATE_TAGS:
         out = os.path.join(HERE, 'golden_%s.npz' % tag)
@@ -655,8 +685,9 @@ def make(tag, ref_root, workdir, full_dir=None):
         d['photo_br'] = np.array([k[1] for k in keys])
     out = os.path.join(HERE, 'golden_%s.npz' % tag)
     np.savez_compressed(out, **d)
-    net.to_npz(os.path.join(HERE, 'net_%s.npz' % spec.network.replace('_network.txt', '')
-                            + ('_photo' if spec.use_photo and 'photo' not in spec.network else '')))
+    net.to_npz(os.path.join(HERE, 'net_%s.npz' % (
+        spec.network.replace('_network.txt', '')
+        + ('_photo' if spec.use_photo and 'photo' not in spec.network else ''))))
     if full_dir and tag not in ('c2conv', 'c2tight', 'c2slow'):
         os.makedirs(full_dir, exist_ok=True)
         shutil.copy(os.path.join(dst, 'golden_full.npz'),

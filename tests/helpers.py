@@ -15,7 +15,8 @@ NETS = {'c0': 'net_CHO_thermo.npz', 'c1': 'net_NCHO_photo.npz', 'c2': 'net_NCHO_
         'c0bc': 'net_CHO_thermo.npz', 'c0nomol': 'net_CHO_thermo.npz',
         'c0vz': 'net_CHO_thermo.npz', 'c0n2': 'net_CHO_thermo.npz',
         'c0o2': 'net_CHO_thermo.npz', 'c0co2': 'net_CHO_thermo.npz',
-        'c0rocky': 'net_CHO_thermo.npz', 'c3s': 'net_SNCHO_photo.npz'}
+        'c0rocky': 'net_CHO_thermo.npz', 'c3s': 'net_SNCHO_photo.npz',
+        'c4s': 'net_SYN150_photo.npz'}
 
 
 def golden(tag):

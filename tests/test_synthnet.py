@@ -1,6 +1,8 @@
 """Synthetic 150-species stress network (ni = 150, 1200 reversible reactions,
-60 frozen photolysis channels, nz = 200): generator checks on the CPU, and on
-the GPU the chemistry and whole Ros2 attempts against the oracle."""
+60 frozen photolysis channels, nz = 200): generator checks on the CPU; the
+oracle and the device tables' gather form against the reference's own run on
+this network (fixture c4s: its code generator, rate set-up and Ros2 attempts);
+on the GPU the chemistry and whole Ros2 attempts against the oracle."""
 import os
 
 import numpy as np
@@ -173,3 +175,76 @@ def test_species_missing_from_composition_file_is_named(tmp_path):
     with pytest.raises(ValueError, match=victim):
         Network.from_file(src, use_photo=True)
     shutil.rmtree(d)
+
+
+# ---- pinned to the reference itself: fixture c4s, recorded by running the
+# unmodified reference (its own code generator, rate set-up and Ros2 loop) on
+# the generator's files installed into a copy (tests/golden/make_golden.py)
+
+def test_reference_fixture_is_this_generator(syn):
+    """The network the reference ran is the one this generator writes: the
+    same species in the reference's own order, the same rate slots."""
+    from helpers import golden, network
+    g = golden('c4s')
+    net = network('c4s')
+    assert [str(s) for s in g['spec_list']] == list(net.species) == list(syn[1].species)
+    assert int(g['nr']) == net.nr == syn[1].nr
+    assert [r.text for r in net.reactions] == [r.text for r in syn[1].reactions]
+
+
+def test_oracle_chemistry_matches_reference_c4s():
+    """chemdf bit for bit, -J within 1e-14 of the block scale with the same
+    sparsity as the reference's sympy Jacobian (150 species, 2522 rate slots)."""
+    from helpers import golden, oracle_net
+    g = golden('c4s')
+    on = oracle_net('c4s', g)
+    np.testing.assert_array_equal(O.chemdf(on, g['y_ini'], g['M'], g['k']), g['chemdf0'])
+    J = O.neg_jac_blocks(on, g['y_ini'], g['M'], g['k'])
+    for i, l in enumerate(g['negjac_layers']):
+        ref = g['negjac_blocks'][i]
+        assert np.max(np.abs(J[l] - ref)) <= 1e-14 * np.abs(ref).max()
+        assert np.all((J[l] != 0) == (ref != 0))
+
+
+@pytest.mark.parametrize('n', range(5))
+def test_oracle_attempts_match_reference_c4s(n):
+    """Recorded Ros2 attempts (accepted and rejected, from const_mix) on the
+    150-species network: the banded (the reference's LAPACK solve) and the
+    block-Thomas restatements within 1e-10."""
+    from helpers import attempt_atm, golden, oracle_net
+    g = golden('c4s')
+    on = oracle_net('c4s', g)
+    args = (on, g['att_y'][n], g['att_ymix'][n], float(g['att_dt'][n]), g['k'],
+            attempt_atm(g, n), O.Flags(), O.Tol())
+    for solve in ('banded', 'block'):
+        r = O.ros2_attempt(*args, solve)
+        assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
+        assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
+
+
+def test_gather_form_matches_reference_c4s():
+    """The device tables' host evaluation (vk_network_eval_host: the rate
+    kernel's gather form, operations and order) on every layer of the
+    recorded start: chemdf bit for bit, -J within 1e-14."""
+    import ctypes as C
+    from helpers import golden, network
+    from vulcan_gb300 import _build, capi
+    from vulcan_gb300.solver import GPUNetwork
+    _build.build()
+    g = golden('c4s')
+    net = network('c4s')
+    gn = GPUNetwork(net, ATOMS)
+    rows, cols = gn.jac_pattern()
+    lib = capi.lib()
+    p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    for l in range(g['y_ini'].shape[0]):
+        y = np.ascontiguousarray(g['y_ini'][l])
+        k = np.ascontiguousarray(g['k'][:, l])
+        f, jv = np.zeros(net.ni), np.zeros(gn.nnz)
+        assert lib.vk_network_eval_host(gn.handle, p(y), p(k), float(g['M'][l]), p(f), p(jv)) == 0
+        np.testing.assert_array_equal(f, g['chemdf0'][l])
+        if l in g['negjac_layers']:
+            ref = g['negjac_blocks'][list(g['negjac_layers']).index(l)]
+            J = np.zeros((net.ni, net.ni))
+            J[rows, cols] = jv
+            assert np.abs(J - ref).max() <= 1e-14 * np.abs(ref).max()
