@@ -135,3 +135,60 @@ def test_mlp_training_reduces_loss():
     m = MLP(23, 69, width=128, depth=2, seed=0)
     hist = m.fit(X, Y, epochs=8, batch=1024, lr=3e-3)
     assert hist[-1] < 0.3 * hist[0]
+
+
+class _RhsHandle:
+    """Stand-in for a device handle: f(y) = y - target, so a state's residual
+    is its distance from the target; records the state it is given back."""
+
+    def __init__(self, target):
+        self.target = target
+        self.set = None
+
+    def rhs(self, y, flags):
+        return y - self.target
+
+    def set_state(self, y, ymix):
+        self.set = (y.copy(), ymix.copy())
+
+
+def test_judge_keeps_a_proposal_only_where_it_lowers_the_residual():
+    """judge_proposals (host logic): per column, the residual of the Ros2
+    system (mean over the column's layers of max_i |f_i| / (|y_i| + 1e-10
+    n_0)) at the proposal against const_mix; the proposal stays where it is
+    not larger, and the const_mix state of the others goes back into the
+    handle, column by column in layer order."""
+    import types
+    from vulcan_gb300.warmstart import judge_proposals, rhs_residual
+    nz, ni = (3, 2, 4), 5
+    off = np.concatenate([[0], np.cumsum(nz)])
+    b = types.SimpleNamespace(ncols=3, off=off)
+    target = np.full((off[-1], ni), 1e6)
+    rng = np.random.default_rng(0)
+    const, warm = [], []
+    for c, n in enumerate(nz):
+        col = types.SimpleNamespace(n_0=np.full(n, 1e8))
+        yc = target[off[c]:off[c + 1]] * (1 + rng.uniform(0.5, 1.0, (n, ni)))
+        # columns 0 and 2: the proposal is closer to the target; column 1: farther
+        scale = 0.1 if c != 1 else 3.0
+        yw = target[off[c]:off[c + 1]] + scale * (yc - target[off[c]:off[c + 1]])
+        const.append(dict(col=col, y=yc, ymix=yc / yc.sum(1, keepdims=True)))
+        warm.append(dict(col=col, y=yw, ymix=yw / yw.sum(1, keepdims=True)))
+    h = _RhsHandle(target)
+    n0 = np.full(off[-1], 1e8)
+    y_all = np.concatenate([it['y'] for it in warm])
+    r = np.abs(y_all - target) / (np.abs(y_all) + 1e-10 * n0[:, None])
+    want = [r[off[c]:off[c + 1]].max(axis=1).mean() for c in range(3)]
+    np.testing.assert_allclose(rhs_residual(h, y_all, n0, b), want, rtol=0, atol=0)
+    items, used = judge_proposals(h, b, warm, const)
+    assert used.tolist() == [True, False, True]
+    assert [it is w for it, w in zip(items, warm)] == [True, False, True]
+    assert items[1] is const[1]
+    np.testing.assert_array_equal(h.set[0], np.concatenate([warm[0]['y'], const[1]['y'], warm[2]['y']]))
+    np.testing.assert_array_equal(h.set[1], np.concatenate([warm[0]['ymix'], const[1]['ymix'],
+                                                            warm[2]['ymix']]))
+    # every proposal kept: the handle's state is left alone
+    h2 = _RhsHandle(target)
+    warm_all = [warm[0], dict(warm[1], y=const[1]['y']), warm[2]]      # ties keep the proposal
+    items, used = judge_proposals(h2, b, warm_all, const)
+    assert used.all() and h2.set is None
