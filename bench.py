@@ -777,6 +777,57 @@ def run_c1_converge(args):
     print(json.dumps(res))
 
 
+def run_group(args):
+    """Several networks in one launch: 64 NCHO-thermo columns (69 species)
+    and 16 columns of the 150-species synthetic network (nz = 200), 10 steps
+    of every column after 10 warm-up steps, the two handles run one after
+    the other (vk_run each) and as one group (vk_group_run), mixed and FP64;
+    wall time of the calls and whether the group's final states equal the
+    separate runs' bit for bit."""
+    from vulcan_gb300 import _build, batch, capi, configs, synthnet
+    from vulcan_gb300.network import Network
+    from vulcan_gb300.solver import Ros2Group, ctrl_from
+    _build.build()
+    ncho = Network.from_npz(NET)
+    ia = batch.build_items(configs.config2_columns(ncols=64, seed=11), ncho)
+    syn = Network.from_file(synthnet.generate(os.path.join(REPO, '_build', 'syn150')),
+                            use_photo=True)
+    ib = batch.build_items(configs.config4_columns(sorted(syn.photo_index()), ncols=16, nz=200),
+                           syn)
+    ctrl = ctrl_from(None, gs=configs.GS, Rp=configs.RP)
+    out = {}
+    for prec in (capi.VK_PREC_MIXED, capi.VK_PREC_FP64):
+        def handles():
+            return [batch.make_batch_handle(ncho, ia, ATOMS, prec)[0],
+                    batch.make_batch_handle(syn, ib, ATOMS, prec)[0]]
+        hs = handles()
+        for h in hs:
+            h.run(ctrl, max_steps=10, timeout_s=600)
+        per = []
+        for h in hs:
+            t1 = time.perf_counter()
+            h.run(ctrl, max_steps=10, timeout_s=600)
+            per.append(time.perf_counter() - t1)
+        ys = [h.state()['y'].copy() for h in hs]
+        for h in hs:
+            h.close()
+        hs = handles()
+        g = Ros2Group(hs)
+        g.run(ctrl, max_steps=10, timeout_s=600)
+        t1 = time.perf_counter()
+        g.run(ctrl, max_steps=10, timeout_s=600)
+        grp = time.perf_counter() - t1
+        same = all(np.array_equal(y, h.state()['y']) for y, h in zip(ys, hs))
+        g.close()
+        for h in hs:
+            h.close()
+        out['mixed' if prec else 'fp64'] = dict(separate_s=[round(x, 4) for x in per],
+                                                separate_total_s=round(sum(per), 4),
+                                                group_s=round(grp, 4), bit_identical=same)
+    print(json.dumps({'group': out, 'workload': '64 NCHO-thermo columns + 16 columns of the '
+                      '150-species synthetic network (nz = 200), 10 steps each after 10'}))
+
+
 def run_photo(args):
     """Radiative transfer throughput: vk_photo_update over --ncols columns of
     the NCHO photochemistry workload (nz = 150) on the reference's binned
@@ -879,6 +930,8 @@ def main():
     ap.add_argument('--attempts', type=int, default=2)
     ap.add_argument('--lu-variant', type=int, default=-1,
                     help='profile mode: FP32 factorisation variant (vk_set_launch; -1: default)')
+    ap.add_argument('--group', action='store_true',
+                    help='two networks (69 and 150 species) in one graph launch against one after the other')
     ap.add_argument('--photo', action='store_true',
                     help='radiative-transfer update throughput (photochemistry workload)')
     ap.add_argument('--precision', default='mixed', choices=['mixed', 'fp64'])
@@ -929,6 +982,9 @@ def main():
         return
     if args.profile:
         run_profile(args)
+        return
+    if args.group:
+        run_group(args)
         return
     if args.photo:
         run_photo(args)
