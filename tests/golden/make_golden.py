@@ -32,7 +32,9 @@ Workloads:
   lowT, rmlist, snchok   rate constants (low-temperature caps, reactions
       removed, the sulfur network);
   c4s   Ros2 attempts on the seeded 150-species synthetic network
-      (vulcan_gb300.synthnet, installed into the copy), 20 layers.
+      (vulcan_gb300.synthnet, installed into the copy), 20 layers;
+  n_<network>   every shipped network the reference can set up: rate
+      constants, chemdf at a seeded state with seeded J, -J blocks.
 
 Usage:  python tests/golden/make_golden.py [tag ...] [--ref <VULCAN tree>]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
@@ -123,6 +125,34 @@ EXTRA_CFG['c1rtA'] = ('dbin1 = 2.0\nsl_angle = 60. / 180. * 3.14159\nedd = 0.669
 # the sulfur network's radiative transfer (37 absorbers, 60 channels)
 EXTRA_CFG['c3rt'] = 'dbin1 = 2.0\n'
 PHOTO_TAGS = ('c1rt', 'c1rtT', 'c1rtA', 'c3rt')
+# every network file the reference ships that its own set-up can use (two
+# cannot: SNCHO_photo_network_2025 names a species without a NASA-9 file,
+# SNCHO_photo_network_C3 species missing from all_compose.txt): rate
+# constants, the generated chemistry source at a seeded positive state with
+# seeded J in the photolysis slots, and -J blocks (rate driver, 8 layers)
+NET_FILES = ('CHO_photo_network.txt', 'CHO_photo_network_lowT.txt', 'CHO_thermo_network.txt',
+             'NCHO_earth_photo_network.txt', 'NCHO_full_photo_network.txt',
+             'NCHO_photo_network.txt', 'NCHO_photo_network_lowT.txt',
+             'NCHO_photo_network_lowT_Jupiter.txt', 'NCHO_photo_oxidising_network.txt',
+             'NCHO_thermo_network.txt', 'SNCHO_DMS_photo_network_Tsai2024.txt',
+             'SNCHO_full_photo_network.txt', 'SNCHO_photo_network.txt',
+             'SNCHO_photo_network_2024.txt', 'TiSNCHO_photo_network.txt')
+NET_TAGS = {'n_' + f.replace('_network', '').replace('.txt', ''): f for f in NET_FILES}
+for _t in NET_TAGS:
+    KEEP[_t], NSTEPS[_t] = (0,), 1
+
+
+def net_atoms(fname):
+    """The elements of a shipped network family."""
+    if fname.startswith('TiSNCHO'):
+        return ['H', 'O', 'C', 'He', 'N', 'S', 'Ti', 'V']
+    if fname.startswith('SNCHO'):
+        return ['H', 'O', 'C', 'He', 'N', 'S']
+    if fname.startswith('NCHO'):
+        return ['H', 'O', 'C', 'He', 'N']
+    return ['H', 'O', 'C', 'He']
+
+
 # the seeded 150-species synthetic network (vulcan_gb300.synthnet: network
 # file, NASA-9 files and composition table in the reference's formats,
 # installed into the temporary copy) on a 20-layer column with frozen J on
@@ -377,7 +407,7 @@ print('photo records', len(REC), 'nbins', len(var.bins), 'counts', [r['count'] f
 '''
 
 RATE_DRIVER = r'''
-import os, sys
+import os, sys, json
 import numpy as np
 sys.path.insert(0, os.getcwd())
 sys.path.insert(0, os.path.join(os.getcwd(), '_mplstub'))
@@ -398,6 +428,9 @@ k_plain = np.array([np.array(var.k[i], dtype=float) for i in range(1, chem_funs.
 var = rate.lim_lowT_rates(var, atm)
 var = rate.rev_rate(var, atm)
 var = rate.remove_rate(var)
+meta = json.load(open('golden_meta.json'))
+for key, J in zip(meta['photo_keys'], inp['photo_J']):     # seeded J (photolysis networks)
+    var.k[var.pho_rate_index[(key[0], int(key[1]))]] = J.copy()
 K = np.array([var.k[i] for i in range(1, chem_funs.nr + 1)])
 # the generated chemistry source at a seeded positive state (term-order pin)
 Y = 10.0 ** np.random.default_rng(7).uniform(0.0, 18.0, (atm.Tco.size, chem_funs.ni))
@@ -406,6 +439,7 @@ J0 = chem_funs.neg_symjac(Y, atm.M, var.k)
 lays = [0, atm.Tco.size // 2]
 np.savez_compressed('golden_out.npz', Tco=atm.Tco, M=atm.M, pco=atm.pco, k_plain=k_plain,
                     k=K, y_rand=Y, chemdf_rand=chem_funs.chemdf(Y, atm.M, var.k),
+                    spec_list=np.array(chem_funs.spec_list), nr=chem_funs.nr,
                     negjac_layers=np.array(lays),
                     negjac_blocks=np.array([J0[l*ni:(l+1)*ni, l*ni:(l+1)*ni] for l in lays]))
 print('rate constants', chem_funs.nr, 'layers', atm.Tco.size)
@@ -526,7 +560,8 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir, syn_dir=None):
     # for the radiative-transfer fixtures, which record the reference's own J
     with open(os.path.join(dst, 'vulcan_cfg.py'), 'w') as f:
         f.write(base_cfg + cfg_overrides(spec, nz, nsteps - 1,
-                                         tag in PHOTO_TAGS or tag in RATE_PHOTO_TAGS,
+                                         tag in PHOTO_TAGS or tag in RATE_PHOTO_TAGS
+                                         or (tag in NET_TAGS and spec.use_photo),
                                          EXTRA_CFG.get(tag, '')))
     keys = sorted(spec.photo_J) if spec.photo_J else []
     extra_in = {}
@@ -540,7 +575,8 @@ def run_reference(ref_root, tag, spec, nsteps, keep, workdir, syn_dir=None):
         json.dump({'photo_keys': [[k[0], k[1]] for k in keys], 'keep': list(keep),
                    'save_vul': tag == 'c0vul'}, f)
     with open(os.path.join(dst, 'golden_driver.py'), 'w') as f:
-        f.write(PHOTO_DRIVER if tag in PHOTO_TAGS else RATE_DRIVER if tag in RATE_TAGS else DRIVER)
+        f.write(PHOTO_DRIVER if tag in PHOTO_TAGS
+                else RATE_DRIVER if tag in RATE_TAGS or tag in NET_TAGS else DRIVER)
     r = subprocess.run([sys.executable, 'golden_driver.py'], cwd=dst, env=env,
                        capture_output=True, text=True)
     if r.returncode != 0:
@@ -635,6 +671,17 @@ def make(tag, ref_root, workdir, full_dir=None):
         # a cold column (150 -> 450 K) crossing the three low-temperature caps
         spec = configs.config2_columns(ncols=1, seed=2, nz_range=(40, 40))[0]
         spec.Tco = configs.linear_logp_T(spec.pco, 450., 150.)
+    elif tag in NET_TAGS:
+        import dataclasses
+        fname = NET_TAGS[tag]
+        photo_net = 'photo' in fname
+        spec = dataclasses.replace(configs.config2_columns(ncols=1, seed=2, nz_range=(8, 8))[0],
+                                   network=fname, use_photo=photo_net, atom_list=net_atoms(fname),
+                                   const_mix={'H2': 0.9, 'He': 0.1}, conver_ignore=[])
+        if photo_net:
+            pnet = Network.from_file(os.path.join(ref_root, 'thermo', fname), use_photo=True)
+            spec.photo_J = configs.photo_J_profile(np.random.default_rng(3), spec.pco,
+                                                   sorted(pnet.photo_index()))
     elif tag in SYN_TAGS:
         from vulcan_gb300 import synthnet
         syn_dir = os.path.join(workdir, 'syn150')
@@ -650,6 +697,17 @@ def make(tag, ref_root, workdir, full_dir=None):
                             use_photo=spec.use_photo)
     dst = run_reference(ref_root, tag, spec, NSTEPS[tag], KEEP[tag], workdir, syn_dir)
     d = dict(np.load(os.path.join(dst, 'golden_out.npz'), allow_pickle=False))
+    if tag in NET_TAGS:
+        if spec.photo_J:
+            keys = sorted(spec.photo_J)
+            d['photo_sp'] = np.array([k[0] for k in keys])
+            d['photo_br'] = np.array([k[1] for k in keys])
+        d['atom_list'] = np.array(spec.atom_list)
+        out = os.path.join(HERE, 'golden_%s.npz' % tag)
+        np.savez_compressed(out, **d)
+        net.to_npz(os.path.join(HERE, 'net_%s.npz' % tag[2:]))
+        print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
+        return
     if tag in RATE_TAGS:
         out = os.path.join(HERE, 'golden_%s.npz' % tag)
         np.savez_compressed(out, **d)
