@@ -34,7 +34,8 @@ Workloads:
   c4s   Ros2 attempts on the seeded 150-species synthetic network
       (vulcan_gb300.synthnet, installed into the copy), 20 layers;
   n_<network>   every shipped network the reference can set up: rate
-      constants, chemdf at a seeded state with seeded J, -J blocks.
+      constants, chemdf at a seeded state with seeded J, -J blocks;
+  a_<network>   Ros2 attempts on five more shipped networks (seeded J).
 
 Usage:  python tests/golden/make_golden.py [tag ...] [--ref <VULCAN tree>]
         python tests/golden/make_golden.py --setup-only c1rt c1rtT
@@ -140,6 +141,28 @@ NET_FILES = ('CHO_photo_network.txt', 'CHO_photo_network_lowT.txt', 'CHO_thermo_
 NET_TAGS = {'n_' + f.replace('_network', '').replace('.txt', ''): f for f in NET_FILES}
 for _t in NET_TAGS:
     KEEP[_t], NSTEPS[_t] = (0,), 1
+# Ros2 attempts (10 steps of a 20-layer column, seeded J) on shipped networks
+# beyond the c0 / c1 / c2 / c3s ones: the largest of each family, the
+# titanium one and the one with condensation species
+ATT_TAGS = {'a_' + f.replace('_network', '').replace('.txt', ''): f
+            for f in ('CHO_photo_network.txt', 'NCHO_full_photo_network.txt',
+                      'NCHO_photo_network_lowT_Jupiter.txt', 'SNCHO_full_photo_network.txt',
+                      'TiSNCHO_photo_network.txt')}
+for _t in ATT_TAGS:
+    KEEP[_t], NSTEPS[_t] = (0, 1, 2, 5, 9), 10
+
+
+def family_mix(fname):
+    """A start with the family's main carriers of each element."""
+    mix = {'H2': 0.85, 'He': 0.145, 'H2O': 1e-3, 'CH4': 5e-4}
+    if 'NCHO' in fname:
+        mix['NH3'] = 1e-4
+    if 'SNCHO' in fname:
+        mix['H2S'] = 3e-5
+    if fname.startswith('TiSNCHO'):
+        mix['TiO'] = 1e-8
+        mix['VO'] = 1e-9
+    return mix
 
 
 def net_atoms(fname):
@@ -682,6 +705,15 @@ def make(tag, ref_root, workdir, full_dir=None):
             pnet = Network.from_file(os.path.join(ref_root, 'thermo', fname), use_photo=True)
             spec.photo_J = configs.photo_J_profile(np.random.default_rng(3), spec.pco,
                                                    sorted(pnet.photo_index()))
+    elif tag in ATT_TAGS:
+        import dataclasses
+        fname = ATT_TAGS[tag]
+        spec = dataclasses.replace(configs.config2_columns(ncols=1, seed=2, nz_range=(20, 20))[0],
+                                   network=fname, use_photo=True, atom_list=net_atoms(fname),
+                                   const_mix=family_mix(fname), conver_ignore=[])
+        pnet = Network.from_file(os.path.join(ref_root, 'thermo', fname), use_photo=True)
+        spec.photo_J = configs.photo_J_profile(np.random.default_rng(5), spec.pco,
+                                               sorted(pnet.photo_index()))
     elif tag in SYN_TAGS:
         from vulcan_gb300 import synthnet
         syn_dir = os.path.join(workdir, 'syn150')
@@ -743,6 +775,10 @@ def make(tag, ref_root, workdir, full_dir=None):
         d['photo_br'] = np.array([k[1] for k in keys])
     out = os.path.join(HERE, 'golden_%s.npz' % tag)
     np.savez_compressed(out, **d)
+    if tag in ATT_TAGS:                   # the same tables as the n_ fixture of the network
+        net.to_npz(os.path.join(HERE, 'net_%s.npz' % tag[2:]))
+        print('wrote', out, os.path.getsize(out) // 1024, 'KiB')
+        return
     net.to_npz(os.path.join(HERE, 'net_%s.npz' % (
         spec.network.replace('_network.txt', '')
         + ('_photo' if spec.use_photo and 'photo' not in spec.network else ''))))

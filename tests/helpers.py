@@ -16,7 +16,10 @@ NETS = {'c0': 'net_CHO_thermo.npz', 'c1': 'net_NCHO_photo.npz', 'c2': 'net_NCHO_
         'c0vz': 'net_CHO_thermo.npz', 'c0n2': 'net_CHO_thermo.npz',
         'c0o2': 'net_CHO_thermo.npz', 'c0co2': 'net_CHO_thermo.npz',
         'c0rocky': 'net_CHO_thermo.npz', 'c3s': 'net_SNCHO_photo.npz',
-        'c4s': 'net_SYN150_photo.npz'}
+        'c4s': 'net_SYN150_photo.npz',
+        'a_CHO_photo': 'net_CHO_photo.npz', 'a_NCHO_full_photo': 'net_NCHO_full_photo.npz',
+        'a_NCHO_photo_lowT_Jupiter': 'net_NCHO_photo_lowT_Jupiter.npz',
+        'a_SNCHO_full_photo': 'net_SNCHO_full_photo.npz', 'a_TiSNCHO_photo': 'net_TiSNCHO_photo.npz'}
 
 
 def golden(tag):

@@ -6,8 +6,14 @@ from helpers import column_from_golden, golden, network
 from vulcan_gb300 import column as C
 from vulcan_gb300 import configs
 
+# Ros2-attempt fixtures on five more shipped networks (CHO photo, the full
+# NCHO and SNCHO networks, the Jupiter network with condensation species,
+# TiSNCHO), recorded from the reference with seeded J
+A_TAGS = ['a_CHO_photo', 'a_NCHO_full_photo', 'a_NCHO_photo_lowT_Jupiter', 'a_SNCHO_full_photo',
+          'a_TiSNCHO_photo']
 
-@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'])
+
+@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'] + A_TAGS)
 def test_species_order_and_nr(tag):
     g = golden(tag)
     net = network(tag)
@@ -15,12 +21,13 @@ def test_species_order_and_nr(tag):
     assert net.nr == int(g['nr'])
 
 
-@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'])
+@pytest.mark.parametrize('tag', ['c0', 'c1', 'c2'] + A_TAGS)
 def test_rate_constants_bit_exact(tag):
     """k (forward Arrhenius / fall-off / special, reverse via NASA-9 Gibbs)."""
     g = golden(tag)
     net = network(tag)
-    k = net.rate_constants(g['Tco'], g['M'])
+    with np.errstate(over='ignore'):
+        k = net.rate_constants(g['Tco'], g['M'])
     if 'photo_sp' in g:
         pidx = net.photo_index()
         for sp, br in zip(g['photo_sp'], g['photo_br']):
@@ -30,7 +37,7 @@ def test_rate_constants_bit_exact(tag):
     np.testing.assert_array_equal(k, g['k'])
 
 
-@pytest.mark.parametrize('tag', ['c0', 'c2', 'c0n2', 'c0o2', 'c0co2', 'c0rocky', 'c0nomol'])
+@pytest.mark.parametrize('tag', ['c0', 'c2', 'c0n2', 'c0o2', 'c0co2', 'c0rocky', 'c0nomol'] + A_TAGS)
 def test_column_setup_bit_exact(tag):
     """pico, M, n_0, mu, g, Hp, dz, dzi, Ti, Hpi, Dzz, ms, alpha as the
     reference's f_pico / f_mu_dz / mol_diff built them, for the H2 base gas

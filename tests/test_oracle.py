@@ -239,3 +239,29 @@ def test_sulfur_network_attempts_match_reference(tag, n):
         r = O.ros2_attempt(*args, solve)
         assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
         assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
+
+
+A_TAGS = ['a_CHO_photo', 'a_NCHO_full_photo', 'a_NCHO_photo_lowT_Jupiter', 'a_SNCHO_full_photo',
+          'a_TiSNCHO_photo']
+
+
+@pytest.mark.parametrize('tag', A_TAGS)
+def test_more_networks_chemdf_bit_exact(tag):
+    g = golden(tag)
+    on = oracle_net(tag, g)
+    np.testing.assert_array_equal(O.chemdf(on, g['y_ini'], g['M'], g['k']), g['chemdf0'])
+
+
+@pytest.mark.parametrize('tag,n', [a for t in A_TAGS for a in _attempts(t)])
+def test_more_networks_attempts_match_reference(tag, n):
+    """Recorded Ros2 attempts on five more shipped networks (CHO photo, full
+    NCHO and SNCHO, the Jupiter network with its condensation species,
+    TiSNCHO; seeded J): banded and block-Thomas restatements within 1e-10."""
+    g = golden(tag)
+    on = oracle_net(tag, g)
+    args = (on, g['att_y'][n], g['att_ymix'][n], float(g['att_dt'][n]), g['k'],
+            attempt_atm(g, n), O.Flags(), O.Tol())
+    for solve in ('banded', 'block'):
+        r = O.ros2_attempt(*args, solve)
+        assert floor_err(r.sol, g['att_sol'][n], g['n_0']) <= 1e-10, solve
+        assert abs(r.delta / g['att_delta'][n] - 1) <= 1e-6, solve
